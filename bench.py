@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""Benchmark: one SCF grid step of the 64-atom Si precision-form workload.
+
+A step is density assembly from D, FFT Poisson, LDA xc + potential (+ V_na),
+grid matrix elements and the FP64 energy terms, on a 96^3 grid with 13
+orbitals per atom (see lcpgrid/workloads.py).  Prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32|bf16x3]
+    python bench.py --impl reference ...   (the CPU restatement on the host cores)
+
+Multi-GPU runs (torchrun) are independent replicas of the same cell: the
+path is never sharded, there is no data-path collective.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lcpaodft.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "ms per SCF grid step & jobs/s (p50/p99) split-BF16 vs FP64, <=1uHa/atom err"
+UNIT = "grid steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def pair_work(ucell):
+    """Algorithmic flops of one grid step's pair contractions, counting each
+    unordered pair {(i,j,R), (j,i,-R)} once: density (2*NOi*NOj + 2*NOi) and
+    H (2*NOi*NOj + NOi) per lens point and spin."""
+    import numpy as np
+    no = np.asarray(ucell.Total_NumOrbs, dtype=np.float64)
+    a = ucell.MPI_atom - 1
+    b = ucell.MPI_natn - 1
+    olg = ucell.MPI_NumOLG.astype(np.float64)
+    # ordered pairs count each unordered pair twice, except self pairs (i,i,0)
+    selfp = (a == b) & (ucell.MPI_ncn == 0)
+    w = np.where(selfp, 1.0, 0.5)
+    dens = float(np.sum(w * olg * (2 * no[a] * no[b] + 2 * no[a])))
+    ham = float(np.sum(w * olg * (2 * no[a] * no[b] + no[a])))
+    return dens, ham
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle port)
+
+SAMPLE_ATOMS = 8  # the CPU sample: pairs among the first conventional cell's 8 atoms
+
+
+def _cpu_inputs(wl, sample):
+    from lcpgrid.workloads import psd_density_matrices_oracle, smooth_vna
+    from oracle import lcp_oracle as O
+    u = O.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+                total_numorbs=wl["numorbs"], pair_subset=sample)
+    pao = wl["paos"][0]
+    opao = O.PAO(pao.Spe_MaxL_Basis, pao.Spe_Num_Basis, pao.Spe_PAO_RV, pao.Spe_PAO_RWF)
+    orbs = O.set_orbitals_grid([opao], u, atoms=set(range(SAMPLE_ATOMS)))
+    dm = psd_density_matrices_oracle(u, wl["dm_seed"], trace=wl["trace"])[0]
+    vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
+    return u, orbs, dm, vna
+
+
+def _cpu_run(u, orbs, dm, vna, reps):
+    from oracle import lcp_oracle as O
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.set_density_grid("off", u, orbs, [dm])
+        O.calc_matrix_elements(u, orbs, [vna], 1)
+    return time.perf_counter() - t0
+
+
+def _cpu_proc(wl, sample, reps, barrier, queue):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    u, orbs, dm, vna = _cpu_inputs(wl, sample)
+    barrier.wait()
+    queue.put(_cpu_run(u, orbs, dm, vna, reps))
+
+
+def cpu_baseline(wl, ucell_gpu, budget_s, all_cores):
+    """Time the oracle (a restatement of the reference's per-pair, 512-point
+    blocked BLAS algorithm) on a bounded sample of the workload -- density + H
+    over the pairs among the first 8 atoms -- with one process per host core,
+    each single-threaded BLAS, as the reference's MPI pair split runs.  The full
+    step is extrapolated by the reference's own work weight NO_i*NO_j*NumOLG;
+    Poisson and xc are timed on the full grid.  Processes are spawned (this
+    runs after GPU work)."""
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import multiprocessing as mp
+
+    import numpy as np
+    from oracle import lcp_oracle as O
+
+    sample = [p for p in range(ucell_gpu.Nloop)
+              if ucell_gpu.MPI_atom[p] <= SAMPLE_ATOMS and ucell_gpu.MPI_natn[p] <= SAMPLE_ATOMS]
+    no = np.asarray(wl["numorbs"], dtype=np.float64)
+    olg = ucell_gpu.MPI_NumOLG.astype(np.float64)
+    wt = no[ucell_gpu.MPI_atom - 1] * no[ucell_gpu.MPI_natn - 1] * olg
+    w_sample = float(wt[sample].sum())
+    w_total = float(wt.sum())
+    u, orbs, dm, vna = _cpu_inputs(wl, sample)
+    t1 = _cpu_run(u, orbs, dm, vna, 1)
+    cores = (os.cpu_count() or 1) if all_cores else 1
+    reps = max(1, int(budget_s / max(t1, 1e-3)))
+    if cores > 1:
+        ctx = mp.get_context("spawn")
+        barrier = ctx.Barrier(cores)
+        queue = ctx.Queue()
+        procs = [ctx.Process(target=_cpu_proc, args=(wl, sample, reps, barrier, queue)) for _ in range(cores)]
+        for pr in procs:
+            pr.start()
+        times = [queue.get() for _ in procs]
+        for pr in procs:
+            pr.join()
+        wall = max(times)
+    else:
+        wall = _cpu_run(u, orbs, dm, vna, reps)
+    rate = cores * reps * w_sample / wall
+    t_pairs = w_total / rate
+    rho = np.abs(np.random.default_rng(0).normal(size=int(np.prod(wl["ngrid"])))) * 0.01
+    t0 = time.perf_counter()
+    O.solve_poisson_xyz(wl["ngrid"], 2 * np.pi * np.linalg.inv(np.asarray(wl["latvecs"]).T),
+                        O.set_density_xyz("off", wl["ngrid"], [rho], np.zeros_like(rho)))
+    O.set_xc_grid("LDA", "off", np.zeros_like(rho), [rho])
+    O.calc_exc1("off", "LDA", 1.0, np.zeros_like(rho), np.zeros_like(rho), [rho])
+    t_grid = time.perf_counter() - t0
+    step_s = t_pairs + t_grid
+    return {"value": 1.0 / step_s, "unit": UNIT, "cores": cores, "kind": "port",
+            "ms_per_step": step_s * 1e3,
+            "sample": "numpy oracle (per-pair 512-point blocks + BLAS, 1 BLAS thread/process): density+H over "
+                      "the %d pairs among atoms 1-%d (%.2f%% of the pair work) x %d reps on each of %d processes "
+                      "(%.1f s wall), extrapolated by NO_i*NO_j*NumOLG; Poisson+xc timed once on the full grid"
+                      % (len(sample), SAMPLE_ATOMS, 100 * w_sample / w_total, reps, cores, wall)}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def build_workload(ctx, wl):
+    import lcpgrid as L
+    from lcpgrid.workloads import psd_density_matrices, smooth_vna
+    t0 = time.perf_counter()
+    u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+                Total_NumOrbs=wl["numorbs"])
+    t_geom = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx)
+    t_tab = time.perf_counter() - t0
+    dm = psd_density_matrices(u, wl["dm_seed"], trace=wl["trace"])
+    vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
+    return u, orbs, dm, vna, t_geom, t_tab
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import lcpgrid as L
+    from lcpgrid.workloads import si64_workload
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    wl = si64_workload()
+    ctx = L.Context(local)
+    u, orbs, dm, vna, t_geom, t_tab = build_workload(ctx, wl)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    # FP64 reference energy of this step (the drop-in), for the error of other forms
+    job = L.GridStepJob(u, orbs, "off", "LDA", None, None, vna)
+    job.set_dm(dm)
+    ctx.set_precision("fp64")
+    job.step()
+    e_fp64 = job.energies()
+    h_fp64 = job.hks()[0]
+    ctx.set_precision(args.precision)
+
+    for _ in range(max(3, args.warmup)):
+        job.step()
+    torch.cuda.synchronize()
+    stages = job.step_timed()
+
+    # timed, device-resident: inputs larger than L2 (phi tables ~1 GB)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    l0 = ctx.launch_count
+    ev[0].record(stream)
+    for k in range(args.steps):
+        job.step()
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count - l0
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    per = np.array([ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)])
+    total_ms = float(ev[0].elapsed_time(ev[-1]))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    e_now = job.energies()
+    h_now = job.hks()[0]
+
+    # e2e through the public API: pinned host D in, H and energies out, every step
+    pin_dm = torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True)
+    pin_dm.numpy()[:] = dm[0]
+    pin_h = torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True)
+    e2e_n = max(1, args.e2e_steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_n):
+        job.set_dm([pin_dm.numpy()])
+        job.step()
+        out = job._get(L.api.lib.lcp_job_get_hks, u.Total_Hsize)
+        e2e_e = job.energies()
+    e2e_s = (time.perf_counter() - t0) / e2e_n
+
+    dens_flops, ham_flops = pair_work(u)
+    peaks, psrc = measured_peaks()
+    # dominant kernel: the larger of the two pair contractions
+    names = ["density", "poisson", "xc_vpot", "energy_sums", "hamiltonian", "dot_finish"]
+    dom = int(np.argmax(stages))
+    dom_flops = dens_flops if names[dom] == "density" else ham_flops
+    if args.precision == "fp64":
+        fp64_peak = ctx.probe_fp64_tflops()
+        roof = {"bound": "fp64-alu", "kernel": names[dom], "achieved": dom_flops / (stages[dom] * 1e-3) / 1e12,
+                "peak": fp64_peak, "unit": "TFLOP/s", "peak_source": "probe: FP64 FMA loop on this GPU",
+                "traffic": None}
+    else:
+        pk = peaks.get("bf16_tflops_sustained", 1700.0)
+        roof = {"bound": "tensor", "kernel": names[dom], "achieved": dom_flops / (stages[dom] * 1e-3) / 1e12,
+                "peak": pk, "unit": "TFLOP/s", "peak_source": psrc + " bf16_tflops_sustained", "traffic": None}
+    roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
+
+    ms_step = total_ms / args.steps
+    line = {
+        "metric": METRIC, "value": world * 1000.0 / ms_step, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
+        "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp32": "f32", "bf16x3": "bf16x3/f32-acc"}[args.precision],
+        "data": "synthetic (seeded: Gaussian radial functions, PSD D, smooth V_na)",
+        "config": {"workload": wl["name"], "atoms": wl["natom"], "orbitals_per_atom": wl["numorbs"][0],
+                   "ngrid": list(wl["ngrid"]), "pairs": int(u.Nloop), "folded_pairs": int(u.n_unique),
+                   "lens_points": int(u.sum_numolg), "precision": args.precision, "spinpol": "off", "xc": "LDA",
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (phi tables %.0f MB)" % (u.sum_gridn * 13 * 8 / 1e6)},
+        "stage_ms": dict(zip(names, [float(x) for x in stages])),
+        "setup_s": {"ucell_host": t_geom, "tabulation": t_tab},
+        "roofline": roof,
+        "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(u.Total_Hsize * 8),
+                "d2h_bytes_per_step": int(u.Total_Hsize * 8 + 40), "ms_per_step": e2e_s * 1e3},
+        "energy": {"E_grid": float(e_now[4]), "E_grid_fp64": float(e_fp64[4]),
+                   "err_per_atom_uHa": abs(float(e_now[4] - e_fp64[4])) / wl["natom"] * 1e6,
+                   "max_abs_dH": float(np.max(np.abs(h_now - h_fp64)))},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "gpu_launches_note": "library kernels per timed region; cuFFT adds 2 FFT launches per step",
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(wl, u, args.cpu_seconds, all_cores=True)
+        except Exception as exc:  # the baseline must not hide the GPU line
+            line["cpu_baseline"] = {"value": None, "error": repr(exc)}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import lcpgrid as L
+    from lcpgrid.workloads import si64_workload
+    wl = si64_workload()
+    u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+                Total_NumOrbs=wl["numorbs"])
+    vals = []
+    t0 = time.perf_counter()
+    budget = max(4.0, 60.0 / max(1, args.steps + args.warmup))
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(wl, u, budget, all_cores=True)
+        if k >= args.warmup:
+            vals.append(r)
+    wall = time.perf_counter() - t0
+    v = sum(x["value"] for x in vals) / len(vals)
+    ms = 1000.0 / v
+    cb = dict(vals[-1])
+    cb["value"] = v
+    print(json.dumps({
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": wl["name"], "atoms": wl["natom"], "ngrid": list(wl["ngrid"]), "precision": "fp64"},
+        "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+        "note": "Julia is not available on this machine; the reference's CPU path is timed through its numpy "
+                "restatement (oracle/), parallel over the host cores like the reference's MPI pair split"}))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,218 @@
+/*
+ * lcpgrid.h -- C ABI of the GB300 (sm_103a) real-space grid path of LCPAODFT.jl.
+ *
+ * Plain C types only: pointers, sizes, int32/int64/double.  Every call
+ * returns an lcp_status; no exception crosses the ABI.  lcp_last_error()
+ * gives the message of the last failing call on the calling thread.
+ *
+ * Conventions shared with the reference (LCPAODFT.jl):
+ *   - grids are C-order flat vectors of length NN = N1*N2*N3, index
+ *     n1*N2*N3 + n2*N3 + n3 (src/UCell.jl:380);
+ *   - atoms are 1-based where the reference stores them 1-based (atom2spe,
+ *     natn); grid/cell/overlap indices are 0-based as the reference stores
+ *     them (GridListAtom, CellListAtom, GListTAtoms1/2);
+ *   - DM and H use the flat pair-block layout of the reference: pairs in
+ *     (atom 1..Natom, neighbour 1..FNAN+1) order, each block NO(jatom) rows x
+ *     NO(atom) columns, column-major (src/Hamiltonian.jl:16-38,
+ *     src/Matrix/Set_Density_Grid.jl:94-97);
+ *   - SpinPol "off"/"on"/"nc" is LCP_SPIN_OFF/ON/NC with 1/2/4 channels.
+ *
+ * Threading: one lcp_ctx per host thread; calls on one context run in order
+ * on its CUDA stream.  Host buffers passed to a call are read or written
+ * before the call returns and are not retained.
+ */
+#ifndef LCPGRID_H
+#define LCPGRID_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t lcp_status;
+enum {
+  LCP_OK = 0,
+  LCP_EINVAL = 1,    /* invalid argument (the reference raises error()) */
+  LCP_ENOMEM = 2,    /* host or device allocation failed */
+  LCP_EDEVICE = 3,   /* CUDA error */
+  LCP_ETIMEDOUT = 4, /* a bounded device wait gave up */
+  LCP_ENOTSUP = 5,   /* unsupported shape or mode */
+  LCP_ESTATE = 6     /* object used in the wrong state */
+};
+
+enum { LCP_SPIN_OFF = 0, LCP_SPIN_ON = 1, LCP_SPIN_NC = 2 };
+enum { LCP_XC_LDA = 0, LCP_XC_LSDA = 1 };
+/* arithmetic of the pair contractions (density assembly, grid H) */
+enum { LCP_PREC_FP64 = 0, LCP_PREC_FP32 = 1, LCP_PREC_BF16X3 = 2 };
+
+typedef struct lcp_ucell lcp_ucell; /* host grid geometry (struct UCell) */
+typedef struct lcp_ctx lcp_ctx;     /* device context: stream, handles, workspaces */
+typedef struct lcp_orbs lcp_orbs;   /* device orbital tables (PackedOrbitalsGrid) */
+typedef struct lcp_job lcp_job;     /* device-resident SCF grid-step state */
+
+/* Radial tables of one species: the fields of struct PAO the grid path reads
+ * (src/Atoms/Read_PAO.jl:1-18). */
+typedef struct {
+  int32_t max_l;         /* Spe_MaxL_Basis, 0..3 */
+  int32_t num_basis[4];  /* Spe_Num_Basis[l] */
+  int32_t num_mesh;      /* Spe_Num_Mesh_PAO (>= 8) */
+  const double* rv;      /* Spe_PAO_RV[num_mesh], increasing */
+  const double* rwf;     /* Spe_PAO_RWF: for l, for p < num_basis[l]: num_mesh values */
+} lcp_pao;
+
+const char* lcp_last_error(void);
+const char* lcp_version(void);
+
+/* ---------------------------------------------------------------- geometry */
+
+/* UCell(Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin;
+ *       Total_NumOrbs)  -- src/UCell.jl:210-294 (one MPI rank).
+ * latvecs: 3x3 row vectors (row-major); gxyz: natom x 3 (bohr);
+ * atom2spe: 1-based species per atom; total_numorbs may be NULL (zeros). */
+lcp_status lcp_ucell_create(int32_t nspin, const double* latvecs, int32_t natom,
+                            const int32_t* atom2spe, const double* gxyz,
+                            const double* atoms_cut1, const int32_t* ngrid,
+                            const double* grid_origin, const int32_t* total_numorbs,
+                            lcp_ucell** out);
+void lcp_ucell_destroy(lcp_ucell* ucell);
+
+typedef struct {
+  int32_t cpycell;      /* System_Grid.CpyCell */
+  int32_t natom;
+  int32_t nloop;        /* number of (atom, neighbour) pairs, System_Grid.Nloop */
+  int32_t ncell;        /* (2*CpyCell+1)^3 */
+  int32_t ngrid[3];
+  int32_t max_numorbs;
+  int64_t total_hsize;  /* System_Grid.Total_Hsize */
+  int64_t sum_gridn;    /* sum of GridN_Atom */
+  int64_t sum_numolg;   /* sum of MPI_NumOLG over all pairs */
+  int64_t n_unique;     /* pairs kept after folding (i,j,R) with (j,i,-R) */
+  double gridvol;       /* System_Grid.GridVol */
+} lcp_ucell_info;
+lcp_status lcp_ucell_get_info(const lcp_ucell* ucell, lcp_ucell_info* info);
+
+/* Integer fields of UCell, copied to dst[count]; `index` selects the atom or
+ * pair for per-atom / per-pair lists (0-based), ignored otherwise. */
+enum {
+  LCP_F_FNAN = 0,         /* [natom] */
+  LCP_F_NATN = 1,         /* per atom [FNAN+1], 1-based atoms */
+  LCP_F_NCN = 2,          /* per atom [FNAN+1] */
+  LCP_F_GRIDN_ATOM = 3,   /* [natom] */
+  LCP_F_GRIDLIST = 4,     /* per atom [GridN] */
+  LCP_F_CELLLIST = 5,     /* per atom [GridN] */
+  LCP_F_PAIR_ATOM = 6,    /* [nloop], 1-based */
+  LCP_F_PAIR_NATN = 7,    /* [nloop], 1-based */
+  LCP_F_PAIR_NCN = 8,     /* [nloop] */
+  LCP_F_NUMOLG = 9,       /* [nloop] */
+  LCP_F_GLIST1 = 10,      /* per pair [NumOLG] (GListTAtoms1) */
+  LCP_F_GLIST2 = 11,      /* per pair [NumOLG] (GListTAtoms2) */
+  LCP_F_ATV_IJK = 12      /* [ncell*3] */
+};
+lcp_status lcp_ucell_get_int(const lcp_ucell* ucell, int32_t field, int64_t index,
+                             int32_t* dst, int64_t count);
+lcp_status lcp_ucell_get_atv(const lcp_ucell* ucell, double* dst /* [ncell*3] */);
+
+/* Calc_Ngrid(Ecut, Latvecs) -- src/utils/Calc_Ngrid.jl:1-76 */
+lcp_status lcp_calc_ngrid(double ecut, const double* latvecs, int32_t* ngrid_out);
+
+/* ---------------------------------------------------------------- context */
+
+lcp_status lcp_ctx_create(int32_t device, lcp_ctx** out);
+void lcp_ctx_destroy(lcp_ctx* ctx);
+/* Run subsequent work on an external cudaStream_t (NULL: the context's own). */
+lcp_status lcp_ctx_set_stream(lcp_ctx* ctx, void* stream);
+lcp_status lcp_ctx_set_precision(lcp_ctx* ctx, int32_t precision);
+lcp_status lcp_ctx_synchronize(lcp_ctx* ctx);
+/* Number of kernels this library launched on the context so far. */
+int64_t lcp_ctx_launch_count(const lcp_ctx* ctx);
+
+/* ---------------------------------------------------------------- the grid path */
+
+/* Set_Orbitals_Grid(pao, ucell) and, with with_grad != 0, Set_dOrbitals_Grid
+ * (src/Matrix/Set_Orbitals_Grid.jl:26-277, src/Matrix/Set_dOrbitals_Grid.jl:1-362).
+ * paos[spe-1] is the species of atom2spe. Tables stay on the device. */
+lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t nspecies,
+                                 const lcp_pao* paos, int32_t with_grad, lcp_orbs** out);
+void lcp_orbs_destroy(lcp_orbs* orbs);
+/* Copy one atom's table to the host, point-major [GridN x NO] (the memory of
+ * PackedOrbitalsGrid.data[atom]).  component: 0 = phi, 1..3 = d/dx, d/dy, d/dz. */
+lcp_status lcp_orbs_download(lcp_ctx* ctx, const lcp_orbs* orbs, int32_t component,
+                             int32_t atom, double* dst, int64_t count);
+
+/* Set_Density_Grid!(SpinPol, ucell, Orbs_Grid, DM, Density_Grid)
+ * (src/Matrix/Set_Density_Grid.jl:1-304).  dm[s]: Total_Hsize doubles;
+ * density_grid[s]: NN doubles, overwritten. */
+lcp_status lcp_set_density_grid(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
+                                int32_t spinpol, const double* const* dm,
+                                double* const* density_grid);
+
+/* Solve_Poisson!(SpinPol, dft_mixing, Density_Grid, ADensity_Grid, dVHart_Grid)
+ * (src/Poisson.jl:1-26).  recvecs = 2*pi*inv(Latvecs') row vectors. */
+lcp_status lcp_solve_poisson(lcp_ctx* ctx, const int32_t* ngrid, const double* recvecs,
+                             int32_t spinpol, const double* const* density_grid,
+                             const double* adensity_grid, double* dvhart_grid);
+/* Inner Solve_Poisson!(Ngrid, Recvecs, Density_xyz, dVHart_Grid) for a real
+ * Density_xyz (src/Poisson.jl:29-108). */
+lcp_status lcp_solve_poisson_xyz(lcp_ctx* ctx, const int32_t* ngrid, const double* recvecs,
+                                 const double* density_xyz, double* dvhart_grid);
+
+/* Set_XC_Grid!(xc_func::XC_LDA|XC_LSDA, PCCDensity_Grid, Density_Grid)
+ * (src/XC/XC_Func.jl:111-145). nc additionally reads Density_Grid[3:4]. */
+lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn,
+                           const double* pcc, const double* const* density_grid,
+                           double* const* vxc_grid);
+
+/* Set_Vpot_Grid!(xc_func, dVHart_Grid, Vpot_Grid) (src/Matrix/Set_Vpot_Grid.jl:1-19);
+ * vna (may be NULL) is added to the spin-diagonal channels. */
+lcp_status lcp_set_vpot_grid(lcp_ctx* ctx, int32_t spinpol, int64_t nn, const double* dvhart,
+                             const double* const* vxc, const double* vna, double* const* vpot);
+
+/* Calc_MatrixElements_dVH_Vxc_{off,on,nc}!(ucell, Orbs_Grid, Vpot_Grid, MPI_Hks)
+ * (src/Hamiltonian.jl:235-429): hks[ch] (Total_Hsize) overwritten with the grid
+ * part, scaled by GridVol. */
+lcp_status lcp_calc_matrix_elements(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
+                                    int32_t spinpol, const double* const* vpot, double* const* hks);
+
+/* Calc_EH1 (src/Energy.jl:655-666) and Calc_EXC1 (src/Energy.jl:669-700). */
+lcp_status lcp_calc_eh1(lcp_ctx* ctx, int32_t spinpol, int64_t nn, double gridvol,
+                        const double* adensity, const double* const* density,
+                        const double* dvhart, double* eh1);
+lcp_status lcp_calc_exc1(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn, double gridvol,
+                         const double* adensity, const double* pcc,
+                         const double* const* density, double* exc /* [2] */);
+
+/* ---------------------------------------------------------------- device-resident step */
+
+/* One SCF grid step with all state on the device: density from D, Poisson,
+ * xc, potential (+ optional V_na), grid H and the FP64 energy terms.  The
+ * inputs adensity/pcc/vna (NN doubles each, may be NULL = zero) are copied at
+ * creation. */
+lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
+                          int32_t spinpol, int32_t xc, const double* adensity,
+                          const double* pcc, const double* vna, lcp_job** out);
+void lcp_job_destroy(lcp_job* job);
+/* Host -> device copy of the density matrices (Nspin x Total_Hsize). */
+lcp_status lcp_job_set_dm(lcp_ctx* ctx, lcp_job* job, const double* const* dm);
+/* Launch one grid step on the context stream (asynchronous). */
+lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job);
+/* The same step with CUDA events between its stages (synchronises); stage_ms[6] =
+ * density, Poisson, xc+potential, energy sums, grid H, <D,H> + job energy
+ * (the stage names of the reference's TimerOutputs sections). */
+lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms);
+/* Energies of the last step: [E_H1, EXC1[1], EXC1[2], sum_s <D_s,H_s>, E_grid]. */
+lcp_status lcp_job_energies(lcp_ctx* ctx, lcp_job* job, double* out5);
+/* Device -> host copies of the last step's outputs. */
+lcp_status lcp_job_get_density(lcp_ctx* ctx, lcp_job* job, double* const* density);
+lcp_status lcp_job_get_hks(lcp_ctx* ctx, lcp_job* job, double* const* hks);
+lcp_status lcp_job_get_vpot(lcp_ctx* ctx, lcp_job* job, double* const* vpot);
+
+/* Measured FP64 FMA throughput of the device (TFLOP/s), a roofline denominator
+ * for the FP64 contractions. */
+lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LCPGRID_H */

@@ -1,0 +1,1077 @@
+// C ABI of the lcpgrid library: argument checking, device memory, and the
+// orchestration of the kernels.  Declarations and conventions: lcpgrid.h.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "lcp_device.h"
+#include "lcp_internal.h"
+
+using lcp::DevGeom;
+using lcp::DevPairs;
+using lcp::DevSpecies;
+
+namespace lcp {
+namespace {
+thread_local std::string g_last_error;
+}
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+}  // namespace lcp
+
+namespace {
+
+lcp_status fail(lcp_status code, const std::string& msg) {
+  lcp::set_error(msg);
+  return code;
+}
+
+lcp_status cuda_fail(cudaError_t e, const char* where) {
+  return fail(e == cudaErrorMemoryAllocation ? LCP_ENOMEM : LCP_EDEVICE,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define API_CUDA(expr, where)                       \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_fail(_e, where); \
+  } while (0)
+
+// Owning device buffer.
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+template <class T>
+cudaError_t upload(DBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  cudaError_t e = b.ensure(v.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  e = cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
+}
+
+int channels(int32_t spinpol) { return spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4); }
+
+}  // namespace
+
+struct lcp_ucell {
+  lcp::UCell u;
+};
+
+struct FftPlans {
+  cufftHandle fwd = 0, inv = 0;
+  bool ok = false;
+};
+
+struct lcp_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  int32_t precision = LCP_PREC_FP64;
+  int64_t launches = 0;
+  std::map<std::tuple<int, int, int>, FftPlans> plans;
+  // workspaces of the host-buffer entry points
+  DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
+  ~lcp_ctx() {
+    cudaSetDevice(device);
+    for (auto& kv : plans) {
+      if (kv.second.fwd) cufftDestroy(kv.second.fwd);
+      if (kv.second.inv) cufftDestroy(kv.second.inv);
+    }
+    if (own) cudaStreamDestroy(own);
+  }
+};
+
+struct lcp_orbs {
+  const lcp_ucell* ucell = nullptr;
+  int device = 0;
+  bool grad = false;
+  int max_no = 0;
+  DevGeom geom{};
+  DevPairs pairs{};
+  // device arrays
+  DBuf atv, gxyz, spe, sph_off, glist, clist, phi_off, numorbs;
+  DBuf species, radial;
+  DBuf phi, dphi[3], phi32;
+  DBuf p_atom, p_jatom, p_boffp, p_boffq, p_self, p_lensoff, p_g1, p_g2, it_pair, it_start, it_count;
+  int64_t table_elems = 0;
+};
+
+struct lcp_job {
+  const lcp_ucell* ucell = nullptr;
+  const lcp_orbs* orbs = nullptr;
+  int32_t spinpol = LCP_SPIN_OFF, xc = LCP_XC_LDA;
+  int nspin = 1;
+  int64_t nn = 0, hsize = 0;
+  double recvecs[9] = {};
+  DBuf dm[4], rho[4], hks[4], vpot[4];
+  DBuf aden, pcc, vna, dvh, real, spec, part, scal;
+  bool has_aden = false, has_pcc = false, has_vna = false;
+  FftPlans* plans = nullptr;
+};
+
+namespace {
+
+lcp_status get_plans(lcp_ctx* ctx, const int32_t* ng, FftPlans** out) {
+  auto key = std::make_tuple((int)ng[0], (int)ng[1], (int)ng[2]);
+  auto it = ctx->plans.find(key);
+  if (it == ctx->plans.end()) {
+    FftPlans p;
+    if (cufftPlan3d(&p.fwd, ng[0], ng[1], ng[2], CUFFT_D2Z) != CUFFT_SUCCESS ||
+        cufftPlan3d(&p.inv, ng[0], ng[1], ng[2], CUFFT_Z2D) != CUFFT_SUCCESS)
+      return fail(LCP_EDEVICE, "cuFFT plan creation failed");
+    p.ok = true;
+    it = ctx->plans.emplace(key, p).first;
+  }
+  cufftSetStream(it->second.fwd, ctx->stream);
+  cufftSetStream(it->second.inv, ctx->stream);
+  *out = &it->second;
+  return LCP_OK;
+}
+
+// dvh = Poisson(real source already in `real`); spec is scratch.
+lcp_status poisson_device(lcp_ctx* ctx, FftPlans* pl, const int32_t* ng, const double* recvecs, double* real,
+                          void* spec, double* dvh) {
+  if (cufftExecD2Z(pl->fwd, real, reinterpret_cast<cufftDoubleComplex*>(spec)) != CUFFT_SUCCESS)
+    return fail(LCP_EDEVICE, "cufftExecD2Z failed");
+  API_CUDA(lcp::launch_poisson_scale(ng, recvecs, spec, ctx->stream), "poisson_scale");
+  ctx->launches++;
+  if (cufftExecZ2D(pl->inv, reinterpret_cast<cufftDoubleComplex*>(spec), dvh) != CUFFT_SUCCESS)
+    return fail(LCP_EDEVICE, "cufftExecZ2D failed");
+  return LCP_OK;
+}
+
+lcp_status check_ctx(lcp_ctx* ctx) {
+  if (!ctx) return fail(LCP_EINVAL, "context is NULL");
+  API_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return LCP_OK;
+}
+
+lcp_status check_pair(const lcp_ucell* ucell, const lcp_orbs* orbs) {
+  if (!ucell || !orbs) return fail(LCP_EINVAL, "ucell/orbs is NULL");
+  if (orbs->ucell != ucell) return fail(LCP_EINVAL, "Orbs_Grid was tabulated for a different UCell");
+  return LCP_OK;
+}
+
+lcp_status ensure_phi32(lcp_ctx* ctx, lcp_orbs* o) {
+  if (o->phi32.p) return LCP_OK;
+  API_CUDA(o->phi32.ensure(o->table_elems * sizeof(float)), "phi32 alloc");
+  API_CUDA(lcp::launch_convert_f32(o->phi.as<double>(), o->phi32.as<float>(), o->table_elems, ctx->stream),
+           "convert_f32");
+  ctx->launches++;
+  return LCP_OK;
+}
+
+lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const double* const* dm, double* const* rho,
+                          int64_t nn) {
+  for (int s = 0; s < nspin; ++s) API_CUDA(cudaMemsetAsync(rho[s], 0, nn * sizeof(double), ctx->stream), "memset");
+  int prec = ctx->precision;
+  if (prec == LCP_PREC_BF16X3) return fail(LCP_ENOTSUP, "BF16x3 contractions are not available in this build");
+  if (prec == LCP_PREC_FP32) {
+    lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
+    if (s != LCP_OK) return s;
+  }
+  API_CUDA(lcp::launch_density_pairs(prec, orbs->geom, orbs->pairs, nspin, orbs->phi.as<double>(),
+                                     orbs->phi32.as<float>(), dm, rho, orbs->max_no, ctx->stream),
+           "density kernel");
+  ctx->launches++;
+  return LCP_OK;
+}
+
+lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const double* const* vpot,
+                              double* const* hks, int64_t hsize) {
+  for (int c = 0; c < nch; ++c) API_CUDA(cudaMemsetAsync(hks[c], 0, hsize * sizeof(double), ctx->stream), "memset");
+  int prec = ctx->precision;
+  if (prec == LCP_PREC_BF16X3) return fail(LCP_ENOTSUP, "BF16x3 contractions are not available in this build");
+  if (prec == LCP_PREC_FP32) {
+    lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
+    if (s != LCP_OK) return s;
+  }
+  API_CUDA(lcp::launch_hamiltonian_pairs(prec, orbs->geom, orbs->pairs, nch, orbs->phi.as<double>(),
+                                         orbs->phi32.as<float>(), vpot, hks, orbs->max_no, ctx->stream),
+           "hamiltonian kernel");
+  ctx->launches++;
+  return LCP_OK;
+}
+
+}  // namespace
+
+
+extern "C" {
+
+const char* lcp_last_error(void) { return lcp::last_error_cstr(); }
+const char* lcp_version(void) { return "lcpgrid 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------- geometry
+
+lcp_status lcp_ucell_create(int32_t nspin, const double* latvecs, int32_t natom, const int32_t* atom2spe,
+                            const double* gxyz, const double* atoms_cut1, const int32_t* ngrid,
+                            const double* grid_origin, const int32_t* total_numorbs, lcp_ucell** out) {
+  if (!out || !latvecs || !atom2spe || !gxyz || !atoms_cut1 || !ngrid) return fail(LCP_EINVAL, "NULL argument");
+  *out = nullptr;
+  std::unique_ptr<lcp_ucell> u(new (std::nothrow) lcp_ucell());
+  if (!u) return fail(LCP_ENOMEM, "out of host memory");
+  try {
+    std::string err = lcp::build_ucell(u->u, nspin, latvecs, natom, atom2spe, gxyz, atoms_cut1, ngrid, grid_origin,
+                                       total_numorbs);
+    if (!err.empty()) return fail(LCP_EINVAL, err);
+  } catch (const std::bad_alloc&) {
+    return fail(LCP_ENOMEM, "out of host memory building UCell");
+  }
+  *out = u.release();
+  return LCP_OK;
+}
+
+void lcp_ucell_destroy(lcp_ucell* ucell) { delete ucell; }
+
+lcp_status lcp_ucell_get_info(const lcp_ucell* ucell, lcp_ucell_info* info) {
+  if (!ucell || !info) return fail(LCP_EINVAL, "NULL argument");
+  const lcp::UCell& u = ucell->u;
+  info->cpycell = u.cpycell;
+  info->natom = u.natom;
+  info->nloop = u.nloop;
+  info->ncell = u.ncell;
+  for (int d = 0; d < 3; ++d) info->ngrid[d] = u.ngrid[d];
+  info->max_numorbs = u.max_numorbs();
+  info->total_hsize = u.total_hsize;
+  info->sum_gridn = u.sphere_off.empty() ? 0 : u.sphere_off.back();
+  int64_t so = 0;
+  for (auto v : u.numolg) so += v;
+  info->sum_numolg = so;
+  info->n_unique = (int64_t)u.uniq_pair.size();
+  info->gridvol = u.gridvol;
+  return LCP_OK;
+}
+
+lcp_status lcp_ucell_get_int(const lcp_ucell* ucell, int32_t field, int64_t index, int32_t* dst, int64_t count) {
+  if (!ucell || (!dst && count > 0)) return fail(LCP_EINVAL, "NULL argument");
+  const lcp::UCell& u = ucell->u;
+  std::vector<int32_t> tmp;
+  const int32_t* src = nullptr;
+  int64_t n = 0;
+  auto need_atom = [&]() { return index >= 0 && index < u.natom; };
+  auto need_pair = [&]() { return index >= 0 && index < u.nloop; };
+  switch (field) {
+    case LCP_F_FNAN: src = u.fnan.data(); n = u.natom; break;
+    case LCP_F_NATN:
+      if (!need_atom()) return fail(LCP_EINVAL, "atom index out of range");
+      src = u.natn[index].data(); n = (int64_t)u.natn[index].size(); break;
+    case LCP_F_NCN:
+      if (!need_atom()) return fail(LCP_EINVAL, "atom index out of range");
+      src = u.ncn[index].data(); n = (int64_t)u.ncn[index].size(); break;
+    case LCP_F_GRIDN_ATOM:
+      for (int a = 0; a < u.natom; ++a) tmp.push_back((int32_t)(u.sphere_off[a + 1] - u.sphere_off[a]));
+      src = tmp.data(); n = u.natom; break;
+    case LCP_F_GRIDLIST:
+    case LCP_F_CELLLIST:
+      if (!need_atom()) return fail(LCP_EINVAL, "atom index out of range");
+      src = (field == LCP_F_GRIDLIST ? u.glist.data() : u.clist.data()) + u.sphere_off[index];
+      n = u.sphere_off[index + 1] - u.sphere_off[index]; break;
+    case LCP_F_PAIR_ATOM:
+    case LCP_F_PAIR_NATN:
+      for (int p = 0; p < u.nloop; ++p) tmp.push_back((field == LCP_F_PAIR_ATOM ? u.pair_atom[p] : u.pair_jatom[p]) + 1);
+      src = tmp.data(); n = u.nloop; break;
+    case LCP_F_PAIR_NCN: src = u.pair_cell.data(); n = u.nloop; break;
+    case LCP_F_NUMOLG:
+      for (int p = 0; p < u.nloop; ++p) tmp.push_back((int32_t)u.numolg[p]);
+      src = tmp.data(); n = u.nloop; break;
+    case LCP_F_GLIST1:
+    case LCP_F_GLIST2: {
+      if (!need_pair()) return fail(LCP_EINVAL, "pair index out of range");
+      std::vector<int32_t> g1, g2;
+      lcp::pair_overlap(u, (int32_t)index, g1, g2);
+      tmp = field == LCP_F_GLIST1 ? g1 : g2;
+      src = tmp.data(); n = (int64_t)tmp.size(); break;
+    }
+    case LCP_F_ATV_IJK: src = u.atv_ijk.data(); n = (int64_t)u.atv_ijk.size(); break;
+    default: return fail(LCP_EINVAL, "unknown field");
+  }
+  if (count != n) return fail(LCP_EINVAL, "count does not match the field length " + std::to_string(n));
+  if (n) std::memcpy(dst, src, n * sizeof(int32_t));
+  return LCP_OK;
+}
+
+lcp_status lcp_ucell_get_atv(const lcp_ucell* ucell, double* dst) {
+  if (!ucell || !dst) return fail(LCP_EINVAL, "NULL argument");
+  std::memcpy(dst, ucell->u.atv.data(), ucell->u.atv.size() * sizeof(double));
+  return LCP_OK;
+}
+
+lcp_status lcp_calc_ngrid(double ecut, const double* L, int32_t* ngrid_out) {
+  if (!L || !ngrid_out) return fail(LCP_EINVAL, "NULL argument");
+  if (ecut < 0.0) return fail(LCP_EINVAL, "please check Ecut.");
+  // src/utils/Calc_Ngrid.jl:1-76
+  auto cross_norm = [&](int a, int b) {
+    double x = L[a * 3 + 1] * L[b * 3 + 2] - L[a * 3 + 2] * L[b * 3 + 1];
+    double y = L[a * 3 + 2] * L[b * 3 + 0] - L[a * 3 + 0] * L[b * 3 + 2];
+    double z = L[a * 3 + 0] * L[b * 3 + 1] - L[a * 3 + 1] * L[b * 3 + 0];
+    return std::sqrt(x * x + y * y + z * z);
+  };
+  double det = L[0] * (L[4] * L[8] - L[5] * L[7]) - L[1] * (L[3] * L[8] - L[5] * L[6]) + L[2] * (L[3] * L[7] - L[4] * L[6]);
+  double temp = std::fabs(det) / 3.14159265358979323846 * std::sqrt(ecut);
+  double ns[3] = {temp / cross_norm(1, 2), temp / cross_norm(2, 0), temp / cross_norm(0, 1)};
+  for (int d = 0; d < 3; ++d) {
+    double lgn = std::log(ns[d]);
+    double best = 1e10;
+    int bp = 0, bq = 0, br = 0, bs = 0;
+    const double l2 = std::log(2.0), l3 = std::log(3.0), l5 = std::log(5.0), l7 = std::log(7.0);
+    for (int p = 0; p <= (int)std::ceil(lgn / l2); ++p)
+      for (int q = 0; q <= (int)std::ceil((lgn - p * l2) / l3); ++q)
+        for (int r = 0; r <= (int)std::ceil((lgn - p * l2 - q * l3) / l5); ++r)
+          for (int s = 0; s <= (int)std::ceil((lgn - p * l2 - q * l3 - r * l5) / l7); ++s) {
+            double lg = p * l2 + q * l3 + r * l5 + s * l7;
+            if (std::fabs(lg - lgn) < best) {
+              best = std::fabs(lg - lgn);
+              bp = p; bq = q; br = r; bs = s;
+            }
+          }
+    int k = 1;
+    for (int i = 0; i < bp; ++i) k *= 2;
+    for (int i = 0; i < bq; ++i) k *= 3;
+    for (int i = 0; i < br; ++i) k *= 5;
+    for (int i = 0; i < bs; ++i) k *= 7;
+    ngrid_out[d] = k;
+  }
+  return LCP_OK;
+}
+
+// ---------------------------------------------------------------- context
+
+lcp_status lcp_ctx_create(int32_t device, lcp_ctx** out) {
+  if (!out) return fail(LCP_EINVAL, "NULL argument");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(LCP_EDEVICE, "no CUDA device available");
+  if (device < 0 || device >= n) return fail(LCP_EINVAL, "device index out of range");
+  API_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  std::unique_ptr<lcp_ctx> c(new lcp_ctx());
+  c->device = device;
+  API_CUDA(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking), "cudaStreamCreate");
+  c->stream = c->own;
+  *out = c.release();
+  return LCP_OK;
+}
+
+void lcp_ctx_destroy(lcp_ctx* ctx) { delete ctx; }
+
+lcp_status lcp_ctx_set_stream(lcp_ctx* ctx, void* stream) {
+  if (!ctx) return fail(LCP_EINVAL, "context is NULL");
+  ctx->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->own;
+  return LCP_OK;
+}
+
+lcp_status lcp_ctx_set_precision(lcp_ctx* ctx, int32_t precision) {
+  if (!ctx) return fail(LCP_EINVAL, "context is NULL");
+  if (precision < LCP_PREC_FP64 || precision > LCP_PREC_BF16X3) return fail(LCP_EINVAL, "unknown precision");
+  ctx->precision = precision;
+  return LCP_OK;
+}
+
+lcp_status lcp_ctx_synchronize(lcp_ctx* ctx) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return LCP_OK;
+}
+
+int64_t lcp_ctx_launch_count(const lcp_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+// ---------------------------------------------------------------- orbitals
+
+lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t nspecies, const lcp_pao* paos,
+                                 int32_t with_grad, lcp_orbs** out) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!ucell || !paos || !out || nspecies <= 0) return fail(LCP_EINVAL, "NULL argument");
+  *out = nullptr;
+  const lcp::UCell& u = ucell->u;
+  // species tables
+  std::vector<DevSpecies> sp(nspecies);
+  std::vector<double> radial;
+  for (int k = 0; k < nspecies; ++k) {
+    const lcp_pao& p = paos[k];
+    if (p.max_l < 0 || p.max_l > 3) return fail(LCP_ENOTSUP, "not support PAO l > 3");
+    if (p.num_mesh < 8 || !p.rv || !p.rwf) return fail(LCP_EINVAL, "PAO mesh must have >= 8 points");
+    for (int i = 1; i < p.num_mesh; ++i)
+      if (!(p.rv[i] > p.rv[i - 1])) return fail(LCP_EINVAL, "Spe_PAO_RV must be strictly increasing");
+    DevSpecies d{};
+    d.max_l = p.max_l;
+    d.nmesh = p.num_mesh;
+    d.nrad = 0;
+    d.no = 0;
+    for (int l = 0; l <= p.max_l; ++l) {
+      if (p.num_basis[l] < 0) return fail(LCP_EINVAL, "negative Num_Basis");
+      d.nb[l] = p.num_basis[l];
+      d.nrad += p.num_basis[l];
+      d.no += p.num_basis[l] * (2 * l + 1);
+    }
+    if (d.no > 64) return fail(LCP_ENOTSUP, "more than 64 orbitals per atom");
+    d.rv_off = (int64_t)radial.size();
+    radial.insert(radial.end(), p.rv, p.rv + p.num_mesh);
+    d.rwf_off = (int64_t)radial.size();
+    radial.insert(radial.end(), p.rwf, p.rwf + (size_t)d.nrad * p.num_mesh);
+    sp[k] = d;
+  }
+  std::vector<int32_t> spe0(u.natom);
+  for (int a = 0; a < u.natom; ++a) {
+    int k = u.atom2spe[a] - 1;
+    if (k < 0 || k >= nspecies) return fail(LCP_EINVAL, "atom2spe out of range");
+    if (sp[k].no != u.numorbs[a])
+      return fail(LCP_EINVAL, "Total_NumOrbs of atom " + std::to_string(a + 1) + " does not match its species basis");
+    spe0[a] = k;
+  }
+  std::unique_ptr<lcp_orbs> o(new lcp_orbs());
+  o->ucell = ucell;
+  o->device = ctx->device;
+  o->grad = with_grad != 0;
+  o->max_no = u.max_numorbs();
+  if (o->max_no > 32) return fail(LCP_ENOTSUP, "pair contractions support up to 32 orbitals per atom");
+  std::vector<int64_t> phi_off(u.natom + 1, 0);
+  for (int a = 0; a < u.natom; ++a)
+    phi_off[a + 1] = phi_off[a] + (u.sphere_off[a + 1] - u.sphere_off[a]) * (int64_t)u.numorbs[a];
+  o->table_elems = phi_off[u.natom];
+  cudaStream_t st = ctx->stream;
+  API_CUDA(upload(o->atv, u.atv, st), "upload");
+  API_CUDA(upload(o->gxyz, u.gxyz, st), "upload");
+  API_CUDA(upload(o->spe, spe0, st), "upload");
+  API_CUDA(upload(o->sph_off, u.sphere_off, st), "upload");
+  API_CUDA(upload(o->glist, u.glist, st), "upload");
+  API_CUDA(upload(o->clist, u.clist, st), "upload");
+  API_CUDA(upload(o->phi_off, phi_off, st), "upload");
+  API_CUDA(upload(o->numorbs, u.numorbs, st), "upload");
+  API_CUDA(upload(o->species, sp, st), "upload");
+  API_CUDA(upload(o->radial, radial, st), "upload");
+  DevGeom& g = o->geom;
+  g.natom = u.natom;
+  for (int d = 0; d < 3; ++d) {
+    g.ngrid[d] = u.ngrid[d];
+    g.origin[d] = u.origin[d];
+    for (int c = 0; c < 3; ++c) g.glat[d * 3 + c] = u.glat[d][c];
+  }
+  g.gridvol = u.gridvol;
+  g.atv = o->atv.as<double>();
+  g.gxyz = o->gxyz.as<double>();
+  g.spe = o->spe.as<int32_t>();
+  g.sph_off = o->sph_off.as<int64_t>();
+  g.glist = o->glist.as<int32_t>();
+  g.clist = o->clist.as<int32_t>();
+  g.phi_off = o->phi_off.as<int64_t>();
+  g.numorbs = o->numorbs.as<int32_t>();
+
+  // folded pair lists and 512-entry work items
+  const int64_t nu = (int64_t)u.uniq_pair.size();
+  std::vector<int32_t> pa(nu), pj(nu), pself(nu);
+  std::vector<int64_t> bp(nu), bq(nu);
+  std::vector<int64_t> ip, is;
+  std::vector<int32_t> ic;
+  const int64_t chunk = 512;
+  for (int64_t q = 0; q < nu; ++q) {
+    int p = u.uniq_pair[q];
+    pa[q] = u.pair_atom[p];
+    pj[q] = u.pair_jatom[p];
+    bp[q] = u.block_off[p];
+    bq[q] = u.block_off[u.partner[p]];
+    pself[q] = u.partner[p] == p;
+    if (u.numorbs[pa[q]] == 0 || u.numorbs[pj[q]] == 0) continue;
+    for (int64_t s0 = u.uniq_off[q]; s0 < u.uniq_off[q + 1]; s0 += chunk) {
+      ip.push_back(q);
+      is.push_back(s0);
+      ic.push_back((int32_t)std::min<int64_t>(chunk, u.uniq_off[q + 1] - s0));
+    }
+  }
+  API_CUDA(upload(o->p_atom, pa, st), "upload");
+  API_CUDA(upload(o->p_jatom, pj, st), "upload");
+  API_CUDA(upload(o->p_boffp, bp, st), "upload");
+  API_CUDA(upload(o->p_boffq, bq, st), "upload");
+  API_CUDA(upload(o->p_self, pself, st), "upload");
+  API_CUDA(upload(o->p_lensoff, u.uniq_off, st), "upload");
+  API_CUDA(upload(o->p_g1, u.uniq_g1, st), "upload");
+  API_CUDA(upload(o->p_g2, u.uniq_g2, st), "upload");
+  API_CUDA(upload(o->it_pair, ip, st), "upload");
+  API_CUDA(upload(o->it_start, is, st), "upload");
+  API_CUDA(upload(o->it_count, ic, st), "upload");
+  DevPairs& pr = o->pairs;
+  pr.nu = nu;
+  pr.atom = o->p_atom.as<int32_t>();
+  pr.jatom = o->p_jatom.as<int32_t>();
+  pr.boff_p = o->p_boffp.as<int64_t>();
+  pr.boff_q = o->p_boffq.as<int64_t>();
+  pr.self = o->p_self.as<int32_t>();
+  pr.lens_off = o->p_lensoff.as<int64_t>();
+  pr.g1 = o->p_g1.as<int32_t>();
+  pr.g2 = o->p_g2.as<int32_t>();
+  pr.nitems = (int64_t)ip.size();
+  pr.item_pair = o->it_pair.as<int64_t>();
+  pr.item_start = o->it_start.as<int64_t>();
+  pr.item_count = o->it_count.as<int32_t>();
+
+  // tabulation
+  API_CUDA(o->phi.ensure(o->table_elems * sizeof(double)), "phi alloc");
+  if (o->grad)
+    for (int k = 0; k < 3; ++k) API_CUDA(o->dphi[k].ensure(o->table_elems * sizeof(double)), "dphi alloc");
+  std::vector<int32_t> batom;
+  std::vector<int64_t> bstart;
+  for (int a = 0; a < u.natom; ++a)
+    for (int64_t k = u.sphere_off[a]; k < u.sphere_off[a + 1]; k += 64) {
+      batom.push_back(a);
+      bstart.push_back(k);
+    }
+  DBuf d_batom, d_bstart;
+  API_CUDA(upload(d_batom, batom, st), "upload");
+  API_CUDA(upload(d_bstart, bstart, st), "upload");
+  API_CUDA(lcp::launch_tabulate(g, o->species.as<DevSpecies>(), o->radial.as<double>(), (int64_t)batom.size(),
+                                d_batom.as<int32_t>(), d_bstart.as<int64_t>(), o->phi.as<double>(),
+                                o->grad ? o->dphi[0].as<double>() : nullptr, o->grad ? o->dphi[1].as<double>() : nullptr,
+                                o->grad ? o->dphi[2].as<double>() : nullptr, st),
+           "tabulate kernel");
+  ctx->launches++;
+  API_CUDA(cudaStreamSynchronize(st), "tabulate");
+  *out = o.release();
+  return LCP_OK;
+}
+
+void lcp_orbs_destroy(lcp_orbs* orbs) {
+  if (!orbs) return;
+  cudaSetDevice(orbs->device);
+  delete orbs;
+}
+
+lcp_status lcp_orbs_download(lcp_ctx* ctx, const lcp_orbs* orbs, int32_t component, int32_t atom, double* dst,
+                             int64_t count) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!orbs || !dst) return fail(LCP_EINVAL, "NULL argument");
+  const lcp::UCell& u = orbs->ucell->u;
+  if (atom < 0 || atom >= u.natom) return fail(LCP_EINVAL, "atom index out of range");
+  if (component < 0 || component > 3) return fail(LCP_EINVAL, "component must be 0..3");
+  if (component > 0 && !orbs->grad) return fail(LCP_ESTATE, "gradient tables were not requested");
+  int64_t n = (u.sphere_off[atom + 1] - u.sphere_off[atom]) * (int64_t)u.numorbs[atom];
+  if (count != n) return fail(LCP_EINVAL, "count must be GridN*NumOrbs = " + std::to_string(n));
+  int64_t off = 0;
+  for (int a = 0; a < atom; ++a) off += (u.sphere_off[a + 1] - u.sphere_off[a]) * (int64_t)u.numorbs[a];
+  const DBuf& b = component == 0 ? orbs->phi : orbs->dphi[component - 1];
+  API_CUDA(cudaMemcpyAsync(dst, b.as<double>() + off, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "download");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "download");
+  return LCP_OK;
+}
+
+// ---------------------------------------------------------------- density / H (host buffers)
+
+lcp_status lcp_set_density_grid(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs, int32_t spinpol,
+                                const double* const* dm, double* const* density_grid) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if ((s = check_pair(ucell, orbs))) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol.");
+  if (!dm || !density_grid) return fail(LCP_EINVAL, "NULL argument");
+  const int ns = channels(spinpol);
+  const lcp::UCell& u = ucell->u;
+  const int64_t nn = u.nn(), hs = u.total_hsize;
+  const double* ddm[4];
+  double* drho[4];
+  for (int c = 0; c < ns; ++c) {
+    if (!dm[c] || !density_grid[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(hs * sizeof(double)), "alloc");
+    API_CUDA(ctx->w_out[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, dm[c], hs * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    ddm[c] = ctx->w_in[c].as<double>();
+    drho[c] = ctx->w_out[c].as<double>();
+  }
+  if ((s = density_device(ctx, orbs, ns, ddm, drho, nn))) return s;
+  for (int c = 0; c < ns; ++c)
+    API_CUDA(cudaMemcpyAsync(density_grid[c], drho[c], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "density");
+  return LCP_OK;
+}
+
+lcp_status lcp_calc_matrix_elements(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs, int32_t spinpol,
+                                    const double* const* vpot, double* const* hks) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if ((s = check_pair(ucell, orbs))) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol.");
+  if (!vpot || !hks) return fail(LCP_EINVAL, "NULL argument");
+  const int nc = channels(spinpol);
+  const lcp::UCell& u = ucell->u;
+  const int64_t nn = u.nn(), hs = u.total_hsize;
+  const double* dv[4];
+  double* dh[4];
+  for (int c = 0; c < nc; ++c) {
+    if (!vpot[c] || !hks[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(ctx->w_out[c].ensure(hs * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, vpot[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    dv[c] = ctx->w_in[c].as<double>();
+    dh[c] = ctx->w_out[c].as<double>();
+  }
+  if ((s = hamiltonian_device(ctx, orbs, nc, dv, dh, hs))) return s;
+  for (int c = 0; c < nc; ++c)
+    API_CUDA(cudaMemcpyAsync(hks[c], dh[c], hs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "hamiltonian");
+  return LCP_OK;
+}
+
+// ---------------------------------------------------------------- Poisson / xc / energies (host buffers)
+
+static lcp_status check_grid(const int32_t* ng) {
+  if (!ng) return fail(LCP_EINVAL, "NULL Ngrid");
+  for (int d = 0; d < 3; ++d)
+    if (ng[d] <= 0) return fail(LCP_EINVAL, "Ngrid entries must be positive");
+  return LCP_OK;
+}
+
+static lcp_status poisson_host(lcp_ctx* ctx, const int32_t* ng, const double* recvecs, double* dvhart) {
+  const int64_t nn = (int64_t)ng[0] * ng[1] * ng[2];
+  const int64_t nspec = (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1);
+  FftPlans* pl = nullptr;
+  lcp_status s = get_plans(ctx, ng, &pl);
+  if (s) return s;
+  API_CUDA(ctx->w_spec.ensure(nspec * 2 * sizeof(double)), "alloc");
+  API_CUDA(ctx->w_a.ensure(nn * sizeof(double)), "alloc");
+  if ((s = poisson_device(ctx, pl, ng, recvecs, ctx->w_real.as<double>(), ctx->w_spec.p, ctx->w_a.as<double>())))
+    return s;
+  API_CUDA(cudaMemcpyAsync(dvhart, ctx->w_a.p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "poisson");
+  return LCP_OK;
+}
+
+lcp_status lcp_solve_poisson_xyz(lcp_ctx* ctx, const int32_t* ngrid, const double* recvecs, const double* density_xyz,
+                                 double* dvhart_grid) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if ((s = check_grid(ngrid))) return s;
+  if (!recvecs || !density_xyz || !dvhart_grid) return fail(LCP_EINVAL, "NULL argument");
+  const int64_t nn = (int64_t)ngrid[0] * ngrid[1] * ngrid[2];
+  API_CUDA(ctx->w_real.ensure(nn * sizeof(double)), "alloc");
+  API_CUDA(cudaMemcpyAsync(ctx->w_real.p, density_xyz, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  return poisson_host(ctx, ngrid, recvecs, dvhart_grid);
+}
+
+lcp_status lcp_solve_poisson(lcp_ctx* ctx, const int32_t* ngrid, const double* recvecs, int32_t spinpol,
+                             const double* const* density_grid, const double* adensity_grid, double* dvhart_grid) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if ((s = check_grid(ngrid))) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol.");
+  if (!recvecs || !density_grid || !density_grid[0] || !dvhart_grid) return fail(LCP_EINVAL, "NULL argument");
+  if (spinpol != LCP_SPIN_OFF && !density_grid[1]) return fail(LCP_EINVAL, "NULL spin channel");
+  const int64_t nn = (int64_t)ngrid[0] * ngrid[1] * ngrid[2];
+  const int nr = spinpol == LCP_SPIN_OFF ? 1 : 2;
+  for (int c = 0; c < nr; ++c) {
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, density_grid[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+  }
+  const double* ad = nullptr;
+  if (adensity_grid) {
+    API_CUDA(ctx->w_b.ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_b.p, adensity_grid, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    ad = ctx->w_b.as<double>();
+  }
+  API_CUDA(ctx->w_real.ensure(nn * sizeof(double)), "alloc");
+  API_CUDA(lcp::launch_poisson_prep(spinpol, nn, ctx->w_in[0].as<double>(), nr > 1 ? ctx->w_in[1].as<double>() : nullptr,
+                                    ad, ctx->w_real.as<double>(), ctx->stream),
+           "poisson_prep");
+  ctx->launches++;
+  return poisson_host(ctx, ngrid, recvecs, dvhart_grid);
+}
+
+lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn, const double* pcc,
+                           const double* const* density_grid, double* const* vxc_grid) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA) return fail(LCP_EINVAL, "please check xc_type name");
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol name");
+  if ((xc == LCP_XC_LDA) != (spinpol == LCP_SPIN_OFF)) return fail(LCP_EINVAL, "please check xc_type and SpinPol");
+  if (nn <= 0 || !density_grid || !vxc_grid) return fail(LCP_EINVAL, "NULL argument");
+  const int nr = channels(spinpol);
+  const double* dr[4];
+  double* dv[4];
+  for (int c = 0; c < nr; ++c) {
+    if (!density_grid[c] || !vxc_grid[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(ctx->w_out[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, density_grid[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+    dr[c] = ctx->w_in[c].as<double>();
+    dv[c] = ctx->w_out[c].as<double>();
+  }
+  const double* dp = nullptr;
+  if (pcc) {
+    API_CUDA(ctx->w_b.ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_b.p, pcc, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    dp = ctx->w_b.as<double>();
+  }
+  API_CUDA(lcp::launch_xc_vpot(xc, spinpol, nn, dp, dr, nullptr, nullptr, dv, nullptr, ctx->stream), "xc");
+  ctx->launches++;
+  for (int c = 0; c < nr; ++c)
+    API_CUDA(cudaMemcpyAsync(vxc_grid[c], dv[c], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "xc");
+  return LCP_OK;
+}
+
+lcp_status lcp_set_vpot_grid(lcp_ctx* ctx, int32_t spinpol, int64_t nn, const double* dvhart, const double* const* vxc,
+                             const double* vna, double* const* vpot) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol");
+  if (nn <= 0 || !dvhart || !vxc || !vpot) return fail(LCP_EINVAL, "NULL argument");
+  const int nv = channels(spinpol);
+  const double* dx[4];
+  double* dp[4];
+  API_CUDA(ctx->w_a.ensure(nn * sizeof(double)), "alloc");
+  API_CUDA(cudaMemcpyAsync(ctx->w_a.p, dvhart, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  for (int c = 0; c < nv; ++c) {
+    if (!vxc[c] || !vpot[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(ctx->w_out[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, vxc[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    dx[c] = ctx->w_in[c].as<double>();
+    dp[c] = ctx->w_out[c].as<double>();
+  }
+  const double* dn = nullptr;
+  if (vna) {
+    API_CUDA(ctx->w_b.ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_b.p, vna, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    dn = ctx->w_b.as<double>();
+  }
+  API_CUDA(lcp::launch_vpot(spinpol, nn, ctx->w_a.as<double>(), dx, dn, dp, ctx->stream), "vpot");
+  ctx->launches++;
+  for (int c = 0; c < nv; ++c)
+    API_CUDA(cudaMemcpyAsync(vpot[c], dp[c], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "vpot");
+  return LCP_OK;
+}
+
+static lcp_status energy_host(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn, const double* aden,
+                              const double* pcc, const double* const* density, const double* dvhart, double out[3]) {
+  const int nr = spinpol == LCP_SPIN_OFF ? 1 : 2;
+  const double* dr[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int c = 0; c < nr; ++c) {
+    if (!density[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, density[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    dr[c] = ctx->w_in[c].as<double>();
+  }
+  const double* d_ad = nullptr;
+  const double* d_pc = nullptr;
+  const double* d_vh = nullptr;
+  if (aden) {
+    API_CUDA(ctx->w_aux[0].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_aux[0].p, aden, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    d_ad = ctx->w_aux[0].as<double>();
+  }
+  if (pcc) {
+    API_CUDA(ctx->w_aux[1].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_aux[1].p, pcc, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    d_pc = ctx->w_aux[1].as<double>();
+  }
+  if (dvhart) {
+    API_CUDA(ctx->w_aux[2].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_aux[2].p, dvhart, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    d_vh = ctx->w_aux[2].as<double>();
+  }
+  API_CUDA(ctx->w_part.ensure((size_t)lcp::kReduceBlocks * 3 * sizeof(double)), "alloc");
+  API_CUDA(ctx->w_scal.ensure(8 * sizeof(double)), "alloc");
+  API_CUDA(lcp::launch_energy_sums(xc, spinpol, nn, d_ad, d_pc, dr, d_vh, ctx->w_part.as<double>(),
+                                   ctx->w_scal.as<double>(), ctx->stream),
+           "energy");
+  ctx->launches += 2;
+  API_CUDA(cudaMemcpyAsync(out, ctx->w_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "energy");
+  return LCP_OK;
+}
+
+lcp_status lcp_calc_eh1(lcp_ctx* ctx, int32_t spinpol, int64_t nn, double gridvol, const double* adensity,
+                        const double* const* density, const double* dvhart, double* eh1) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol");
+  if (nn <= 0 || !density || !dvhart || !eh1) return fail(LCP_EINVAL, "NULL argument");
+  double out[3];
+  if ((s = energy_host(ctx, spinpol == LCP_SPIN_OFF ? LCP_XC_LDA : LCP_XC_LSDA, spinpol, nn, adensity, nullptr, density,
+                       dvhart, out)))
+    return s;
+  *eh1 = out[0] * gridvol * 0.5;
+  return LCP_OK;
+}
+
+lcp_status lcp_calc_exc1(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn, double gridvol, const double* adensity,
+                         const double* pcc, const double* const* density, double* exc) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA) return fail(LCP_EINVAL, "please check xc_type");
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol");
+  if (nn <= 0 || !density || !exc) return fail(LCP_EINVAL, "NULL argument");
+  double out[3];
+  if ((s = energy_host(ctx, xc, spinpol, nn, adensity, pcc, density, nullptr, out))) return s;
+  exc[0] = out[1] * gridvol;
+  exc[1] = out[2] * gridvol;
+  return LCP_OK;
+}
+
+// ---------------------------------------------------------------- device-resident job
+
+lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs, int32_t spinpol, int32_t xc,
+                          const double* adensity, const double* pcc, const double* vna, lcp_job** out) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if ((s = check_pair(ucell, orbs))) return s;
+  if (!out) return fail(LCP_EINVAL, "NULL argument");
+  *out = nullptr;
+  if (spinpol != LCP_SPIN_OFF && spinpol != LCP_SPIN_ON)
+    return fail(LCP_ENOTSUP, "the device-resident step supports SpinPol off/on");
+  if ((xc == LCP_XC_LDA) != (spinpol == LCP_SPIN_OFF)) return fail(LCP_EINVAL, "please check xc_type and SpinPol");
+  const lcp::UCell& u = ucell->u;
+  std::unique_ptr<lcp_job> j(new lcp_job());
+  j->ucell = ucell;
+  j->orbs = orbs;
+  j->spinpol = spinpol;
+  j->xc = xc;
+  j->nspin = channels(spinpol);
+  j->nn = u.nn();
+  j->hsize = u.total_hsize;
+  // Recvecs = 2*pi*inv(Latvecs') (src/Mixing/DFT_Mixing.jl:91): rows b_i with a_i.b_j = 2*pi*delta_ij
+  {
+    const double(&L)[3][3] = u.lat;
+    double det = L[0][0] * (L[1][1] * L[2][2] - L[1][2] * L[2][1]) - L[0][1] * (L[1][0] * L[2][2] - L[1][2] * L[2][0]) +
+                 L[0][2] * (L[1][0] * L[2][1] - L[1][1] * L[2][0]);
+    double c = 2 * 3.14159265358979323846 / det;
+    for (int i = 0; i < 3; ++i) {
+      int a = (i + 1) % 3, b = (i + 2) % 3;
+      j->recvecs[i * 3 + 0] = c * (L[a][1] * L[b][2] - L[a][2] * L[b][1]);
+      j->recvecs[i * 3 + 1] = c * (L[a][2] * L[b][0] - L[a][0] * L[b][2]);
+      j->recvecs[i * 3 + 2] = c * (L[a][0] * L[b][1] - L[a][1] * L[b][0]);
+    }
+  }
+  const int64_t nn = j->nn, hs = j->hsize;
+  const int64_t nspec = (int64_t)u.ngrid[0] * u.ngrid[1] * (u.ngrid[2] / 2 + 1);
+  for (int c = 0; c < j->nspin; ++c) {
+    API_CUDA(j->dm[c].ensure(hs * sizeof(double)), "alloc");
+    API_CUDA(j->hks[c].ensure(hs * sizeof(double)), "alloc");
+    API_CUDA(j->rho[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(j->vpot[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemsetAsync(j->dm[c].p, 0, hs * sizeof(double), ctx->stream), "memset");
+  }
+  API_CUDA(j->dvh.ensure(nn * sizeof(double)), "alloc");
+  API_CUDA(j->real.ensure(nn * sizeof(double)), "alloc");
+  API_CUDA(j->spec.ensure(nspec * 2 * sizeof(double)), "alloc");
+  API_CUDA(j->part.ensure((size_t)lcp::kReduceBlocks * 3 * sizeof(double)), "alloc");
+  API_CUDA(j->scal.ensure(16 * sizeof(double)), "alloc");
+  auto put = [&](DBuf& b, const double* src, bool& flag) -> cudaError_t {
+    flag = src != nullptr;
+    if (!src) return cudaSuccess;
+    cudaError_t e = b.ensure(nn * sizeof(double));
+    if (e) return e;
+    return cudaMemcpyAsync(b.p, src, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  };
+  API_CUDA(put(j->aden, adensity, j->has_aden), "H2D");
+  API_CUDA(put(j->pcc, pcc, j->has_pcc), "H2D");
+  API_CUDA(put(j->vna, vna, j->has_vna), "H2D");
+  if ((s = get_plans(ctx, u.ngrid, &j->plans))) return s;
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "job create");
+  *out = j.release();
+  return LCP_OK;
+}
+
+void lcp_job_destroy(lcp_job* job) { delete job; }
+
+lcp_status lcp_job_set_dm(lcp_ctx* ctx, lcp_job* job, const double* const* dm) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job || !dm) return fail(LCP_EINVAL, "NULL argument");
+  for (int c = 0; c < job->nspin; ++c) {
+    if (!dm[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(cudaMemcpyAsync(job->dm[c].p, dm[c], job->hsize * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+  }
+  return LCP_OK;
+}
+
+__global__ void job_finish_kernel(const double* sc, double gridvol, int spinpol, double* out) {
+  // sc: [0..2] = (sum dRho*dVH, xc sum up, xc sum down), [3] = sum <D,H>
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double eh1 = sc[0] * gridvol * 0.5;
+    const double x1 = sc[1] * gridvol;
+    const double x2 = spinpol == LCP_SPIN_OFF ? x1 : sc[2] * gridvol;
+    const double fs = spinpol == LCP_SPIN_OFF ? 2.0 : 1.0;
+    out[0] = eh1;
+    out[1] = x1;
+    out[2] = x2;
+    out[3] = sc[3];
+    out[4] = fs * sc[3] + eh1 + x1 + x2;
+  }
+}
+
+static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job) return fail(LCP_EINVAL, "NULL job");
+  auto mark = [&](int k) {
+    if (ev) cudaEventRecord(ev[k], ctx->stream);
+  };
+  const lcp::UCell& u = job->ucell->u;
+  const int ns = job->nspin;
+  cudaStream_t st = ctx->stream;
+  const double* dm[4];
+  double* rho[4];
+  const double* crho[4];
+  double* vp[4];
+  const double* cvp[4];
+  double* hk[4];
+  const double* chk[4];
+  for (int c = 0; c < ns; ++c) {
+    dm[c] = job->dm[c].as<double>();
+    rho[c] = job->rho[c].as<double>();
+    crho[c] = rho[c];
+    vp[c] = job->vpot[c].as<double>();
+    cvp[c] = vp[c];
+    hk[c] = job->hks[c].as<double>();
+    chk[c] = hk[c];
+  }
+  const double* ad = job->has_aden ? job->aden.as<double>() : nullptr;
+  const double* pc = job->has_pcc ? job->pcc.as<double>() : nullptr;
+  const double* na = job->has_vna ? job->vna.as<double>() : nullptr;
+  // 1. density
+  mark(0);
+  if ((s = density_device(ctx, job->orbs, ns, dm, rho, job->nn))) return s;
+  mark(1);
+  // 2. Poisson
+  API_CUDA(lcp::launch_poisson_prep(job->spinpol, job->nn, rho[0], ns > 1 ? rho[1] : nullptr, ad,
+                                    job->real.as<double>(), st),
+           "poisson_prep");
+  ctx->launches++;
+  if ((s = poisson_device(ctx, job->plans, u.ngrid, job->recvecs, job->real.as<double>(), job->spec.p,
+                          job->dvh.as<double>())))
+    return s;
+  mark(2);
+  // 3. xc + potential
+  API_CUDA(lcp::launch_xc_vpot(job->xc, job->spinpol, job->nn, pc, crho, job->dvh.as<double>(), na, nullptr, vp, st),
+           "xc_vpot");
+  ctx->launches++;
+  mark(3);
+  // 4. FP64 energy terms
+  API_CUDA(lcp::launch_energy_sums(job->xc, job->spinpol, job->nn, ad, pc, crho, job->dvh.as<double>(),
+                                   job->part.as<double>(), job->scal.as<double>(), st),
+           "energy");
+  ctx->launches += 2;
+  mark(4);
+  // 5. grid matrix elements
+  if ((s = hamiltonian_device(ctx, job->orbs, ns, cvp, hk, job->hsize))) return s;
+  mark(5);
+  // 6. sum_s <D_s, H_s> and the job energy
+  API_CUDA(lcp::launch_dot_sum(ns, job->hsize, dm, chk, job->part.as<double>(), job->scal.as<double>() + 3, st), "dot");
+  ctx->launches += 2;
+  job_finish_kernel<<<1, 32, 0, st>>>(job->scal.as<double>(), u.gridvol, job->spinpol, job->scal.as<double>() + 8);
+  API_CUDA(cudaGetLastError(), "finish");
+  ctx->launches++;
+  mark(6);
+  return LCP_OK;
+}
+
+lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job) { return job_step_impl(ctx, job, nullptr); }
+
+lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms) {
+  if (!stage_ms) return fail(LCP_EINVAL, "NULL argument");
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  cudaEvent_t ev[7];
+  for (int k = 0; k < 7; ++k) API_CUDA(cudaEventCreate(&ev[k]), "cudaEventCreate");
+  s = job_step_impl(ctx, job, ev);
+  if (s == LCP_OK) {
+    cudaError_t e = cudaEventSynchronize(ev[6]);
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+      float ms = 0.f;
+      e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      stage_ms[k] = ms;
+    }
+    if (e != cudaSuccess) s = cuda_fail(e, "stage timing");
+  }
+  for (int k = 0; k < 7; ++k) cudaEventDestroy(ev[k]);
+  return s;
+}
+
+lcp_status lcp_job_energies(lcp_ctx* ctx, lcp_job* job, double* out5) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job || !out5) return fail(LCP_EINVAL, "NULL argument");
+  API_CUDA(cudaMemcpyAsync(out5, job->scal.as<double>() + 8, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "energies");
+  return LCP_OK;
+}
+
+static lcp_status job_get(lcp_ctx* ctx, lcp_job* job, DBuf* src, int64_t n, double* const* dst) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job || !dst) return fail(LCP_EINVAL, "NULL argument");
+  for (int c = 0; c < job->nspin; ++c) {
+    if (!dst[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(cudaMemcpyAsync(dst[c], src[c].p, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  }
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "job get");
+  return LCP_OK;
+}
+
+lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!tflops) return fail(LCP_EINVAL, "NULL argument");
+  int sms = 0;
+  API_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "attr");
+  DBuf out;
+  API_CUDA(out.ensure(64), "alloc");
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  cudaEvent_t a, b;
+  API_CUDA(cudaEventCreate(&a), "event");
+  API_CUDA(cudaEventCreate(&b), "event");
+  API_CUDA(lcp::launch_fp64_probe(out.as<double>(), blocks, threads, 64, ctx->stream), "probe");
+  cudaEventRecord(a, ctx->stream);
+  API_CUDA(lcp::launch_fp64_probe(out.as<double>(), blocks, threads, iters, ctx->stream), "probe");
+  cudaEventRecord(b, ctx->stream);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->launches += 2;
+  *tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (ms * 1e-3) / 1e12;
+  return LCP_OK;
+}
+
+lcp_status lcp_job_get_density(lcp_ctx* ctx, lcp_job* job, double* const* d) { return job_get(ctx, job, job ? job->rho : nullptr, job ? job->nn : 0, d); }
+lcp_status lcp_job_get_hks(lcp_ctx* ctx, lcp_job* job, double* const* h) { return job_get(ctx, job, job ? job->hks : nullptr, job ? job->hsize : 0, h); }
+lcp_status lcp_job_get_vpot(lcp_ctx* ctx, lcp_job* job, double* const* v) { return job_get(ctx, job, job ? job->vpot : nullptr, job ? job->nn : 0, v); }
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+// Device-side structures and kernel launchers shared by the .cu files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <algorithm>
+
+#include "lcpgrid.h"
+
+namespace lcp {
+
+#define LCP_CUDA_TRY(expr)                                                   \
+  do {                                                                       \
+    cudaError_t _e = (expr);                                                 \
+    if (_e != cudaSuccess) return _e;                                        \
+  } while (0)
+
+constexpr int kMaxL = 3;
+
+// Radial tables of one species in device memory.
+struct DevSpecies {
+  int32_t max_l;
+  int32_t nb[4];
+  int32_t nmesh;
+  int32_t nrad;      // number of radial functions = sum_l nb[l]
+  int32_t no;        // orbitals = sum_l nb[l]*(2l+1)
+  int64_t rv_off;    // offset of RV in the packed radial array
+  int64_t rwf_off;   // offset of RWF[(l,p)][mesh] in the packed radial array
+};
+
+// Geometry the kernels read (device pointers).
+struct DevGeom {
+  int32_t natom;
+  int32_t ngrid[3];
+  double glat[9];     // row d = Latvecs[d,:]/Ngrid[d]
+  double origin[3];
+  double gridvol;
+  const double* atv;         // ncell*3
+  const double* gxyz;        // natom*3
+  const int32_t* spe;        // natom, 0-based species
+  const int64_t* sph_off;    // natom+1, offsets into glist/clist
+  const int32_t* glist;
+  const int32_t* clist;
+  const int64_t* phi_off;    // natom+1, offset of each atom's table (elements)
+  const int32_t* numorbs;    // natom
+};
+
+// Folded pair list (one of each {(i,j,R), (j,i,-R)}) with exact lens lists.
+struct DevPairs {
+  int64_t nu;
+  const int32_t* atom;       // nu, 0-based
+  const int32_t* jatom;      // nu
+  const int64_t* boff_p;     // block offset of the kept orientation
+  const int64_t* boff_q;     // block offset of the partner (== boff_p for self pairs)
+  const int32_t* self;       // nu, 1 when the pair is its own partner
+  const int64_t* lens_off;   // nu+1
+  const int32_t* g1;         // index into atom's sphere list
+  const int32_t* g2;         // index into jatom's sphere list
+  // chunked work items over the lens lists
+  int64_t nitems;
+  const int64_t* item_pair;  // folded pair of each item
+  const int64_t* item_start; // first lens entry
+  const int32_t* item_count; // number of lens entries
+};
+
+// tabulation
+cudaError_t launch_tabulate(const DevGeom& g, const DevSpecies* dspe, const double* radial,
+                            int64_t nblocks, const int32_t* block_atom, const int64_t* block_start,
+                            double* phi, double* dphi_x, double* dphi_y, double* dphi_z,
+                            cudaStream_t st);
+cudaError_t launch_convert_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+
+// exact-lens pair contractions
+cudaError_t launch_density_pairs(int prec, const DevGeom& g, const DevPairs& pr, int nspin,
+                                 const double* phi64, const float* phi32, const double* const* dm,
+                                 double* const* rho, int max_no, cudaStream_t st);
+cudaError_t launch_hamiltonian_pairs(int prec, const DevGeom& g, const DevPairs& pr, int nch,
+                                     const double* phi64, const float* phi32,
+                                     const double* const* vpot, double* const* hks, int max_no,
+                                     cudaStream_t st);
+
+// grid kernels
+cudaError_t launch_poisson_prep(int spinpol, int64_t nn, const double* rho0, const double* rho1,
+                                const double* aden, double* out, cudaStream_t st);
+cudaError_t launch_poisson_scale(const int32_t* ngrid, const double* recvecs, void* spectrum,
+                                 cudaStream_t st);
+cudaError_t launch_xc_vpot(int xc, int spinpol, int64_t nn, const double* pcc,
+                           const double* const* rho, const double* dvh, const double* vna,
+                           double* const* vxc_out, double* const* vpot_out, cudaStream_t st);
+cudaError_t launch_vpot(int spinpol, int64_t nn, const double* dvh, const double* const* vxc,
+                        const double* vna, double* const* vpot, cudaStream_t st);
+// Deterministic FP64 energy sums: out[0] = sum dRho*dVH, out[1..2] = xc sums.
+cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* aden,
+                               const double* pcc, const double* const* rho, const double* dvh,
+                               double* partials, double* out, cudaStream_t st);
+cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const double* const* b,
+                           double* partials, double* out, cudaStream_t st);
+constexpr int kReduceBlocks = 1024;
+cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
+
+}  // namespace lcp

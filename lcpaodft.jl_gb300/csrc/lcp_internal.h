@@ -1,0 +1,77 @@
+// Internal declarations of the lcpgrid library (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lcpgrid.h"
+
+namespace lcp {
+
+// Host grid geometry: the fields of struct UCell / System_Grid
+// (src/UCell.jl:1-46) plus the folded pair list the device kernels use.
+struct UCell {
+  int32_t nspin = 1;
+  int32_t natom = 0;
+  int32_t cpycell = 0;
+  double lat[3][3] = {};     // rows are lattice vectors (bohr)
+  double glat[3][3] = {};    // Latvecs[d,:] / Ngrid[d]
+  int32_t ngrid[3] = {};
+  double origin[3] = {};
+  double gridvol = 0.0;
+  std::vector<int32_t> atom2spe;  // 1-based species
+  std::vector<double> gxyz;       // natom*3
+  std::vector<double> cut;        // Atoms_Cut1
+  std::vector<int32_t> numorbs;   // Total_NumOrbs
+
+  // image cells (src/utils/Generation_ATV.jl)
+  int32_t ncell = 0;
+  std::vector<double> atv;       // ncell*3
+  std::vector<int32_t> atv_ijk;  // ncell*3
+  std::vector<int32_t> ratv;     // (2C+1)^3 -> cell
+
+  // neighbour lists (src/UCell.jl:612-672)
+  std::vector<int32_t> fnan;
+  std::vector<std::vector<int32_t>> natn, ncn;  // natn 1-based
+
+  // sphere lists (src/UCell.jl:297-411), CSR over atoms
+  std::vector<int64_t> sphere_off;  // natom+1
+  std::vector<int32_t> glist;       // GridListAtom (flat)
+  std::vector<int32_t> clist;       // CellListAtom (flat)
+
+  // pair list in reference order (src/UCell.jl:90-99)
+  int32_t nloop = 0;
+  std::vector<int32_t> pair_atom, pair_jatom, pair_cell;  // 0-based atoms
+  std::vector<int64_t> block_off;                          // offset of each DM/H block
+  int64_t total_hsize = 0;
+  std::vector<int32_t> partner;     // pair index of (j, i, -R)
+  std::vector<int64_t> numolg;      // per pair
+
+  // folded ("unique") pairs: one of each {(i,j,R), (j,i,-R)}, with the
+  // exact overlap lists of the kept orientation (CSR)
+  std::vector<int32_t> uniq_pair;   // pair index kept
+  std::vector<int64_t> uniq_off;    // n_unique+1
+  std::vector<int32_t> uniq_g1;     // index into atom's sphere list
+  std::vector<int32_t> uniq_g2;     // index into jatom's sphere list
+
+  int32_t max_numorbs() const {
+    int32_t m = 0;
+    for (auto v : numorbs) m = v > m ? v : m;
+    return m;
+  }
+  int64_t nn() const { return (int64_t)ngrid[0] * ngrid[1] * ngrid[2]; }
+};
+
+// Builds everything above; returns an error message or "".
+std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,
+                        const int32_t* atom2spe, const double* gxyz, const double* cut,
+                        const int32_t* ngrid, const double* origin, const int32_t* numorbs);
+
+// Overlap lists of one pair in reference orientation and order
+// (GListTAtoms1/2 of src/UCell.jl:425-516).
+void pair_overlap(const UCell& u, int32_t pair, std::vector<int32_t>& g1, std::vector<int32_t>& g2);
+
+void set_error(const std::string& msg);
+
+}  // namespace lcp

@@ -1,0 +1,400 @@
+// Pointwise grid kernels (FP64): Poisson source and reciprocal-space scaling,
+// LDA/LSDA exchange-correlation, effective potential, and deterministic
+// energy reductions.
+#include <cuda_runtime.h>
+#include <cuComplex.h>
+
+#include "lcp_device.h"
+
+namespace lcp {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+int grid_blocks(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+}
+
+// ------------------------------------------------------------ Poisson
+
+// Set_Density_xyz! (src/Poisson.jl:10-26): 2rho - 2rho_a ("off") or
+// rho_up + rho_down - 2rho_a ("on", "nc"), as a real array.
+__global__ void poisson_prep_kernel(int spinpol, int64_t nn, const double* __restrict__ r0,
+                                    const double* __restrict__ r1, const double* __restrict__ aden,
+                                    double* __restrict__ out) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nn; x += (int64_t)gridDim.x * blockDim.x) {
+    double a = aden ? aden[x] : 0.0;
+    out[x] = spinpol == LCP_SPIN_OFF ? 2 * r0[x] - 2 * a : r0[x] + r1[x] - 2 * a;
+  }
+}
+
+__device__ __forceinline__ int signed_freq(int i, int n) { return i < n / 2 ? i : i - n; }
+
+__device__ __forceinline__ double inv_g2_scale(int i, int j, int k, const int* ng, const double* rv) {
+  const int s1 = signed_freq(i, ng[0]), s2 = signed_freq(j, ng[1]), s3 = signed_freq(k, ng[2]);
+  const double gx = s1 * rv[0] + s2 * rv[3] + s3 * rv[6];
+  const double gy = s1 * rv[1] + s2 * rv[4] + s3 * rv[7];
+  const double gz = s1 * rv[2] + s2 * rv[5] + s3 * rv[8];
+  return 4 * kPi / (gx * gx + gy * gy + gz * gz);
+}
+
+// 4*pi/|G|^2 with the reference's signed frequencies s = i < N/2 ? i : i-N
+// (src/Poisson.jl:60-76) on the R2C half spectrum, G = 0 set to zero, the
+// inverse transform's 1/NN folded in.  The reference keeps the real part of a
+// full complex inverse transform; with a real source that equals the C2R
+// transform of the spectrum scaled by (S(k) + S(-k))/2.  For even N the two
+// terms agree; for odd N the reference's map sends index (N-1)/2 to
+// -(N+1)/2, and the average reproduces exactly what its real part keeps.
+struct PoissonArgs {
+  int ng[3];
+  double rv[9];
+  double inv_nn;
+};
+__global__ void poisson_scale_kernel(PoissonArgs a, cuDoubleComplex* __restrict__ spec) {
+  const int N1 = a.ng[0], N2 = a.ng[1], N3 = a.ng[2];
+  const int H3 = N3 / 2 + 1;
+  const int64_t total = (int64_t)N1 * N2 * H3;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(x % H3);
+    const int64_t ij = x / H3;
+    const int j = (int)(ij % N2);
+    const int i = (int)(ij / N2);
+    double s;
+    if (i == 0 && j == 0 && k == 0) {
+      s = 0.0;
+    } else {
+      const int mi = (N1 - i) % N1, mj = (N2 - j) % N2, mk = (N3 - k) % N3;
+      s = 0.5 * (inv_g2_scale(i, j, k, a.ng, a.rv) + inv_g2_scale(mi, mj, mk, a.ng, a.rv)) * a.inv_nn;
+    }
+    cuDoubleComplex v = spec[x];
+    spec[x] = make_cuDoubleComplex(v.x * s, v.y * s);
+  }
+}
+
+// ------------------------------------------------------------ exchange-correlation
+
+// LDA_CA (src/XC/LDA_CA.jl:4-41): exc (switch 0) and vxc (switch 1).
+__device__ __forceinline__ void lda_ca(double den, double& exc, double& vxc) {
+  if (den <= 1e-15) {
+    exc = 0.0;
+    vxc = 0.0;
+    return;
+  }
+  const double coe = 0.6203504908994;
+  const double rs = coe * rcbrt(den);
+  const double tmp0 = 0.458165293632163 / rs;
+  const double Ex = -tmp0, dEx = tmp0 / rs;
+  double Ec, dEc;
+  if (rs >= 1.0) {
+    const double t = sqrt(rs);
+    const double dum = 1.0 + 1.0529 * t + 0.3334 * rs;
+    const double t1 = 0.1423 / dum;
+    Ec = -t1;
+    dEc = t1 / dum * (0.52645 / t + 0.3334);
+  } else {
+    const double lr = log(rs);
+    Ec = -0.0480 + 0.0311 * lr + rs * (0.0020 * lr - 0.0116);
+    dEc = 0.0311 / rs + 0.0020 * lr - 0.0096;
+  }
+  exc = Ex + Ec;
+  vxc = Ex + Ec - 1.0 / 3.0 * rs * (dEx + dEc);
+}
+
+// LSDA_CA (src/XC/LSDA_CA.jl:1-138): switch 0 (exc, both spins equal) and
+// switch 1 (vxc up/down).
+__device__ __forceinline__ void lsda_ca(double up, double dn, double& exc, double& vu, double& vd) {
+  const double tden = up + dn;
+  const double min_den = 1e-15;
+  if (tden <= min_den) {
+    exc = vu = vd = 0.0;
+    return;
+  }
+  double zeta = (up - dn) / tden;
+  zeta = zeta > 1.0 ? 1 - min_den : zeta;
+  zeta = zeta < -1.0 ? -1 + min_den : zeta;
+  const double coe = 0.6203504908994;
+  const double rs = tden < min_den ? 62035.04908994 : coe * rcbrt(tden);
+  const double tmp0 = 0.458165293632163 / rs;
+  const double ExP = -tmp0, dExP = tmp0 / rs;
+  const double ExF = 1.25992104989487 * ExP, dExF = 1.25992104989487 * dExP;
+  double EcP, dEcP, EcF, dEcF;
+  if (rs >= 1.0) {
+    const double t = sqrt(rs);
+    double dum = 1.0 + 1.0529 * t + 0.3334 * rs;
+    double t1 = 0.1423 / dum;
+    EcP = -t1;
+    dEcP = t1 / dum * (0.52645 / t + 0.3334);
+    dum = 1.0 + 1.3981 * t + 0.2611 * rs;
+    t1 = 0.0843 / dum;
+    EcF = -t1;
+    dEcF = t1 / dum * (0.69905 / t + 0.2611);
+  } else {
+    const double lr = log(rs);
+    EcP = -0.0480 + 0.0311 * lr + rs * (0.0020 * lr - 0.0116);
+    dEcP = 0.0311 / rs + 0.0020 * lr - 0.0096;
+    EcF = -0.0269 + 0.01555 * lr + rs * (0.0007 * lr - 0.0048);
+    dEcF = 0.01555 / rs + 0.0007 * lr - 0.0041;
+  }
+  const double z0 = cbrt(1 + zeta), z1 = cbrt(1 - zeta);
+  const double z02 = z0 * z0, z04 = z02 * z02, z12 = z1 * z1, z14 = z12 * z12;
+  // switch 0 uses (1 +- zeta)^(4/3) directly
+  const double fz0 = 1.92366105093154 * ((1 + zeta) * z0 + (1 - zeta) * z1 - 2.0);
+  exc = ExP + EcP + (ExF + EcF - ExP - EcP) * fz0;
+  const double fz = 1.92366105093154 * (z04 + z14 - 2.0);
+  const double dfz = 2.56488140124205 * (z0 - z1);
+  const double t0 = ExF + EcF - ExP - EcP;
+  const double e1 = ExP + EcP + t0 * fz;
+  const double de = dExP + dEcP + (dExF + dEcF - dExP - dEcP) * fz;
+  const double v = e1 - 1.0 / 3.0 * rs * de;
+  vu = v + t0 * (1 - zeta) * dfz;
+  vd = v + t0 * (-1 - zeta) * dfz;
+}
+
+struct XcArgs {
+  int xc, spinpol;
+  int64_t nn;
+  const double* pcc;
+  const double* rho[4];
+  const double* dvh;
+  const double* vna;
+  double* vxc[4];
+  double* vpot[4];
+};
+
+// Set_XC_Grid! (src/XC/XC_Func.jl:111-145) and, where vpot is given,
+// Set_Vpot_Grid! (src/Matrix/Set_Vpot_Grid.jl:1-19) in the same pass.
+__global__ void xc_vpot_kernel(XcArgs a) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < a.nn; x += (int64_t)gridDim.x * blockDim.x) {
+    const double pc = a.pcc ? a.pcc[x] : 0.0;
+    double v[4] = {0, 0, 0, 0};
+    if (a.xc == LCP_XC_LDA) {
+      double e;
+      lda_ca(2 * (a.rho[0][x] + pc), e, v[0]);
+    } else {
+      double e;
+      lsda_ca(a.rho[0][x] + pc, a.rho[1][x] + pc, e, v[0], v[1]);
+      if (a.spinpol == LCP_SPIN_NC) {
+        const double th = a.rho[2][x], ph = a.rho[3][x];
+        const double t0 = 0.5 * (v[0] + v[1]), t1 = 0.5 * (v[0] - v[1]);
+        v[3] = -t1 * sin(th) * sin(ph);
+        v[2] = t1 * sin(th) * cos(ph);
+        v[1] = t0 - t1 * cos(th);
+        v[0] = t0 + t1 * cos(th);
+      }
+    }
+    const int nv = a.spinpol == LCP_SPIN_OFF ? 1 : (a.spinpol == LCP_SPIN_ON ? 2 : 4);
+    for (int c = 0; c < nv; ++c)
+      if (a.vxc[c]) a.vxc[c][x] = v[c];
+    if (a.vpot[0]) {
+      const double dv = a.dvh[x];
+      const double na = a.vna ? a.vna[x] : 0.0;
+      for (int c = 0; c < nv; ++c) a.vpot[c][x] = c < 2 ? dv + v[c] + na : v[c];
+    }
+  }
+}
+
+struct VpotArgs {
+  int spinpol;
+  int64_t nn;
+  const double* dvh;
+  const double* vxc[4];
+  const double* vna;
+  double* vpot[4];
+};
+__global__ void vpot_kernel(VpotArgs a) {
+  const int nv = a.spinpol == LCP_SPIN_OFF ? 1 : (a.spinpol == LCP_SPIN_ON ? 2 : 4);
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < a.nn; x += (int64_t)gridDim.x * blockDim.x) {
+    const double na = a.vna ? a.vna[x] : 0.0;
+    for (int c = 0; c < nv; ++c) a.vpot[c][x] = c < 2 ? a.dvh[x] + a.vxc[c][x] + na : a.vxc[c][x];
+  }
+}
+
+// ------------------------------------------------------------ deterministic reductions
+
+constexpr int kRedThreads = 256;
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out) {
+  __shared__ double sh[NV][kRedThreads];
+  for (int c = 0; c < NV; ++c) sh[c][threadIdx.x] = v[c];
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int c = 0; c < NV; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < NV; ++c) out[c] = sh[c][0];
+}
+
+struct EnergyArgs {
+  int xc, spinpol;
+  int64_t nn;
+  const double* aden;
+  const double* pcc;
+  const double* rho[2];
+  const double* dvh;
+  double* partials;  // [kReduceBlocks][3]
+};
+
+// Per-block partial sums of Calc_EH1 (src/Energy.jl:655-666) and Calc_EXC1
+// (src/Energy.jl:669-700, with Calc_Vxc_Grid switch 0 of src/XC/XC_Func.jl:164-189).
+__global__ void __launch_bounds__(kRedThreads) energy_partials_kernel(EnergyArgs a) {
+  double v[3] = {0, 0, 0};
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < a.nn; x += (int64_t)gridDim.x * blockDim.x) {
+    const double ad = a.aden ? a.aden[x] : 0.0;
+    const double pc = a.pcc ? a.pcc[x] : 0.0;
+    const double drho = a.spinpol == LCP_SPIN_OFF ? 2 * (a.rho[0][x] - ad) : a.rho[0][x] + a.rho[1][x] - 2 * ad;
+    if (a.dvh) v[0] += drho * a.dvh[x];
+    const double temp = ad + pc;
+    double ea, va;
+    lda_ca(2 * temp, ea, va);
+    if (a.xc == LCP_XC_LDA) {
+      double e, vv;
+      lda_ca(2 * (a.rho[0][x] + pc), e, vv);
+      v[1] += (a.rho[0][x] + pc) * e - temp * ea;
+    } else {
+      double e, vu, vd;
+      lsda_ca(a.rho[0][x] + pc, a.rho[1][x] + pc, e, vu, vd);
+      v[1] += (a.rho[0][x] + pc) * e - temp * ea;
+      v[2] += (a.rho[1][x] + pc) * e - temp * ea;
+    }
+  }
+  block_reduce_store<3>(v, a.partials + (size_t)blockIdx.x * 3);
+}
+
+template <int NV>
+__global__ void __launch_bounds__(kRedThreads) finish_sums_kernel(const double* __restrict__ partials, int nblocks,
+                                                                  double* out) {
+  double v[NV];
+  for (int c = 0; c < NV; ++c) v[c] = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+    for (int c = 0; c < NV; ++c) v[c] += partials[(size_t)b * NV + c];
+  block_reduce_store<NV>(v, out);
+}
+
+struct DotArgs {
+  int nvec;
+  int64_t n;
+  const double* a[4];
+  const double* b[4];
+  double* partials;
+};
+__global__ void __launch_bounds__(kRedThreads) dot_partials_kernel(DotArgs d) {
+  double v[1] = {0.0};
+  for (int c = 0; c < d.nvec; ++c)
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < d.n; x += (int64_t)gridDim.x * blockDim.x)
+      v[0] += d.a[c][x] * d.b[c][x];
+  block_reduce_store<1>(v, d.partials + blockIdx.x);
+}
+
+// FP64 FMA throughput probe: 8 independent dependency chains per thread.
+__global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
+  double x[8];
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 1234.5) out[0] = s;  // keeps the chains live
+}
+
+}  // namespace
+
+cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st) {
+  fp64_probe_kernel<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_prep(int spinpol, int64_t nn, const double* rho0, const double* rho1, const double* aden,
+                                double* out, cudaStream_t st) {
+  poisson_prep_kernel<<<grid_blocks(nn, 256), 256, 0, st>>>(spinpol, nn, rho0, rho1, aden, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_scale(const int32_t* ngrid, const double* recvecs, void* spectrum, cudaStream_t st) {
+  PoissonArgs a;
+  for (int d = 0; d < 3; ++d) a.ng[d] = ngrid[d];
+  for (int d = 0; d < 9; ++d) a.rv[d] = recvecs[d];
+  a.inv_nn = 1.0 / ((double)ngrid[0] * ngrid[1] * ngrid[2]);
+  int64_t total = (int64_t)ngrid[0] * ngrid[1] * (ngrid[2] / 2 + 1);
+  poisson_scale_kernel<<<grid_blocks(total, 256), 256, 0, st>>>(a, reinterpret_cast<cuDoubleComplex*>(spectrum));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_xc_vpot(int xc, int spinpol, int64_t nn, const double* pcc, const double* const* rho,
+                           const double* dvh, const double* vna, double* const* vxc_out, double* const* vpot_out,
+                           cudaStream_t st) {
+  XcArgs a{};
+  a.xc = xc;
+  a.spinpol = spinpol;
+  a.nn = nn;
+  a.pcc = pcc;
+  const int nr = spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4);
+  for (int c = 0; c < nr; ++c) {
+    a.rho[c] = rho[c];
+    a.vxc[c] = vxc_out ? vxc_out[c] : nullptr;
+    a.vpot[c] = vpot_out ? vpot_out[c] : nullptr;
+  }
+  a.dvh = dvh;
+  a.vna = vna;
+  xc_vpot_kernel<<<grid_blocks(nn, 256), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vpot(int spinpol, int64_t nn, const double* dvh, const double* const* vxc, const double* vna,
+                        double* const* vpot, cudaStream_t st) {
+  VpotArgs a{};
+  a.spinpol = spinpol;
+  a.nn = nn;
+  a.dvh = dvh;
+  a.vna = vna;
+  const int nv = spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4);
+  for (int c = 0; c < nv; ++c) {
+    a.vxc[c] = vxc[c];
+    a.vpot[c] = vpot[c];
+  }
+  vpot_kernel<<<grid_blocks(nn, 256), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* aden, const double* pcc,
+                               const double* const* rho, const double* dvh, double* partials, double* out,
+                               cudaStream_t st) {
+  EnergyArgs a{};
+  a.xc = xc;
+  a.spinpol = spinpol;
+  a.nn = nn;
+  a.aden = aden;
+  a.pcc = pcc;
+  a.rho[0] = rho[0];
+  a.rho[1] = spinpol == LCP_SPIN_OFF ? nullptr : rho[1];
+  a.dvh = dvh;
+  a.partials = partials;
+  energy_partials_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(a);
+  LCP_CUDA_TRY(cudaGetLastError());
+  finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const double* const* b, double* partials,
+                           double* out, cudaStream_t st) {
+  DotArgs d{};
+  d.nvec = nvec;
+  d.n = n;
+  for (int c = 0; c < nvec; ++c) {
+    d.a[c] = a[c];
+    d.b[c] = b[c];
+  }
+  d.partials = partials;
+  dot_partials_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(d);
+  LCP_CUDA_TRY(cudaGetLastError());
+  finish_sums_kernel<1><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
+  return cudaGetLastError();
+}
+
+}  // namespace lcp

@@ -1,0 +1,244 @@
+// Exact-lens pair contractions on CUDA cores: density assembly and grid
+// matrix elements in FP64 (the drop-in) or FP32 (comparison form).
+//
+// The reference walks every ordered pair (i, j, R) of the neighbour list over
+// the pair's overlap ("lens") points in 512-point blocks, with a small dgemm
+// per block (src/Matrix/Set_Density_Grid.jl:268-304,
+// src/Hamiltonian.jl:384-429).  Here each unordered pair {(i,j,R), (j,i,-R)}
+// is visited once:
+//   density: rho(p) += phi_i(p)^T (D_(i,j,R) + D_(j,i,-R)^T) phi_j(p)
+//            -- exactly the sum of the two ordered contributions for any D;
+//   H:       Hm[a][b] = sum_p phi_i,a(p) V(p) phi_j,b(p) is written to both
+//            blocks, H_(i,j,R)[b,a] and H_(j,i,-R)[a,b] (V real).
+// The lens lists are the reference's GListTAtoms1/2 of the kept orientation.
+// Work items are 512-entry chunks of those lists; a persistent grid walks the
+// items.  FP64 results reach the grids/blocks through FP64 atomics.
+#include <cuda_runtime.h>
+
+#include "lcp_device.h"
+
+namespace lcp {
+
+namespace {
+
+constexpr int kPairThreads = 256;
+constexpr int kTile = 64;  // lens points staged per H tile
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T* p) {
+  return __ldg(p);
+}
+
+struct Ptr4 {
+  const double* c[4];
+};
+struct MPtr4 {
+  double* c[4];
+};
+
+// ---------------------------------------------------------------- density
+
+template <typename T, int NOMAX>
+__global__ void __launch_bounds__(kPairThreads) density_pairs_kernel(DevGeom g, DevPairs pr, int nspin,
+                                                                     const T* __restrict__ phi, Ptr4 dm,
+                                                                     MPtr4 rho) {
+  __shared__ T Ds[4][NOMAX * NOMAX];
+  for (int64_t item = blockIdx.x; item < pr.nitems; item += gridDim.x) {
+    const int64_t q = pr.item_pair[item];
+    const int i = pr.atom[q], j = pr.jatom[q];
+    const int noi = g.numorbs[i], noj = g.numorbs[j];
+    const int64_t bp = pr.boff_p[q], bq = pr.boff_q[q];
+    const bool self = pr.self[q] != 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < noi * noj; e += blockDim.x) {
+      const int a = e / noj, b = e - a * noj;
+      for (int s = 0; s < nspin; ++s) {
+        double v = dm.c[s][bp + (int64_t)a * noj + b];
+        if (!self) v += dm.c[s][bq + (int64_t)b * noi + a];
+        Ds[s][a * NOMAX + b] = (T)v;
+      }
+    }
+    __syncthreads();
+    const int64_t start = pr.item_start[item];
+    const int count = pr.item_count[item];
+    const T* phi_i = phi + g.phi_off[i];
+    const T* phi_j = phi + g.phi_off[j];
+    const int32_t* gl_i = g.glist + g.sph_off[i];
+    for (int pt = threadIdx.x; pt < count; pt += blockDim.x) {
+      const int64_t k = start + pt;
+      const int g1 = pr.g1[k], g2 = pr.g2[k];
+      T pi[NOMAX], pj[NOMAX];
+#pragma unroll
+      for (int a = 0; a < NOMAX; ++a) pi[a] = a < noi ? ldg(phi_i + (int64_t)g1 * noi + a) : T(0);
+#pragma unroll
+      for (int b = 0; b < NOMAX; ++b) pj[b] = b < noj ? ldg(phi_j + (int64_t)g2 * noj + b) : T(0);
+      const int gidx = gl_i[g1];
+      for (int s = 0; s < nspin; ++s) {
+        T acc = T(0);
+#pragma unroll
+        for (int a = 0; a < NOMAX; ++a) {
+          if (a < noi) {
+            T t = T(0);
+#pragma unroll
+            for (int b = 0; b < NOMAX; ++b) t += Ds[s][a * NOMAX + b] * pj[b];
+            acc += pi[a] * t;
+          }
+        }
+        atomicAdd(rho.c[s] + gidx, (double)acc);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- grid H
+
+template <typename T, int NOMAX>
+__global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom g, DevPairs pr, int nch,
+                                                                         const T* __restrict__ phi, Ptr4 vpot,
+                                                                         MPtr4 hks) {
+  constexpr int kSlots = (NOMAX * NOMAX + kPairThreads - 1) / kPairThreads;
+  extern __shared__ unsigned char smem_raw[];
+  T* W = reinterpret_cast<T*>(smem_raw);           // [nch][kTile][NOMAX]
+  T* P = W + (size_t)4 * kTile * NOMAX;            // [kTile][NOMAX]
+  for (int64_t item = blockIdx.x; item < pr.nitems; item += gridDim.x) {
+    const int64_t q = pr.item_pair[item];
+    const int i = pr.atom[q], j = pr.jatom[q];
+    const int noi = g.numorbs[i], noj = g.numorbs[j];
+    const int64_t start = pr.item_start[item];
+    const int count = pr.item_count[item];
+    const T* phi_i = phi + g.phi_off[i];
+    const T* phi_j = phi + g.phi_off[j];
+    const int32_t* gl_i = g.glist + g.sph_off[i];
+    T acc[4][kSlots];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s) acc[c][s] = T(0);
+    for (int t0 = 0; t0 < count; t0 += kTile) {
+      const int nt = min(kTile, count - t0);
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < kTile * NOMAX; idx += blockDim.x) {
+        const int pt = idx / NOMAX, a = idx - pt * NOMAX;
+        T wi = T(0), wj = T(0);
+        double v[4] = {0, 0, 0, 0};
+        if (pt < nt) {
+          const int64_t k = start + t0 + pt;
+          const int g1 = pr.g1[k], g2 = pr.g2[k];
+          if (a < noi) {
+            wi = ldg(phi_i + (int64_t)g1 * noi + a);
+            const int gidx = gl_i[g1];
+            for (int c = 0; c < nch; ++c) v[c] = ldg(vpot.c[c] + gidx);
+          }
+          if (a < noj) wj = ldg(phi_j + (int64_t)g2 * noj + a);
+        }
+        for (int c = 0; c < nch; ++c) W[((size_t)c * kTile + pt) * NOMAX + a] = wi * (T)v[c];
+        P[pt * NOMAX + a] = wj;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s) {
+        const int e = threadIdx.x + s * kPairThreads;
+        if (e < NOMAX * NOMAX) {
+          const int a = e / NOMAX, b = e - (e / NOMAX) * NOMAX;
+          if (a < noi && b < noj) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (c < nch) {
+                T sum = T(0);
+                const T* wr = W + (size_t)c * kTile * NOMAX + a;
+                const T* pr_ = P + b;
+                for (int pt = 0; pt < nt; ++pt) sum += wr[pt * NOMAX] * pr_[pt * NOMAX];
+                acc[c][s] += sum;
+              }
+            }
+          }
+        }
+      }
+    }
+    const bool self = pr.self[q] != 0;
+    const int64_t bp = pr.boff_p[q], bq = pr.boff_q[q];
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) {
+      const int e = threadIdx.x + s * kPairThreads;
+      if (e < NOMAX * NOMAX) {
+        const int a = e / NOMAX, b = e - (e / NOMAX) * NOMAX;
+        if (a < noi && b < noj) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (c < nch) {
+              const double val = (double)acc[c][s] * g.gridvol;
+              atomicAdd(hks.c[c] + bp + (int64_t)a * noj + b, val);
+              if (!self) atomicAdd(hks.c[c] + bq + (int64_t)b * noi + a, val);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+int persistent_blocks(int64_t nitems, int per_sm) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t b = (int64_t)sms * per_sm;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, nitems));
+}
+
+template <typename T, int NOMAX>
+cudaError_t run_density(const DevGeom& g, const DevPairs& pr, int nspin, const T* phi, const double* const* dm,
+                        double* const* rho, cudaStream_t st) {
+  Ptr4 d{};
+  MPtr4 r{};
+  for (int s = 0; s < nspin; ++s) {
+    d.c[s] = dm[s];
+    r.c[s] = rho[s];
+  }
+  density_pairs_kernel<T, NOMAX><<<persistent_blocks(pr.nitems, 8), kPairThreads, 0, st>>>(g, pr, nspin, phi, d, r);
+  return cudaGetLastError();
+}
+
+template <typename T, int NOMAX>
+cudaError_t run_hamiltonian(const DevGeom& g, const DevPairs& pr, int nch, const T* phi, const double* const* vp,
+                            double* const* h, cudaStream_t st) {
+  Ptr4 v{};
+  MPtr4 o{};
+  for (int c = 0; c < nch; ++c) {
+    v.c[c] = vp[c];
+    o.c[c] = h[c];
+  }
+  size_t smem = (size_t)5 * kTile * NOMAX * sizeof(T);
+  LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_pairs_kernel<T, NOMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+  hamiltonian_pairs_kernel<T, NOMAX><<<persistent_blocks(pr.nitems, 4), kPairThreads, smem, st>>>(g, pr, nch, phi,
+                                                                                                   v, o);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_density_pairs(int prec, const DevGeom& g, const DevPairs& pr, int nspin, const double* phi64,
+                                 const float* phi32, const double* const* dm, double* const* rho, int max_no,
+                                 cudaStream_t st) {
+  if (pr.nitems == 0) return cudaSuccess;
+  if (prec == LCP_PREC_FP32) {
+    if (max_no <= 16) return run_density<float, 16>(g, pr, nspin, phi32, dm, rho, st);
+    return run_density<float, 32>(g, pr, nspin, phi32, dm, rho, st);
+  }
+  if (max_no <= 16) return run_density<double, 16>(g, pr, nspin, phi64, dm, rho, st);
+  return run_density<double, 32>(g, pr, nspin, phi64, dm, rho, st);
+}
+
+cudaError_t launch_hamiltonian_pairs(int prec, const DevGeom& g, const DevPairs& pr, int nch, const double* phi64,
+                                     const float* phi32, const double* const* vpot, double* const* hks, int max_no,
+                                     cudaStream_t st) {
+  if (pr.nitems == 0) return cudaSuccess;
+  if (prec == LCP_PREC_FP32) {
+    if (max_no <= 16) return run_hamiltonian<float, 16>(g, pr, nch, phi32, vpot, hks, st);
+    return run_hamiltonian<float, 32>(g, pr, nch, phi32, vpot, hks, st);
+  }
+  if (max_no <= 16) return run_hamiltonian<double, 16>(g, pr, nch, phi64, vpot, hks, st);
+  return run_hamiltonian<double, 32>(g, pr, nch, phi64, vpot, hks, st);
+}
+
+}  // namespace lcp

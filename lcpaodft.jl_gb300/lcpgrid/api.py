@@ -1,0 +1,472 @@
+"""Host-side mirror of LCPAODFT.jl's grid-path interface over the C ABI.
+
+Each function keeps the reference's name, argument order and meaning.  The
+Julia ``!`` suffix (mutates its last arguments) maps to writing into the numpy
+arrays passed in; errors the reference raises with ``error()`` raise
+``LCPError``.  All arithmetic runs in liblcpgrid.so on the GPU.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import LCPError, check, dptr, dptrs, iptr, lib
+
+__all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob",
+           "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "Solve_Poisson", "Solve_Poisson_xyz",
+           "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
+           "Calc_MatrixElements_dVH_Vxc_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """A device context (CUDA stream, FFT plans, workspaces) on one GPU.
+
+    ``precision`` selects the arithmetic of the pair contractions:
+    "fp64" (the drop-in), "fp32" or "bf16x3"."""
+
+    def __init__(self, device=0, precision="fp64"):
+        h = ctypes.c_void_p()
+        check(lib.lcp_ctx_create(int(device), ctypes.byref(h)))
+        self._h = h
+        self.device = int(device)
+        self.set_precision(precision)
+
+    def set_precision(self, precision):
+        check(lib.lcp_ctx_set_precision(self._h, _lib.PREC[precision]))
+        self.precision = precision
+
+    def set_stream(self, stream_handle):
+        """Run on an external cudaStream_t (an int handle, e.g. torch's
+        ``torch.cuda.current_stream().cuda_stream``); None restores the own stream."""
+        check(lib.lcp_ctx_set_stream(self._h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+
+    def synchronize(self):
+        check(lib.lcp_ctx_synchronize(self._h))
+
+    def probe_fp64_tflops(self):
+        """Measured FP64 FMA throughput of the device (TFLOP/s)."""
+        out = ctypes.c_double()
+        check(lib.lcp_probe_fp64_tflops(self._h, ctypes.byref(out)))
+        return out.value
+
+    @property
+    def launch_count(self):
+        return int(lib.lcp_ctx_launch_count(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.lcp_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_DEFAULT = {}
+
+
+def default_context(device=0):
+    if device not in _DEFAULT:
+        _DEFAULT[device] = Context(device)
+    return _DEFAULT[device]
+
+
+class UCell:
+    """``UCell(Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin; Total_NumOrbs)``
+    (src/UCell.jl:210-294), built by the library on the host.
+
+    Lists are exposed with the reference's names: GridN_Atom, GridListAtom,
+    CellListAtom (per atom), FNAN, natn, ncn, MPI_atom/MPI_natn/MPI_ncn,
+    MPI_NumOLG and MPI_GListTAtoms1/2 (per pair)."""
+
+    def __init__(self, Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin, Total_NumOrbs=None):
+        self.Latvecs = _f64(Latvecs).reshape(3, 3)
+        self.Natom = int(Natom)
+        self.atom2spe = np.ascontiguousarray(atom2spe, dtype=np.int32)
+        self.Gxyz = _f64(Gxyz).reshape(self.Natom, 3)
+        self.Atoms_Cut1 = _f64(Atoms_Cut1)
+        self.Ngrid = tuple(int(x) for x in Ngrid)
+        self.Grid_Origin = _f64(Grid_Origin)
+        self.Nspin = int(Nspin)
+        self.Total_NumOrbs = np.zeros(self.Natom, dtype=np.int32) if Total_NumOrbs is None else \
+            np.ascontiguousarray(Total_NumOrbs, dtype=np.int32)
+        if self.atom2spe.size != self.Natom or self.Atoms_Cut1.size != self.Natom or self.Total_NumOrbs.size != self.Natom:
+            raise LCPError(_lib.LCP_EINVAL, "per-atom arrays must have Natom entries")
+        h = ctypes.c_void_p()
+        ng = np.array(self.Ngrid, dtype=np.int32)
+        check(lib.lcp_ucell_create(self.Nspin, dptr(self.Latvecs), self.Natom, iptr(self.atom2spe), dptr(self.Gxyz),
+                                   dptr(self.Atoms_Cut1), iptr(ng), dptr(self.Grid_Origin), iptr(self.Total_NumOrbs),
+                                   ctypes.byref(h)))
+        self._h = h
+        info = _lib.lcp_ucell_info()
+        check(lib.lcp_ucell_get_info(self._h, ctypes.byref(info)))
+        self.CpyCell = info.cpycell
+        self.Nloop = info.nloop
+        self.ncell = info.ncell
+        self.Total_Hsize = int(info.total_hsize)
+        self.GridVol = info.gridvol
+        self.sum_gridn = int(info.sum_gridn)
+        self.sum_numolg = int(info.sum_numolg)
+        self.n_unique = int(info.n_unique)
+        self.max_numorbs = info.max_numorbs
+        self.FNAN = self._ints(_lib.F_FNAN, 0, self.Natom)
+        self.GridN_Atom = self._ints(_lib.F_GRIDN_ATOM, 0, self.Natom)
+        self.MPI_atom = self._ints(_lib.F_PAIR_ATOM, 0, self.Nloop)
+        self.MPI_natn = self._ints(_lib.F_PAIR_NATN, 0, self.Nloop)
+        self.MPI_ncn = self._ints(_lib.F_PAIR_NCN, 0, self.Nloop)
+        self.MPI_NumOLG = self._ints(_lib.F_NUMOLG, 0, self.Nloop)
+        offs = [0]
+        for a, b in zip(self.MPI_atom, self.MPI_natn):
+            offs.append(offs[-1] + int(self.Total_NumOrbs[a - 1]) * int(self.Total_NumOrbs[b - 1]))
+        self.block_offset = np.array(offs[:-1], dtype=np.int64)
+
+    def _ints(self, field, index, count):
+        out = np.zeros(int(count), dtype=np.int32)
+        check(lib.lcp_ucell_get_int(self._h, field, int(index), iptr(out), int(count)))
+        return out
+
+    @property
+    def natn(self):
+        return [self._ints(_lib.F_NATN, a, self.FNAN[a] + 1) for a in range(self.Natom)]
+
+    @property
+    def ncn(self):
+        return [self._ints(_lib.F_NCN, a, self.FNAN[a] + 1) for a in range(self.Natom)]
+
+    @property
+    def GridListAtom(self):
+        return [self._ints(_lib.F_GRIDLIST, a, self.GridN_Atom[a]) for a in range(self.Natom)]
+
+    @property
+    def CellListAtom(self):
+        return [self._ints(_lib.F_CELLLIST, a, self.GridN_Atom[a]) for a in range(self.Natom)]
+
+    def GListTAtoms(self, pair):
+        """(MPI_GListTAtoms1[pair], MPI_GListTAtoms2[pair]), 0-based pair index."""
+        n = int(self.MPI_NumOLG[pair])
+        return self._ints(_lib.F_GLIST1, pair, n), self._ints(_lib.F_GLIST2, pair, n)
+
+    @property
+    def atv(self):
+        out = np.zeros((self.ncell, 3))
+        check(lib.lcp_ucell_get_atv(self._h, dptr(out)))
+        return out
+
+    @property
+    def atv_ijk(self):
+        return self._ints(_lib.F_ATV_IJK, 0, self.ncell * 3).reshape(self.ncell, 3)
+
+    @property
+    def NN(self):
+        return int(np.prod(self.Ngrid))
+
+    def Recvecs(self):
+        """2*pi*inv(Latvecs') (src/Mixing/DFT_Mixing.jl:91)."""
+        return 2 * np.pi * np.linalg.inv(self.Latvecs.T)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib.lcp_ucell_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class DeviceOrbitalsGrid:
+    """Device-resident orbital tables, the GPU counterpart of
+    ``PackedOrbitalsGrid`` (src/Matrix/Set_Orbitals_Grid.jl:1-23).
+
+    ``data(atom)`` copies atom's table to the host as [NumOrbs, GridN], the
+    shape of ``PackedOrbitalsGrid.data[atom]``; component 1..3 selects the
+    gradient tables when they were tabulated."""
+
+    def __init__(self, ctx, ucell, handle, with_grad):
+        self.ctx = ctx
+        self.ucell = ucell
+        self._h = handle
+        self.with_grad = with_grad
+
+    def data(self, atom, component=0):
+        a = int(atom)
+        n = int(self.ucell.GridN_Atom[a]) * int(self.ucell.Total_NumOrbs[a])
+        out = np.zeros(n)
+        check(lib.lcp_orbs_download(self.ctx._h, self._h, int(component), a, dptr(out), n))
+        return out.reshape(int(self.ucell.GridN_Atom[a]), int(self.ucell.Total_NumOrbs[a])).T.copy()
+
+    def __len__(self):
+        return self.ucell.Natom
+
+    def __getitem__(self, atom):
+        return self.data(atom)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib.lcp_orbs_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def _paos_struct(paos):
+    arr = (_lib.lcp_pao * len(paos))()
+    keep = []
+    for k, p in enumerate(paos):
+        rv = _f64(p.Spe_PAO_RV)
+        rwf = p.packed_rwf()
+        keep += [rv, rwf]
+        arr[k].max_l = p.Spe_MaxL_Basis
+        for l in range(4):
+            arr[k].num_basis[l] = p.Spe_Num_Basis[l] if l <= p.Spe_MaxL_Basis else 0
+        arr[k].num_mesh = rv.size
+        arr[k].rv = dptr(rv)
+        arr[k].rwf = dptr(rwf)
+    return arr, keep
+
+
+def _tabulate(pao, ucell, ctx, grad):
+    ctx = ctx or default_context()
+    arr, keep = _paos_struct(list(pao))
+    h = ctypes.c_void_p()
+    check(lib.lcp_set_orbitals_grid(ctx._h, ucell._h, len(keep) // 2, arr, 1 if grad else 0, ctypes.byref(h)))
+    return DeviceOrbitalsGrid(ctx, ucell, h, grad)
+
+
+def Set_Orbitals_Grid(pao, ucell, ctx=None):
+    """src/Matrix/Set_Orbitals_Grid.jl:26-42."""
+    return _tabulate(pao, ucell, ctx, False)
+
+
+def Set_dOrbitals_Grid(pao, ucell, ctx=None):
+    """Values and gradient tables (src/Matrix/Set_dOrbitals_Grid.jl:1-20);
+    ``.data(atom, k)`` for k = 1, 2, 3 gives d/dx, d/dy, d/dz."""
+    return _tabulate(pao, ucell, ctx, True)
+
+
+def _spin(SpinPol):
+    s = SpinPol.lower()
+    if s not in _lib.SPIN:
+        raise LCPError(_lib.LCP_EINVAL, "please check SpinPol.")
+    return s
+
+
+def Set_Density_Grid(SpinPol, ucell, Orbs_Grid, DM, Density_Grid):
+    """``Set_Density_Grid!`` (src/Matrix/Set_Density_Grid.jl:1-9): fills Density_Grid[s]."""
+    s = _spin(SpinPol)
+    n = _lib.NCHAN[s]
+    dm = [_f64(DM[c]) for c in range(n)]
+    for c in range(n):
+        if Density_Grid[c].dtype != np.float64 or not Density_Grid[c].flags["C_CONTIGUOUS"]:
+            raise TypeError("Density_Grid must hold C-contiguous float64 arrays")
+        if dm[c].size != ucell.Total_Hsize or Density_Grid[c].size != ucell.NN:
+            raise LCPError(_lib.LCP_EINVAL, "DM/Density_Grid sizes do not match the UCell")
+    pdm, k1 = dptrs(dm)
+    pr, k2 = dptrs([Density_Grid[c] for c in range(n)])
+    check(lib.lcp_set_density_grid(Orbs_Grid.ctx._h, ucell._h, Orbs_Grid._h, _lib.SPIN[s], pdm, pr))
+
+
+class Rhor_Mixing:
+    """The parts of ``DFT_Mixing`` the Poisson solve reads: Ngrid and Recvecs
+    (src/Mixing/DFT_Mixing.jl:47-95)."""
+
+    def __init__(self, Ngrid, Latvecs):
+        self.Ngrid = tuple(int(x) for x in Ngrid)
+        self.Latvecs = _f64(Latvecs).reshape(3, 3)
+        self.Recvecs = 2 * np.pi * np.linalg.inv(self.Latvecs.T)
+
+
+def Solve_Poisson(SpinPol, dft_mixing, Density_Grid, ADensity_Grid, dVHart_Grid, ctx=None):
+    """``Solve_Poisson!`` (src/Poisson.jl:1-7): fills dVHart_Grid."""
+    ctx = ctx or default_context()
+    s = _spin(SpinPol)
+    nr = 1 if s == "off" else 2
+    rho = [_f64(Density_Grid[c]) for c in range(nr)]
+    pr, keep = dptrs(rho)
+    ng = np.array(dft_mixing.Ngrid, dtype=np.int32)
+    rv = _f64(dft_mixing.Recvecs)
+    ad = None if ADensity_Grid is None else _f64(ADensity_Grid)
+    check(lib.lcp_solve_poisson(ctx._h, iptr(ng), dptr(rv), _lib.SPIN[s], pr, dptr(ad), dptr(dVHart_Grid)))
+
+
+def Solve_Poisson_xyz(Ngrid, Recvecs, Density_xyz, dVHart_Grid, ctx=None):
+    """Inner ``Solve_Poisson!(Ngrid, Recvecs, Density_xyz, dVHart_Grid)`` for a
+    real Density_xyz (src/Poisson.jl:29-108)."""
+    ctx = ctx or default_context()
+    ng = np.array(Ngrid, dtype=np.int32)
+    src = _f64(np.real(np.asarray(Density_xyz)).reshape(-1))
+    check(lib.lcp_solve_poisson_xyz(ctx._h, iptr(ng), dptr(_f64(Recvecs)), dptr(src), dptr(dVHart_Grid)))
+
+
+class XC_Func:
+    """``XC_Func(xc_type, SpinPol, Nspin, Ngrid)`` for LDA/LSDA
+    (src/XC/XC_Func.jl:47-108)."""
+
+    def __init__(self, xc_type, SpinPol, Nspin, Ngrid):
+        xc = xc_type.upper()
+        sp = SpinPol.lower()
+        if xc not in ("LDA", "LSDA"):
+            raise LCPError(_lib.LCP_ENOTSUP if xc.replace("-", "_") == "GGA_PBE" else _lib.LCP_EINVAL,
+                           "please check xc_type name")
+        if sp not in _lib.SPIN:
+            raise LCPError(_lib.LCP_EINVAL, "please check SpinPol name")
+        if (xc == "LDA") != (sp == "off"):
+            raise LCPError(_lib.LCP_EINVAL, "please check xc_type and SpinPol")
+        self.xc_type = xc
+        self.SpinPol = sp
+        self.Nspin = int(Nspin)
+        self.Ngrid = tuple(int(x) for x in Ngrid)
+        nn = int(np.prod(self.Ngrid))
+        self.Vxc_Grid = [np.zeros(nn) for _ in range(_lib.NCHAN[sp])]
+
+
+def Set_XC_Grid(xc_func, PCCDensity_Grid, Density_Grid, ctx=None):
+    """``Set_XC_Grid!`` (src/XC/XC_Func.jl:111-145): fills xc_func.Vxc_Grid."""
+    ctx = ctx or default_context()
+    n = _lib.NCHAN[xc_func.SpinPol]
+    nn = int(np.prod(xc_func.Ngrid))
+    rho = [_f64(Density_Grid[c]) for c in range(n)]
+    pr, k1 = dptrs(rho)
+    pv, k2 = dptrs(xc_func.Vxc_Grid)
+    pcc = None if PCCDensity_Grid is None else _f64(PCCDensity_Grid)
+    check(lib.lcp_set_xc_grid(ctx._h, _lib.XC[xc_func.xc_type], _lib.SPIN[xc_func.SpinPol], nn, dptr(pcc), pr, pv))
+
+
+def Set_Vpot_Grid(xc_func, dVHart_Grid, Vpot_Grid, Vna_Grid=None, ctx=None):
+    """``Set_Vpot_Grid!`` (src/Matrix/Set_Vpot_Grid.jl:1-19); Vna_Grid, when
+    given, is added to the spin-diagonal channels."""
+    ctx = ctx or default_context()
+    n = _lib.NCHAN[xc_func.SpinPol]
+    nn = int(np.prod(xc_func.Ngrid))
+    px, k1 = dptrs([_f64(v) for v in xc_func.Vxc_Grid])
+    pv, k2 = dptrs([Vpot_Grid[c] for c in range(n)])
+    vna = None if Vna_Grid is None else _f64(Vna_Grid)
+    check(lib.lcp_set_vpot_grid(ctx._h, _lib.SPIN[xc_func.SpinPol], nn, dptr(_f64(dVHart_Grid)), px, dptr(vna), pv))
+
+
+def _matrix_elements(spin, ucell, Orbs_Grid, Vpot_Grid, MPI_Hks):
+    n = _lib.NCHAN[spin]
+    pv, k1 = dptrs([_f64(Vpot_Grid[c]) for c in range(n)])
+    for c in range(n):
+        if MPI_Hks[c].size != ucell.Total_Hsize:
+            raise LCPError(_lib.LCP_EINVAL, "MPI_Hks size does not match Total_Hsize")
+    ph, k2 = dptrs([MPI_Hks[c] for c in range(n)])
+    check(lib.lcp_calc_matrix_elements(Orbs_Grid.ctx._h, ucell._h, Orbs_Grid._h, _lib.SPIN[spin], pv, ph))
+
+
+def Calc_MatrixElements_dVH_Vxc_off(ucell, Orbs_Grid, Vpot_Grid, MPI_Hks):
+    """src/Hamiltonian.jl:235-277."""
+    _matrix_elements("off", ucell, Orbs_Grid, Vpot_Grid, MPI_Hks)
+
+
+def Calc_MatrixElements_dVH_Vxc_on(ucell, Orbs_Grid, Vpot_Grid, MPI_Hks):
+    """src/Hamiltonian.jl:280-324."""
+    _matrix_elements("on", ucell, Orbs_Grid, Vpot_Grid, MPI_Hks)
+
+
+def Calc_MatrixElements_dVH_Vxc_nc(ucell, Orbs_Grid, Vpot_Grid, MPI_Hks):
+    """src/Hamiltonian.jl:327-380."""
+    _matrix_elements("nc", ucell, Orbs_Grid, Vpot_Grid, MPI_Hks)
+
+
+def Calc_EH1(SpinPol, GridVol, ADensity_Grid, Density_Grid, dVHart_Grid, ctx=None):
+    """src/Energy.jl:655-666."""
+    ctx = ctx or default_context()
+    s = _spin(SpinPol)
+    nr = 1 if s == "off" else 2
+    rho = [_f64(Density_Grid[c]) for c in range(nr)]
+    pr, keep = dptrs(rho)
+    out = ctypes.c_double()
+    ad = None if ADensity_Grid is None else _f64(ADensity_Grid)
+    check(lib.lcp_calc_eh1(ctx._h, _lib.SPIN[s], rho[0].size, float(GridVol), dptr(ad), pr, dptr(_f64(dVHart_Grid)),
+                           ctypes.byref(out)))
+    return out.value
+
+
+def Calc_EXC1(SpinPol, xc_type, system_grid, ADensity_Grid, PCCDensity_Grid, Density_Grid, ctx=None):
+    """src/Energy.jl:669-700; ``system_grid`` supplies GridVol (a UCell works)."""
+    ctx = ctx or default_context()
+    s = _spin(SpinPol)
+    nr = 1 if s == "off" else 2
+    rho = [_f64(Density_Grid[c]) for c in range(nr)]
+    pr, keep = dptrs(rho)
+    out = np.zeros(2)
+    ad = None if ADensity_Grid is None else _f64(ADensity_Grid)
+    pcc = None if PCCDensity_Grid is None else _f64(PCCDensity_Grid)
+    check(lib.lcp_calc_exc1(ctx._h, _lib.XC[xc_type.upper()], _lib.SPIN[s], rho[0].size, float(system_grid.GridVol),
+                            dptr(ad), dptr(pcc), pr, dptr(out)))
+    return out
+
+
+def Calc_Ngrid(Ecut, Latvecs):
+    """src/utils/Calc_Ngrid.jl:1-20."""
+    out = np.zeros(3, dtype=np.int32)
+    check(lib.lcp_calc_ngrid(float(Ecut), dptr(_f64(Latvecs).reshape(-1)), iptr(out)))
+    return tuple(int(x) for x in out)
+
+
+class GridStepJob:
+    """Device-resident SCF grid step: density from D, Poisson, xc, potential
+    (+ V_na), grid H and the FP64 energy terms, all on the GPU."""
+
+    def __init__(self, ucell, Orbs_Grid, SpinPol, xc_type, ADensity_Grid=None, PCCDensity_Grid=None, Vna_Grid=None):
+        self.ctx = Orbs_Grid.ctx
+        self.ucell = ucell
+        self.SpinPol = _spin(SpinPol)
+        self.nspin = _lib.NCHAN[self.SpinPol]
+        keep = [None if x is None else _f64(x) for x in (ADensity_Grid, PCCDensity_Grid, Vna_Grid)]
+        h = ctypes.c_void_p()
+        check(lib.lcp_job_create(self.ctx._h, ucell._h, Orbs_Grid._h, _lib.SPIN[self.SpinPol],
+                                 _lib.XC[xc_type.upper()], dptr(keep[0]), dptr(keep[1]), dptr(keep[2]),
+                                 ctypes.byref(h)))
+        self._h = h
+
+    def set_dm(self, DM):
+        p, keep = dptrs([_f64(DM[c]) for c in range(self.nspin)])
+        check(lib.lcp_job_set_dm(self.ctx._h, self._h, p))
+
+    def step(self):
+        check(lib.lcp_job_step(self.ctx._h, self._h))
+
+    def step_timed(self):
+        """One step with per-stage CUDA-event times (ms): density, Poisson,
+        xc+potential, energy sums, grid H, <D,H> + energy."""
+        out = np.zeros(6)
+        check(lib.lcp_job_step_timed(self.ctx._h, self._h, dptr(out)))
+        return out
+
+    def energies(self):
+        """[E_H1, EXC1[1], EXC1[2], sum_s <D_s, H_s>, E_grid]."""
+        out = np.zeros(5)
+        check(lib.lcp_job_energies(self.ctx._h, self._h, dptr(out)))
+        return out
+
+    def _get(self, fn, n):
+        outs = [np.zeros(n) for _ in range(self.nspin)]
+        p, keep = dptrs(outs)
+        check(fn(self.ctx._h, self._h, p))
+        return outs
+
+    def density(self):
+        return self._get(lib.lcp_job_get_density, self.ucell.NN)
+
+    def hks(self):
+        return self._get(lib.lcp_job_get_hks, self.ucell.Total_Hsize)
+
+    def vpot(self):
+        return self._get(lib.lcp_job_get_vpot, self.ucell.NN)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib.lcp_job_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass

@@ -1,0 +1,142 @@
+"""Seeded synthetic inputs for the grid-step workloads.
+
+* ``si2_primitive``: the plain small case -- Si diamond primitive cell
+  (a = 5.43 A, fcc vectors as examples/Si/Si.jl:5-10), Si7.0-s2p2d1 basis,
+  grid from Calc_Ngrid(150 Ry) = 24^3.
+* ``si64_supercell``: the precision-form cell -- 64-atom cubic Si
+  (2x2x2 conventional cells, a = 10.86 A), 13 orbitals per atom with
+  synthetic radial functions (sums of 3 Gaussians, exponents 0.2-3 bohr^-2,
+  smooth cutoff at 7 bohr) tabulated on a 1000-point log mesh, grid 96^3,
+  PSD density matrix with trace 256, smooth V_na with |G| < 3 bohr^-1 and
+  amplitude 0.5 Ha.
+
+Everything is generated from a seed with numpy; nothing is read from disk.
+"""
+import math
+
+import numpy as np
+
+from .pao import ANG_TO_BOHR, PAO
+
+DIAMOND_BASIS = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0],
+                          [.25, .25, .25], [.25, .75, .75], [.75, .25, .75], [.75, .75, .25]])
+
+
+def synthetic_species(seed, max_l=2, num_basis=(2, 2, 1), rc=7.0, nmesh=1000, r_lo=1e-4, r_hi=None):
+    """Radial functions R_lp(r) = sum_k c_k exp(-alpha_k r^2) r^l * (1-(r/rc)^2)^3,
+    alpha_k ~ U[0.2, 3], c_k ~ N(0,1), normalised (int R^2 r^2 dr = 1), zero beyond rc,
+    tabulated on a log mesh x = log r uniform in [log r_lo, log r_hi]."""
+    rng = np.random.default_rng(seed)
+    r_hi = r_hi if r_hi is not None else rc + 1.0
+    x = np.linspace(math.log(r_lo), math.log(r_hi), nmesh)
+    rv = np.exp(x)
+    fine = np.linspace(0.0, rc, 20001)
+    rwf = []
+    for l in range(max_l + 1):
+        row = []
+        for _ in range(num_basis[l]):
+            alpha = rng.uniform(0.2, 3.0, size=3)
+            c = rng.normal(size=3)
+
+            def f(r):
+                cut = np.where(r < rc, (1 - (r / rc) ** 2) ** 3, 0.0)
+                return (c[None, :] * np.exp(-alpha[None, :] * (r[:, None] ** 2))).sum(1) * r ** l * cut
+
+            norm = math.sqrt(np.trapezoid(f(fine) ** 2 * fine ** 2, fine))
+            row.append(f(rv) / norm)
+        rwf.append(row)
+    return PAO(max_l, list(num_basis), rv, rwf, Spe_PAO_XV=x, Spe_Atom_Cut1=rc)
+
+
+def si2_primitive():
+    """Lattice (rows), Cartesian positions (bohr) of the Si2 primitive cell."""
+    a = 5.43 * ANG_TO_BOHR
+    lat = np.array([[0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]]) * a
+    frac = np.array([[0, 0, 0], [0.25, 0.25, 0.25]])
+    return lat, frac @ lat
+
+
+def si_supercell(nrep=2, a_ang=5.43):
+    """Cubic diamond Si supercell of nrep^3 conventional cells (8*nrep^3 atoms)."""
+    a = a_ang * ANG_TO_BOHR
+    lat = np.eye(3) * a * nrep
+    pos = []
+    for i in range(nrep):
+        for j in range(nrep):
+            for k in range(nrep):
+                for b in DIAMOND_BASIS:
+                    pos.append((np.array([i, j, k]) + b) * a)
+    return lat, np.array(pos)
+
+
+def psd_density_matrices_oracle(ucell, seed, nspin=1, trace=256.0, nocc=None):
+    """Same matrices for a UCell whose pair list is ``pairs`` of (atom, jatom, cell)."""
+    class _View:
+        Total_NumOrbs = ucell.Total_NumOrbs
+        Total_Hsize = ucell.Total_Hsize
+        MPI_atom = np.array([p[0] for p in ucell.pairs])
+        MPI_natn = np.array([p[1] for p in ucell.pairs])
+        block_offset = ucell.block_offset
+    return psd_density_matrices(_View, seed, nspin, trace, nocc)
+
+
+def psd_density_matrices(ucell, seed, nspin=1, trace=256.0, nocc=None):
+    """Flat pair-block density matrices D(i,j,R) = M[i-block, j-block] of a
+    seeded PSD M = C C^T (the Gamma-point Bloch sum), scaled to Tr(M) = trace.
+
+    Blocks follow the reference layout: for pair (atom, jatom), entry
+    a*NO(jatom) + b holds D between orbital a of atom and b of jatom."""
+    rng = np.random.default_rng(seed)
+    no = np.asarray(ucell.Total_NumOrbs, dtype=np.int64)
+    off = np.concatenate([[0], np.cumsum(no)])
+    norb = int(off[-1])
+    nocc = nocc or max(1, norb // 4)
+    out = []
+    for _ in range(nspin):
+        C = rng.normal(size=(norb, nocc))
+        M = C @ C.T
+        M *= trace / np.trace(M)
+        dm = np.zeros(ucell.Total_Hsize)
+        for p, (a, b) in enumerate(zip(ucell.MPI_atom, ucell.MPI_natn)):
+            i, j = a - 1, b - 1
+            blk = M[off[i]:off[i + 1], off[j]:off[j + 1]]
+            dm[ucell.block_offset[p]:ucell.block_offset[p] + blk.size] = blk.reshape(-1)
+        out.append(dm)
+    return out
+
+
+def smooth_vna(ngrid, latvecs, seed, gmax=3.0, amplitude=0.5):
+    """Real field from Fourier modes with |G| < gmax, random phases,
+    scaled to max |V| = amplitude (Ha), C-order flat."""
+    rng = np.random.default_rng(seed)
+    N1, N2, N3 = ngrid
+    rec = 2 * np.pi * np.linalg.inv(np.asarray(latvecs, float).T)
+
+    def sf(n):
+        i = np.arange(n)
+        return np.where(i < n // 2, i, i - n)
+
+    s1, s2, s3 = np.meshgrid(sf(N1), sf(N2), sf(N3), indexing="ij")
+    G = s1[..., None] * rec[0] + s2[..., None] * rec[1] + s3[..., None] * rec[2]
+    mask = np.linalg.norm(G, axis=-1) < gmax
+    coef = np.zeros((N1, N2, N3), dtype=np.complex128)
+    n = int(mask.sum())
+    coef[mask] = rng.normal(size=n) * np.exp(2j * np.pi * rng.uniform(size=n))
+    coef[0, 0, 0] = 0.0
+    v = np.real(np.fft.ifftn(coef))
+    v *= amplitude / np.max(np.abs(v))
+    return np.ascontiguousarray(v.reshape(-1))
+
+
+def si64_workload(seed=1234, ngrid=(96, 96, 96), nrep=2):
+    """The 64-atom precision-form workload; returns a dict of host inputs."""
+    lat, pos = si_supercell(nrep)
+    natom = pos.shape[0]
+    pao = synthetic_species(seed)
+    return {
+        "name": "si%d_cubic_%dx%dx%d" % (natom, *ngrid),
+        "latvecs": lat, "gxyz": pos, "natom": natom, "atom2spe": [1] * natom,
+        "cut": [7.0] * natom, "ngrid": tuple(ngrid), "origin": [0.0, 0.0, 0.0],
+        "numorbs": [pao.Spe_Total_NumOrbs] * natom, "paos": [pao],
+        "vna_seed": seed + 1, "dm_seed": seed + 2, "trace": 256.0,
+    }
