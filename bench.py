@@ -247,7 +247,10 @@ def run_ours(args):
     wl = si64_workload()
     ctx = L.Context(local)
     u, orbs, dm, vna, t_geom, t_tab = build_workload(ctx, wl)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the library launches on it and the
+    # CUDA events below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
     # FP64 reference energy of this step (the drop-in), for the error of other forms

@@ -50,11 +50,16 @@ __global__ void __launch_bounds__(kPairThreads) density_pairs_kernel(DevGeom g, 
     const int64_t bp = pr.boff_p[q], bq = pr.boff_q[q];
     const bool self = pr.self[q] != 0;
     __syncthreads();
-    for (int e = threadIdx.x; e < noi * noj; e += blockDim.x) {
-      const int a = e / noj, b = e - a * noj;
+    // the whole NOMAX x NOMAX tile is written (zeros outside NOi x NOj): the
+    // contraction below reads every column, multiplying the padding by zero
+    for (int e = threadIdx.x; e < NOMAX * NOMAX; e += blockDim.x) {
+      const int a = e / NOMAX, b = e - a * NOMAX;
       for (int s = 0; s < nspin; ++s) {
-        double v = dm.c[s][bp + (int64_t)a * noj + b];
-        if (!self) v += dm.c[s][bq + (int64_t)b * noi + a];
+        double v = 0.0;
+        if (a < noi && b < noj) {
+          v = dm.c[s][bp + (int64_t)a * noj + b];
+          if (!self) v += dm.c[s][bq + (int64_t)b * noi + a];
+        }
         Ds[s][a * NOMAX + b] = (T)v;
       }
     }
