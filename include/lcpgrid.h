@@ -210,6 +210,10 @@ lcp_status lcp_job_get_vpot(lcp_ctx* ctx, lcp_job* job, double* const* vpot);
 /* Measured FP64 FMA throughput of the device (TFLOP/s), a roofline denominator
  * for the FP64 contractions. */
 lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops);
+/* Tensor-core self-test: d[128 x n] = bf16(a[128 x k]) * bf16(b[n x k])^T with the
+ * operands staged K-major or MN-major (row-major host inputs, FP32 result). */
+lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t n, int32_t k,
+                           const float* a, const float* b, float* d);
 
 #ifdef __cplusplus
 }

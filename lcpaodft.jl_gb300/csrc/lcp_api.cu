@@ -1044,6 +1044,32 @@ static lcp_status job_get(lcp_ctx* ctx, lcp_job* job, DBuf* src, int64_t n, doub
   return LCP_OK;
 }
 
+lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t n, int32_t k,
+                           const float* a, const float* b, float* d) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!a || !b || !d) return fail(LCP_EINVAL, "NULL argument");
+  if (n < 16 || n > 256 || n % 16 || k < 16 || k > 64 || k % 16) return fail(LCP_EINVAL, "N in 16..256, K in 16..64, multiples of 16");
+  DBuf da, db, dd, dst;
+  API_CUDA(da.ensure(128 * k * sizeof(float)), "alloc");
+  API_CUDA(db.ensure((size_t)n * k * sizeof(float)), "alloc");
+  API_CUDA(dd.ensure((size_t)128 * n * sizeof(float)), "alloc");
+  API_CUDA(dst.ensure(sizeof(int)), "alloc");
+  API_CUDA(cudaMemsetAsync(dst.p, 0, sizeof(int), ctx->stream), "memset");
+  API_CUDA(cudaMemcpyAsync(da.p, a, 128 * k * sizeof(float), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  API_CUDA(cudaMemcpyAsync(db.p, b, (size_t)n * k * sizeof(float), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  API_CUDA(lcp::launch_tc_selftest(da.as<float>(), db.as<float>(), dd.as<float>(), n, k, a_mn_major, b_mn_major,
+                                   dst.as<int>(), ctx->stream),
+           "tc selftest");
+  ctx->launches++;
+  int st = 0;
+  API_CUDA(cudaMemcpyAsync(&st, dst.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaMemcpyAsync(d, dd.p, (size_t)128 * n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "tc selftest");
+  if (st) return fail(st, "tensor-core self-test: MMA completion wait timed out");
+  return LCP_OK;
+}
+
 lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;

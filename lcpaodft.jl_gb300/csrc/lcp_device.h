@@ -98,5 +98,7 @@ cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const do
                            double* partials, double* out, cudaStream_t st);
 constexpr int kReduceBlocks = 1024;
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
+cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int K, int a_mn, int b_mn,
+                               int* status, cudaStream_t st);
 
 }  // namespace lcp

@@ -92,6 +92,7 @@ _SIGS = {
     "lcp_job_get_hks": ([_vp, _vp, _ppd], _i32),
     "lcp_job_get_vpot": ([_vp, _vp, _ppd], _i32),
     "lcp_probe_fp64_tflops": ([_vp, _pd], _i32),
+    "lcp_tc_selftest": ([_vp, _i32, _i32, _i32, _i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], _i32),
 }
 
 for _name, (_args, _res) in _SIGS.items():

@@ -53,6 +53,15 @@ class Context:
         check(lib.lcp_probe_fp64_tflops(self._h, ctypes.byref(out)))
         return out.value
 
+    def tc_selftest(self, a, b, a_mn=False, b_mn=False):
+        """d = bf16(a) @ bf16(b).T on the tensor cores (a: 128 x k, b: n x k)."""
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        b = np.ascontiguousarray(b, dtype=np.float32)
+        d = np.zeros((128, b.shape[0]), dtype=np.float32)
+        check(lib.lcp_tc_selftest(self._h, int(a_mn), int(b_mn), b.shape[0], a.shape[1], a.ctypes.data,
+                                  b.ctypes.data, d.ctypes.data))
+        return d
+
     @property
     def launch_count(self):
         return int(lib.lcp_ctx_launch_count(self._h))
