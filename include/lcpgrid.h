@@ -112,6 +112,10 @@ enum {
 lcp_status lcp_ucell_get_int(const lcp_ucell* ucell, int32_t field, int64_t index,
                              int32_t* dst, int64_t count);
 lcp_status lcp_ucell_get_atv(const lcp_ucell* ucell, double* dst /* [ncell*3] */);
+/* Grid-brick tiling of the tensor-core path: info[12] = brick dims (3), bricks
+ * per axis (3), points per brick, bricks, table blocks, max atom images of a
+ * brick, total images, image pairs that are neighbour pairs. */
+lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info);
 
 /* Calc_Ngrid(Ecut, Latvecs) -- src/utils/Calc_Ngrid.jl:1-76 */
 lcp_status lcp_calc_ngrid(double ecut, const double* latvecs, int32_t* ngrid_out);
@@ -211,9 +215,10 @@ lcp_status lcp_job_get_vpot(lcp_ctx* ctx, lcp_job* job, double* const* vpot);
  * for the FP64 contractions. */
 lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops);
 /* Tensor-core self-test: d[128 x n] = bf16(a[128 x k]) * bf16(b[n x k])^T with the
- * operands staged K-major or MN-major (row-major host inputs, FP32 result). */
-lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t n, int32_t k,
-                           const float* a, const float* b, float* d);
+ * operands staged K-major or MN-major, core matrices ordered K-groups outer
+ * (order 0) or MN-groups outer (order 1); row-major host inputs, FP32 result. */
+lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t order, int32_t n,
+                           int32_t k, const float* a, const float* b, float* d);
 
 #ifdef __cplusplus
 }

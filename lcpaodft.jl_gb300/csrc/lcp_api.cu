@@ -101,6 +101,7 @@ struct lcp_ctx {
   std::map<std::tuple<int, int, int>, FftPlans> plans;
   // workspaces of the host-buffer entry points
   DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
+  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp;
   ~lcp_ctx() {
     cudaSetDevice(device);
     for (auto& kv : plans) {
@@ -124,6 +125,14 @@ struct lcp_orbs {
   DBuf phi, dphi[3], phi32;
   DBuf p_atom, p_jatom, p_boffp, p_boffq, p_self, p_lensoff, p_g1, p_g2, it_pair, it_start, it_count;
   int64_t table_elems = 0;
+  // brick tiling and split-BF16 tables of the tensor-core path (built on first use)
+  bool bricks_ready = false;
+  lcp::Bricks bricks;
+  lcp::TcBrickGeom bgeom{};
+  DBuf b_code, b_imgoff, b_imgblk, b_taboff, b_tabpair, b_tab, b_tabslot, b_slotbase, b_redoff, b_redslot;
+  DBuf o_atom, o_jatom, o_boff, o_partner;  // ordered pair list
+  DBuf b_scale, b_tmp;                       // fixed-point scale of the tables: [S_phi, 1/S_phi]
+  double phi_scale = 1.0;
 };
 
 struct lcp_job {
@@ -191,11 +200,95 @@ lcp_status ensure_phi32(lcp_ctx* ctx, lcp_orbs* o) {
   return LCP_OK;
 }
 
+// Brick tiling, split-BF16 orbital tables and the ordered pair list of the
+// tensor-core path, built once per tabulation.
+lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
+  if (o->bricks_ready) return LCP_OK;
+  const lcp::UCell& u = o->ucell->u;
+  if (o->max_no > 16) return fail(LCP_ENOTSUP, "the tensor-core path supports up to 16 orbitals per atom");
+  lcp::Bricks& b = o->bricks;
+  std::string err = lcp::build_bricks(u, b);
+  if (!err.empty()) return fail(LCP_EINVAL, err);
+  if (b.max_images > 32)
+    return fail(LCP_ENOTSUP, "a grid brick is touched by " + std::to_string(b.max_images) +
+                                 " atom images; the tensor-core path supports 32");
+  cudaStream_t st = ctx->stream;
+  API_CUDA(upload(o->b_code, b.point_code, st), "upload");
+  API_CUDA(upload(o->b_imgoff, b.img_off, st), "upload");
+  API_CUDA(upload(o->b_imgblk, b.img_block, st), "upload");
+  API_CUDA(upload(o->b_taboff, b.tab_off, st), "upload");
+  API_CUDA(upload(o->b_tabpair, b.tab_pair, st), "upload");
+  API_CUDA(upload(o->b_tabslot, b.tab_slot, st), "upload");
+  API_CUDA(upload(o->b_slotbase, b.slot_base, st), "upload");
+  API_CUDA(upload(o->b_redoff, b.red_off, st), "upload");
+  API_CUDA(upload(o->b_redslot, b.red_slot, st), "upload");
+  std::vector<int64_t> boff(u.block_off.begin(), u.block_off.end());
+  API_CUDA(upload(o->o_atom, u.pair_atom, st), "upload");
+  API_CUDA(upload(o->o_jatom, u.pair_jatom, st), "upload");
+  API_CUDA(upload(o->o_boff, boff, st), "upload");
+  API_CUDA(upload(o->o_partner, u.partner, st), "upload");
+  API_CUDA(o->b_tab.ensure((size_t)std::max<int64_t>(b.nblocks, 1) * 6144 * 2), "brick table alloc");
+  API_CUDA(o->b_scale.ensure(2 * sizeof(double)), "alloc");
+  API_CUDA(o->b_tmp.ensure(sizeof(unsigned long long)), "alloc");
+  API_CUDA(lcp::launch_absmax_scale(o->phi.as<double>(), o->table_elems, 1.0, o->b_tmp.as<unsigned long long>(),
+                                    o->b_scale.as<double>(), st),
+           "table scale");
+  API_CUDA(lcp::launch_brick_table(o->phi.as<double>(), o->geom.phi_off, o->geom.numorbs, o->geom.sph_off, u.natom,
+                                   o->b_code.as<int32_t>(), (int64_t)b.point_code.size(), o->b_scale.as<double>(),
+                                   o->b_tab.as<__nv_bfloat16>(), b.nblocks, st),
+           "brick table");
+  ctx->launches += 3;
+  API_CUDA(cudaMemcpyAsync(&o->phi_scale, o->b_scale.p, sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+  lcp::TcBrickGeom& g = o->bgeom;
+  g.nbricks = b.nbricks;
+  for (int d = 0; d < 3; ++d) {
+    g.bdim[d] = b.bdim[d];
+    g.nb[d] = b.nb[d];
+    g.ngrid[d] = u.ngrid[d];
+  }
+  g.npts = b.npts;
+  g.max_images = b.max_images;
+  g.img_off = o->b_imgoff.as<int64_t>();
+  g.img_block = o->b_imgblk.as<int32_t>();
+  g.tab_off = o->b_taboff.as<int64_t>();
+  g.tab_pair = o->b_tabpair.as<int32_t>();
+  API_CUDA(cudaStreamSynchronize(st), "bricks");
+  o->bricks_ready = true;
+  return LCP_OK;
+}
+
+lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, const double* const* dm,
+                             double* const* rho) {
+  lcp_orbs* o = const_cast<lcp_orbs*>(orbs_c);
+  lcp_status s = ensure_bricks(ctx, o);
+  if (s) return s;
+  const lcp::UCell& u = o->ucell->u;
+  API_CUDA(ctx->w_dsym.ensure((size_t)(u.nloop + 1) * 768 * 2), "dsym alloc");
+  API_CUDA(ctx->w_dscale.ensure(2 * sizeof(double)), "alloc");
+  API_CUDA(ctx->w_dtmp.ensure(sizeof(unsigned long long)), "alloc");
+  for (int c = 0; c < nspin; ++c) {
+    // |D + D'^T| <= 2 max|D|: the fixed-point scale of the symmetrised blocks
+    API_CUDA(lcp::launch_absmax_scale(dm[c], u.total_hsize, 2.0, ctx->w_dtmp.as<unsigned long long>(),
+                                      ctx->w_dscale.as<double>(), ctx->stream),
+             "dm scale");
+    API_CUDA(lcp::launch_dsym(u.nloop, o->o_atom.as<int32_t>(), o->o_jatom.as<int32_t>(), o->o_boff.as<int64_t>(),
+                              o->o_partner.as<int32_t>(), o->geom.numorbs, dm[c], ctx->w_dscale.as<double>(),
+                              ctx->w_dsym.as<__nv_bfloat16>(), ctx->stream),
+             "dsym");
+    API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale,
+                                    ctx->w_dsym.as<__nv_bfloat16>(), ctx->w_dscale.as<double>(), u.nloop, rho[c],
+                                    ctx->w_status.as<int>(), ctx->stream),
+             "density_tc");
+    ctx->launches += 4;
+  }
+  return LCP_OK;
+}
+
 lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const double* const* dm, double* const* rho,
                           int64_t nn) {
-  for (int s = 0; s < nspin; ++s) API_CUDA(cudaMemsetAsync(rho[s], 0, nn * sizeof(double), ctx->stream), "memset");
   int prec = ctx->precision;
-  if (prec == LCP_PREC_BF16X3) return fail(LCP_ENOTSUP, "BF16x3 contractions are not available in this build");
+  if (prec == LCP_PREC_BF16X3) return density_tc_device(ctx, orbs, nspin, dm, rho);
+  for (int s = 0; s < nspin; ++s) API_CUDA(cudaMemsetAsync(rho[s], 0, nn * sizeof(double), ctx->stream), "memset");
   if (prec == LCP_PREC_FP32) {
     lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
     if (s != LCP_OK) return s;
@@ -207,11 +300,44 @@ lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const d
   return LCP_OK;
 }
 
+// Error word written by kernels whose bounded waits gave up; read and cleared.
+lcp_status device_status(lcp_ctx* ctx) {
+  int st = 0;
+  API_CUDA(cudaMemcpy(&st, ctx->w_status.p, sizeof(int), cudaMemcpyDeviceToHost), "status");
+  if (st) {
+    cudaMemset(ctx->w_status.p, 0, sizeof(int));
+    return fail(st, "a device wait timed out (tensor-core completion)");
+  }
+  return LCP_OK;
+}
+
+lcp_status hamiltonian_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nch, const double* const* vpot,
+                                 double* const* hks) {
+  lcp_orbs* o = const_cast<lcp_orbs*>(orbs_c);
+  lcp_status s = ensure_bricks(ctx, o);
+  if (s) return s;
+  const lcp::UCell& u = o->ucell->u;
+  const int64_t nslots = o->bricks.slot_base.back();
+  API_CUDA(ctx->w_hscratch.ensure((size_t)std::max<int64_t>(nslots, 1) * 256 * sizeof(float)), "H scratch alloc");
+  for (int c = 0; c < nch; ++c) {
+    API_CUDA(lcp::launch_hamiltonian_tc(o->bgeom, o->b_tabslot.as<int32_t>(), o->b_slotbase.as<int64_t>(),
+                                        o->b_tab.as<__nv_bfloat16>(), o->phi_scale, vpot[c],
+                                        ctx->w_hscratch.as<float>(), ctx->w_status.as<int>(), ctx->stream),
+             "hamiltonian_tc");
+    API_CUDA(lcp::launch_h_reduce(o->pairs.nu, o->b_redoff.as<int64_t>(), o->b_redslot.as<int64_t>(),
+                                  ctx->w_hscratch.as<float>(), o->pairs, o->geom.numorbs, u.gridvol, hks[c],
+                                  ctx->stream),
+             "h_reduce");
+    ctx->launches += 2;
+  }
+  return LCP_OK;
+}
+
 lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const double* const* vpot,
                               double* const* hks, int64_t hsize) {
-  for (int c = 0; c < nch; ++c) API_CUDA(cudaMemsetAsync(hks[c], 0, hsize * sizeof(double), ctx->stream), "memset");
   int prec = ctx->precision;
-  if (prec == LCP_PREC_BF16X3) return fail(LCP_ENOTSUP, "BF16x3 contractions are not available in this build");
+  if (prec == LCP_PREC_BF16X3) return hamiltonian_tc_device(ctx, orbs, nch, vpot, hks);
+  for (int c = 0; c < nch; ++c) API_CUDA(cudaMemsetAsync(hks[c], 0, hsize * sizeof(double), ctx->stream), "memset");
   if (prec == LCP_PREC_FP32) {
     lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
     if (s != LCP_OK) return s;
@@ -320,6 +446,26 @@ lcp_status lcp_ucell_get_int(const lcp_ucell* ucell, int32_t field, int64_t inde
   return LCP_OK;
 }
 
+lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info) {
+  if (!ucell || !info) return fail(LCP_EINVAL, "NULL argument");
+  lcp::Bricks b;
+  std::string err = lcp::build_bricks(ucell->u, b);
+  if (!err.empty()) return fail(LCP_EINVAL, err);
+  for (int d = 0; d < 3; ++d) {
+    info[d] = b.bdim[d];
+    info[3 + d] = b.nb[d];
+  }
+  info[6] = b.npts;
+  info[7] = b.nbricks;
+  info[8] = b.nblocks;
+  info[9] = b.max_images;
+  int64_t paired = 0;
+  for (auto v : b.tab_pair) paired += v >= 0;
+  info[10] = (int64_t)b.img_block.size();
+  info[11] = paired;
+  return LCP_OK;
+}
+
 lcp_status lcp_ucell_get_atv(const lcp_ucell* ucell, double* dst) {
   if (!ucell || !dst) return fail(LCP_EINVAL, "NULL argument");
   std::memcpy(dst, ucell->u.atv.data(), ucell->u.atv.size() * sizeof(double));
@@ -378,6 +524,8 @@ lcp_status lcp_ctx_create(int32_t device, lcp_ctx** out) {
   c->device = device;
   API_CUDA(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking), "cudaStreamCreate");
   c->stream = c->own;
+  API_CUDA(c->w_status.ensure(sizeof(int)), "status alloc");
+  API_CUDA(cudaMemset(c->w_status.p, 0, sizeof(int)), "memset");
   *out = c.release();
   return LCP_OK;
 }
@@ -612,7 +760,7 @@ lcp_status lcp_set_density_grid(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_
   for (int c = 0; c < ns; ++c)
     API_CUDA(cudaMemcpyAsync(density_grid[c], drho[c], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
   API_CUDA(cudaStreamSynchronize(ctx->stream), "density");
-  return LCP_OK;
+  return device_status(ctx);
 }
 
 lcp_status lcp_calc_matrix_elements(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs, int32_t spinpol,
@@ -639,7 +787,7 @@ lcp_status lcp_calc_matrix_elements(lcp_ctx* ctx, const lcp_ucell* ucell, const 
   for (int c = 0; c < nc; ++c)
     API_CUDA(cudaMemcpyAsync(hks[c], dh[c], hs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
   API_CUDA(cudaStreamSynchronize(ctx->stream), "hamiltonian");
-  return LCP_OK;
+  return device_status(ctx);
 }
 
 // ---------------------------------------------------------------- Poisson / xc / energies (host buffers)
@@ -1029,7 +1177,7 @@ lcp_status lcp_job_energies(lcp_ctx* ctx, lcp_job* job, double* out5) {
   API_CUDA(cudaMemcpyAsync(out5, job->scal.as<double>() + 8, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
            "D2H");
   API_CUDA(cudaStreamSynchronize(ctx->stream), "energies");
-  return LCP_OK;
+  return device_status(ctx);
 }
 
 static lcp_status job_get(lcp_ctx* ctx, lcp_job* job, DBuf* src, int64_t n, double* const* dst) {
@@ -1044,8 +1192,8 @@ static lcp_status job_get(lcp_ctx* ctx, lcp_job* job, DBuf* src, int64_t n, doub
   return LCP_OK;
 }
 
-lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t n, int32_t k,
-                           const float* a, const float* b, float* d) {
+lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t order, int32_t n,
+                           int32_t k, const float* a, const float* b, float* d) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;
   if (!a || !b || !d) return fail(LCP_EINVAL, "NULL argument");
@@ -1059,7 +1207,7 @@ lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major,
   API_CUDA(cudaMemcpyAsync(da.p, a, 128 * k * sizeof(float), cudaMemcpyHostToDevice, ctx->stream), "H2D");
   API_CUDA(cudaMemcpyAsync(db.p, b, (size_t)n * k * sizeof(float), cudaMemcpyHostToDevice, ctx->stream), "H2D");
   API_CUDA(lcp::launch_tc_selftest(da.as<float>(), db.as<float>(), dd.as<float>(), n, k, a_mn_major, b_mn_major,
-                                   dst.as<int>(), ctx->stream),
+                                   order, dst.as<int>(), ctx->stream),
            "tc selftest");
   ctx->launches++;
   int st = 0;

@@ -1,6 +1,7 @@
 // Device-side structures and kernel launchers shared by the .cu files.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -98,7 +99,33 @@ cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const do
                            double* partials, double* out, cudaStream_t st);
 constexpr int kReduceBlocks = 1024;
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
+// Device copy of the brick tiling (see struct Bricks in lcp_internal.h).
+struct TcBrickGeom {
+  int64_t nbricks;
+  int32_t bdim[3], nb[3], ngrid[3];
+  int32_t npts, max_images;
+  const int64_t* img_off;
+  const int32_t* img_block;
+  const int64_t* tab_off;
+  const int32_t* tab_pair;
+};
+cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,
+                                cudaStream_t st);
+cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const int32_t* numorbs,
+                               const int64_t* sph_off, int natom, const int32_t* point_code, int64_t npoints,
+                               const double* scale, __nv_bfloat16* tab, int64_t nblocks, cudaStream_t st);
+cudaError_t launch_dsym(int nloop, const int32_t* pair_atom, const int32_t* pair_jatom, const int64_t* boff,
+                        const int32_t* partner, const int32_t* numorbs, const double* dm, const double* scale,
+                        __nv_bfloat16* out, cudaStream_t st);
+cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
+                              const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
+                              int* status, cudaStream_t st);
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int K, int a_mn, int b_mn,
-                               int* status, cudaStream_t st);
+                               int order, int* status, cudaStream_t st);
+cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
+                                  const __nv_bfloat16* tab, double phi_scale, const double* vpot, float* scratch,
+                                  int* status, cudaStream_t st);
+cudaError_t launch_h_reduce(int64_t nu, const int64_t* red_off, const int64_t* red_slot, const float* scratch,
+                            const DevPairs& pr, const int32_t* numorbs, double dv, double* H, cudaStream_t st);
 
 }  // namespace lcp

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <map>
 #include <thread>
+#include <tuple>
 
 #include "lcp_internal.h"
 
@@ -461,6 +462,142 @@ std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t 
     int p = u.uniq_pair[q];
     u.numolg[p] = (int64_t)ug1[q].size();
     u.numolg[u.partner[p]] = (int64_t)ug1[q].size();
+  }
+  return "";
+}
+
+std::string build_bricks(const UCell& u, Bricks& b) {
+  // brick shape: divisors of Ngrid up to 8 per axis, the largest point count
+  // <= 128, then the most cubic, then the longest innermost side
+  int best[3] = {1, 1, 1};
+  long best_score = -1;
+  for (int b0 = 1; b0 <= 8; ++b0) {
+    if (u.ngrid[0] % b0) continue;
+    for (int b1 = 1; b1 <= 8; ++b1) {
+      if (u.ngrid[1] % b1) continue;
+      for (int b2 = 1; b2 <= 8; ++b2) {
+        if (u.ngrid[2] % b2) continue;
+        int prod = b0 * b1 * b2;
+        if (prod > 128) continue;
+        int mx = std::max(b0, std::max(b1, b2)), mn = std::min(b0, std::min(b1, b2));
+        long score = (long)prod * 10000 - (mx - mn) * 10 + b2;
+        if (score > best_score) {
+          best_score = score;
+          best[0] = b0;
+          best[1] = b1;
+          best[2] = b2;
+        }
+      }
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    b.bdim[d] = best[d];
+    b.nb[d] = u.ngrid[d] / best[d];
+  }
+  b.npts = best[0] * best[1] * best[2];
+  b.nbricks = (int64_t)b.nb[0] * b.nb[1] * b.nb[2];
+  const int64_t npoints = u.sphere_off.empty() ? 0 : u.sphere_off.back();
+  b.point_code.assign(npoints, 0);
+  b.block_atom.clear();
+  struct Img {
+    int32_t atom, block, r0, r1, r2;
+  };
+  std::vector<std::vector<Img>> per_brick(b.nbricks);
+  for (int a = 0; a < u.natom; ++a) {
+    std::map<std::tuple<int, int, int>, int32_t> blocks;
+    for (int64_t k = u.sphere_off[a]; k < u.sphere_off[a + 1]; ++k) {
+      int x, y, z;
+      unrolled(u, u.glist[k], u.clist[k], x, y, z);
+      int c0 = floordiv(x, b.bdim[0]), c1 = floordiv(y, b.bdim[1]), c2 = floordiv(z, b.bdim[2]);
+      auto key = std::make_tuple(c0, c1, c2);
+      auto it = blocks.find(key);
+      int32_t blk;
+      if (it == blocks.end()) {
+        blk = (int32_t)b.block_atom.size();
+        b.block_atom.push_back(a);
+        blocks.emplace(key, blk);
+        int h0 = c0 - floordiv(c0, b.nb[0]) * b.nb[0];
+        int h1 = c1 - floordiv(c1, b.nb[1]) * b.nb[1];
+        int h2 = c2 - floordiv(c2, b.nb[2]) * b.nb[2];
+        int64_t hb = ((int64_t)h0 * b.nb[1] + h1) * b.nb[2] + h2;
+        per_brick[hb].push_back({a, blk, floordiv(c0, b.nb[0]), floordiv(c1, b.nb[1]), floordiv(c2, b.nb[2])});
+      } else {
+        blk = it->second;
+      }
+      int l0 = x - c0 * b.bdim[0], l1 = y - c1 * b.bdim[1], l2 = z - c2 * b.bdim[2];
+      int slot = (l0 * b.bdim[1] + l1) * b.bdim[2] + l2;
+      b.point_code[k] = blk * 128 + slot;
+    }
+  }
+  b.nblocks = (int64_t)b.block_atom.size();
+  // ordered pair of (atom, jatom, cell)
+  std::map<std::tuple<int, int, int>, int32_t> pair_of;
+  for (int p = 0; p < u.nloop; ++p) pair_of[{u.pair_atom[p], u.pair_jatom[p], u.pair_cell[p]}] = p;
+  const int C = u.cpycell, n = 2 * C + 1;
+  b.img_off.assign(b.nbricks + 1, 0);
+  b.tab_off.assign(b.nbricks + 1, 0);
+  b.img_block.clear();
+  b.img_atom.clear();
+  b.tab_pair.clear();
+  b.max_images = 0;
+  for (int64_t hb = 0; hb < b.nbricks; ++hb) {
+    auto& v = per_brick[hb];
+    std::sort(v.begin(), v.end(), [](const Img& x, const Img& y) {
+      return std::make_tuple(x.atom, x.r0, x.r1, x.r2) < std::make_tuple(y.atom, y.r0, y.r1, y.r2);
+    });
+    const int m = (int)v.size();
+    b.max_images = std::max(b.max_images, m);
+    for (auto& im : v) {
+      b.img_block.push_back(im.block);
+      b.img_atom.push_back(im.atom);
+    }
+    b.img_off[hb + 1] = (int64_t)b.img_block.size();
+    // image s = atom shifted by -R_s; pair (atom_s, atom_t, R_s - R_t)
+    for (int s = 0; s < m; ++s)
+      for (int t = 0; t < m; ++t) {
+        int d0 = v[s].r0 - v[t].r0, d1 = v[s].r1 - v[t].r1, d2 = v[s].r2 - v[t].r2;
+        int32_t pair = -1;
+        if (std::abs(d0) <= C && std::abs(d1) <= C && std::abs(d2) <= C) {
+          int cell = u.ratv[((size_t)(d0 + C) * n + (d1 + C)) * n + (d2 + C)];
+          auto it = pair_of.find({v[s].atom, v[t].atom, cell});
+          if (it != pair_of.end()) pair = it->second;
+        }
+        b.tab_pair.push_back(pair);
+      }
+    b.tab_off[hb + 1] = (int64_t)b.tab_pair.size();
+  }
+  // grid-H slots: (s <= t) image pairs of each brick that are neighbour pairs
+  std::vector<int32_t> fold(u.nloop, -1);
+  for (size_t q = 0; q < u.uniq_pair.size(); ++q) {
+    fold[u.uniq_pair[q]] = (int32_t)q;
+    fold[u.partner[u.uniq_pair[q]]] = (int32_t)q;
+  }
+  b.tab_slot.assign(b.tab_pair.size(), -1);
+  b.slot_base.assign(b.nbricks + 1, 0);
+  std::vector<std::vector<int64_t>> per_fold(u.uniq_pair.size());
+  int64_t gslot = 0;
+  for (int64_t hb = 0; hb < b.nbricks; ++hb) {
+    const int m = (int)(b.img_off[hb + 1] - b.img_off[hb]);
+    const int64_t t0 = b.tab_off[hb];
+    b.slot_base[hb] = gslot;
+    int local = 0;
+    for (int s = 0; s < m; ++s)
+      for (int t = s; t < m; ++t) {
+        const int32_t p = b.tab_pair[t0 + s * m + t];
+        if (p < 0) continue;
+        b.tab_slot[t0 + s * m + t] = local++;
+        const int32_t q = fold[p];
+        per_fold[q].push_back(gslot * 2 + (u.uniq_pair[q] == p ? 0 : 1));
+        ++gslot;
+      }
+  }
+  b.slot_base[b.nbricks] = gslot;
+  b.red_off.assign(u.uniq_pair.size() + 1, 0);
+  b.red_slot.clear();
+  b.red_slot.reserve(gslot);
+  for (size_t q = 0; q < per_fold.size(); ++q) {
+    b.red_slot.insert(b.red_slot.end(), per_fold[q].begin(), per_fold[q].end());
+    b.red_off[q + 1] = (int64_t)b.red_slot.size();
   }
   return "";
 }

@@ -63,6 +63,35 @@ struct UCell {
   int64_t nn() const { return (int64_t)ngrid[0] * ngrid[1] * ngrid[2]; }
 };
 
+// Grid bricks for the tensor-core contractions.  The home cell is tiled by
+// bricks of bdim points (bdim[d] divides Ngrid[d], at most 128 points); the
+// point slot of a brick-local coordinate l is (l0*bdim1 + l1)*bdim2 + l2.
+// Each atom's sphere is covered by "blocks": the bricks of the unrolled
+// lattice it touches, each holding the atom's orbitals on the brick's points
+// (zero outside the sphere).  A home brick sees every block whose brick maps
+// to it, i.e. every atom image touching it.
+struct Bricks {
+  int32_t bdim[3] = {1, 1, 1};
+  int32_t nb[3] = {1, 1, 1};       // home bricks per axis
+  int32_t npts = 1;                // points per brick
+  int64_t nbricks = 0;
+  int64_t nblocks = 0;
+  int32_t max_images = 0;
+  std::vector<int32_t> block_atom;   // [nblocks]
+  std::vector<int32_t> point_code;   // per sphere point: block*128 + slot
+  std::vector<int64_t> img_off;      // [nbricks+1]
+  std::vector<int32_t> img_block;    // block of each image of a home brick
+  std::vector<int32_t> img_atom;
+  std::vector<int64_t> tab_off;      // [nbricks+1] offsets of the m x m pair tables
+  std::vector<int32_t> tab_pair;     // ordered pair of images (s, t), -1 if none
+  // grid-H partial blocks: one per (brick, s <= t) image pair that is a pair
+  std::vector<int32_t> tab_slot;     // m x m per brick: slot within the brick, -1 if none
+  std::vector<int64_t> slot_base;    // [nbricks+1]
+  std::vector<int64_t> red_off;      // [n_unique+1] CSR of slots per folded pair
+  std::vector<int64_t> red_slot;     // global slot * 2 + (1 if the slot is the partner orientation)
+};
+std::string build_bricks(const UCell& u, Bricks& b);
+
 // Builds everything above; returns an error message or "".
 std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,
                         const int32_t* atom2spe, const double* gxyz, const double* cut,

@@ -64,6 +64,7 @@ _SIGS = {
     "lcp_ucell_get_info": ([_vp, ctypes.POINTER(lcp_ucell_info)], _i32),
     "lcp_ucell_get_int": ([_vp, _i32, _i64, _pi32, _i64], _i32),
     "lcp_ucell_get_atv": ([_vp, _pd], _i32),
+    "lcp_ucell_get_bricks": ([_vp, ctypes.POINTER(ctypes.c_int64)], _i32),
     "lcp_calc_ngrid": ([_dbl, _pd, _pi32], _i32),
     "lcp_ctx_create": ([_i32, ctypes.POINTER(_vp)], _i32),
     "lcp_ctx_destroy": ([_vp], None),
@@ -92,7 +93,8 @@ _SIGS = {
     "lcp_job_get_hks": ([_vp, _vp, _ppd], _i32),
     "lcp_job_get_vpot": ([_vp, _vp, _ppd], _i32),
     "lcp_probe_fp64_tflops": ([_vp, _pd], _i32),
-    "lcp_tc_selftest": ([_vp, _i32, _i32, _i32, _i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], _i32),
+    "lcp_tc_selftest": ([_vp, _i32, _i32, _i32, _i32, _i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+                        _i32),
 }
 
 for _name, (_args, _res) in _SIGS.items():

@@ -53,12 +53,12 @@ class Context:
         check(lib.lcp_probe_fp64_tflops(self._h, ctypes.byref(out)))
         return out.value
 
-    def tc_selftest(self, a, b, a_mn=False, b_mn=False):
+    def tc_selftest(self, a, b, a_mn=False, b_mn=False, order=0):
         """d = bf16(a) @ bf16(b).T on the tensor cores (a: 128 x k, b: n x k)."""
         a = np.ascontiguousarray(a, dtype=np.float32)
         b = np.ascontiguousarray(b, dtype=np.float32)
         d = np.zeros((128, b.shape[0]), dtype=np.float32)
-        check(lib.lcp_tc_selftest(self._h, int(a_mn), int(b_mn), b.shape[0], a.shape[1], a.ctypes.data,
+        check(lib.lcp_tc_selftest(self._h, int(a_mn), int(b_mn), int(order), b.shape[0], a.shape[1], a.ctypes.data,
                                   b.ctypes.data, d.ctypes.data))
         return d
 
@@ -175,6 +175,14 @@ class UCell:
     @property
     def NN(self):
         return int(np.prod(self.Ngrid))
+
+    def brick_info(self):
+        """Grid-brick tiling of the tensor-core path."""
+        out = (ctypes.c_int64 * 12)()
+        check(lib.lcp_ucell_get_bricks(self._h, out))
+        v = list(out)
+        return {"bdim": v[0:3], "nbricks_axis": v[3:6], "points": v[6], "bricks": v[7], "blocks": v[8],
+                "max_images": v[9], "images": v[10], "paired": v[11]}
 
     def Recvecs(self):
         """2*pi*inv(Latvecs') (src/Mixing/DFT_Mixing.jl:91)."""

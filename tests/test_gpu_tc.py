@@ -19,12 +19,128 @@ def ctx():
     return L.Context(0)
 
 
+@pytest.mark.parametrize("order", [0, 1])
 @pytest.mark.parametrize("a_mn,b_mn", [(0, 0), (1, 1), (0, 1), (1, 0)])
 @pytest.mark.parametrize("n,k", [(16, 16), (64, 32), (256, 64), (48, 48)])
-def test_tc_selftest(ctx, a_mn, b_mn, n, k):
+def test_tc_selftest(ctx, a_mn, b_mn, n, k, order):
     rng = np.random.default_rng(n * 100 + k)
     a = rng.normal(size=(128, k)).astype(np.float32)
     b = rng.normal(size=(n, k)).astype(np.float32)
-    d = ctx.tc_selftest(a, b, a_mn=bool(a_mn), b_mn=bool(b_mn))
+    d = ctx.tc_selftest(a, b, a_mn=bool(a_mn), b_mn=bool(b_mn), order=order)
     ref = bf16(a) @ bf16(b).T
     np.testing.assert_allclose(d, ref, rtol=0, atol=2e-5 * np.sqrt(k) * np.max(np.abs(ref)))
+
+
+def _si2(ctx):
+    from helpers import product_pao, si2_cell
+    lat, pos, ng = si2_cell()
+    u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
+    return u, L.Set_Orbitals_Grid([product_pao()], u, ctx)
+
+
+def _si64(ctx):
+    from lcpgrid.workloads import psd_density_matrices, si64_workload, smooth_vna
+    wl = si64_workload()
+    u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+                Total_NumOrbs=wl["numorbs"])
+    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx)
+    dm = psd_density_matrices(u, wl["dm_seed"], trace=wl["trace"])
+    vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
+    return u, orbs, dm, vna
+
+
+def _density(ctx, u, orbs, dm, precision, spin="off"):
+    n = {"off": 1, "on": 2}[spin]
+    rho = [np.zeros(u.NN) for _ in range(n)]
+    ctx.set_precision(precision)
+    try:
+        L.Set_Density_Grid(spin, u, orbs, dm, rho)
+    finally:
+        ctx.set_precision("fp64")
+    return rho
+
+
+# Split-BF16 bounds.  Every operand is quantised to 2^-24 of its power-of-two
+# scale and all nine part products are accumulated exactly, so the error is
+# the input quantisation: observed ~1e-6 of max|rho| / max|H| on these cells
+# (bounds below carry a 5x margin), electron count and <D,H> to ~4e-8.
+RHO_TOL = 5e-6
+H_TOL = 5e-6
+SUM_TOL = 2e-7
+
+
+def test_density_bf16x3_si2(ctx):
+    """Split-BF16 density (tcgen05) vs the FP64 drop-in on the Si2 24^3 cell."""
+    from test_gpu_parity import psd_dm
+    u, orbs = _si2(ctx)
+    for spin, n in (("off", 1), ("on", 2)):
+        dm = psd_dm(u, 77, nspin=n)
+        r64 = _density(ctx, u, orbs, dm, "fp64", spin)
+        rtc = _density(ctx, u, orbs, dm, "bf16x3", spin)
+        for c in range(n):
+            scale = np.max(np.abs(r64[c]))
+            err = np.max(np.abs(rtc[c] - r64[c]))
+            assert err <= RHO_TOL * scale, (err, scale)
+            assert abs(rtc[c].sum() - r64[c].sum()) <= SUM_TOL * abs(r64[c].sum())
+
+
+def test_density_bf16x3_si64(ctx):
+    u, orbs, dm, vna = _si64(ctx)
+    r64 = _density(ctx, u, orbs, dm, "fp64")[0]
+    rtc = _density(ctx, u, orbs, dm, "bf16x3")[0]
+    scale = np.max(np.abs(r64))
+    err = np.max(np.abs(rtc - r64))
+    assert err <= RHO_TOL * scale, (err, scale)
+    assert abs(rtc.sum() - r64.sum()) <= SUM_TOL * abs(r64.sum())
+
+
+def _hks(ctx, u, orbs, vp, precision, spin="off"):
+    n = {"off": 1, "on": 2}[spin]
+    H = [np.zeros(u.Total_Hsize) for _ in range(n)]
+    ctx.set_precision(precision)
+    try:
+        getattr(L, "Calc_MatrixElements_dVH_Vxc_" + spin)(u, orbs, vp, H)
+    finally:
+        ctx.set_precision("fp64")
+    return H
+
+
+def test_hamiltonian_bf16x3_si2(ctx):
+    u, orbs = _si2(ctx)
+    rng = np.random.default_rng(5)
+    for spin, n in (("off", 1), ("on", 2)):
+        vp = [rng.normal(size=u.NN) for _ in range(n)]
+        h64 = _hks(ctx, u, orbs, vp, "fp64", spin)
+        htc = _hks(ctx, u, orbs, vp, "bf16x3", spin)
+        for c in range(n):
+            scale = np.max(np.abs(h64[c]))
+            err = np.max(np.abs(htc[c] - h64[c]))
+            assert err <= H_TOL * scale, (err, scale)
+
+
+def test_hamiltonian_bf16x3_si64(ctx):
+    u, orbs, dm, vna = _si64(ctx)
+    h64 = _hks(ctx, u, orbs, [vna], "fp64")[0]
+    htc = _hks(ctx, u, orbs, [vna], "bf16x3")[0]
+    scale = np.max(np.abs(h64))
+    err = np.max(np.abs(htc - h64))
+    e64, etc = float(np.dot(dm[0], h64)), float(np.dot(dm[0], htc))
+    assert err <= H_TOL * scale, (err, scale)
+    assert abs(etc - e64) <= SUM_TOL * abs(e64), (etc, e64)
+
+
+def test_job_energy_bf16x3_si64(ctx):
+    """Grid energy of one full step (rho, Poisson, LDA, H, energies) on the
+    64-atom 96^3 cell: split-BF16 contractions vs FP64, <= 1 uHa/atom."""
+    u, orbs, dm, vna = _si64(ctx)
+    E = {}
+    for prec in ("fp64", "bf16x3"):
+        ctx.set_precision(prec)
+        try:
+            job = L.GridStepJob(u, orbs, "off", "LDA", None, None, vna)
+            job.set_dm(dm)
+            job.step()
+            E[prec] = job.energies()[4]
+        finally:
+            ctx.set_precision("fp64")
+    assert abs(E["bf16x3"] - E["fp64"]) / u.Natom <= 1e-6, E
