@@ -220,6 +220,27 @@ lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops);
 lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t order, int32_t n,
                            int32_t k, const float* a, const float* b, float* d);
 
+/* Split-BF16 density that allocates no device memory.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc at call time --
+ * hosts whose own pool allocator owns the device memory, and serving loops
+ * that cannot afford the device-wide synchronisation cudaMalloc/cudaFree may
+ * cause.  Same result as lcp_set_density_grid at LCP_PREC_BF16X3 (whatever
+ * the context's precision), but dm_dev[s] (Total_Hsize doubles) and
+ * density_grid_dev[s] (NN doubles, overwritten) are DEVICE pointers owned by
+ * the caller.  Scratch lives in one fixed 16 MiB device array per device,
+ * held from the library's load on that device until exit; it fits cells of
+ * up to 10921 neighbour pairs (Nloop) and larger ones are rejected with
+ * LCP_EINVAL.  The orbitals' split-BF16 tables must already exist (any
+ * allocating split-BF16 call on them builds them), else LCP_ESTATE.  The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture.  Every call on a device shares the array: calls that
+ * overlap on the GPU (other host threads, other contexts of that device)
+ * race and must be serialised by the caller.  Runs on the context's stream
+ * and returns after it completes. */
+lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
+                                        int32_t spinpol, const double* const* dm_dev,
+                                        double* const* density_grid_dev);
+
 #ifdef __cplusplus
 }
 #endif

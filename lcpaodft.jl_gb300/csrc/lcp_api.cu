@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1247,5 +1248,97 @@ lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops) {
 lcp_status lcp_job_get_density(lcp_ctx* ctx, lcp_job* job, double* const* d) { return job_get(ctx, job, job ? job->rho : nullptr, job ? job->nn : 0, d); }
 lcp_status lcp_job_get_hks(lcp_ctx* ctx, lcp_job* job, double* const* h) { return job_get(ctx, job, job ? job->hks : nullptr, job ? job->hsize : 0, h); }
 lcp_status lcp_job_get_vpot(lcp_ctx* ctx, lcp_job* job, double* const* v) { return job_get(ctx, job, job ? job->vpot : nullptr, job ? job->nn : 0, v); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- split-BF16 density without allocation
+//
+// For callers that must not allocate device memory at call time: hosts whose
+// own pool allocator owns the device memory (a cudaMalloc behind its back can
+// fail under that pool's reservation or fragment it), and latency-bound
+// serving loops, where cudaMalloc/cudaFree may synchronise the whole device
+// and stall the other streams in flight.  The scratch of the split-BF16
+// density (the symmetrised fixed-point D blocks, the D scale, the |D| maximum
+// and the error word) lives in the fixed array below instead of in context
+// workspaces.  Its limit: 16 MiB, which holds the D blocks of up to
+// kNoAllocMaxPairs neighbour pairs (1.5 KB each).  The array exists once per
+// device that loads this library and is held until the process exits.
+
+namespace {
+
+constexpr size_t kNoAllocBytes = size_t(16) << 20;
+constexpr size_t kNoAllocHeader = 256;  // [0,16) D scale, [16,24) |D| max bits, [24,28) error word
+constexpr size_t kNoAllocPairBytes = 768 * sizeof(uint16_t);
+constexpr int64_t kNoAllocMaxPairs = (int64_t)((kNoAllocBytes - kNoAllocHeader) / kNoAllocPairBytes) - 1;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (host code must not pass the symbol itself to a kernel).
+lcp_status noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return fail(LCP_EDEVICE, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+    g_noalloc_addr[device] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_addr[device]);
+  return LCP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
+                                        int32_t spinpol, const double* const* dm_dev,
+                                        double* const* density_grid_dev) {
+  lcp_status s = check_ctx(ctx);  // makes the context's device current
+  if (s) return s;
+  if ((s = check_pair(ucell, orbs))) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol.");
+  if (!dm_dev || !density_grid_dev) return fail(LCP_EINVAL, "NULL argument");
+  const int ns = channels(spinpol);
+  for (int c = 0; c < ns; ++c)
+    if (!dm_dev[c] || !density_grid_dev[c]) return fail(LCP_EINVAL, "NULL channel");
+  const lcp::UCell& u = ucell->u;
+  if ((int64_t)u.nloop > kNoAllocMaxPairs)
+    return fail(LCP_EINVAL, "the no-allocation density holds the D blocks of at most " +
+                                std::to_string(kNoAllocMaxPairs) + " neighbour pairs (16 MiB); this cell has " +
+                                std::to_string(u.nloop));
+  if (!orbs->bricks_ready)
+    return fail(LCP_ESTATE,
+                "the split-BF16 tables of these orbitals are not built; one allocating split-BF16 call "
+                "(lcp_set_density_grid or lcp_calc_matrix_elements at LCP_PREC_BF16X3) builds them");
+  unsigned char* base = nullptr;
+  if ((s = noalloc_scratch(ctx->device, &base))) return s;
+  double* dscale = reinterpret_cast<double*>(base);
+  unsigned long long* dmax = reinterpret_cast<unsigned long long*>(base + 16);
+  int* status = reinterpret_cast<int*>(base + 24);
+  __nv_bfloat16* dsym = reinterpret_cast<__nv_bfloat16*>(base + kNoAllocHeader);
+  const lcp_orbs* o = orbs;
+  API_CUDA(cudaMemsetAsync(status, 0, sizeof(int), ctx->stream), "memset");
+  for (int c = 0; c < ns; ++c) {
+    API_CUDA(lcp::launch_absmax_scale(dm_dev[c], u.total_hsize, 2.0, dmax, dscale, ctx->stream), "dm scale");
+    API_CUDA(lcp::launch_dsym(u.nloop, o->o_atom.as<int32_t>(), o->o_jatom.as<int32_t>(), o->o_boff.as<int64_t>(),
+                              o->o_partner.as<int32_t>(), o->geom.numorbs, dm_dev[c], dscale, dsym, ctx->stream),
+             "dsym");
+    API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale, dsym, dscale, u.nloop,
+                                    density_grid_dev[c], status, ctx->stream),
+             "density_tc");
+    ctx->launches += 4;
+  }
+  int st = 0;
+  API_CUDA(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "density");
+  if (st) return fail(st, "a device wait timed out (tensor-core completion)");
+  return LCP_OK;
+}
 
 }  // extern "C"
