@@ -5,8 +5,12 @@ A step is density assembly from D, FFT Poisson, LDA xc + potential (+ V_na),
 grid matrix elements and the FP64 energy terms, on a 96^3 grid with 13
 orbitals per atom (see lcpgrid/workloads.py).  Prints one JSON line.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32|bf16x3]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision bf16x3|fp32|fp64]
     python bench.py --impl reference ...   (the CPU restatement on the host cores)
+
+The headline form is split-BF16 (tensor cores); the FP64 drop-in is timed in
+the same run and reported beside it.  --workload si8 runs the 8-atom cell of
+the same crystal and grid spacing (48^3), small enough for a profiler capture.
 
 Multi-GPU runs (torchrun) are independent replicas of the same cell: the
 path is never sharded, there is no data-path collective.
@@ -35,7 +39,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32", "fp64"])
+    ap.add_argument("--workload", default="si64", choices=["si64", "si8"])
+    ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 drop-in form")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -232,19 +238,25 @@ def build_workload(ctx, wl):
     return u, orbs, dm, vna, t_geom, t_tab
 
 
+def workload(args):
+    from lcpgrid.workloads import si64_workload
+    if args.workload == "si8":
+        return si64_workload(nrep=1, ngrid=(48, 48, 48))
+    return si64_workload()
+
+
 def run_ours(args):
     import numpy as np
     import torch
 
     import lcpgrid as L
-    from lcpgrid.workloads import si64_workload
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    wl = si64_workload()
+    wl = workload(args)
     ctx = L.Context(local)
     u, orbs, dm, vna, t_geom, t_tab = build_workload(ctx, wl)
     # a dedicated (non-default) stream: the library launches on it and the
@@ -260,6 +272,16 @@ def run_ours(args):
     job.step()
     e_fp64 = job.energies()
     h_fp64 = job.hks()[0]
+    fp64_ms = None
+    if args.precision != "fp64" and args.fp64_steps > 0:
+        fe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        fe[0].record(stream)
+        for _ in range(args.fp64_steps):
+            job.step()
+        fe[1].record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = fe[0].elapsed_time(fe[1]) / args.fp64_steps
     ctx.set_precision(args.precision)
 
     for _ in range(max(3, args.warmup)):
@@ -346,6 +368,8 @@ def run_ours(args):
         "energy": {"E_grid": float(e_now[4]), "E_grid_fp64": float(e_fp64[4]),
                    "err_per_atom_uHa": abs(float(e_now[4] - e_fp64[4])) / wl["natom"] * 1e6,
                    "max_abs_dH": float(np.max(np.abs(h_now - h_fp64)))},
+        "fp64_dropin": None if fp64_ms is None else {
+            "ms_per_step": fp64_ms, "steps": args.fp64_steps, "speedup_of_this_form": fp64_ms / ms_step},
         "clocks": clk,
         "gpu_launches": int(launches),
         "gpu_launches_note": "library kernels per timed region; cuFFT adds 2 FFT launches per step",
@@ -366,8 +390,7 @@ def run_reference(args):
     if rank != 0:
         return
     import lcpgrid as L
-    from lcpgrid.workloads import si64_workload
-    wl = si64_workload()
+    wl = workload(args)
     u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
                 Total_NumOrbs=wl["numorbs"])
     vals = []

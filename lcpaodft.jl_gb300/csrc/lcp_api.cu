@@ -242,6 +242,7 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   API_CUDA(cudaMemcpyAsync(&o->phi_scale, o->b_scale.p, sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   lcp::TcBrickGeom& g = o->bgeom;
   g.nbricks = b.nbricks;
+  g.nblocks = b.nblocks;
   for (int d = 0; d < 3; ++d) {
     g.bdim[d] = b.bdim[d];
     g.nb[d] = b.nb[d];

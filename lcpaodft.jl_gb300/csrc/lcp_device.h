@@ -102,6 +102,7 @@ cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, c
 // Device copy of the brick tiling (see struct Bricks in lcp_internal.h).
 struct TcBrickGeom {
   int64_t nbricks;
+  int64_t nblocks;  // table blocks = images; brick hb's images are blocks img_off[hb] .. img_off[hb+1]-1
   int32_t bdim[3], nb[3], ngrid[3];
   int32_t npts, max_images;
   const int64_t* img_off;

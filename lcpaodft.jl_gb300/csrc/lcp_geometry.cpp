@@ -566,6 +566,18 @@ std::string build_bricks(const UCell& u, Bricks& b) {
       }
     b.tab_off[hb + 1] = (int64_t)b.tab_pair.size();
   }
+  // Number the blocks in image order: every block is an image of exactly one
+  // home brick, so a brick's images become consecutive blocks and a window of
+  // them is one contiguous range of the tables.
+  {
+    std::vector<int32_t> perm(b.nblocks, -1);
+    for (size_t i = 0; i < b.img_block.size(); ++i) perm[b.img_block[i]] = (int32_t)i;
+    std::vector<int32_t> atom_of(b.nblocks);
+    for (int64_t k = 0; k < b.nblocks; ++k) atom_of[perm[k]] = b.block_atom[k];
+    b.block_atom.swap(atom_of);
+    for (auto& c : b.point_code) c = perm[c >> 7] * 128 + (c & 127);
+    for (size_t i = 0; i < b.img_block.size(); ++i) b.img_block[i] = (int32_t)i;
+  }
   // grid-H slots: (s <= t) image pairs of each brick that are neighbour pairs
   std::vector<int32_t> fold(u.nloop, -1);
   for (size_t q = 0; q < u.uniq_pair.size(); ++q) {

@@ -80,7 +80,7 @@ struct Bricks {
   std::vector<int32_t> block_atom;   // [nblocks]
   std::vector<int32_t> point_code;   // per sphere point: block*128 + slot
   std::vector<int64_t> img_off;      // [nbricks+1]
-  std::vector<int32_t> img_block;    // block of each image of a home brick
+  std::vector<int32_t> img_block;    // block of each image of a home brick (blocks are numbered in image order)
   std::vector<int32_t> img_atom;
   std::vector<int64_t> tab_off;      // [nbricks+1] offsets of the m x m pair tables
   std::vector<int32_t> tab_pair;     // ordered pair of images (s, t), -1 if none

@@ -29,7 +29,6 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restric
   // order 1: [mn-group][k-group][128 B core matrix]: LBO = 128 B, SBO = K/8 * 128 B
   const uint32_t lbo_a = order ? 128 : (kSelfM / 8) * 128, lbo_b = order ? 128 : (N / 8) * 128;
   const uint32_t sbo_a = order ? (K / 8) * 128 : 128, sbo_b = sbo_a;
-  const uint32_t sbo = sbo_a;
   for (int idx = tid; idx < kSelfM * K; idx += blockDim.x) {
     const int m = idx / K, k = idx - m * K;
     const uint32_t off = a_mn ? tc::mnmajor_off(m, k, lbo_a, sbo_a) : tc::kmajor_off(m, k, lbo_a, sbo_a);
@@ -115,13 +114,9 @@ namespace {
 
 constexpr int kPart = 2048;                    // bf16 per part of a table block
 constexpr int kBlockElems = 3 * kPart;         // table block: hi, mid, lo
+// The tables are part-major: part p of block b at tab + (p * nblocks + b) * kPart.
 constexpr int kDsymElems = 768;                // D block: hi, mid, lo (256 each)
 constexpr uint32_t kALbo = 2048, kASbo = 128;  // table block [h][g][8 pt][8 orb] as K-major A
-constexpr int kDWin = 16;                      // density: images per column window
-constexpr uint32_t kBLbo = kDWin * 2 * 128;    // B: [kh][n-group (<= 32)][8 n][8 k]
-constexpr int kASmem = 3 * 4096;               // hi, mid, lo
-constexpr int kBSmem = 3 * 2 * kBLbo;          // (hi, mid, lo) x (kh) x LBO
-constexpr uint32_t kCross = 256;               // TMEM column of the cross-term accumulator
 
 __device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
   const double h = rint(u * 128.0) * (1.0 / 128.0);
@@ -134,19 +129,24 @@ __device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloa
 }
 
 // Same split for a float p (|p| <= 1) carrying a small correction e
-// (|e| <= 2^-23 |p|): every step but the last rounding is exact in FP32 --
-// p - hi and r1 - mid are multiples of ulp(p) (resp. ulp(r1)) below 2^24 of
-// them -- so the parts are those of p + e up to |lo residual| <= 2^-24.
+// (|e| <= 2^-23 |p|), in full-rate FP32 instructions only.  Rounding to an
+// integer uses the constant C = 1.5 * 2^23: for |x| <= 2^22, fma(y, 2^k, C)
+// lies in [2^23, 2^24) where the spacing is 1, so it rounds y * 2^k (exact)
+// to the nearest integer (ties to even) and subtracting C is exact.  Every
+// step but the last rounding is exact: p - hi and r1 - mid are multiples of
+// ulp(p) (resp. ulp(r1)) below 2^24 of them, so the parts are those of p + e
+// up to |lo residual| <= 2^-24.
 __device__ __forceinline__ void fx_split_f(float p, float e, __nv_bfloat16& hi, __nv_bfloat16& mid,
                                            __nv_bfloat16& lo) {
-  const float h = rintf(p * 128.0f) * 0.0078125f;
-  const float r1 = p - h;
-  const float m = rintf(r1 * 32768.0f) * (1.0f / 32768.0f);
-  const float r2 = (r1 - m) + e;
-  const float l = rintf(r2 * 8388608.0f) * (1.0f / 8388608.0f);
-  hi = __float2bfloat16_rn(h);
-  mid = __float2bfloat16_rn(m);
-  lo = __float2bfloat16_rn(l);
+  constexpr float C = 12582912.0f;
+  const float hs = fmaf(p, 128.0f, C) - C;              // 2^7 * hi, an integer in [-128, 128]
+  const float r1 = fmaf(hs, -0.0078125f, p);            // p - hi, exact
+  const float ms = fmaf(r1, 32768.0f, C) - C;           // 2^15 * mid
+  const float r2 = fmaf(ms, -(1.0f / 32768.0f), r1) + e;
+  const float ls = fmaf(r2, 8388608.0f, C) - C;         // 2^23 * lo
+  hi = __float2bfloat16_rn(hs * 0.0078125f);
+  mid = __float2bfloat16_rn(ms * (1.0f / 32768.0f));
+  lo = __float2bfloat16_rn(ls * (1.0f / 8388608.0f));
 }
 
 // Float-float accumulation (Knuth's TwoSum): hi + lo carries the running sum
@@ -169,8 +169,10 @@ __device__ __forceinline__ double pow2_ceil(double x) {
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(sdst)), "l"(gsrc) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // max |x| over n doubles (non-negative doubles order like their bit patterns)
@@ -194,7 +196,8 @@ __global__ void pow2_scale_kernel(const unsigned long long* mx, double factor, d
 __global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t* __restrict__ phi_off,
                                    const int32_t* __restrict__ numorbs, const int64_t* __restrict__ sph_off,
                                    int natom, const int32_t* __restrict__ point_code, int64_t npoints,
-                                   const double* __restrict__ scale, __nv_bfloat16* __restrict__ tab) {
+                                   const double* __restrict__ scale, __nv_bfloat16* __restrict__ tab,
+                                   int64_t nblocks) {
   const double inv = scale[1];
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npoints; k += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = natom;  // atom with sph_off[atom] <= k < sph_off[atom+1]
@@ -209,14 +212,14 @@ __global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t
     const int code = point_code[k];
     const int64_t blk = code >> 7;
     const int slot = code & 127, g = slot >> 3, r = slot & 7;
-    __nv_bfloat16* base = tab + blk * kBlockElems;
+    __nv_bfloat16* base = tab + blk * kPart;  // part p of block blk at (p * nblocks + blk) * kPart
     for (int a = 0; a < no && a < 16; ++a) {
       __nv_bfloat16 h, m, l;
       fx_split(src[a] * inv, h, m, l);
       const int off = ((a >> 3) * 16 + g) * 64 + r * 8 + (a & 7);
       base[off] = h;
-      base[kPart + off] = m;
-      base[2 * kPart + off] = l;
+      base[nblocks * kPart + off] = m;
+      base[2 * nblocks * kPart + off] = l;
     }
   }
 }
@@ -262,37 +265,24 @@ __device__ __forceinline__ int64_t brick_point_index(int64_t hb, int p, const in
   return (x * ngrid[1] + y) * ngrid[2] + z;
 }
 
-// Sum of the three parts of 8 consecutive values (one 16-byte chunk per part).
-__device__ __forceinline__ void load_chunk3(const __nv_bfloat16* p0, double* u) {
-  const uint4 vh = *reinterpret_cast<const uint4*>(p0);
-  const uint4 vm = *reinterpret_cast<const uint4*>(p0 + kPart);
-  const uint4 vl = *reinterpret_cast<const uint4*>(p0 + 2 * kPart);
-  const __nv_bfloat16* bh = reinterpret_cast<const __nv_bfloat16*>(&vh);
-  const __nv_bfloat16* bm = reinterpret_cast<const __nv_bfloat16*>(&vm);
-  const __nv_bfloat16* bl = reinterpret_cast<const __nv_bfloat16*>(&vl);
-#pragma unroll
-  for (int c = 0; c < 8; ++c)
-    u[c] = (double)__bfloat162float(bh[c]) + (double)__bfloat162float(bm[c]) + (double)__bfloat162float(bl[c]);
-}
-
-// FP32 form: hi + mid + lo is a multiple of 2^-23 of magnitude <= 1, so the
-// sum is exact in FP32.
-__device__ __forceinline__ void load_chunk3f(const __nv_bfloat16* p0, float* u) {
-  const uint4 vh = *reinterpret_cast<const uint4*>(p0);
-  const uint4 vm = *reinterpret_cast<const uint4*>(p0 + kPart);
-  const uint4 vl = *reinterpret_cast<const uint4*>(p0 + 2 * kPart);
-  const __nv_bfloat16* bh = reinterpret_cast<const __nv_bfloat16*>(&vh);
-  const __nv_bfloat16* bm = reinterpret_cast<const __nv_bfloat16*>(&vm);
-  const __nv_bfloat16* bl = reinterpret_cast<const __nv_bfloat16*>(&vl);
-#pragma unroll
-  for (int c = 0; c < 8; ++c) u[c] = (__bfloat162float(bh[c]) + __bfloat162float(bm[c])) + __bfloat162float(bl[c]);
-}
-
-// The 16 fixed-point values of one point of a table block.
-__device__ __forceinline__ void load_point_row(const __nv_bfloat16* blk, int p, float* u) {
+// The 16 fixed-point values of point p of a table block staged in shared
+// memory ([part][h][g][8 pt][8 orb]); hi + mid + lo is a multiple of 2^-23 of
+// magnitude <= 1, so the FP32 sum is exact.
+__device__ __forceinline__ void smem_point_row(const uint8_t* blk, int p, float* u) {
   const int g = p >> 3, r = p & 7;
 #pragma unroll
-  for (int h = 0; h < 2; ++h) load_chunk3f(blk + (h * 16 + g) * 64 + r * 8, u + h * 8);
+  for (int h = 0; h < 2; ++h) {
+    const uint8_t* c = blk + (h * 16 + g) * 128 + r * 16;
+    const uint4 vh = *reinterpret_cast<const uint4*>(c);
+    const uint4 vm = *reinterpret_cast<const uint4*>(c + 4096);
+    const uint4 vl = *reinterpret_cast<const uint4*>(c + 8192);
+    const __nv_bfloat16* bh = reinterpret_cast<const __nv_bfloat16*>(&vh);
+    const __nv_bfloat16* bm = reinterpret_cast<const __nv_bfloat16*>(&vm);
+    const __nv_bfloat16* bl = reinterpret_cast<const __nv_bfloat16*>(&vl);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      u[h * 8 + k] = (__bfloat162float(bh[k]) + __bfloat162float(bm[k])) + __bfloat162float(bl[k]);
+  }
 }
 
 // ==========================================================================
@@ -311,21 +301,20 @@ __device__ __forceinline__ void load_point_row(const __nv_bfloat16* blk, int p, 
 //   Y[p, (s,a)] = sum_{t >= s} sum_b phi_t(p)_b Dsym_st[a][b],
 //   rho(p)      = sum_{s,a} phi_s(p)_a Y[p, (s,a)],
 //
-// with Y in TMEM, 16 columns per image of a window of up to 16 images s.  K
+// with Y in TMEM, 16 columns per image of a window of up to 8 images s.  K
 // steps run t = m-1 ... c0 so the first step writes every column of the
-// window.  The epilogue (one thread per point) sums in FP64; every grid point
-// lies in one brick, so rho is written once, without atomics.
+// window.  The epilogue (one thread per point) sums in float-float; every
+// grid point lies in one brick, so rho is written once, without atomics.
 // ==========================================================================
 
 struct TcDensArgs {
-  int64_t nbricks;
+  int64_t nbricks, nblocks;
   int32_t bdim[3], nb[3], ngrid[3];
   int32_t npts;
   int32_t zero_pair;
   double phi_scale;      // S_phi
   const double* dscale;  // [S_D, 1/S_D]
   const int64_t* img_off;
-  const int32_t* img_block;
   const int64_t* tab_off;
   const int32_t* tab_pair;
   const __nv_bfloat16* tab;
@@ -334,18 +323,53 @@ struct TcDensArgs {
   int* status;
 };
 
-__global__ void __launch_bounds__(128) density_tc_kernel(TcDensArgs args) {
+// Density kernel roles (320 threads, one CTA per SM, persistent over bricks):
+//   warp 0     table producer: per K step (brick, window, image t) three 4 KB
+//              bulk copies of t's table block (operand A), completing as
+//              transactions on full[stage] of a ring of kDStages stages;
+//   warps 6-9  D gatherers: the Dsym(s, t) pieces of the window (operand B)
+//              as 16-byte cp.async copies (one warp's cp.async issue costs
+//              ~35 cycles, a small bulk copy ~70, whatever its size), each
+//              warp publishing its share on full[stage] kDLag steps later,
+//              once landed and fenced for the tensor core;
+//   warp 1     MMA issuer (one elected lane): nine tcgen05 MMAs per K step
+//              into one of two TMEM window buffers.  After step t of a
+//              window, column block t is final: the commit goes to
+//              mdone[stage]; other steps commit empty[stage] (4 arrivals);
+//   warps 2-5  epilogue: one thread per point (its TMEM lane).  On
+//              mdone[stage] it contracts column block t with phi_t(p), read
+//              from the stage's A operand, then frees the stage; after a
+//              window it frees the TMEM buffer, after a brick it writes rho.
+// Every wait is bounded; a timeout sets *status and stops all roles.
+constexpr int kDWin = 8;                          // images s per window (N <= 128)
+constexpr int kDStages = 6;
+constexpr uint32_t kDBLbo = kDWin * 2 * 128;      // B: [part][kh][n-group][8 n][8 k]
+constexpr int kDStageA = 3 * 4096;                // table block: hi, mid, lo
+constexpr int kDStageB = 3 * 2 * kDBLbo;          // Dsym pieces: (part, kh) x LBO
+constexpr int kDStageBytes = kDStageA + kDStageB;  // 24 KB
+constexpr size_t kDSmem = (size_t)kDStages * kDStageBytes;
+constexpr int kDMaxImages = 32;                   // atom images per brick (checked at launch)
+constexpr int kDLag = 2;                          // K steps whose D pieces may still be in flight
+constexpr int kDGatherWarps = 4;                  // warps gathering D pieces (cp.async)
+constexpr uint32_t kDBufCols = 256;               // TMEM columns per window buffer
+constexpr uint32_t kDCross = 128;                 // cross accumulator within a buffer
+
+__global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t mbar[2];
+  __shared__ uint64_t full_bar[kDStages], empty_bar[kDStages], mdone_bar[kDStages], tempty_bar[2], drain_bar;
+  __shared__ int32_t s_pair[kDGatherWarps][kDMaxImages * kDMaxImages];  // each gatherer's copy of the pair table
   __shared__ uint32_t tslot;
-  __shared__ int abort_flag;
+  __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  uint8_t* sA[2] = {smem, smem + kASmem};
-  uint8_t* sB[2] = {smem + 2 * kASmem, smem + 2 * kASmem + kBSmem};
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
-  if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+  if (tid == 32) {
+    for (int s = 0; s < kDStages; ++s) {
+      tc::mbar_init(&full_bar[s], 1 + kDGatherWarps);  // A transactions + each gatherer's D pieces
+      tc::mbar_init(&empty_bar[s], 4);
+      tc::mbar_init(&mdone_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) tc::mbar_init(&tempty_bar[b], 4);
+    tc::mbar_init(&drain_bar, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
   }
@@ -353,103 +377,202 @@ __global__ void __launch_bounds__(128) density_tc_kernel(TcDensArgs args) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tslot;
-  const double out_scale = args.phi_scale * args.phi_scale * args.dscale[0];
-  uint32_t uses[2] = {0, 0};
-  bool pending[2] = {false, false};
+  auto give_up = [&]() {
+    if (!abort_flag) atomicExch(args.status, LCP_ETIMEDOUT);
+    abort_flag = 1;
+  };
 
-  for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-    const int64_t i0 = args.img_off[hb];
-    const int m = (int)(args.img_off[hb + 1] - i0);
-    const int32_t* ptab = args.tab_pair + args.tab_off[hb];
-    const int p = warp * 32 + lane;
-    float acc_hi = 0.0f, acc_lo = 0.0f;
-    for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin) {
-      const int c1 = min(c0 + kDWin, m);
-      const int nsteps = m - c0;
-      for (int k = 0; k < nsteps; ++k) {
-        const int t = m - 1 - k;
-        const int s_hi = min(t, c1 - 1);
-        const int buf = k & 1;
-        if (pending[buf]) {
-          if (!tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1)) {
-            if (tid == 0) atomicExch(args.status, LCP_ETIMEDOUT);
-            abort_flag = 1;
+  if (warp == 0) {
+    // ------------------------------------------------------------ table producer
+    uint32_t it = 0;
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin) {
+        for (int k = 0; k < m - c0; ++k, ++it) {
+          const int t = m - 1 - k;
+          const int stage = (int)(it % kDStages);
+          const uint32_t use = it / kDStages;
+          if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[stage], (use - 1) & 1, &abort_flag)) {
+            give_up();
+            break;
           }
-          pending[buf] = false;
-        }
-        __syncthreads();
-        if (abort_flag) break;
-        const uint8_t* gA = reinterpret_cast<const uint8_t*>(args.tab + (int64_t)args.img_block[i0 + t] * kBlockElems);
-        for (int c = tid; c < kASmem / 16; c += blockDim.x) cp_async16(sA[buf] + c * 16, gA + c * 16);
-        const int nimg = s_hi - c0 + 1;
-        for (int c = tid; c < nimg * 96; c += blockDim.x) {
-          const int si = c / 96, w = c - si * 96;  // 96 x 16 B per image: (part, kh, 16 chunks)
-          const int part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
-          int pr = ptab[(c0 + si) * m + t];
-          if (pr < 0) pr = args.zero_pair;
-          const uint8_t* src = reinterpret_cast<const uint8_t*>(args.dsym + (int64_t)pr * kDsymElems) +
-                               part * 512 + kh * 256 + q * 16;
-          uint8_t* dst = sB[buf] + part * (2 * kBLbo) + kh * kBLbo + si * 256 + q * 16;
-          cp_async16(dst, src);
-        }
-        cp_async_wait_all();
-        tc::fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-          tc::fence_after_sync();
-          const uint32_t idesc = tc::idesc_bf16_f32(128, 16 * nimg, 0, 0);
-          const uint32_t a0 = tc::smem_u32(sA[buf]), b0 = tc::smem_u32(sB[buf]);
-          const uint64_t dah = tc::smem_desc(a0, kALbo, kASbo), dam = tc::smem_desc(a0 + 4096, kALbo, kASbo),
-                         dal = tc::smem_desc(a0 + 8192, kALbo, kASbo);
-          const uint64_t dbh = tc::smem_desc(b0, kBLbo, 128), dbm = tc::smem_desc(b0 + 2 * kBLbo, kBLbo, 128),
-                         dbl = tc::smem_desc(b0 + 4 * kBLbo, kBLbo, 128);
-          tc::mma_bf16(tmem, dah, dbh, idesc, k > 0 ? 1u : 0u);
-          tc::mma_bf16(tmem + kCross, dah, dbm, idesc, k > 0 ? 1u : 0u);
-          tc::mma_bf16(tmem + kCross, dam, dbh, idesc, 1u);
-          tc::mma_bf16(tmem + kCross, dah, dbl, idesc, 1u);
-          tc::mma_bf16(tmem + kCross, dal, dbh, idesc, 1u);
-          tc::mma_bf16(tmem + kCross, dam, dbm, idesc, 1u);
-          tc::mma_bf16(tmem + kCross, dam, dbl, idesc, 1u);
-          tc::mma_bf16(tmem + kCross, dal, dbm, idesc, 1u);
-          tc::mma_bf16(tmem + kCross, dal, dbl, idesc, 1u);
-          tc::mma_commit(&mbar[buf]);
-        }
-        uses[buf]++;
-        pending[buf] = true;
-      }
-      bool ok = !abort_flag;
-      for (int b = 0; b < 2; ++b) {
-        if (pending[b]) {
-          if (!tc::mbar_wait(&mbar[b], (uses[b] - 1) & 1)) ok = false;
-          pending[b] = false;
+          if (lane == 0) {
+            uint8_t* sA = smem + stage * kDStageBytes;
+            tc::mbar_arrive_expect_tx(&full_bar[stage], kDStageA);
+            for (int part = 0; part < 3; ++part)
+              tc::bulk_g2s(sA + part * 4096, args.tab + ((int64_t)part * args.nblocks + i0 + t) * kPart, 4096,
+                           &full_bar[stage]);
+          }
+          __syncwarp();
         }
       }
-      if (!ok) {
-        if (tid == 0) atomicExch(args.status, LCP_ETIMEDOUT);
-        abort_flag = 1;
-      }
-      tc::fence_after_sync();
-      __syncthreads();
-      if (abort_flag) break;
-      for (int s = c0; s < c1; ++s) {
-        float ym[16], yc[16];
-        tc::tmem_ld16(tc::tmem_addr(tmem, warp * 32, 16 * (s - c0)), ym);
-        tc::tmem_ld16(tc::tmem_addr(tmem, warp * 32, kCross + 16 * (s - c0)), yc);
-        float u[16];
-        load_point_row(args.tab + (int64_t)args.img_block[i0 + s] * kBlockElems, p, u);
-        float d = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 16; ++c) d = fmaf(u[c], ym[c] + yc[c], d);
-        ff_add(acc_hi, acc_lo, d);
-      }
-      tc::fence_before_sync();
-      __syncthreads();
     }
-    if (p < args.npts && !abort_flag) args.rho[brick_point_index(hb, p, args.bdim, args.nb, args.ngrid)] =
-          ((double)acc_hi + (double)acc_lo) * out_scale;
+    // wait for the copies still in flight before the CTA's shared memory goes away
+    for (int s = 0; s < kDStages; ++s) {
+      const uint32_t uses = it / kDStages + ((uint32_t)s < it % kDStages ? 1u : 0u);
+      if (uses > 0 && !tc::mbar_wait(&full_bar[s], (uses - 1) & 1, 1u << 24)) give_up();
+    }
+  } else if (warp >= 6) {
+    // ------------------------------------------------------------ D gatherers
+    const int gw = warp - 6;
+    int32_t* pair = s_pair[gw];
+    const uint8_t* dsym = reinterpret_cast<const uint8_t*>(args.dsym);
+    uint32_t it = 0;
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      if (m == 0) continue;
+      const int32_t* ptab = args.tab_pair + args.tab_off[hb];
+      __syncwarp();
+      for (int e = lane; e < m * m; e += 32) pair[e] = ptab[e];
+      __syncwarp();
+      for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin) {
+        const int c1 = min(c0 + kDWin, m);
+        for (int k = 0; k < m - c0; ++k, ++it) {
+          const int t = m - 1 - k;
+          const int nimg = min(t, c1 - 1) - c0 + 1;
+          const int stage = (int)(it % kDStages);
+          const uint32_t use = it / kDStages;
+          if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[stage], (use - 1) & 1, &abort_flag)) {
+            give_up();
+            break;
+          }
+          uint8_t* sB = smem + stage * kDStageBytes + kDStageA;
+          for (int c = gw * 32 + lane; c < nimg * 96; c += kDGatherWarps * 32) {
+            // 16-byte pieces: (image, part, kh, 16 x 16 B)
+            const int si = c / 96, w = c - si * 96, part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
+            int pr = pair[(c0 + si) * m + t];
+            if (pr < 0) pr = args.zero_pair;
+            cp_async16(sB + part * (2 * kDBLbo) + kh * kDBLbo + si * 256 + q * 16,
+                       dsym + (int64_t)pr * (kDsymElems * 2) + part * 512 + kh * 256 + q * 16);
+          }
+          cp_async_commit();
+          if (it >= (uint32_t)kDLag) {
+            // this warp's pieces of step it - kDLag have landed: make them
+            // visible to the tensor core and publish them
+            cp_async_wait<kDLag>();
+            tc::fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&full_bar[(it - kDLag) % kDStages]);
+          }
+          __syncwarp();
+        }
+      }
+    }
+    cp_async_wait<0>();
+    tc::fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0)
+      for (uint32_t j = it >= (uint32_t)kDLag ? it - kDLag : 0; j < it; ++j) tc::mbar_arrive(&full_bar[j % kDStages]);
+    __syncwarp();
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    uint32_t it = 0, win = 0;
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin, ++win) {
+        const int c1 = min(c0 + kDWin, m);
+        const uint32_t buf = win & 1, wuse = win >> 1;
+        if (wuse > 0 && !tc::mbar_wait_abortable(&tempty_bar[buf], (wuse - 1) & 1, &abort_flag)) {
+          give_up();
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t d0 = tmem + buf * kDBufCols, d1 = d0 + kDCross;
+        for (int k = 0; k < m - c0; ++k, ++it) {
+          const int t = m - 1 - k;
+          const int nimg = min(t, c1 - 1) - c0 + 1;
+          const int stage = (int)(it % kDStages);
+          if (!tc::mbar_wait_abortable(&full_bar[stage], (it / kDStages) & 1, &abort_flag)) {
+            give_up();
+            break;
+          }
+          tc::fence_after_sync();
+          if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(128, 16 * nimg, 0, 0);
+            const uint32_t a0 = tc::smem_u32(smem + stage * kDStageBytes), b0 = a0 + kDStageA;
+            const uint64_t dah = tc::smem_desc(a0, kALbo, kASbo), dam = tc::smem_desc(a0 + 4096, kALbo, kASbo),
+                           dal = tc::smem_desc(a0 + 8192, kALbo, kASbo);
+            const uint64_t dbh = tc::smem_desc(b0, kDBLbo, 128), dbm = tc::smem_desc(b0 + 2 * kDBLbo, kDBLbo, 128),
+                           dbl = tc::smem_desc(b0 + 4 * kDBLbo, kDBLbo, 128);
+            const uint32_t acc = k > 0 ? 1u : 0u;
+            tc::mma_bf16(d0, dah, dbh, idesc, acc);
+            tc::mma_bf16(d1, dah, dbm, idesc, acc);
+            tc::mma_bf16(d1, dam, dbh, idesc, 1u);
+            tc::mma_bf16(d1, dah, dbl, idesc, 1u);
+            tc::mma_bf16(d1, dal, dbh, idesc, 1u);
+            tc::mma_bf16(d1, dam, dbm, idesc, 1u);
+            tc::mma_bf16(d1, dam, dbl, idesc, 1u);
+            tc::mma_bf16(d1, dal, dbm, idesc, 1u);
+            tc::mma_bf16(d1, dal, dbl, idesc, 1u);
+            if (t < c1) {
+              // column block t is final once these MMAs finish; the epilogue
+              // reads it with phi_t from this stage and then frees the stage
+              tc::mma_commit(&mdone_bar[stage]);
+            } else {
+              for (int r = 0; r < 4; ++r) tc::mma_commit(&empty_bar[stage]);
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+    // every MMA issued by this thread has finished before TMEM is released
+    if (lane == 0) {
+      tc::mma_commit(&drain_bar);
+      if (!tc::mbar_wait(&drain_bar, 0, 1u << 24)) give_up();
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const uint32_t quarter = warp & 3;  // TMEM lanes [32 * quarter, 32 * quarter + 32)
+    const int p = (int)quarter * 32 + lane;
+    const double out_scale = args.phi_scale * args.phi_scale * args.dscale[0];
+    uint32_t it = 0, win = 0, mpar = 0;  // mpar: phase bit of mdone_bar per stage
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      float acc_hi = 0.0f, acc_lo = 0.0f;
+      for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin, ++win) {
+        const int c1 = min(c0 + kDWin, m);
+        const uint32_t buf = win & 1;
+        it += (uint32_t)(m - c1);  // steps t >= c1 touch no final column
+        for (int t = c1 - 1; t >= c0; --t, ++it) {
+          const int stage = (int)(it % kDStages);
+          if (!tc::mbar_wait_abortable(&mdone_bar[stage], (mpar >> stage) & 1u, &abort_flag)) {
+            give_up();
+            break;
+          }
+          mpar ^= 1u << stage;
+          tc::fence_after_sync();
+          float ym[16], yc[16], u[16];
+          const uint32_t col = buf * kDBufCols + 16 * (t - c0);
+          tc::tmem_ld16(tc::tmem_addr(tmem, quarter * 32, col), ym);
+          tc::tmem_ld16(tc::tmem_addr(tmem, quarter * 32, col + kDCross), yc);
+          smem_point_row(smem + stage * kDStageBytes, p, u);
+          float d = 0.0f;
+#pragma unroll
+          for (int c = 0; c < 16; ++c) d = fmaf(u[c], ym[c] + yc[c], d);
+          ff_add(acc_hi, acc_lo, d);
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&empty_bar[stage]);
+        }
+        if (abort_flag) break;
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&tempty_bar[buf]);
+      }
+      if (abort_flag) break;
+      if (p < args.npts)
+        args.rho[brick_point_index(hb, p, args.bdim, args.nb, args.ngrid)] =
+            ((double)acc_hi + (double)acc_lo) * out_scale;
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
+  tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
@@ -462,36 +585,56 @@ __global__ void __launch_bounds__(128) density_tc_kernel(TcDensArgs args) {
 //   G_st[a][b] = sum_{p in brick} phi_s(p)_a V(p) phi_t(p)_b
 //
 // (src/Hamiltonian.jl:384-429 restricted to the brick).  M = 128 rows are the
-// orbitals of 8 images s (V-weighted, built in shared memory with a per-brick
-// scale of V), N the orbitals of a window of up to 16 images t >= s (the
-// brick tables as stored), K the brick's 128 point slots.  Both operands are
+// orbitals of 8 images s (the brick tables as stored), N the orbitals of a
+// window of up to 4 images t (V-weighted in shared memory with a per-brick
+// scale of V), K the brick's 128 point slots.  Both operands are
 // MN-major: the table block [h][g][8 pt][8 orb] is that layout with
 // LBO = 128 B (point groups) and SBO = 2048 B (orbital halves; images 4096 B
 // apart).  Partial blocks go to a scratch array (FP32); h_reduce_kernel sums
-// them per folded pair in FP64 in a fixed order and writes both orientations
-// of H -- no atomics.
+// them per folded pair in a fixed order and writes both orientations of H --
+// no atomics.
 // ==========================================================================
 
-constexpr int kHWin = 8;                   // t images per window
-constexpr int kHGroup = 8;                 // s images per M tile
+// Roles (448 threads, one CTA per SM, persistent over bricks).  A tile is
+// (brick, s-group of kHGroup images, t-window of kHWin images t >= the
+// group's first image); V weights the t side:
+//   warp 0     producer: per s-group the plain tables of its images into the
+//              A region (after a_free), per tile the raw t window into one of
+//              kHStages B stages -- one bulk copy per part, the images of a
+//              brick being consecutive blocks;
+//   warps 6-13 per brick the V scale; per tile the V-weighted fixed-point
+//              split of the B stage, in place (b_ready);
+//   warp 1     MMA issuer: 8 K steps x 4 MMAs per tile into one of two TMEM
+//              tile buffers (4 accumulators x 64 columns each); after the
+//              group's last tile it commits a_free;
+//   warps 2-5  epilogue: per tile the FP32 partial blocks, TMEM read four
+//              loads per wait, then the buffer is freed.
+// Every wait is bounded; a timeout sets *status and stops all roles.
+constexpr int kHGroup = 8;                 // s images per M tile (M = 128)
+constexpr int kHWin = 4;                   // t images per N tile (N <= 64)
+constexpr int kHStages = 2;
+constexpr int kHXformWarps = 8;            // warps V-weighting the B stages
 constexpr int kImgBytes = 4096;            // one part of an image block
-constexpr int kHBBytes = kHWin * kImgBytes;
-constexpr int kHABytes = kHGroup * kImgBytes;
-constexpr size_t kHSmem = 3 * kHBBytes + 3 * kHABytes;  // 192 KB
-// TMEM columns of the four accumulators (N <= 16 * kHWin = 128 each), one per
-// quantum of the products: hi*hi (2^-14), hi*mid + mid*hi (2^-22),
-// hi*lo + lo*hi + mid*mid (2^-30), mid*lo + lo*mid + lo*lo (2^-38; lo*lo is
-// the only term finer than its quantum).  Over the 128 points of a brick the
-// first three sums stay below 2^24 of their quanta, so they are exact in FP32.
-constexpr uint32_t kHAcc1 = 128, kHAcc2 = 256, kHAcc3 = 384;
+constexpr int kHABytes = kHGroup * kImgBytes;   // one part of the A operand
+constexpr int kHBBytes = kHWin * kImgBytes;     // one part of a B stage
+constexpr size_t kHSmem = 3 * (size_t)kHABytes + (size_t)kHStages * 3 * kHBBytes;  // 192 KB
+// TMEM: two tile buffers of 256 columns; inside one, the four accumulators
+// (64 columns each), one per quantum of the products: hi*hi (2^-14),
+// hi*mid + mid*hi (2^-22), hi*lo + lo*hi + mid*mid (2^-30),
+// mid*lo + lo*mid + lo*lo (2^-38; lo*lo is the only term finer than its
+// quantum).  Over the 128 points of a brick the first three sums stay below
+// 2^24 of their quanta, so they are exact in FP32.  Four MMAs per K step
+// fill them (B parts stacked along N), reading 34 KB of operands instead of
+// the 54 KB of nine separate products: the MMAs are bound by shared-memory
+// operand bandwidth (~128 B/clock), not by the tensor pipe.
+constexpr uint32_t kHBufCols = 256, kHAccCols = 64;
 
 struct TcHamArgs {
-  int64_t nbricks;
+  int64_t nbricks, nblocks;
   int32_t bdim[3], nb[3], ngrid[3];
   int32_t npts;
   double phi_scale;
   const int64_t* img_off;
-  const int32_t* img_block;
   const int64_t* tab_off;
   const int32_t* tab_slot;
   const int64_t* slot_base;
@@ -501,19 +644,30 @@ struct TcHamArgs {
   int* status;
 };
 
-__global__ void __launch_bounds__(128) hamiltonian_tc_kernel(TcHamArgs args) {
+__global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_kernel(TcHamArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t mbar;
+  __shared__ uint64_t bfull_bar[kHStages], bready_bar[kHStages], bempty_bar[kHStages], tfull_bar[2], tempty_bar[2];
+  __shared__ uint64_t afull_bar, afree_bar, drain_bar;
   __shared__ uint32_t tslot;
-  __shared__ float sVh[128], sVl[128];
-  __shared__ double sVmax[4];
-  __shared__ int abort_flag;
+  __shared__ float sVh[kHXformWarps][128], sVl[kHXformWarps][128];
+  __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  uint8_t* sB = smem;                 // [part][image][4096 B]
-  uint8_t* sA = smem + 3 * kHBBytes;  // [part][image][4096 B]
+  uint8_t* sA = smem;                  // [part][s image][4096 B], plain tables
+  uint8_t* sB0 = smem + 3 * kHABytes;  // stages of [part][t image][4096 B], V-weighted in place
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
-  if (tid == 0) {
-    tc::mbar_init(&mbar, 1);
+  if (tid == 32) {
+    for (int s = 0; s < kHStages; ++s) {
+      tc::mbar_init(&bfull_bar[s], 1);
+      tc::mbar_init(&bready_bar[s], 32 * kHXformWarps);
+      tc::mbar_init(&bempty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&tfull_bar[b], 1);
+      tc::mbar_init(&tempty_bar[b], 4);
+    }
+    tc::mbar_init(&afull_bar, 1);
+    tc::mbar_init(&afree_bar, 1);
+    tc::mbar_init(&drain_bar, 1);
     tc::fence_mbar_init();
     abort_flag = 0;
   }
@@ -521,146 +675,343 @@ __global__ void __launch_bounds__(128) hamiltonian_tc_kernel(TcHamArgs args) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tslot;
-  uint32_t commits = 0;
-  for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-    const int64_t i0 = args.img_off[hb];
-    const int m = (int)(args.img_off[hb + 1] - i0);
-    const int64_t t0 = args.tab_off[hb];
-    const int64_t sbase = args.slot_base[hb];
-    const double v = tid < args.npts ? args.vpot[brick_point_index(hb, tid, args.bdim, args.nb, args.ngrid)] : 0.0;
-    double vm = fabs(v);
-    for (int o = 16; o > 0; o >>= 1) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
-    if (lane == 0) sVmax[warp] = vm;
-    __syncthreads();
-    const double sv = pow2_ceil(fmax(fmax(sVmax[0], sVmax[1]), fmax(sVmax[2], sVmax[3])));
-    {
-      const double vs = v / sv;  // exact: sv is a power of two
-      const float vh = (float)vs;
-      sVh[tid] = vh;
-      sVl[tid] = (float)(vs - (double)vh);
-    }
-    const float out_scale = (float)(sv * args.phi_scale * args.phi_scale);  // a power of two
-    for (int w0 = 0; w0 < m && !abort_flag; w0 += kHWin) {
-      const int w1 = min(w0 + kHWin, m);
-      __syncthreads();
-      for (int c = tid; c < (w1 - w0) * 768; c += blockDim.x) {
-        const int img = c / 768, q = c - img * 768;  // q: 16-byte chunk of the 12 KB block
-        const int part = q >> 8;
-        const uint8_t* src =
-            reinterpret_cast<const uint8_t*>(args.tab + (int64_t)args.img_block[i0 + w0 + img] * kBlockElems) + q * 16;
-        uint8_t* dst = sB + part * kHBBytes + img * kImgBytes + (q & 255) * 16;
-        cp_async16(dst, src);
+  auto give_up = [&]() {
+    if (!abort_flag) atomicExch(args.status, LCP_ETIMEDOUT);
+    abort_flag = 1;
+  };
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    uint32_t it = 0, grp = 0;
+    // B tile `it` (images t0 .. t0+nt-1 of brick i0) into its stage
+    auto load_b = [&](int64_t i0, int t0, int nt) -> bool {
+      const int stage = (int)(it % kHStages);
+      const uint32_t use = it / kHStages;
+      if (use > 0 && !tc::mbar_wait_abortable(&bempty_bar[stage], (use - 1) & 1, &abort_flag)) return false;
+      uint8_t* sB = sB0 + stage * 3 * kHBBytes;
+      if (lane == 0) {
+        tc::mbar_arrive_expect_tx(&bfull_bar[stage], nt * 3 * kImgBytes);
+        for (int part = 0; part < 3; ++part)
+          tc::bulk_g2s(sB + part * kHBBytes, args.tab + ((int64_t)part * args.nblocks + i0 + t0) * kPart,
+                       nt * kImgBytes, &bfull_bar[stage]);
       }
-      cp_async_wait_all();
-      for (int s0 = 0; s0 < w1 && !abort_flag; s0 += kHGroup) {
-        const int tstart = max(w0, s0);
-        for (int c = tid; c < kHGroup * 256; c += blockDim.x) {
-          const int img = c >> 8, q = c & 255;  // q = (h*16 + g)*8 + r: 8 orbitals of slot g*8 + r
-          const int s = s0 + img;
-          uint4 oh = make_uint4(0, 0, 0, 0), om = make_uint4(0, 0, 0, 0), ol = make_uint4(0, 0, 0, 0);
-          if (s < m) {
+      __syncwarp();
+      ++it;
+      return true;
+    };
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup, ++grp) {
+        // the group's first B tile goes ahead of the A refill, which waits
+        // for the previous group's MMAs
+        if (!load_b(i0, s0, min(kHWin, m - s0))) {
+          give_up();
+          break;
+        }
+        if (grp > 0 && !tc::mbar_wait_abortable(&afree_bar, (grp - 1) & 1, &abort_flag)) {
+          give_up();
+          break;
+        }
+        const int na = min(kHGroup, m - s0);
+        if (lane == 0) {
+          tc::mbar_arrive_expect_tx(&afull_bar, na * 3 * kImgBytes);
+          for (int part = 0; part < 3; ++part)
+            tc::bulk_g2s(sA + part * kHABytes, args.tab + ((int64_t)part * args.nblocks + i0 + s0) * kPart,
+                         na * kImgBytes, &afull_bar);
+        }
+        __syncwarp();
+        bool ok = true;
+        for (int t0 = s0 + kHWin; t0 < m && ok; t0 += kHWin) ok = load_b(i0, t0, min(kHWin, m - t0));
+        if (!ok) {
+          give_up();
+          break;
+        }
+      }
+    }
+    for (int s = 0; s < kHStages; ++s) {
+      const uint32_t uses = it / kHStages + ((uint32_t)s < it % kHStages ? 1u : 0u);
+      if (uses > 0 && !tc::mbar_wait(&bfull_bar[s], (uses - 1) & 1, 1u << 24)) give_up();
+    }
+    if (grp > 0 && !tc::mbar_wait(&afull_bar, (grp - 1) & 1, 1u << 24)) give_up();
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    uint32_t it = 0, grp = 0;
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup, ++grp) {
+        if (!tc::mbar_wait_abortable(&afull_bar, grp & 1, &abort_flag)) {
+          give_up();
+          break;
+        }
+        for (int t0 = s0; t0 < m; t0 += kHWin, ++it) {
+          const int stage = (int)(it % kHStages);
+          const uint32_t buf = it & 1, tuse = it >> 1;
+          if (tuse > 0 && !tc::mbar_wait_abortable(&tempty_bar[buf], (tuse - 1) & 1, &abort_flag)) {
+            give_up();
+            break;
+          }
+          if (!tc::mbar_wait_abortable(&bready_bar[stage], (it / kHStages) & 1, &abort_flag)) {
+            give_up();
+            break;
+          }
+          tc::fence_after_sync();
+          if (lane == 0) {
+            // B parts stacked along N: the stage is [hi | mid | lo] x kHWin images,
+            // one MN-major operand of N = 3 * 16 * kHWin with uniform SBO.  Image
+            // slots beyond the tile hold stale data and feed only unused columns.
+            const uint32_t idesc3 = tc::idesc_bf16_f32(128, 3 * 16 * kHWin, 1, 1);
+            const uint32_t idesc2 = tc::idesc_bf16_f32(128, 2 * 16 * kHWin, 1, 1);
+            const uint32_t idesc1 = tc::idesc_bf16_f32(128, 16 * kHWin, 1, 1);
+            const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB0 + stage * 3 * kHBBytes);
+            const uint32_t d0 = tmem + buf * kHBufCols;
+            for (int ks = 0; ks < 8; ++ks) {
+              const uint32_t ko = ks * 256;
+              const uint64_t dah = tc::smem_desc(a0 + ko, 128, 2048),
+                             dam = tc::smem_desc(a0 + kHABytes + ko, 128, 2048),
+                             dal = tc::smem_desc(a0 + 2 * kHABytes + ko, 128, 2048);
+              const uint64_t dbh = tc::smem_desc(b0 + ko, 128, 2048),  // [hi | mid | lo] from here
+                             dbl = tc::smem_desc(b0 + 2 * kHBBytes + ko, 128, 2048);
+              // Accumulator k (quantum 2^-(14+8k)) at columns d0 + 64k: a product
+              // of parts (i, j) lands in accumulator i + j when the MMA with
+              // A part i starts at column d0 + 64 i.  lo*lo shares the last one.
+              const uint32_t acc = ks > 0 ? 1u : 0u;
+              tc::mma_bf16(d0 + 3 * kHAccCols, dal, dbl, idesc1, acc);  // lo*lo (first write of acc 3)
+              tc::mma_bf16(d0, dah, dbh, idesc3, acc);                   // hi * [hi, mid, lo] -> acc 0, 1, 2
+              tc::mma_bf16(d0 + kHAccCols, dam, dbh, idesc3, 1u);        // mid * [hi, mid, lo] -> acc 1, 2, 3
+              tc::mma_bf16(d0 + 2 * kHAccCols, dal, dbh, idesc2, 1u);    // lo * [hi, mid] -> acc 2, 3
+            }
+            tc::mma_commit(&bempty_bar[stage]);
+            tc::mma_commit(&tfull_bar[buf]);
+          }
+          __syncwarp();
+        }
+        if (abort_flag) break;
+        if (lane == 0) tc::mma_commit(&afree_bar);  // the A region may be refilled
+        __syncwarp();
+      }
+    }
+    if (lane == 0) {
+      tc::mma_commit(&drain_bar);
+      if (!tc::mbar_wait(&drain_bar, 0, 1u << 24)) give_up();
+    }
+    __syncwarp();
+  } else if (warp >= 6) {
+    // ------------------------------------------------------------ V-weighting of the B tiles
+    const int tw = warp - 6, tt = tid - 192;  // transform warp and thread
+    float* vh_w = sVh[tw];
+    float* vl_w = sVl[tw];
+    uint32_t it = 0;
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      if (m == 0) continue;
+      // Per-brick power-of-two scale of V.  Every transform warp computes it
+      // over all 128 points and keeps its own copy of V / scale, so the
+      // warps need no barrier among themselves.
+      double vv[4], vm = 0.0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int pt = lane + 32 * k;
+        vv[k] = pt < args.npts ? args.vpot[brick_point_index(hb, pt, args.bdim, args.nb, args.ngrid)] : 0.0;
+        vm = fmax(vm, fabs(vv[k]));
+      }
+      for (int o = 16; o > 0; o >>= 1) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+      const double sv = pow2_ceil(vm);
+      __syncwarp();  // this warp's reads of the previous brick's copy are done
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const double vs = vv[k] / sv;  // exact: sv is a power of two
+        const float vh = (float)vs;
+        vh_w[lane + 32 * k] = vh;
+        vl_w[lane + 32 * k] = (float)(vs - (double)vh);
+      }
+      __syncwarp();
+      for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
+        for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
+          const int nt = min(kHWin, m - t0);
+          const int stage = (int)(it % kHStages);
+          if (!tc::mbar_wait_abortable(&bfull_bar[stage], (it / kHStages) & 1, &abort_flag)) {
+            give_up();
+            break;
+          }
+          uint8_t* sB = sB0 + stage * 3 * kHBBytes;
+          // in place: V-weighted fixed-point split of the raw t images; chunk c
+          // = (image, q): 8 orbitals of point slot q's point (all three parts)
+          for (int c = tt; c < nt * 256; c += 32 * kHXformWarps) {
+            const int img = c >> 8, q = c & 255;  // q = (h*16 + g)*8 + r
+            uint4* ph = reinterpret_cast<uint4*>(sB + img * kImgBytes + q * 16);
+            uint4* pm = reinterpret_cast<uint4*>(sB + kHBBytes + img * kImgBytes + q * 16);
+            uint4* pl = reinterpret_cast<uint4*>(sB + 2 * kHBBytes + img * kImgBytes + q * 16);
             const int pt = ((q >> 3) & 15) * 8 + (q & 7);
-            const float vh = sVh[pt], vl = sVl[pt];
-            float u[8];
-            load_chunk3f(args.tab + (int64_t)args.img_block[i0 + s] * kBlockElems + q * 8, u);
+            const float vh = vh_w[pt], vl = vl_w[pt];
+            const uint4 rh = *ph, rm = *pm, rl = *pl;
+            const __nv_bfloat16* xb_h = reinterpret_cast<const __nv_bfloat16*>(&rh);
+            const __nv_bfloat16* xb_m = reinterpret_cast<const __nv_bfloat16*>(&rm);
+            const __nv_bfloat16* xb_l = reinterpret_cast<const __nv_bfloat16*>(&rl);
+            uint4 oh, om, ol;
             __nv_bfloat16* xh = reinterpret_cast<__nv_bfloat16*>(&oh);
             __nv_bfloat16* xm = reinterpret_cast<__nv_bfloat16*>(&om);
             __nv_bfloat16* xl = reinterpret_cast<__nv_bfloat16*>(&ol);
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
+              const float u = (__bfloat162float(xb_h[e]) + __bfloat162float(xb_m[e])) + __bfloat162float(xb_l[e]);
               // u * (vh + vl) = pr + er exactly up to u*vl's rounding (~2^-48)
-              const float pr = u[e] * vh;
-              const float er = fmaf(u[e], vh, -pr) + u[e] * vl;
+              const float pr = u * vh;
+              const float er = fmaf(u, vh, -pr) + u * vl;
               fx_split_f(pr, er, xh[e], xm[e], xl[e]);
             }
+            *ph = oh;
+            *pm = om;
+            *pl = ol;
           }
-          *reinterpret_cast<uint4*>(sA + img * kImgBytes + q * 16) = oh;
-          *reinterpret_cast<uint4*>(sA + kHABytes + img * kImgBytes + q * 16) = om;
-          *reinterpret_cast<uint4*>(sA + 2 * kHABytes + img * kImgBytes + q * 16) = ol;
+          tc::fence_proxy_async_smem();
+          tc::mbar_arrive(&bready_bar[stage]);
         }
-        tc::fence_proxy_async_smem();
-        __syncthreads();
-        const int nimg = w1 - tstart;
-        if (tid == 0) {
-          tc::fence_after_sync();
-          const uint32_t idesc = tc::idesc_bf16_f32(128, 16 * nimg, 1, 1);
-          const uint32_t a0 = tc::smem_u32(sA);
-          const uint32_t b0 = tc::smem_u32(sB) + (tstart - w0) * kImgBytes;
-          for (int ks = 0; ks < 8; ++ks) {
-            const uint32_t ko = ks * 256;
-            const uint64_t dah = tc::smem_desc(a0 + ko, 128, 2048), dam = tc::smem_desc(a0 + kHABytes + ko, 128, 2048),
-                           dal = tc::smem_desc(a0 + 2 * kHABytes + ko, 128, 2048);
-            const uint64_t dbh = tc::smem_desc(b0 + ko, 128, 2048), dbm = tc::smem_desc(b0 + kHBBytes + ko, 128, 2048),
-                           dbl = tc::smem_desc(b0 + 2 * kHBBytes + ko, 128, 2048);
-            const uint32_t acc = ks > 0 ? 1u : 0u;
-            tc::mma_bf16(tmem, dah, dbh, idesc, acc);
-            tc::mma_bf16(tmem + kHAcc1, dah, dbm, idesc, acc);
-            tc::mma_bf16(tmem + kHAcc1, dam, dbh, idesc, 1u);
-            tc::mma_bf16(tmem + kHAcc2, dah, dbl, idesc, acc);
-            tc::mma_bf16(tmem + kHAcc2, dal, dbh, idesc, 1u);
-            tc::mma_bf16(tmem + kHAcc2, dam, dbm, idesc, 1u);
-            tc::mma_bf16(tmem + kHAcc3, dam, dbl, idesc, acc);
-            tc::mma_bf16(tmem + kHAcc3, dal, dbm, idesc, 1u);
-            tc::mma_bf16(tmem + kHAcc3, dal, dbl, idesc, 1u);
-          }
-          tc::mma_commit(&mbar);
-        }
-        if (!tc::mbar_wait(&mbar, commits & 1)) {
-          if (tid == 0) atomicExch(args.status, LCP_ETIMEDOUT);
-          abort_flag = 1;
-          tc::mbar_wait(&mbar, commits & 1);  // second bounded window for MMAs still in flight
-        }
-        ++commits;
-        tc::fence_after_sync();
-        const int row = warp * 32 + lane;
-        const int s = s0 + (row >> 4), a = row & 15;
-        for (int t = tstart; t < w1; ++t) {
-          float y0[16], y1[16], y2[16], y3[16];
-          tc::tmem_ld16(tc::tmem_addr(tmem, warp * 32, 16 * (t - tstart)), y0);
-          tc::tmem_ld16(tc::tmem_addr(tmem, warp * 32, kHAcc1 + 16 * (t - tstart)), y1);
-          tc::tmem_ld16(tc::tmem_addr(tmem, warp * 32, kHAcc2 + 16 * (t - tstart)), y2);
-          tc::tmem_ld16(tc::tmem_addr(tmem, warp * 32, kHAcc3 + 16 * (t - tstart)), y3);
-          if (s < m && s <= t) {
-            const int slot = args.tab_slot[t0 + s * m + t];
-            if (slot >= 0) {
-              float o[16];
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue (warps 2-5)
+    const uint32_t quarter = warp & 3;
+    const int row = (int)quarter * 32 + lane;  // TMEM lane = M row = (s image, orbital)
+    uint32_t it = 0;
+    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
+      const int64_t i0 = args.img_off[hb];
+      const int m = (int)(args.img_off[hb + 1] - i0);
+      if (m == 0) continue;
+      const int64_t tb = args.tab_off[hb];
+      const int64_t sbase = args.slot_base[hb];
+      // the brick's V scale, as the transform warps compute it (exact, so identical)
+      double vm = 0.0;
 #pragma unroll
-              for (int c = 0; c < 16; ++c) o[c] = (y0[c] + (y1[c] + (y2[c] + y3[c]))) * out_scale;
-              float4* dst = reinterpret_cast<float4*>(args.scratch + (sbase + slot) * 256 + a * 16);
-              dst[0] = make_float4(o[0], o[1], o[2], o[3]);
-              dst[1] = make_float4(o[4], o[5], o[6], o[7]);
-              dst[2] = make_float4(o[8], o[9], o[10], o[11]);
-              dst[3] = make_float4(o[12], o[13], o[14], o[15]);
+      for (int k = 0; k < 4; ++k) {
+        const int pt = lane + 32 * k;
+        if (pt < args.npts) vm = fmax(vm, fabs(args.vpot[brick_point_index(hb, pt, args.bdim, args.nb, args.ngrid)]));
+      }
+      for (int o = 16; o > 0; o >>= 1) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+      const float out_scale = (float)(pow2_ceil(vm) * args.phi_scale * args.phi_scale);  // a power of two
+      for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
+        const int s = s0 + (row >> 4), a = row & 15;
+        for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
+          const int nt = min(kHWin, m - t0);
+          const uint32_t buf = it & 1;
+          int slot[kHWin];
+#pragma unroll
+          for (int j = 0; j < kHWin; ++j)
+            slot[j] = (j < nt && s < m && s <= t0 + j) ? args.tab_slot[tb + s * m + t0 + j] : -1;
+          if (!tc::mbar_wait_abortable(&tfull_bar[buf], (it >> 1) & 1, &abort_flag)) {
+            give_up();
+            break;
+          }
+          tc::fence_after_sync();
+#pragma unroll
+          for (int j = 0; j < kHWin; ++j) {
+            if (j < nt) {
+              uint32_t y[4][16];
+              const uint32_t col = buf * kHBufCols + 16 * j;
+#pragma unroll
+              for (int k = 0; k < 4; ++k) tc::tmem_ld16_nowait(tc::tmem_addr(tmem, quarter * 32, col + k * kHAccCols), y[k]);
+              tc::tmem_wait_ld();
+#pragma unroll
+              for (int k = 0; k < 4; ++k) tc::tmem_regs_ready(y[k]);
+              if (slot[j] >= 0) {
+                float o[16];
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                  o[c] = (__uint_as_float(y[0][c]) +
+                          (__uint_as_float(y[1][c]) + (__uint_as_float(y[2][c]) + __uint_as_float(y[3][c])))) *
+                         out_scale;
+                float4* dst = reinterpret_cast<float4*>(args.scratch + (sbase + slot[j]) * 256 + a * 16);
+                dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+                dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+                dst[2] = make_float4(o[8], o[9], o[10], o[11]);
+                dst[3] = make_float4(o[12], o[13], o[14], o[15]);
+              }
             }
           }
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&tempty_bar[buf]);
         }
-        tc::fence_before_sync();
-        __syncthreads();
       }
     }
   }
   tc::fence_before_sync();
   __syncthreads();
+  tc::fence_after_sync();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // Float-float sum of the partial blocks of each folded pair in a fixed order,
-// written (x dV, as FP64) to both blocks.
+// written (x dV, as FP64) to both blocks.  One block of 256 threads per folded
+// pair; warp w sums every 8th slot of the pair with coalesced float4 loads
+// (lane l holds entries 8l .. 8l+7 of the 16 x 16 partial), keeping partials
+// of the pair's own orientation and of the partner orientation apart.  The
+// eight warps' sums are then combined in warp order through shared memory,
+// the partner ones transposed -- the same order on every run.
+__device__ __forceinline__ void ff_add8(float* hi, float* lo, float4 a, float4 b) {
+  ff_add(hi[0], lo[0], a.x); ff_add(hi[1], lo[1], a.y); ff_add(hi[2], lo[2], a.z); ff_add(hi[3], lo[3], a.w);
+  ff_add(hi[4], lo[4], b.x); ff_add(hi[5], lo[5], b.y); ff_add(hi[6], lo[6], b.z); ff_add(hi[7], lo[7], b.w);
+}
+
 __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nu, const int64_t* __restrict__ red_off,
                                                        const int64_t* __restrict__ red_slot,
                                                        const float* __restrict__ scratch, DevPairs pr,
                                                        const int32_t* __restrict__ numorbs, double dv, double* H) {
-  const int e = threadIdx.x, a = e >> 4, b = e & 15;
+  __shared__ int64_t s_code[256];
+  __shared__ float s_part[4][8][256];  // [own hi, own lo, partner hi, partner lo][warp][entry]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int64_t u = blockIdx.x; u < nu; u += gridDim.x) {
-    float acc_hi = 0.0f, acc_lo = 0.0f;
-    for (int64_t k = red_off[u]; k < red_off[u + 1]; ++k) {
-      const int64_t code = red_slot[k];
-      const int64_t slot = code >> 1;
-      ff_add(acc_hi, acc_lo, scratch[slot * 256 + ((code & 1) ? b * 16 + a : a * 16 + b)]);
+    float dh[8], dl[8], th[8], tl[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) dh[i] = dl[i] = th[i] = tl[i] = 0.0f;
+    const int64_t k0 = red_off[u], k1 = red_off[u + 1];
+    for (int64_t kb = k0; kb < k1; kb += 256) {
+      const int n = (int)min((int64_t)256, k1 - kb);
+      __syncthreads();
+      if (tid < n) s_code[tid] = red_slot[kb + tid];
+      __syncthreads();
+      for (int j = warp; j < n; j += 32) {  // slots j, j+8, j+16, j+24 in flight together
+        float4 v[4][2];
+        int64_t c[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int jj = j + 8 * q;
+          c[q] = jj < n ? s_code[jj] : -1;
+          if (c[q] >= 0) {
+            const float4* src = reinterpret_cast<const float4*>(scratch + (c[q] >> 1) * 256) + lane * 2;
+            v[q][0] = __ldg(src);
+            v[q][1] = __ldg(src + 1);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (c[q] < 0) continue;
+          if (c[q] & 1) ff_add8(th, tl, v[q][0], v[q][1]);
+          else ff_add8(dh, dl, v[q][0], v[q][1]);
+        }
+      }
     }
-    const double acc = (double)acc_hi + (double)acc_lo;
-    const int i = pr.atom[u], j = pr.jatom[u];
-    const int noi = numorbs[i], noj = numorbs[j];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      s_part[0][warp][lane * 8 + i] = dh[i];
+      s_part[1][warp][lane * 8 + i] = dl[i];
+      s_part[2][warp][lane * 8 + i] = th[i];
+      s_part[3][warp][lane * 8 + i] = tl[i];
+    }
+    __syncthreads();
+    const int a = tid >> 4, b = tid & 15, et = b * 16 + a;
+    float hi = 0.0f, lo = 0.0f;
+    for (int w = 0; w < 8; ++w) {
+      ff_add(hi, lo, s_part[0][w][tid]);
+      lo += s_part[1][w][tid];
+      ff_add(hi, lo, s_part[2][w][et]);
+      lo += s_part[3][w][et];
+    }
+    const double acc = (double)hi + (double)lo;
+    const int i = pr.atom[u], jj = pr.jatom[u];
+    const int noi = numorbs[i], noj = numorbs[jj];
     if (a < noi && b < noj) {
       const double v = acc * dv;
       H[pr.boff_p[u] + (int64_t)a * noj + b] = v;
@@ -696,7 +1047,8 @@ cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const 
   LCP_CUDA_TRY(cudaMemsetAsync(tab, 0, (size_t)nblocks * kBlockElems * sizeof(__nv_bfloat16), st));
   if (npoints == 0) return cudaSuccess;
   int blocks = (int)std::min<int64_t>((npoints + 255) / 256, (int64_t)sm_count() * 16);
-  brick_table_kernel<<<blocks, 256, 0, st>>>(phi, phi_off, numorbs, sph_off, natom, point_code, npoints, scale, tab);
+  brick_table_kernel<<<blocks, 256, 0, st>>>(phi, phi_off, numorbs, sph_off, natom, point_code, npoints, scale, tab,
+                                              nblocks);
   return cudaGetLastError();
 }
 
@@ -712,9 +1064,10 @@ cudaError_t launch_dsym(int nloop, const int32_t* pair_atom, const int32_t* pair
 cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
                               const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
                               int* status, cudaStream_t st) {
-  if (bg.max_images > 32) return cudaErrorInvalidValue;
+  if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
   TcDensArgs a{};
   a.nbricks = bg.nbricks;
+  a.nblocks = bg.nblocks;
   for (int d = 0; d < 3; ++d) {
     a.bdim[d] = bg.bdim[d];
     a.nb[d] = bg.nb[d];
@@ -725,26 +1078,27 @@ cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, d
   a.phi_scale = phi_scale;
   a.dscale = dscale;
   a.img_off = bg.img_off;
-  a.img_block = bg.img_block;
   a.tab_off = bg.tab_off;
   a.tab_pair = bg.tab_pair;
   a.tab = tab;
   a.dsym = dsym;
   a.rho = rho;
   a.status = status;
-  // 512 TMEM columns per CTA: reserve enough shared memory to keep one CTA per SM
-  const size_t smem = std::max<size_t>(2 * kASmem + 2 * kBSmem, 120 * 1024);
-  LCP_CUDA_TRY(cudaFuncSetAttribute(density_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // 512 TMEM columns per CTA: the shared-memory ring (> half an SM) keeps one CTA per SM
+  static_assert(kDSmem > 120 * 1024, "one CTA per SM");
+  LCP_CUDA_TRY(cudaFuncSetAttribute(density_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDSmem));
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(bg.nbricks, sm_count()));
-  density_tc_kernel<<<grid, 128, smem, st>>>(a);
+  density_tc_kernel<<<grid, 192 + 32 * kDGatherWarps, kDSmem, st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
                                   const __nv_bfloat16* tab, double phi_scale, const double* vpot, float* scratch,
                                   int* status, cudaStream_t st) {
+  if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
   TcHamArgs a{};
   a.nbricks = bg.nbricks;
+  a.nblocks = bg.nblocks;
   for (int d = 0; d < 3; ++d) {
     a.bdim[d] = bg.bdim[d];
     a.nb[d] = bg.nb[d];
@@ -753,7 +1107,6 @@ cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot
   a.npts = bg.npts;
   a.phi_scale = phi_scale;
   a.img_off = bg.img_off;
-  a.img_block = bg.img_block;
   a.tab_off = bg.tab_off;
   a.tab_slot = tab_slot;
   a.slot_base = slot_base;
@@ -763,7 +1116,8 @@ cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot
   a.status = status;
   LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(bg.nbricks, sm_count()));
-  hamiltonian_tc_kernel<<<grid, 128, kHSmem, st>>>(a);
+  static_assert(kHSmem > 120 * 1024, "one CTA per SM");
+  hamiltonian_tc_kernel<<<grid, 192 + 32 * kHXformWarps, kHSmem, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -11,6 +11,8 @@
 // SBO strides the 8-groups along M/N, LBO the 8-groups along K.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 namespace lcp {
@@ -114,6 +116,44 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
   return false;
 }
 
+// Bounded wait that also gives up as soon as *abort is set by another role of
+// the CTA.  Returns false on timeout or abort.
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* mbar, uint32_t parity, const volatile int* abort,
+                                                    uint32_t max_iters = (1u << 24)) {
+  for (uint32_t i = 0; i < max_iters; ++i) {
+    if (mbar_try_wait(mbar, parity)) return true;
+    if ((i & 63u) == 63u && *abort) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// Arrives once and adds `bytes` to the phase's expected transaction count.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+
+// ---------------------------------------------------------------- bulk copies (TMA, untiled)
+
+// global -> shared copy of `bytes` (multiple of 16; both addresses 16-byte
+// aligned), completing as transactions on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(sdst)),
+      "l"(gsrc), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+
+// Barrier among `nthreads` threads (whole warps) of the CTA.
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // ---------------------------------------------------------------- TMEM -> registers
 
 // 32 lanes x 16 consecutive 32-bit columns: thread t of the warp receives lane
@@ -131,6 +171,26 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// The same load without waiting: several loads can be in flight before one
+// tmem_wait_ld(); the registers are valid only after it.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Ties 16 loaded registers to a point after tmem_wait_ld(): the compiler sees
+// them redefined here, so no use of them is scheduled before the wait.
+__device__ __forceinline__ void tmem_regs_ready(uint32_t* r) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]));
+}
+
 // TMEM address of (lane, column): lane in bits 31..16, column in bits 15..0.
 __device__ __forceinline__ uint32_t tmem_addr(uint32_t base, uint32_t lane, uint32_t col) {
   return base + (lane << 16) + col;
@@ -145,11 +205,6 @@ __device__ __forceinline__ uint32_t mnmajor_off(uint32_t mn, uint32_t k, uint32_
   return (mn >> 3) * sbo + (k >> 3) * lbo + (((k & 7) << 3) + (mn & 7)) * 2;
 }
 
-// bf16 split of an FP32 value: hi = rn(x), lo = rn(x - hi).
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn(x);
-  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-}
 
 }  // namespace tc
 }  // namespace lcp
