@@ -201,7 +201,8 @@ lcp_status lcp_job_set_dm(lcp_ctx* ctx, lcp_job* job, const double* const* dm);
 /* Launch one grid step on the context stream (asynchronous). */
 lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job);
 /* The same step with CUDA events between its stages (synchronises); stage_ms[6] =
- * density, Poisson, xc+potential, energy sums, grid H, <D,H> + job energy
+ * density, Poisson, xc+potential (with the energy partial sums of the same
+ * pass), energy sums (their final reduction), grid H, <D,H> + job energy
  * (the stage names of the reference's TimerOutputs sections). */
 lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms);
 /* Energies of the last step: [E_H1, EXC1[1], EXC1[2], sum_s <D_s,H_s>, E_grid]. */

@@ -102,7 +102,7 @@ struct lcp_ctx {
   std::map<std::tuple<int, int, int>, FftPlans> plans;
   // workspaces of the host-buffer entry points
   DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
-  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp;
+  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale;
   ~lcp_ctx() {
     cudaSetDevice(device);
     for (auto& kv : plans) {
@@ -321,16 +321,20 @@ lcp_status hamiltonian_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nch, 
   const lcp::UCell& u = o->ucell->u;
   const int64_t nslots = o->bricks.slot_base.back();
   API_CUDA(ctx->w_hscratch.ensure((size_t)std::max<int64_t>(nslots, 1) * 256 * sizeof(float)), "H scratch alloc");
+  const size_t nb = (size_t)std::max<int64_t>(o->bgeom.nbricks, 1);
+  API_CUDA(ctx->w_vw.ensure(nb * 128 * sizeof(float2)), "V weight alloc");
+  API_CUDA(ctx->w_vscale.ensure(nb * sizeof(float)), "V scale alloc");
   for (int c = 0; c < nch; ++c) {
     API_CUDA(lcp::launch_hamiltonian_tc(o->bgeom, o->b_tabslot.as<int32_t>(), o->b_slotbase.as<int64_t>(),
-                                        o->b_tab.as<__nv_bfloat16>(), o->phi_scale, vpot[c],
-                                        ctx->w_hscratch.as<float>(), ctx->w_status.as<int>(), ctx->stream),
+                                        o->b_tab.as<__nv_bfloat16>(), o->phi_scale, vpot[c], ctx->w_vw.as<float2>(),
+                                        ctx->w_vscale.as<float>(), ctx->w_hscratch.as<float>(),
+                                        ctx->w_status.as<int>(), ctx->stream),
              "hamiltonian_tc");
     API_CUDA(lcp::launch_h_reduce(o->pairs.nu, o->b_redoff.as<int64_t>(), o->b_redslot.as<int64_t>(),
                                   ctx->w_hscratch.as<float>(), o->pairs, o->geom.numorbs, u.gridvol, hks[c],
                                   ctx->stream),
              "h_reduce");
-    ctx->launches += 2;
+    ctx->launches += 3;
   }
   return LCP_OK;
 }
@@ -1126,16 +1130,15 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
                           job->dvh.as<double>())))
     return s;
   mark(2);
-  // 3. xc + potential
-  API_CUDA(lcp::launch_xc_vpot(job->xc, job->spinpol, job->nn, pc, crho, job->dvh.as<double>(), na, nullptr, vp, st),
-           "xc_vpot");
+  // 3. xc + potential, with the FP64 energy partial sums in the same pass
+  API_CUDA(lcp::launch_xc_vpot_energy(job->xc, job->spinpol, job->nn, ad, pc, crho, job->dvh.as<double>(), na, vp,
+                                      job->part.as<double>(), st),
+           "xc_vpot_energy");
   ctx->launches++;
   mark(3);
-  // 4. FP64 energy terms
-  API_CUDA(lcp::launch_energy_sums(job->xc, job->spinpol, job->nn, ad, pc, crho, job->dvh.as<double>(),
-                                   job->part.as<double>(), job->scal.as<double>(), st),
-           "energy");
-  ctx->launches += 2;
+  // 4. FP64 energy terms: final reduction of the partial sums
+  API_CUDA(lcp::launch_finish_sums3(job->part.as<double>(), job->scal.as<double>(), st), "energy");
+  ctx->launches++;
   mark(4);
   // 5. grid matrix elements
   if ((s = hamiltonian_device(ctx, job->orbs, ns, cvp, hk, job->hsize))) return s;

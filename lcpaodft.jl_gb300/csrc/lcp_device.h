@@ -95,6 +95,12 @@ cudaError_t launch_vpot(int spinpol, int64_t nn, const double* dvh, const double
 cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* aden,
                                const double* pcc, const double* const* rho, const double* dvh,
                                double* partials, double* out, cudaStream_t st);
+// Job step: xc + potential + the energy partial sums in one pass (partials as
+// launch_energy_sums), then the final reduction of the three sums into out.
+cudaError_t launch_xc_vpot_energy(int xc, int spinpol, int64_t nn, const double* aden, const double* pcc,
+                                  const double* const* rho, const double* dvh, const double* vna,
+                                  double* const* vpot_out, double* partials, cudaStream_t st);
+cudaError_t launch_finish_sums3(const double* partials, double* out, cudaStream_t st);
 cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const double* const* b,
                            double* partials, double* out, cudaStream_t st);
 constexpr int kReduceBlocks = 1024;
@@ -123,9 +129,11 @@ cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, d
                               int* status, cudaStream_t st);
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int K, int a_mn, int b_mn,
                                int order, int* status, cudaStream_t st);
+// vw: nbricks * 128 float2 and vscale: nbricks floats of workspace (the
+// per-brick V weights); scratch: the FP32 partial blocks.
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
-                                  const __nv_bfloat16* tab, double phi_scale, const double* vpot, float* scratch,
-                                  int* status, cudaStream_t st);
+                                  const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
+                                  float* vscale, float* scratch, int* status, cudaStream_t st);
 cudaError_t launch_h_reduce(int64_t nu, const int64_t* red_off, const int64_t* red_slot, const float* scratch,
                             const DevPairs& pr, const int32_t* numorbs, double dv, double* H, cudaStream_t st);
 

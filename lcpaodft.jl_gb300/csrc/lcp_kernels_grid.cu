@@ -265,6 +265,53 @@ __global__ void __launch_bounds__(kRedThreads) energy_partials_kernel(EnergyArgs
   block_reduce_store<3>(v, a.partials + (size_t)blockIdx.x * 3);
 }
 
+// The job step's fused pass: Set_XC_Grid! + Set_Vpot_Grid! (as
+// xc_vpot_kernel) and the Calc_EH1 / Calc_EXC1 partial sums (as
+// energy_partials_kernel), evaluating the xc functional once per point.  The
+// partial sums run over the same points in the same order as
+// energy_partials_kernel, so the energies are bit-identical to it.
+__global__ void __launch_bounds__(kRedThreads) xc_vpot_energy_kernel(XcArgs a, EnergyArgs ea) {
+  double acc[3] = {0, 0, 0};
+  const int nv = a.spinpol == LCP_SPIN_OFF ? 1 : (a.spinpol == LCP_SPIN_ON ? 2 : 4);
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < a.nn; x += (int64_t)gridDim.x * blockDim.x) {
+    const double pc = a.pcc ? a.pcc[x] : 0.0;
+    const double r0 = a.rho[0][x];
+    double v[4] = {0, 0, 0, 0};
+    double e;
+    double r1 = 0.0;
+    if (a.xc == LCP_XC_LDA) {
+      lda_ca(2 * (r0 + pc), e, v[0]);
+    } else {
+      r1 = a.rho[1][x];
+      lsda_ca(r0 + pc, r1 + pc, e, v[0], v[1]);
+      if (a.spinpol == LCP_SPIN_NC) {
+        const double th = a.rho[2][x], ph = a.rho[3][x];
+        const double t0 = 0.5 * (v[0] + v[1]), t1 = 0.5 * (v[0] - v[1]);
+        v[3] = -t1 * sin(th) * sin(ph);
+        v[2] = t1 * sin(th) * cos(ph);
+        v[1] = t0 - t1 * cos(th);
+        v[0] = t0 + t1 * cos(th);
+      }
+    }
+    for (int c = 0; c < nv; ++c)
+      if (a.vxc[c]) a.vxc[c][x] = v[c];
+    const double dvh = a.dvh[x];
+    if (a.vpot[0]) {
+      const double na = a.vna ? a.vna[x] : 0.0;
+      for (int c = 0; c < nv; ++c) a.vpot[c][x] = c < 2 ? dvh + v[c] + na : v[c];
+    }
+    const double ad = ea.aden ? ea.aden[x] : 0.0;
+    const double drho = a.spinpol == LCP_SPIN_OFF ? 2 * (r0 - ad) : r0 + r1 - 2 * ad;
+    acc[0] += drho * dvh;
+    const double temp = ad + pc;
+    double eat, vat;
+    lda_ca(2 * temp, eat, vat);
+    acc[1] += (r0 + pc) * e - temp * eat;
+    if (a.xc != LCP_XC_LDA) acc[2] += (r1 + pc) * e - temp * eat;
+  }
+  block_reduce_store<3>(acc, ea.partials + (size_t)blockIdx.x * 3);
+}
+
 template <int NV>
 __global__ void __launch_bounds__(kRedThreads) finish_sums_kernel(const double* __restrict__ partials, int nblocks,
                                                                   double* out) {
@@ -377,6 +424,33 @@ cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* ad
   a.partials = partials;
   energy_partials_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(a);
   LCP_CUDA_TRY(cudaGetLastError());
+  finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_xc_vpot_energy(int xc, int spinpol, int64_t nn, const double* aden, const double* pcc,
+                                  const double* const* rho, const double* dvh, const double* vna,
+                                  double* const* vpot_out, double* partials, cudaStream_t st) {
+  XcArgs a{};
+  a.xc = xc;
+  a.spinpol = spinpol;
+  a.nn = nn;
+  a.pcc = pcc;
+  const int nr = spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4);
+  for (int c = 0; c < nr; ++c) {
+    a.rho[c] = rho[c];
+    a.vpot[c] = vpot_out[c];
+  }
+  a.dvh = dvh;
+  a.vna = vna;
+  EnergyArgs e{};
+  e.aden = aden;
+  e.partials = partials;
+  xc_vpot_energy_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(a, e);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finish_sums3(const double* partials, double* out, cudaStream_t st) {
   finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
   return cudaGetLastError();
 }

@@ -602,8 +602,9 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
 //              A region (after a_free), per tile the raw t window into one of
 //              kHStages B stages -- one bulk copy per part, the images of a
 //              brick being consecutive blocks;
-//   warps 6-13 per brick the V scale; per tile the V-weighted fixed-point
-//              split of the B stage, in place (b_ready);
+//   warps 6-13 per tile the V-weighted fixed-point split of the B stage, in
+//              place (b_ready), with the brick's V / S_V prepared by
+//              vweight_kernel;
 //   warp 1     MMA issuer: 8 K steps x 4 MMAs per tile into one of two TMEM
 //              tile buffers (4 accumulators x 64 columns each); after the
 //              group's last tile it commits a_free;
@@ -639,17 +640,47 @@ struct TcHamArgs {
   const int32_t* tab_slot;
   const int64_t* slot_base;
   const __nv_bfloat16* tab;
-  const double* vpot;
+  const float2* vw;     // per brick and point slot: V / S_V as FP32 hi + lo
+  const float* vscale;  // per brick: S_V * S_phi^2 (a power of two)
   float* scratch;
   int* status;
 };
+
+// Per brick: S_V = power of two >= max|V| over the brick's points, and V / S_V
+// (exact) as an FP32 pair hi + lo, for the V-weighting inside the matrix
+// element kernel.  One block of 128 threads (point slots) per brick.
+__global__ void __launch_bounds__(128) vweight_kernel(int64_t nbricks, int3 bdim, int3 nb, int3 ngrid, int npts,
+                                                      const double* __restrict__ vpot, double phi2,
+                                                      float2* __restrict__ vw, float* __restrict__ vscale) {
+  __shared__ unsigned long long smax[4];
+  const int p = threadIdx.x, warp = p >> 5, lane = p & 31;
+  const int32_t bd[3] = {bdim.x, bdim.y, bdim.z}, nbb[3] = {nb.x, nb.y, nb.z}, ng[3] = {ngrid.x, ngrid.y, ngrid.z};
+  for (int64_t hb = blockIdx.x; hb < nbricks; hb += gridDim.x) {
+    const double v = p < npts ? vpot[brick_point_index(hb, p, bd, nbb, ng)] : 0.0;
+    // |v| as bits: non-negative doubles order like their bit patterns
+    unsigned long long m = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+      m = x > m ? x : m;
+    }
+    if (lane == 0) smax[warp] = m;
+    __syncthreads();
+    unsigned long long mx = smax[0];
+    for (int w = 1; w < 4; ++w) mx = smax[w] > mx ? smax[w] : mx;
+    const double sv = pow2_ceil(__longlong_as_double((long long)mx));
+    const double vs = v * (1.0 / sv);  // exact: sv is a power of two
+    const float vh = (float)vs;
+    vw[hb * 128 + p] = make_float2(vh, (float)(vs - (double)vh));
+    if (p == 0) vscale[hb] = (float)(sv * phi2);
+    __syncthreads();
+  }
+}
 
 __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_kernel(TcHamArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint64_t bfull_bar[kHStages], bready_bar[kHStages], bempty_bar[kHStages], tfull_bar[2], tempty_bar[2];
   __shared__ uint64_t afull_bar, afree_bar, drain_bar;
   __shared__ uint32_t tslot;
-  __shared__ float sVh[kHXformWarps][128], sVl[kHXformWarps][128];
   __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   uint8_t* sA = smem;                  // [part][s image][4096 B], plain tables
@@ -799,35 +830,16 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     __syncwarp();
   } else if (warp >= 6) {
     // ------------------------------------------------------------ V-weighting of the B tiles
-    const int tw = warp - 6, tt = tid - 192;  // transform warp and thread
-    float* vh_w = sVh[tw];
-    float* vl_w = sVl[tw];
+    const int tt = tid - 192;  // transform thread: always the same 8-orbital chunk q = tt of an image
+    static_assert(32 * kHXformWarps == 256, "one transform thread per chunk of an image");
+    const int pt = ((tt >> 3) & 15) * 8 + (tt & 7);  // its point slot
     uint32_t it = 0;
     for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
       const int64_t i0 = args.img_off[hb];
       const int m = (int)(args.img_off[hb + 1] - i0);
       if (m == 0) continue;
-      // Per-brick power-of-two scale of V.  Every transform warp computes it
-      // over all 128 points and keeps its own copy of V / scale, so the
-      // warps need no barrier among themselves.
-      double vv[4], vm = 0.0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int pt = lane + 32 * k;
-        vv[k] = pt < args.npts ? args.vpot[brick_point_index(hb, pt, args.bdim, args.nb, args.ngrid)] : 0.0;
-        vm = fmax(vm, fabs(vv[k]));
-      }
-      for (int o = 16; o > 0; o >>= 1) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
-      const double sv = pow2_ceil(vm);
-      __syncwarp();  // this warp's reads of the previous brick's copy are done
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const double vs = vv[k] / sv;  // exact: sv is a power of two
-        const float vh = (float)vs;
-        vh_w[lane + 32 * k] = vh;
-        vl_w[lane + 32 * k] = (float)(vs - (double)vh);
-      }
-      __syncwarp();
+      const float2 w = args.vw[hb * 128 + pt];
+      const float vh = w.x, vl = w.y;
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
         for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
           const int nt = min(kHWin, m - t0);
@@ -844,8 +856,6 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
             uint4* ph = reinterpret_cast<uint4*>(sB + img * kImgBytes + q * 16);
             uint4* pm = reinterpret_cast<uint4*>(sB + kHBBytes + img * kImgBytes + q * 16);
             uint4* pl = reinterpret_cast<uint4*>(sB + 2 * kHBBytes + img * kImgBytes + q * 16);
-            const int pt = ((q >> 3) & 15) * 8 + (q & 7);
-            const float vh = vh_w[pt], vl = vl_w[pt];
             const uint4 rh = *ph, rm = *pm, rl = *pl;
             const __nv_bfloat16* xb_h = reinterpret_cast<const __nv_bfloat16*>(&rh);
             const __nv_bfloat16* xb_m = reinterpret_cast<const __nv_bfloat16*>(&rm);
@@ -882,15 +892,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
       if (m == 0) continue;
       const int64_t tb = args.tab_off[hb];
       const int64_t sbase = args.slot_base[hb];
-      // the brick's V scale, as the transform warps compute it (exact, so identical)
-      double vm = 0.0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int pt = lane + 32 * k;
-        if (pt < args.npts) vm = fmax(vm, fabs(args.vpot[brick_point_index(hb, pt, args.bdim, args.nb, args.ngrid)]));
-      }
-      for (int o = 16; o > 0; o >>= 1) vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
-      const float out_scale = (float)(pow2_ceil(vm) * args.phi_scale * args.phi_scale);  // a power of two
+      const float out_scale = args.vscale[hb];  // S_V * S_phi^2, a power of two
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
         const int s = s0 + (row >> 4), a = row & 15;
         for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
@@ -1093,8 +1095,8 @@ cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, d
 }
 
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
-                                  const __nv_bfloat16* tab, double phi_scale, const double* vpot, float* scratch,
-                                  int* status, cudaStream_t st) {
+                                  const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
+                                  float* vscale, float* scratch, int* status, cudaStream_t st) {
   if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
   TcHamArgs a{};
   a.nbricks = bg.nbricks;
@@ -1111,11 +1113,20 @@ cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot
   a.tab_slot = tab_slot;
   a.slot_base = slot_base;
   a.tab = tab;
-  a.vpot = vpot;
+  a.vw = vw;
+  a.vscale = vscale;
   a.scratch = scratch;
   a.status = status;
   LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(bg.nbricks, sm_count()));
+  if (bg.nbricks > 0) {
+    const int vgrid = (int)std::min<int64_t>(bg.nbricks, (int64_t)sm_count() * 16);
+    vweight_kernel<<<vgrid, 128, 0, st>>>(bg.nbricks, make_int3(bg.bdim[0], bg.bdim[1], bg.bdim[2]),
+                                          make_int3(bg.nb[0], bg.nb[1], bg.nb[2]),
+                                          make_int3(bg.ngrid[0], bg.ngrid[1], bg.ngrid[2]), bg.npts, vpot,
+                                          phi_scale * phi_scale, vw, vscale);
+    LCP_CUDA_TRY(cudaGetLastError());
+  }
   static_assert(kHSmem > 120 * 1024, "one CTA per SM");
   hamiltonian_tc_kernel<<<grid, 192 + 32 * kHXformWarps, kHSmem, st>>>(a);
   return cudaGetLastError();
