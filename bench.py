@@ -30,6 +30,11 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "ms per SCF grid step & jobs/s (p50/p99) split-BF16 vs FP64, <=1uHa/atom err"
+# DRAM bytes per table block of one split-BF16 stage launch (ncu, 8-atom 48^3
+# cell: density_tc_kernel 149.7 + 3.5 MB; hamiltonian_tc_kernel 150.0 + 55.2 MB
+# and h_reduce_kernel 93.6 + 3.2 MB, over 12076 blocks)
+TRAFFIC_PER_BLOCK = {"density": (149.71e6 + 3.51e6) / 12076,
+                     "hamiltonian": (150.05e6 + 55.20e6 + 93.62e6 + 3.18e6) / 12076}
 UNIT = "grid steps/s"
 
 
@@ -345,6 +350,17 @@ def run_ours(args):
         pk = peaks.get("bf16_tflops_sustained", 1700.0)
         roof = {"bound": "tensor", "kernel": names[dom], "achieved": dom_flops / (stages[dom] * 1e-3) / 1e12,
                 "peak": pk, "unit": "TFLOP/s", "peak_source": psrc + " bf16_tflops_sustained", "traffic": None}
+        if args.precision == "bf16x3":
+            # DRAM bytes (read + write) per launch of the stage's kernels, measured
+            # with ncu on the 8-atom cell of the same crystal and grid spacing and
+            # scaled by table blocks (every brick image is one block)
+            per_block = TRAFFIC_PER_BLOCK.get(names[dom])
+            nblocks = u.brick_info()["blocks"]
+            if per_block is not None:
+                roof["traffic"] = per_block * nblocks
+                roof["traffic_note"] = ("ncu dram__bytes_read+write on the 8-atom 48^3 cell (12076 table blocks), "
+                                        "scaled by table blocks (%d here); partial blocks that stay in L2 there "
+                                        "make it a lower bound" % nblocks)
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     ms_step = total_ms / args.steps

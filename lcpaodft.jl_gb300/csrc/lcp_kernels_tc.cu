@@ -166,6 +166,19 @@ __device__ __forceinline__ double pow2_ceil(double x) {
   return m == 0.5 ? ldexp(1.0, e - 1) : ldexp(1.0, e);
 }
 
+// Exponent e of the smallest power of two >= |x| (x given by its bits with the
+// sign cleared; 0 for x = 0, as pow2_ceil), by integer operations only.
+__device__ __forceinline__ int pow2_ceil_exp(unsigned long long absbits) {
+  if (absbits == 0) return 0;
+  const int be = (int)(absbits >> 52);                  // biased exponent (0: subnormal)
+  const unsigned long long man = absbits & ((1ull << 52) - 1);
+  if (be == 0) return -1022;                            // subnormal: 2^-1022 bounds it
+  return (be - 1023) + (man != 0 ? 1 : 0);
+}
+__device__ __forceinline__ double pow2_from_exp(int e) {  // 2^e for |e| <= 1022, exact
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(sdst)), "l"(gsrc) : "memory");
 }
@@ -177,11 +190,17 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // max |x| over n doubles (non-negative doubles order like their bit patterns)
 __global__ void absmax_kernel(const double* __restrict__ x, int64_t n, unsigned long long* out) {
-  double m = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    m = fmax(m, fabs(x[i]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+  // on the bits with the sign cleared (integer operations only)
+  unsigned long long m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x[i]) & 0x7fffffffffffffffull;
+    m = b > m ? b : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
 }
 
 // scale[0] = power of two >= factor * max, scale[1] = its inverse
@@ -667,8 +686,9 @@ __global__ void __launch_bounds__(128) vweight_kernel(int64_t nbricks, int3 bdim
     __syncthreads();
     unsigned long long mx = smax[0];
     for (int w = 1; w < 4; ++w) mx = smax[w] > mx ? smax[w] : mx;
-    const double sv = pow2_ceil(__longlong_as_double((long long)mx));
-    const double vs = v * (1.0 / sv);  // exact: sv is a power of two
+    const int e = pow2_ceil_exp(mx);
+    const double sv = pow2_from_exp(e);
+    const double vs = v * pow2_from_exp(-e);  // exact: a power-of-two scaling
     const float vh = (float)vs;
     vw[hb * 128 + p] = make_float2(vh, (float)(vs - (double)vh));
     if (p == 0) vscale[hb] = (float)(sv * phi2);
