@@ -131,6 +131,7 @@ struct lcp_orbs {
   lcp::Bricks bricks;
   lcp::TcBrickGeom bgeom{};
   DBuf b_code, b_imgoff, b_imgblk, b_taboff, b_tabpair, b_tab, b_tabslot, b_slotbase, b_redoff, b_redslot;
+  DBuf b_subpair, b_subchunks, b_sbfold, b_sbchunks;  // sub-pairs and H sub-blocks (orbital chunks)
   DBuf o_atom, o_jatom, o_boff, o_partner;  // ordered pair list
   DBuf b_scale, b_tmp;                       // fixed-point scale of the tables: [S_phi, 1/S_phi]
   double phi_scale = 1.0;
@@ -206,13 +207,12 @@ lcp_status ensure_phi32(lcp_ctx* ctx, lcp_orbs* o) {
 lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   if (o->bricks_ready) return LCP_OK;
   const lcp::UCell& u = o->ucell->u;
-  if (o->max_no > 16) return fail(LCP_ENOTSUP, "the tensor-core path supports up to 16 orbitals per atom");
   lcp::Bricks& b = o->bricks;
   std::string err = lcp::build_bricks(u, b);
   if (!err.empty()) return fail(LCP_EINVAL, err);
-  if (b.max_images > 32)
+  if (b.max_images > 64)
     return fail(LCP_ENOTSUP, "a grid brick is touched by " + std::to_string(b.max_images) +
-                                 " atom images; the tensor-core path supports 32");
+                                 " atom images (16-orbital chunks); the tensor-core path supports 64");
   cudaStream_t st = ctx->stream;
   API_CUDA(upload(o->b_code, b.point_code, st), "upload");
   API_CUDA(upload(o->b_imgoff, b.img_off, st), "upload");
@@ -223,6 +223,10 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   API_CUDA(upload(o->b_slotbase, b.slot_base, st), "upload");
   API_CUDA(upload(o->b_redoff, b.red_off, st), "upload");
   API_CUDA(upload(o->b_redslot, b.red_slot, st), "upload");
+  API_CUDA(upload(o->b_subpair, b.sub_pair, st), "upload");
+  API_CUDA(upload(o->b_subchunks, b.sub_chunks, st), "upload");
+  API_CUDA(upload(o->b_sbfold, b.sb_fold, st), "upload");
+  API_CUDA(upload(o->b_sbchunks, b.sb_chunks, st), "upload");
   std::vector<int64_t> boff(u.block_off.begin(), u.block_off.end());
   API_CUDA(upload(o->o_atom, u.pair_atom, st), "upload");
   API_CUDA(upload(o->o_jatom, u.pair_jatom, st), "upload");
@@ -265,7 +269,8 @@ lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, co
   lcp_status s = ensure_bricks(ctx, o);
   if (s) return s;
   const lcp::UCell& u = o->ucell->u;
-  API_CUDA(ctx->w_dsym.ensure((size_t)(u.nloop + 1) * 768 * 2), "dsym alloc");
+  const int64_t nsub = o->bricks.nsub;
+  API_CUDA(ctx->w_dsym.ensure((size_t)(nsub + 1) * 768 * 2), "dsym alloc");
   API_CUDA(ctx->w_dscale.ensure(2 * sizeof(double)), "alloc");
   API_CUDA(ctx->w_dtmp.ensure(sizeof(unsigned long long)), "alloc");
   for (int c = 0; c < nspin; ++c) {
@@ -273,12 +278,13 @@ lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, co
     API_CUDA(lcp::launch_absmax_scale(dm[c], u.total_hsize, 2.0, ctx->w_dtmp.as<unsigned long long>(),
                                       ctx->w_dscale.as<double>(), ctx->stream),
              "dm scale");
-    API_CUDA(lcp::launch_dsym(u.nloop, o->o_atom.as<int32_t>(), o->o_jatom.as<int32_t>(), o->o_boff.as<int64_t>(),
-                              o->o_partner.as<int32_t>(), o->geom.numorbs, dm[c], ctx->w_dscale.as<double>(),
+    API_CUDA(lcp::launch_dsym(nsub, o->b_subpair.as<int32_t>(), o->b_subchunks.as<int32_t>(), o->o_atom.as<int32_t>(),
+                              o->o_jatom.as<int32_t>(), o->o_boff.as<int64_t>(), o->o_partner.as<int32_t>(),
+                              o->geom.numorbs, dm[c], ctx->w_dscale.as<double>(),
                               ctx->w_dsym.as<__nv_bfloat16>(), ctx->stream),
              "dsym");
     API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale,
-                                    ctx->w_dsym.as<__nv_bfloat16>(), ctx->w_dscale.as<double>(), u.nloop, rho[c],
+                                    ctx->w_dsym.as<__nv_bfloat16>(), ctx->w_dscale.as<double>(), (int)nsub, rho[c],
                                     ctx->w_status.as<int>(), ctx->stream),
              "density_tc");
     ctx->launches += 4;
@@ -330,7 +336,8 @@ lcp_status hamiltonian_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nch, 
                                         ctx->w_vscale.as<float>(), ctx->w_hscratch.as<float>(),
                                         ctx->w_status.as<int>(), ctx->stream),
              "hamiltonian_tc");
-    API_CUDA(lcp::launch_h_reduce(o->pairs.nu, o->b_redoff.as<int64_t>(), o->b_redslot.as<int64_t>(),
+    API_CUDA(lcp::launch_h_reduce((int64_t)o->bricks.sb_fold.size(), o->b_redoff.as<int64_t>(),
+                                  o->b_redslot.as<int64_t>(), o->b_sbfold.as<int32_t>(), o->b_sbchunks.as<int32_t>(),
                                   ctx->w_hscratch.as<float>(), o->pairs, o->geom.numorbs, u.gridvol, hks[c],
                                   ctx->stream),
              "h_reduce");
@@ -1320,6 +1327,11 @@ lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, co
     return fail(LCP_ESTATE,
                 "the split-BF16 tables of these orbitals are not built; one allocating split-BF16 call "
                 "(lcp_set_density_grid or lcp_calc_matrix_elements at LCP_PREC_BF16X3) builds them");
+  const int64_t nsub = orbs->bricks.nsub;  // == Nloop unless atoms have more than 16 orbitals
+  if (nsub > kNoAllocMaxPairs)
+    return fail(LCP_EINVAL, "the no-allocation density holds at most " + std::to_string(kNoAllocMaxPairs) +
+                                " D blocks (16 MiB); this cell has " + std::to_string(nsub) +
+                                " (16-orbital sub-blocks of its neighbour pairs)");
   unsigned char* base = nullptr;
   if ((s = noalloc_scratch(ctx->device, &base))) return s;
   double* dscale = reinterpret_cast<double*>(base);
@@ -1330,10 +1342,11 @@ lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, co
   API_CUDA(cudaMemsetAsync(status, 0, sizeof(int), ctx->stream), "memset");
   for (int c = 0; c < ns; ++c) {
     API_CUDA(lcp::launch_absmax_scale(dm_dev[c], u.total_hsize, 2.0, dmax, dscale, ctx->stream), "dm scale");
-    API_CUDA(lcp::launch_dsym(u.nloop, o->o_atom.as<int32_t>(), o->o_jatom.as<int32_t>(), o->o_boff.as<int64_t>(),
-                              o->o_partner.as<int32_t>(), o->geom.numorbs, dm_dev[c], dscale, dsym, ctx->stream),
+    API_CUDA(lcp::launch_dsym(nsub, o->b_subpair.as<int32_t>(), o->b_subchunks.as<int32_t>(), o->o_atom.as<int32_t>(),
+                              o->o_jatom.as<int32_t>(), o->o_boff.as<int64_t>(), o->o_partner.as<int32_t>(),
+                              o->geom.numorbs, dm_dev[c], dscale, dsym, ctx->stream),
              "dsym");
-    API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale, dsym, dscale, u.nloop,
+    API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale, dsym, dscale, (int)nsub,
                                     density_grid_dev[c], status, ctx->stream),
              "density_tc");
     ctx->launches += 4;

@@ -121,9 +121,9 @@ cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsig
 cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const int32_t* numorbs,
                                const int64_t* sph_off, int natom, const int32_t* point_code, int64_t npoints,
                                const double* scale, __nv_bfloat16* tab, int64_t nblocks, cudaStream_t st);
-cudaError_t launch_dsym(int nloop, const int32_t* pair_atom, const int32_t* pair_jatom, const int64_t* boff,
-                        const int32_t* partner, const int32_t* numorbs, const double* dm, const double* scale,
-                        __nv_bfloat16* out, cudaStream_t st);
+cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* sub_chunks, const int32_t* pair_atom,
+                        const int32_t* pair_jatom, const int64_t* boff, const int32_t* partner, const int32_t* numorbs,
+                        const double* dm, const double* scale, __nv_bfloat16* out, cudaStream_t st);
 cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
                               const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
                               int* status, cudaStream_t st);
@@ -134,7 +134,8 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
                                   const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
                                   float* vscale, float* scratch, int* status, cudaStream_t st);
-cudaError_t launch_h_reduce(int64_t nu, const int64_t* red_off, const int64_t* red_slot, const float* scratch,
-                            const DevPairs& pr, const int32_t* numorbs, double dv, double* H, cudaStream_t st);
+cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* red_slot, const int32_t* sb_fold,
+                            const int32_t* sb_chunks, const float* scratch, const DevPairs& pr,
+                            const int32_t* numorbs, double dv, double* H, cudaStream_t st);
 
 }  // namespace lcp

@@ -499,11 +499,15 @@ std::string build_bricks(const UCell& u, Bricks& b) {
   const int64_t npoints = u.sphere_off.empty() ? 0 : u.sphere_off.back();
   b.point_code.assign(npoints, 0);
   b.block_atom.clear();
+  // orbital chunks: an atom with NO orbitals is ceil(NO/16) sub-images of 16
+  std::vector<int32_t> nch(u.natom);
+  for (int a = 0; a < u.natom; ++a) nch[a] = (u.numorbs[a] + 15) / 16;
   struct Img {
     int32_t atom, block, r0, r1, r2;
   };
   std::vector<std::vector<Img>> per_brick(b.nbricks);
   for (int a = 0; a < u.natom; ++a) {
+    if (nch[a] == 0) continue;  // no orbitals: no blocks
     std::map<std::tuple<int, int, int>, int32_t> blocks;
     for (int64_t k = u.sphere_off[a]; k < u.sphere_off[a + 1]; ++k) {
       int x, y, z;
@@ -513,8 +517,8 @@ std::string build_bricks(const UCell& u, Bricks& b) {
       auto it = blocks.find(key);
       int32_t blk;
       if (it == blocks.end()) {
-        blk = (int32_t)b.block_atom.size();
-        b.block_atom.push_back(a);
+        blk = (int32_t)b.block_atom.size();  // the chunks' blocks are blk .. blk + nch - 1
+        for (int c = 0; c < nch[a]; ++c) b.block_atom.push_back(a);
         blocks.emplace(key, blk);
         int h0 = c0 - floordiv(c0, b.nb[0]) * b.nb[0];
         int h1 = c1 - floordiv(c1, b.nb[1]) * b.nb[1];
@@ -533,6 +537,20 @@ std::string build_bricks(const UCell& u, Bricks& b) {
   // ordered pair of (atom, jatom, cell)
   std::map<std::tuple<int, int, int>, int32_t> pair_of;
   for (int p = 0; p < u.nloop; ++p) pair_of[{u.pair_atom[p], u.pair_jatom[p], u.pair_cell[p]}] = p;
+  // sub-pairs: (pair, row chunk, column chunk), numbered pair-major
+  b.sub_off.assign(u.nloop + 1, 0);
+  for (int p = 0; p < u.nloop; ++p)
+    b.sub_off[p + 1] = b.sub_off[p] + (int64_t)nch[u.pair_atom[p]] * nch[u.pair_jatom[p]];
+  b.nsub = b.sub_off[u.nloop];
+  b.sub_pair.resize(b.nsub);
+  b.sub_chunks.resize(b.nsub);
+  for (int p = 0; p < u.nloop; ++p)
+    for (int ca = 0; ca < nch[u.pair_atom[p]]; ++ca)
+      for (int cb = 0; cb < nch[u.pair_jatom[p]]; ++cb) {
+        const int64_t sp = b.sub_off[p] + (int64_t)ca * nch[u.pair_jatom[p]] + cb;
+        b.sub_pair[sp] = p;
+        b.sub_chunks[sp] = (ca << 8) | cb;
+      }
   const int C = u.cpycell, n = 2 * C + 1;
   b.img_off.assign(b.nbricks + 1, 0);
   b.tab_off.assign(b.nbricks + 1, 0);
@@ -545,24 +563,33 @@ std::string build_bricks(const UCell& u, Bricks& b) {
     std::sort(v.begin(), v.end(), [](const Img& x, const Img& y) {
       return std::make_tuple(x.atom, x.r0, x.r1, x.r2) < std::make_tuple(y.atom, y.r0, y.r1, y.r2);
     });
-    const int m = (int)v.size();
+    // sub-images: each image's chunks, consecutive
+    std::vector<int32_t> img_of, chunk_of;
+    for (int s = 0; s < (int)v.size(); ++s)
+      for (int c = 0; c < nch[v[s].atom]; ++c) {
+        b.img_block.push_back(v[s].block + c);
+        b.img_atom.push_back(v[s].atom);
+        img_of.push_back(s);
+        chunk_of.push_back(c);
+      }
+    const int m = (int)img_of.size();
     b.max_images = std::max(b.max_images, m);
-    for (auto& im : v) {
-      b.img_block.push_back(im.block);
-      b.img_atom.push_back(im.atom);
-    }
     b.img_off[hb + 1] = (int64_t)b.img_block.size();
-    // image s = atom shifted by -R_s; pair (atom_s, atom_t, R_s - R_t)
-    for (int s = 0; s < m; ++s)
-      for (int t = 0; t < m; ++t) {
-        int d0 = v[s].r0 - v[t].r0, d1 = v[s].r1 - v[t].r1, d2 = v[s].r2 - v[t].r2;
-        int32_t pair = -1;
+    // image s = atom shifted by -R_s; pair (atom_s, atom_t, R_s - R_t); the
+    // sub-image pair (s, ca), (t, cb) is that pair's sub-pair (ca, cb)
+    for (int si = 0; si < m; ++si)
+      for (int ti = 0; ti < m; ++ti) {
+        const Img& vs = v[img_of[si]];
+        const Img& vt = v[img_of[ti]];
+        int d0 = vs.r0 - vt.r0, d1 = vs.r1 - vt.r1, d2 = vs.r2 - vt.r2;
+        int32_t sub = -1;
         if (std::abs(d0) <= C && std::abs(d1) <= C && std::abs(d2) <= C) {
           int cell = u.ratv[((size_t)(d0 + C) * n + (d1 + C)) * n + (d2 + C)];
-          auto it = pair_of.find({v[s].atom, v[t].atom, cell});
-          if (it != pair_of.end()) pair = it->second;
+          auto it = pair_of.find({vs.atom, vt.atom, cell});
+          if (it != pair_of.end())
+            sub = (int32_t)(b.sub_off[it->second] + (int64_t)chunk_of[si] * nch[vt.atom] + chunk_of[ti]);
         }
-        b.tab_pair.push_back(pair);
+        b.tab_pair.push_back(sub);
       }
     b.tab_off[hb + 1] = (int64_t)b.tab_pair.size();
   }
@@ -578,15 +605,36 @@ std::string build_bricks(const UCell& u, Bricks& b) {
     for (auto& c : b.point_code) c = perm[c >> 7] * 128 + (c & 127);
     for (size_t i = 0; i < b.img_block.size(); ++i) b.img_block[i] = (int32_t)i;
   }
-  // grid-H slots: (s <= t) image pairs of each brick that are neighbour pairs
+  // grid-H slots: (s <= t) sub-image pairs of each brick that are neighbour
+  // pairs.  Each feeds one 16 x 16 sub-block (ca, cb) of its folded pair's
+  // kept orientation: directly when its pair is the kept one, transposed as
+  // (cb, ca) when it is the partner; a self pair's slot between two different
+  // chunks of the same image also feeds the transposed sub-block.
   std::vector<int32_t> fold(u.nloop, -1);
   for (size_t q = 0; q < u.uniq_pair.size(); ++q) {
     fold[u.uniq_pair[q]] = (int32_t)q;
     fold[u.partner[u.uniq_pair[q]]] = (int32_t)q;
   }
+  b.sb_off.assign(u.uniq_pair.size() + 1, 0);
+  for (size_t q = 0; q < u.uniq_pair.size(); ++q) {
+    const int p0 = u.uniq_pair[q];
+    b.sb_off[q + 1] = b.sb_off[q] + (int64_t)nch[u.pair_atom[p0]] * nch[u.pair_jatom[p0]];
+  }
+  const int64_t nsb = b.sb_off.back();
+  b.sb_fold.resize(nsb);
+  b.sb_chunks.resize(nsb);
+  for (size_t q = 0; q < u.uniq_pair.size(); ++q) {
+    const int p0 = u.uniq_pair[q];
+    for (int ca = 0; ca < nch[u.pair_atom[p0]]; ++ca)
+      for (int cb = 0; cb < nch[u.pair_jatom[p0]]; ++cb) {
+        const int64_t k = b.sb_off[q] + (int64_t)ca * nch[u.pair_jatom[p0]] + cb;
+        b.sb_fold[k] = (int32_t)q;
+        b.sb_chunks[k] = (ca << 8) | cb;
+      }
+  }
   b.tab_slot.assign(b.tab_pair.size(), -1);
   b.slot_base.assign(b.nbricks + 1, 0);
-  std::vector<std::vector<int64_t>> per_fold(u.uniq_pair.size());
+  std::vector<std::vector<int64_t>> per_sb(nsb);
   int64_t gslot = 0;
   for (int64_t hb = 0; hb < b.nbricks; ++hb) {
     const int m = (int)(b.img_off[hb + 1] - b.img_off[hb]);
@@ -595,20 +643,29 @@ std::string build_bricks(const UCell& u, Bricks& b) {
     int local = 0;
     for (int s = 0; s < m; ++s)
       for (int t = s; t < m; ++t) {
-        const int32_t p = b.tab_pair[t0 + s * m + t];
-        if (p < 0) continue;
+        const int32_t sp = b.tab_pair[t0 + s * m + t];
+        if (sp < 0) continue;
         b.tab_slot[t0 + s * m + t] = local++;
+        const int32_t p = b.sub_pair[sp];
+        const int ca = b.sub_chunks[sp] >> 8, cb = b.sub_chunks[sp] & 255;
         const int32_t q = fold[p];
-        per_fold[q].push_back(gslot * 2 + (u.uniq_pair[q] == p ? 0 : 1));
+        const int p0 = u.uniq_pair[q];
+        const int ncj = nch[u.pair_jatom[p0]];
+        if (p == p0) {
+          per_sb[b.sb_off[q] + (int64_t)ca * ncj + cb].push_back(gslot * 2);
+          if (u.partner[p0] == p0 && ca != cb) per_sb[b.sb_off[q] + (int64_t)cb * ncj + ca].push_back(gslot * 2 + 1);
+        } else {
+          per_sb[b.sb_off[q] + (int64_t)cb * ncj + ca].push_back(gslot * 2 + 1);
+        }
         ++gslot;
       }
   }
   b.slot_base[b.nbricks] = gslot;
-  b.red_off.assign(u.uniq_pair.size() + 1, 0);
+  b.red_off.assign(nsb + 1, 0);
   b.red_slot.clear();
   b.red_slot.reserve(gslot);
-  for (size_t q = 0; q < per_fold.size(); ++q) {
-    b.red_slot.insert(b.red_slot.end(), per_fold[q].begin(), per_fold[q].end());
+  for (int64_t q = 0; q < nsb; ++q) {
+    b.red_slot.insert(b.red_slot.end(), per_sb[q].begin(), per_sb[q].end());
     b.red_off[q + 1] = (int64_t)b.red_slot.size();
   }
   return "";

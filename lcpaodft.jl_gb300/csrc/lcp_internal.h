@@ -67,9 +67,13 @@ struct UCell {
 // bricks of bdim points (bdim[d] divides Ngrid[d], at most 128 points); the
 // point slot of a brick-local coordinate l is (l0*bdim1 + l1)*bdim2 + l2.
 // Each atom's sphere is covered by "blocks": the bricks of the unrolled
-// lattice it touches, each holding the atom's orbitals on the brick's points
-// (zero outside the sphere).  A home brick sees every block whose brick maps
-// to it, i.e. every atom image touching it.
+// lattice it touches, each holding 16 of the atom's orbitals on the brick's
+// points (zero outside the sphere).  An atom with NO orbitals has
+// ceil(NO/16) consecutive blocks per brick ("chunks"), each an image of its
+// own ("sub-image").  A home brick sees every block whose brick maps to it,
+// i.e. every chunk of every atom image touching it.  Pair tables refer to
+// sub-pairs (pair, row chunk, column chunk); for atoms of <= 16 orbitals a
+// sub-pair is the pair itself.
 struct Bricks {
   int32_t bdim[3] = {1, 1, 1};
   int32_t nb[3] = {1, 1, 1};       // home bricks per axis
@@ -83,12 +87,21 @@ struct Bricks {
   std::vector<int32_t> img_block;    // block of each image of a home brick (blocks are numbered in image order)
   std::vector<int32_t> img_atom;
   std::vector<int64_t> tab_off;      // [nbricks+1] offsets of the m x m pair tables
-  std::vector<int32_t> tab_pair;     // ordered pair of images (s, t), -1 if none
+  std::vector<int32_t> tab_pair;     // sub-pair of sub-images (s, t), -1 if none
   // grid-H partial blocks: one per (brick, s <= t) image pair that is a pair
   std::vector<int32_t> tab_slot;     // m x m per brick: slot within the brick, -1 if none
   std::vector<int64_t> slot_base;    // [nbricks+1]
-  std::vector<int64_t> red_off;      // [n_unique+1] CSR of slots per folded pair
-  std::vector<int64_t> red_slot;     // global slot * 2 + (1 if the slot is the partner orientation)
+  // sub-pairs of the neighbour pairs
+  int64_t nsub = 0;
+  std::vector<int64_t> sub_off;      // [nloop+1]: first sub-pair of each pair
+  std::vector<int32_t> sub_pair;     // [nsub] pair of each sub-pair
+  std::vector<int32_t> sub_chunks;   // [nsub] (row chunk << 8) | column chunk
+  // 16 x 16 sub-blocks of the folded pairs' H blocks (kept orientation)
+  std::vector<int64_t> sb_off;       // [n_unique+1]
+  std::vector<int32_t> sb_fold;      // [nsb] folded pair of each sub-block
+  std::vector<int32_t> sb_chunks;    // [nsb] (row chunk << 8) | column chunk
+  std::vector<int64_t> red_off;      // [nsb+1] CSR of slots per sub-block
+  std::vector<int64_t> red_slot;     // global slot * 2 + (1 if the slot enters transposed)
 };
 std::string build_bricks(const UCell& u, Bricks& b);
 

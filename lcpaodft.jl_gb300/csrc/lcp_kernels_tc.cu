@@ -232,10 +232,11 @@ __global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t
     const int64_t blk = code >> 7;
     const int slot = code & 127, g = slot >> 3, r = slot & 7;
     __nv_bfloat16* base = tab + blk * kPart;  // part p of block blk at (p * nblocks + blk) * kPart
-    for (int a = 0; a < no && a < 16; ++a) {
+    for (int a = 0; a < no; ++a) {  // orbital a: chunk a / 16 (block + a / 16), slot a % 16
       __nv_bfloat16 h, m, l;
       fx_split(src[a] * inv, h, m, l);
-      const int off = ((a >> 3) * 16 + g) * 64 + r * 8 + (a & 7);
+      const int ac = a & 15;
+      const int off = (a >> 4) * kPart + ((ac >> 3) * 16 + g) * 64 + r * 8 + (ac & 7);
       base[off] = h;
       base[nblocks * kPart + off] = m;
       base[2 * nblocks * kPart + off] = l;
@@ -243,36 +244,42 @@ __global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t
   }
 }
 
-// Dsym blocks in the K-major B layout [kh][nh][8 n][8 k]: n = orbital a of the
-// pair's atom, k = orbital b of its jatom; fixed-point with scale[0].
-__global__ void dsym_kernel(int nloop, const int32_t* __restrict__ pair_atom, const int32_t* __restrict__ pair_jatom,
+// Dsym blocks in the K-major B layout [kh][nh][8 n][8 k], one per sub-pair
+// (pair, chunk ca, chunk cb): n = orbital 16 ca + a' of the pair's atom,
+// k = orbital 16 cb + b' of its jatom; fixed-point with scale[0].  Dsym adds
+// the partner's transposed block, except on the diagonal chunks of a self
+// pair (which is its own partner).  Entry nsub is a zero block.
+__global__ void dsym_kernel(int64_t nsub, const int32_t* __restrict__ sub_pair, const int32_t* __restrict__ sub_chunks,
+                            const int32_t* __restrict__ pair_atom, const int32_t* __restrict__ pair_jatom,
                             const int64_t* __restrict__ boff, const int32_t* __restrict__ partner,
                             const int32_t* __restrict__ numorbs, const double* __restrict__ dm,
                             const double* __restrict__ scale, __nv_bfloat16* __restrict__ out) {
   const double inv = scale[1];
-  const int64_t total = (int64_t)(nloop + 1) * 256;
+  const int64_t total = (nsub + 1) * 256;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int p = (int)(e >> 8);
+    const int64_t sp = e >> 8;
     const int w = (int)(e & 255);
     const int kh = w >> 7, nh = (w >> 6) & 1, rr = (w >> 3) & 7, cc = w & 7;
-    const int a = nh * 8 + rr, b = kh * 8 + cc;
     double v = 0.0;
-    if (p < nloop) {
+    if (sp < nsub) {
+      const int p = sub_pair[sp], ch = sub_chunks[sp];
+      const int ca = ch >> 8, cb = ch & 255;
+      const int a = ca * 16 + nh * 8 + rr, b = cb * 16 + kh * 8 + cc;
       const int i = pair_atom[p], j = pair_jatom[p];
       const int noi = numorbs[i], noj = numorbs[j];
       if (a < noi && b < noj) {
         v = dm[boff[p] + (int64_t)a * noj + b];
         const int q = partner[p];
-        if (q != p) v += dm[boff[q] + (int64_t)b * noi + a];
+        if (q != p || ca != cb) v += dm[boff[q] + (int64_t)b * noi + a];
       }
     }
     __nv_bfloat16 h, mm, l;
     const double x = v * inv;
     const float xf = (float)x;
     fx_split_f(xf, (float)(x - (double)xf), h, mm, l);
-    out[(int64_t)p * kDsymElems + w] = h;
-    out[(int64_t)p * kDsymElems + 256 + w] = mm;
-    out[(int64_t)p * kDsymElems + 512 + w] = l;
+    out[sp * kDsymElems + w] = h;
+    out[sp * kDsymElems + 256 + w] = mm;
+    out[sp * kDsymElems + 512 + w] = l;
   }
 }
 
@@ -366,17 +373,18 @@ constexpr uint32_t kDBLbo = kDWin * 2 * 128;      // B: [part][kh][n-group][8 n]
 constexpr int kDStageA = 3 * 4096;                // table block: hi, mid, lo
 constexpr int kDStageB = 3 * 2 * kDBLbo;          // Dsym pieces: (part, kh) x LBO
 constexpr int kDStageBytes = kDStageA + kDStageB;  // 24 KB
-constexpr size_t kDSmem = (size_t)kDStages * kDStageBytes;
-constexpr int kDMaxImages = 32;                   // atom images per brick (checked at launch)
+constexpr size_t kDSmemStages = (size_t)kDStages * kDStageBytes;
+constexpr int kDMaxImages = 64;                   // sub-images per brick (checked at launch)
 constexpr int kDLag = 2;                          // K steps whose D pieces may still be in flight
 constexpr int kDGatherWarps = 4;                  // warps gathering D pieces (cp.async)
+// dynamic shared memory: the stages, then each gatherer's copy of the brick's pair table
+constexpr size_t kDSmem = kDSmemStages + (size_t)kDGatherWarps * kDMaxImages * kDMaxImages * sizeof(int32_t);
 constexpr uint32_t kDBufCols = 256;               // TMEM columns per window buffer
 constexpr uint32_t kDCross = 128;                 // cross accumulator within a buffer
 
 __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint64_t full_bar[kDStages], empty_bar[kDStages], mdone_bar[kDStages], tempty_bar[2], drain_bar;
-  __shared__ int32_t s_pair[kDGatherWarps][kDMaxImages * kDMaxImages];  // each gatherer's copy of the pair table
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -435,7 +443,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
   } else if (warp >= 6) {
     // ------------------------------------------------------------ D gatherers
     const int gw = warp - 6;
-    int32_t* pair = s_pair[gw];
+    int32_t* pair = reinterpret_cast<int32_t*>(smem + kDSmemStages) + gw * kDMaxImages * kDMaxImages;
     const uint8_t* dsym = reinterpret_cast<const uint8_t*>(args.dsym);
     uint32_t it = 0;
     for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
@@ -965,11 +973,12 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// Float-float sum of the partial blocks of each folded pair in a fixed order,
-// written (x dV, as FP64) to both blocks.  One block of 256 threads per folded
-// pair; warp w sums every 8th slot of the pair with coalesced float4 loads
-// (lane l holds entries 8l .. 8l+7 of the 16 x 16 partial), keeping partials
-// of the pair's own orientation and of the partner orientation apart.  The
+// Float-float sum of the partial blocks of each 16 x 16 sub-block of a folded
+// pair's H block in a fixed order, written (x dV, as FP64) to both blocks.  One
+// block of 256 threads per sub-block; warp w sums every 8th slot with
+// coalesced float4 loads
+// (lane l holds entries 8l .. 8l+7 of the 16 x 16 partial), keeping direct
+// and transposed partials apart.  The
 // eight warps' sums are then combined in warp order through shared memory,
 // the partner ones transposed -- the same order on every run.
 __device__ __forceinline__ void ff_add8(float* hi, float* lo, float4 a, float4 b) {
@@ -977,14 +986,16 @@ __device__ __forceinline__ void ff_add8(float* hi, float* lo, float4 a, float4 b
   ff_add(hi[4], lo[4], b.x); ff_add(hi[5], lo[5], b.y); ff_add(hi[6], lo[6], b.z); ff_add(hi[7], lo[7], b.w);
 }
 
-__global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nu, const int64_t* __restrict__ red_off,
+__global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nsb, const int64_t* __restrict__ red_off,
                                                        const int64_t* __restrict__ red_slot,
+                                                       const int32_t* __restrict__ sb_fold,
+                                                       const int32_t* __restrict__ sb_chunks,
                                                        const float* __restrict__ scratch, DevPairs pr,
                                                        const int32_t* __restrict__ numorbs, double dv, double* H) {
   __shared__ int64_t s_code[256];
   __shared__ float s_part[4][8][256];  // [own hi, own lo, partner hi, partner lo][warp][entry]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int64_t u = blockIdx.x; u < nu; u += gridDim.x) {
+  for (int64_t u = blockIdx.x; u < nsb; u += gridDim.x) {
     float dh[8], dl[8], th[8], tl[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) dh[i] = dl[i] = th[i] = tl[i] = 0.0f;
@@ -1032,12 +1043,14 @@ __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nu, const int64_t
       lo += s_part[3][w][et];
     }
     const double acc = (double)hi + (double)lo;
-    const int i = pr.atom[u], jj = pr.jatom[u];
+    const int q = sb_fold[u], ch = sb_chunks[u];
+    const int ra = (ch >> 8) * 16 + a, rb = (ch & 255) * 16 + b;  // entry of the pair's block
+    const int i = pr.atom[q], jj = pr.jatom[q];
     const int noi = numorbs[i], noj = numorbs[jj];
-    if (a < noi && b < noj) {
+    if (ra < noi && rb < noj) {
       const double v = acc * dv;
-      H[pr.boff_p[u] + (int64_t)a * noj + b] = v;
-      if (!pr.self[u]) H[pr.boff_q[u] + (int64_t)b * noi + a] = v;
+      H[pr.boff_p[q] + (int64_t)ra * noj + rb] = v;
+      if (!pr.self[q]) H[pr.boff_q[q] + (int64_t)rb * noi + ra] = v;
     }
   }
 }
@@ -1074,12 +1087,13 @@ cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_dsym(int nloop, const int32_t* pair_atom, const int32_t* pair_jatom, const int64_t* boff,
-                        const int32_t* partner, const int32_t* numorbs, const double* dm, const double* scale,
-                        __nv_bfloat16* out, cudaStream_t st) {
-  int64_t total = (int64_t)(nloop + 1) * 256;
+cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* sub_chunks, const int32_t* pair_atom,
+                        const int32_t* pair_jatom, const int64_t* boff, const int32_t* partner, const int32_t* numorbs,
+                        const double* dm, const double* scale, __nv_bfloat16* out, cudaStream_t st) {
+  int64_t total = (nsub + 1) * 256;
   int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
-  dsym_kernel<<<blocks, 256, 0, st>>>(nloop, pair_atom, pair_jatom, boff, partner, numorbs, dm, scale, out);
+  dsym_kernel<<<blocks, 256, 0, st>>>(nsub, sub_pair, sub_chunks, pair_atom, pair_jatom, boff, partner, numorbs, dm,
+                                      scale, out);
   return cudaGetLastError();
 }
 
@@ -1152,11 +1166,12 @@ cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot
   return cudaGetLastError();
 }
 
-cudaError_t launch_h_reduce(int64_t nu, const int64_t* red_off, const int64_t* red_slot, const float* scratch,
-                            const DevPairs& pr, const int32_t* numorbs, double dv, double* H, cudaStream_t st) {
-  if (nu == 0) return cudaSuccess;
-  const int grid = (int)std::min<int64_t>(nu, (int64_t)sm_count() * 8);
-  h_reduce_kernel<<<grid, 256, 0, st>>>(nu, red_off, red_slot, scratch, pr, numorbs, dv, H);
+cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* red_slot, const int32_t* sb_fold,
+                            const int32_t* sb_chunks, const float* scratch, const DevPairs& pr,
+                            const int32_t* numorbs, double dv, double* H, cudaStream_t st) {
+  if (nsb == 0) return cudaSuccess;
+  const int grid = (int)std::min<int64_t>(nsb, (int64_t)sm_count() * 8);
+  h_reduce_kernel<<<grid, 256, 0, st>>>(nsb, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H);
   return cudaGetLastError();
 }
 

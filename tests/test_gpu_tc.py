@@ -144,3 +144,38 @@ def test_job_energy_bf16x3_si64(ctx):
         finally:
             ctx.set_precision("fp64")
     assert abs(E["bf16x3"] - E["fp64"]) / u.Natom <= 1e-6, E
+
+
+def _mixed_cell(ctx, nrep=1):
+    """Three species of 18 (s2p2d2: two 16-orbital chunks), 13 and 4 orbitals,
+    cutoffs 8 / 7 / 6 bohr, seeded positions in a 11 x 10 x 12 bohr box."""
+    from lcpgrid.workloads import synthetic_species
+    paos = [synthetic_species(11, max_l=2, num_basis=(2, 2, 2), rc=8.0),
+            synthetic_species(12, max_l=2, num_basis=(2, 2, 1), rc=7.0),
+            synthetic_species(13, max_l=1, num_basis=(1, 1), rc=6.0)]
+    lat = np.diag([11.0, 10.0, 12.0])
+    pos = np.array([[1.0, 2.0, 3.0], [5.5, 6.0, 8.5], [8.0, 1.5, 6.0]])
+    u = L.UCell(1, lat, 3, [1, 2, 3], pos, [8.0, 7.0, 6.0], (44, 40, 48), [0, 0, 0], Total_NumOrbs=[18, 13, 4])
+    return u, L.Set_Orbitals_Grid(paos, u, ctx)
+
+
+def test_orbital_chunks_density_and_h(ctx):
+    """Atoms of more than 16 orbitals enter the tensor-core path as 16-orbital
+    chunks: split-BF16 vs FP64 on a mixed 18 / 13 / 4-orbital cell."""
+    from test_gpu_parity import psd_dm
+    u, orbs = _mixed_cell(ctx)
+    for spin, n in (("off", 1), ("on", 2)):
+        dm = psd_dm(u, 31, nspin=n)
+        r64 = _density(ctx, u, orbs, dm, "fp64", spin)
+        rtc = _density(ctx, u, orbs, dm, "bf16x3", spin)
+        for c in range(n):
+            scale = np.max(np.abs(r64[c]))
+            assert np.max(np.abs(rtc[c] - r64[c])) <= RHO_TOL * scale
+            assert abs(rtc[c].sum() - r64[c].sum()) <= SUM_TOL * abs(r64[c].sum())
+    rng = np.random.default_rng(8)
+    vp = [rng.normal(size=u.NN)]
+    h64 = _hks(ctx, u, orbs, vp, "fp64")[0]
+    htc = _hks(ctx, u, orbs, vp, "bf16x3")[0]
+    assert np.max(np.abs(htc - h64)) <= H_TOL * np.max(np.abs(h64))
+    dm = psd_dm(u, 32)[0]
+    assert abs(np.dot(dm, htc) - np.dot(dm, h64)) <= SUM_TOL * np.sum(np.abs(dm * h64))
