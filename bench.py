@@ -50,6 +50,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--serving", action="store_true", help="run the serving form instead of the step bench")
+    ap.add_argument("--serve-structures", type=int, default=24)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-rate", type=float, default=400.0, help="offered Poisson rate, jobs/s")
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-saturate", type=int, default=1500, help="requests of the saturated run")
+    ap.add_argument("--serve-fp64-requests", type=int, default=60)
+    ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     return ap.parse_args()
 
 
@@ -432,10 +440,103 @@ def run_reference(args):
                 "restatement (oracle/), parallel over the host cores like the reference's MPI pair split"}))
 
 
+# ------------------------------------------------------------------ serving form
+
+def serving(args, wl_pool=None):
+    """The serving form: a pool of device-resident structures (2-216 atoms,
+    log-uniform), grid-step requests arriving as a Poisson stream at
+    `--serve-rate` jobs/s for `--serve-seconds`, served by lcp_server with
+    `--serve-slots` concurrent slots in split-BF16.  Reports jobs/s and
+    submission-to-result latency (p50/p99), the saturated throughput of the
+    same pool in split-BF16 and in the FP64 drop-in (one structure at a
+    time), and the worst total-energy error of a structure vs FP64."""
+    import numpy as np
+    import torch
+
+    import lcpgrid as L
+    from lcpgrid.workloads import psd_density_matrices, serving_pool, smooth_vna
+
+    pool = wl_pool or serving_pool(args.serve_structures)
+    ctx = L.Context(0)
+    jobs, dms, natoms = [], [], []
+    t0 = time.perf_counter()
+    for w in pool:
+        u = L.UCell(1, w["latvecs"], w["natom"], w["atom2spe"], w["gxyz"], w["cut"], w["ngrid"], w["origin"],
+                    Total_NumOrbs=w["numorbs"])
+        orbs = L.Set_Orbitals_Grid(w["paos"], u, ctx)
+        vna = smooth_vna(w["ngrid"], w["latvecs"], w["vna_seed"])
+        jobs.append(L.GridStepJob(u, orbs, "off", "LDA", None, None, vna))
+        dms.append(psd_density_matrices(u, w["dm_seed"], trace=w["trace"]))
+        natoms.append(w["natom"])
+    t_setup = time.perf_counter() - t0
+
+    def run_server(precision, nslots, rate, seconds, max_requests):
+        srv = L.Server(0, nslots=nslots, precision=precision, budget_bytes=args.serve_budget_gb * 1e9)
+        ids = [srv.add(j) for j in jobs]
+        # warm-up: every structure once (split-BF16 tables, FFT plans, workspaces)
+        for sid in ids:
+            srv.submit(sid, dms[sid], tag=sid)
+        got = 0
+        energies = {}
+        while got < len(ids):
+            for tag, e, lat in srv.poll(wait_ms=5000):
+                energies[tag] = e
+                got += 1
+        rng = np.random.default_rng(99)
+        if rate > 0:
+            gaps = rng.exponential(1.0 / rate, size=max_requests)
+            n_req = int(min(max_requests, np.searchsorted(np.cumsum(gaps), seconds)))
+        else:
+            gaps = np.zeros(max_requests)
+            n_req = max_requests
+        picks = rng.integers(0, len(ids), size=n_req)
+        lat_ms, done = [], 0
+        t_start = time.perf_counter()
+        t_next = t_start
+        for k in range(n_req):
+            t_next += gaps[k]
+            while True:
+                now = time.perf_counter()
+                if now >= t_next:
+                    break
+                for _tag, _e, lat in srv.poll(wait_ms=0):
+                    lat_ms.append(lat)
+                time.sleep(min(2e-4, t_next - now))
+            srv.submit(ids[picks[k]], dms[picks[k]], tag=10_000 + k)
+        while len(lat_ms) < n_req:
+            for _tag, _e, lat in srv.poll(wait_ms=5000):
+                lat_ms.append(lat)
+        t_end = time.perf_counter()
+        srv.close()
+        lat = np.array(lat_ms)
+        return {"jobs_per_s": n_req / (t_end - t_start), "requests": n_req,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "offered_rate": rate, "slots": nslots, "precision": precision}, energies
+
+    stream, e_tc = run_server("bf16x3", args.serve_slots, args.serve_rate, args.serve_seconds, 100000)
+    sat_tc, _ = run_server("bf16x3", args.serve_slots, 0, 0, args.serve_saturate)
+    sat_64, e_64 = run_server("fp64", 1, 0, 0, args.serve_fp64_requests)
+    err = max(abs(e_tc[k][4] - e_64[k][4]) / natoms[k] * 1e6 for k in range(len(jobs)))
+    return {
+        "stream": stream, "saturated_bf16x3": sat_tc, "saturated_fp64_dropin": sat_64,
+        "jobs_per_s_vs_fp64": sat_tc["jobs_per_s"] / sat_64["jobs_per_s"],
+        "max_err_per_atom_uHa": err,
+        "structures": {"count": len(jobs), "atoms": natoms, "setup_s": t_setup,
+                       "resident_bytes": int(sum(j.footprint() for j in jobs))},
+    }
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.serving:
+        res = serving(args)
+        print(json.dumps({"metric": "serving: jobs/s (p50/p99 latency) split-BF16 vs FP64 drop-in, mixed-size stream",
+                          "value": res["stream"]["jobs_per_s"], "unit": "jobs/s", "higher_is_better": True,
+                          "n_gpus": 1, "data": "synthetic (seeded random Si-density cells, 2-216 atoms)",
+                          "config": {"workload": "serving_pool", "slots": args.serve_slots,
+                                     "rate": args.serve_rate}, **res}))
     else:
         run_ours(args)
 

@@ -198,7 +198,9 @@ lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* 
 void lcp_job_destroy(lcp_job* job);
 /* Host -> device copy of the density matrices (Nspin x Total_Hsize). */
 lcp_status lcp_job_set_dm(lcp_ctx* ctx, lcp_job* job, const double* const* dm);
-/* Launch one grid step on the context stream (asynchronous). */
+/* Launch one grid step on the context stream (asynchronous).  Any context of
+ * the job's device may run it (its workspaces and FFT plans are used); steps
+ * of one job must not overlap. */
 lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job);
 /* The same step with CUDA events between its stages (synchronises); stage_ms[6] =
  * density, Poisson, xc+potential (with the energy partial sums of the same
@@ -207,6 +209,18 @@ lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job);
 lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms);
 /* Energies of the last step: [E_H1, EXC1[1], EXC1[2], sum_s <D_s,H_s>, E_grid]. */
 lcp_status lcp_job_energies(lcp_ctx* ctx, lcp_job* job, double* out5);
+/* The energies without waiting: an asynchronous copy on the context's stream
+ * (out5 should be pinned host memory; valid once the stream reaches it). */
+lcp_status lcp_job_energies_async(lcp_ctx* ctx, lcp_job* job, double* out5);
+/* Builds what the context's precision needs of the job's orbital tables
+ * (split-BF16 brick tables, FP32 copy) ahead of the first step. */
+lcp_status lcp_job_prepare(lcp_ctx* ctx, lcp_job* job);
+/* Device bytes held by the job and its orbital tables (admission by HBM
+ * footprint). */
+lcp_status lcp_job_footprint(const lcp_job* job, int64_t* bytes);
+/* Waits for the context's stream and reports (and clears) a device-side error
+ * of its kernels (a bounded wait that gave up: LCP_ETIMEDOUT). */
+lcp_status lcp_ctx_check_status(lcp_ctx* ctx);
 /* Device -> host copies of the last step's outputs. */
 lcp_status lcp_job_get_density(lcp_ctx* ctx, lcp_job* job, double* const* density);
 lcp_status lcp_job_get_hks(lcp_ctx* ctx, lcp_job* job, double* const* hks);
@@ -220,6 +234,35 @@ lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops);
  * (order 0) or MN-groups outer (order 1); row-major host inputs, FP32 result. */
 lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t order, int32_t n,
                            int32_t k, const float* a, const float* b, float* d);
+
+/* ---------------------------------------------------------------- serving */
+
+/* Serving engine for SCF grid-step requests on many device-resident
+ * structures (the spec serving form; the reference has no serving
+ * layer).  `nslots` execution slots, each a context of its own (stream and
+ * workspaces) at `precision`, run requests concurrently; a worker thread
+ * admits pending requests in arrival order as slots and their structures free
+ * up.  Structures are admitted by device footprint against `budget_bytes`. */
+typedef struct lcp_server lcp_server;
+lcp_status lcp_server_create(int32_t device, int32_t nslots, int32_t precision, int64_t budget_bytes,
+                             lcp_server** out);
+/* Waits for the requests in flight, then frees the server (not the jobs). */
+void lcp_server_destroy(lcp_server* srv);
+/* Admits a job (a structure with its orbital tables and step buffers, created
+ * by the caller, who keeps ownership) if its footprint fits the free budget,
+ * else LCP_ENOMEM.  nspin / hsize: channels and Total_Hsize of its D. */
+lcp_status lcp_server_add(lcp_server* srv, lcp_job* job, int32_t nspin, int64_t hsize, int32_t* id);
+/* Releases a structure's budget (LCP_ESTATE while it has requests queued). */
+lcp_status lcp_server_remove(lcp_server* srv, int32_t id);
+/* Queues one grid step of structure `id` with density matrices dm[nspin]
+ * (copied; the caller's buffers are free on return). */
+lcp_status lcp_server_submit(lcp_server* srv, int32_t id, const double* const* dm, uint64_t tag);
+/* Completed requests (up to max; waits up to wait_ms for the first): tags,
+ * energies[5 each] (as lcp_job_energies) and submission-to-result latency. */
+lcp_status lcp_server_poll(lcp_server* srv, int32_t max, int32_t wait_ms, uint64_t* tags, double* energies,
+                           double* latency_ms, int32_t* n);
+/* out4 = submitted, completed, resident bytes, budget. */
+lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4);
 
 /* Split-BF16 density that allocates no device memory.  No counterpart in the
  * reference: it is for callers that cannot call cudaMalloc at call time --

@@ -1133,7 +1133,9 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
                                     job->real.as<double>(), st),
            "poisson_prep");
   ctx->launches++;
-  if ((s = poisson_device(ctx, job->plans, u.ngrid, job->recvecs, job->real.as<double>(), job->spec.p,
+  FftPlans* plans = nullptr;  // the executing context's plans (any context may run the job)
+  if ((s = get_plans(ctx, u.ngrid, &plans))) return s;
+  if ((s = poisson_device(ctx, plans, u.ngrid, job->recvecs, job->real.as<double>(), job->spec.p,
                           job->dvh.as<double>())))
     return s;
   mark(2);
@@ -1189,6 +1191,60 @@ lcp_status lcp_job_energies(lcp_ctx* ctx, lcp_job* job, double* out5) {
   API_CUDA(cudaMemcpyAsync(out5, job->scal.as<double>() + 8, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
            "D2H");
   API_CUDA(cudaStreamSynchronize(ctx->stream), "energies");
+  return device_status(ctx);
+}
+
+lcp_status lcp_job_energies_async(lcp_ctx* ctx, lcp_job* job, double* out5) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job || !out5) return fail(LCP_EINVAL, "NULL argument");
+  API_CUDA(cudaMemcpyAsync(out5, job->scal.as<double>() + 8, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "D2H");
+  return LCP_OK;
+}
+
+lcp_status lcp_job_footprint(const lcp_job* job, int64_t* bytes) {
+  if (!job || !bytes) return fail(LCP_EINVAL, "NULL argument");
+  int64_t b = 0;
+  auto add = [&](const DBuf& d) { b += (int64_t)d.bytes; };
+  for (int c = 0; c < 4; ++c) {
+    add(job->dm[c]);
+    add(job->rho[c]);
+    add(job->hks[c]);
+    add(job->vpot[c]);
+  }
+  for (const DBuf* d : {&job->aden, &job->pcc, &job->vna, &job->dvh, &job->real, &job->spec, &job->part, &job->scal})
+    add(*d);
+  const lcp_orbs* o = job->orbs;
+  for (const DBuf* d : {&o->atv, &o->gxyz, &o->spe, &o->sph_off, &o->glist, &o->clist, &o->phi_off, &o->numorbs,
+                        &o->species, &o->radial, &o->phi, &o->dphi[0], &o->dphi[1], &o->dphi[2], &o->phi32,
+                        &o->p_atom, &o->p_jatom, &o->p_boffp, &o->p_boffq, &o->p_self, &o->p_lensoff, &o->p_g1,
+                        &o->p_g2, &o->it_pair, &o->it_start, &o->it_count, &o->b_code, &o->b_imgoff, &o->b_imgblk,
+                        &o->b_taboff, &o->b_tabpair, &o->b_tab, &o->b_tabslot, &o->b_slotbase, &o->b_redoff,
+                        &o->b_redslot, &o->b_subpair, &o->b_subchunks, &o->b_sbfold, &o->b_sbchunks, &o->o_atom,
+                        &o->o_jatom, &o->o_boff, &o->o_partner, &o->b_scale, &o->b_tmp})
+    add(*d);
+  *bytes = b;
+  return LCP_OK;
+}
+
+lcp_status lcp_job_prepare(lcp_ctx* ctx, lcp_job* job) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job) return fail(LCP_EINVAL, "NULL job");
+  lcp_orbs* o = const_cast<lcp_orbs*>(job->orbs);
+  if (ctx->precision == LCP_PREC_BF16X3) return ensure_bricks(ctx, o);
+  if (ctx->precision == LCP_PREC_FP32) {
+    if ((s = ensure_phi32(ctx, o))) return s;
+    API_CUDA(cudaStreamSynchronize(ctx->stream), "prepare");
+  }
+  return LCP_OK;
+}
+
+lcp_status lcp_ctx_check_status(lcp_ctx* ctx) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "status");
   return device_status(ctx);
 }
 

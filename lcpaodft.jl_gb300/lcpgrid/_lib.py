@@ -90,6 +90,17 @@ _SIGS = {
     "lcp_job_step": ([_vp, _vp], _i32),
     "lcp_job_step_timed": ([_vp, _vp, _pd], _i32),
     "lcp_job_energies": ([_vp, _vp, _pd], _i32),
+    "lcp_job_energies_async": ([_vp, _vp, _pd], _i32),
+    "lcp_job_footprint": ([_vp, ctypes.POINTER(_i64)], _i32),
+    "lcp_job_prepare": ([_vp, _vp], _i32),
+    "lcp_ctx_check_status": ([_vp], _i32),
+    "lcp_server_create": ([_i32, _i32, _i32, _i64, ctypes.POINTER(_vp)], _i32),
+    "lcp_server_destroy": ([_vp], None),
+    "lcp_server_add": ([_vp, _vp, _i32, _i64, ctypes.POINTER(_i32)], _i32),
+    "lcp_server_remove": ([_vp, _i32], _i32),
+    "lcp_server_submit": ([_vp, _i32, _ppd, ctypes.c_uint64], _i32),
+    "lcp_server_poll": ([_vp, _i32, _i32, ctypes.POINTER(ctypes.c_uint64), _pd, _pd, ctypes.POINTER(_i32)], _i32),
+    "lcp_server_stats": ([_vp, ctypes.POINTER(_i64)], _i32),
     "lcp_job_get_density": ([_vp, _vp, _ppd], _i32),
     "lcp_job_get_hks": ([_vp, _vp, _ppd], _i32),
     "lcp_job_get_vpot": ([_vp, _vp, _ppd], _i32),

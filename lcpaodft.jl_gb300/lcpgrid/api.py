@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib
 from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 
-__all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob",
+__all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Server",
            "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "Solve_Poisson", "Solve_Poisson_xyz",
            "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
            "Calc_MatrixElements_dVH_Vxc_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
@@ -436,6 +436,7 @@ class GridStepJob:
     def __init__(self, ucell, Orbs_Grid, SpinPol, xc_type, ADensity_Grid=None, PCCDensity_Grid=None, Vna_Grid=None):
         self.ctx = Orbs_Grid.ctx
         self.ucell = ucell
+        self.orbs = Orbs_Grid  # the device job reads these tables: keep them alive
         self.SpinPol = _spin(SpinPol)
         self.nspin = _lib.NCHAN[self.SpinPol]
         keep = [None if x is None else _f64(x) for x in (ADensity_Grid, PCCDensity_Grid, Vna_Grid)]
@@ -465,6 +466,12 @@ class GridStepJob:
         check(lib.lcp_job_energies(self.ctx._h, self._h, dptr(out)))
         return out
 
+    def footprint(self):
+        """Device bytes of the job and its orbital tables."""
+        out = ctypes.c_int64()
+        check(lib.lcp_job_footprint(self._h, ctypes.byref(out)))
+        return int(out.value)
+
     def _get(self, fn, n):
         outs = [np.zeros(n) for _ in range(self.nspin)]
         p, keep = dptrs(outs)
@@ -487,3 +494,61 @@ class GridStepJob:
                 self._h = None
         except Exception:
             pass
+
+
+class Server:
+    """Serving engine for SCF grid-step requests on device-resident structures
+    (lcp_server_*): `nslots` concurrent execution slots at one precision,
+    structures admitted by device footprint against `budget_bytes`."""
+
+    def __init__(self, device=0, nslots=4, precision="bf16x3", budget_bytes=160e9):
+        h = ctypes.c_void_p()
+        check(lib.lcp_server_create(int(device), int(nslots), _lib.PREC[precision], int(budget_bytes),
+                                    ctypes.byref(h)))
+        self._h = h
+        self._jobs = {}
+
+    def add(self, job):
+        """Admits a GridStepJob (kept alive by the server object); returns its id.
+        Raises LCPError (LCP_ENOMEM) when its footprint exceeds the free budget."""
+        i = ctypes.c_int32()
+        check(lib.lcp_server_add(self._h, job._h, job.nspin, job.ucell.Total_Hsize, ctypes.byref(i)))
+        self._jobs[i.value] = job
+        return i.value
+
+    def remove(self, sid):
+        check(lib.lcp_server_remove(self._h, int(sid)))
+        self._jobs.pop(sid, None)
+
+    def submit(self, sid, DM, tag):
+        job = self._jobs[sid]
+        p, keep = dptrs([_f64(DM[c]) for c in range(job.nspin)])
+        check(lib.lcp_server_submit(self._h, int(sid), p, ctypes.c_uint64(int(tag))))
+
+    def poll(self, max_results=4096, wait_ms=0):
+        """Completed requests: list of (tag, energies[5], latency_ms)."""
+        tags = (ctypes.c_uint64 * max_results)()
+        en = np.zeros(5 * max_results)
+        lat = np.zeros(max_results)
+        n = ctypes.c_int32()
+        check(lib.lcp_server_poll(self._h, int(max_results), int(wait_ms), tags, dptr(en), dptr(lat),
+                                  ctypes.byref(n)))
+        return [(int(tags[k]), en[5 * k:5 * k + 5].copy(), float(lat[k])) for k in range(n.value)]
+
+    def stats(self):
+        """(submitted, completed, resident bytes, budget bytes)."""
+        out = (ctypes.c_int64 * 4)()
+        check(lib.lcp_server_stats(self._h, out))
+        return tuple(int(x) for x in out)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.lcp_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -140,3 +140,57 @@ def si64_workload(seed=1234, ngrid=(96, 96, 96), nrep=2):
         "numorbs": [pao.Spe_Total_NumOrbs] * natom, "paos": [pao],
         "vna_seed": seed + 1, "dm_seed": seed + 2, "trace": 256.0,
     }
+
+
+SI_DENSITY = 64 / (10.86 * ANG_TO_BOHR) ** 3  # atoms per bohr^3 of diamond Si
+GRID_SPACING = 10.86 * ANG_TO_BOHR / 96       # bohr, as the 64-atom 96^3 cell (0.2138)
+
+
+def random_si_cell(natom, seed, min_sep=3.5):
+    """Cubic cell at the density of diamond Si with `natom` atoms at seeded
+    random positions, pairwise (periodic) distances >= min_sep bohr (sequential
+    rejection sampling); grid at the 64-atom cell's spacing, each dimension a
+    multiple of 8 (>= 24)."""
+    rng = np.random.default_rng(seed)
+    side = (natom / SI_DENSITY) ** (1.0 / 3.0)
+    lat = np.eye(3) * side
+    for _attempt in range(100):
+        pos = []
+        for _ in range(natom):
+            for _try in range(10000):
+                x = rng.uniform(0, side, size=3)
+                ok = True
+                for y in pos:
+                    d = x - y
+                    d -= side * np.round(d / side)
+                    if d @ d < min_sep * min_sep:
+                        ok = False
+                        break
+                if ok:
+                    pos.append(x)
+                    break
+            else:
+                break
+        if len(pos) == natom:
+            break
+    else:
+        raise RuntimeError("could not place %d atoms" % natom)
+    n = max(24, int(math.ceil(side / GRID_SPACING / 8.0)) * 8)
+    return lat, np.array(pos), (n, n, n)
+
+
+def serving_pool(nstruct=24, seed=777, nmin=2, nmax=216):
+    """Structures of the serving form: sizes log-uniform in [nmin, nmax] atoms,
+    random Si-density cells with the synthetic 13-orbital species of the
+    64-atom workload (rc 7), a PSD D (4 electrons per atom) and a smooth V_na."""
+    rng = np.random.default_rng(seed)
+    pao = synthetic_species(1234)
+    out = []
+    for k in range(nstruct):
+        natom = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        lat, pos, ngrid = random_si_cell(natom, seed + 1 + k)
+        out.append({"name": "rand%d_%d" % (natom, k), "latvecs": lat, "gxyz": pos, "natom": natom,
+                    "atom2spe": [1] * natom, "cut": [7.0] * natom, "ngrid": ngrid, "origin": [0.0, 0.0, 0.0],
+                    "numorbs": [pao.Spe_Total_NumOrbs] * natom, "paos": [pao],
+                    "vna_seed": seed + 1000 + k, "dm_seed": seed + 2000 + k, "trace": 2.0 * natom})
+    return out
