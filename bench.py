@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--serving", action="store_true", help="run the serving form instead of the step bench")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving section of the step bench line")
     ap.add_argument("--serve-structures", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-rate", type=float, default=400.0, help="offered Poisson rate, jobs/s")
@@ -339,7 +340,7 @@ def run_ours(args):
     for _ in range(e2e_n):
         job.set_dm([pin_dm.numpy()])
         job.step()
-        out = job._get(L.api.lib.lcp_job_get_hks, u.Total_Hsize)
+        job.hks(out=[pin_h.numpy()])
         e2e_e = job.energies()
     e2e_s = (time.perf_counter() - t0) / e2e_n
 
@@ -398,6 +399,12 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "gpu_launches_note": "library kernels per timed region; cuFFT adds 2 FFT launches per step",
     }
+    if rank == 0 and not args.no_serving and world == 1:
+        # the serving form on the same GPU: Poisson stream of mixed-size structures
+        try:
+            line["serving"] = serving(args)
+        except Exception as exc:  # the serving run must not hide the step line
+            line["serving"] = {"error": repr(exc)}
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(wl, u, args.cpu_seconds, all_cores=True)

@@ -2,15 +2,15 @@
 // orbital tables and step buffers resident on the device (an lcp_job).
 //
 // Structures are admitted by HBM footprint against a budget.  Requests carry
-// a new density matrix; a worker thread launches each pending request as soon
-// as its structure is idle and one of `nslots` execution slots is free.  A
-// slot is a context of its own (stream and workspaces), so requests on
-// different slots run concurrently on the device and new requests start while
-// others are still in flight.  Completion is detected with events; latency
-// is measured from submission to the moment the worker sees the result.
+// a new density matrix.  Each of `nslots` execution slots -- a context of its
+// own (stream and workspaces) with a worker thread -- takes the oldest pending
+// request whose structure is idle, so requests on different slots run
+// concurrently on the device, kernel launches are issued from several host
+// threads, and new requests start while others are still in flight.  Latency
+// is measured from submission to the moment the slot's worker sees the result
+// (its completion event).
 #include <cuda_runtime.h>
 
-#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -65,19 +65,17 @@ struct lcp_server {
   std::vector<lcp_ctx*> slots;
   lcp_ctx* admin = nullptr;  // prepares structures' tables at admission (caller's thread)
   std::vector<cudaStream_t> streams;
-  std::vector<int> free_slots;
   std::map<int32_t, Structure> structs;
   int32_t next_id = 0;
   double* energy_arena = nullptr;  // pinned, 8 doubles per entry
   std::vector<double*> free_energy;
   std::deque<Request*> pending;
-  std::vector<Request*> inflight;
   std::deque<Request*> done;
   std::vector<cudaEvent_t> free_events;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   bool stop = false;
-  std::thread worker;
+  std::vector<std::thread> workers;
   int64_t submitted = 0, completed = 0;
   lcp_status sticky = LCP_OK;
   std::string sticky_msg;
@@ -93,69 +91,53 @@ struct lcp_server {
     r->status = s;
   }
 
-  void run() {
+  // One worker per slot: take the oldest pending request whose structure is
+  // idle, run it on this slot, wait for it, publish the result.
+  void run(int slot) {
     cudaSetDevice(device);
-    std::vector<Request*> to_launch;
     while (true) {
-      to_launch.clear();
+      Request* r = nullptr;
       {
         std::unique_lock<std::mutex> lk(mu);
-        if (stop && pending.empty() && inflight.empty()) break;
-        if (pending.empty() && inflight.empty()) {
+        while (true) {
+          for (auto it = pending.begin(); it != pending.end(); ++it) {
+            Structure& st = structs[(*it)->id];
+            if (!st.busy) {
+              st.busy = true;
+              r = *it;
+              pending.erase(it);
+              break;
+            }
+          }
+          if (r || (stop && pending.empty())) break;
           cv_work.wait_for(lk, std::chrono::milliseconds(5));
-          continue;
-        }
-        // admit pending requests in arrival order as slots free up, one per structure
-        for (auto it = pending.begin(); it != pending.end() && !free_slots.empty();) {
-          Request* r = *it;
-          Structure& st = structs[r->id];
-          if (st.busy) {
-            ++it;
-            continue;
-          }
-          st.busy = true;
-          r->slot = free_slots.back();
-          free_slots.pop_back();
-          to_launch.push_back(r);
-          it = pending.erase(it);
         }
       }
-      for (Request* r : to_launch) {
-        launch(r);
-        inflight.push_back(r);  // only the worker touches `inflight`
+      if (!r) break;
+      r->slot = slot;
+      launch(r);
+      if (r->status == LCP_OK) {
+        const cudaError_t e = cudaEventSynchronize(r->done);
+        if (e != cudaSuccess) r->status = LCP_EDEVICE;
       }
-      bool finished = false;
-      for (size_t k = 0; k < inflight.size();) {
-        Request* r = inflight[k];
-        const cudaError_t q = r->status == LCP_OK ? cudaEventQuery(r->done) : cudaSuccess;
-        if (q == cudaErrorNotReady) {
-          ++k;
-          continue;
+      if (r->status == LCP_OK) r->status = lcp_ctx_check_status(slots[slot]);
+      r->t_done = Clock::now();
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        Structure& st = structs[r->id];
+        st.busy = false;
+        st.queued--;
+        st.free_dm.push_back(r->dm);
+        r->dm = nullptr;
+        if (r->status != LCP_OK && sticky == LCP_OK) {
+          sticky = r->status;
+          sticky_msg = lcp_last_error() ? lcp_last_error() : "request failed";
         }
-        if (r->status == LCP_OK && q != cudaSuccess) r->status = LCP_EDEVICE;
-        if (r->status == LCP_OK) r->status = lcp_ctx_check_status(slots[r->slot]);
-        r->t_done = Clock::now();
-        {
-          std::lock_guard<std::mutex> lk(mu);
-          Structure& st = structs[r->id];
-          st.busy = false;
-          st.queued--;
-          st.free_dm.push_back(r->dm);
-          r->dm = nullptr;
-          free_slots.push_back(r->slot);
-          if (r->status != LCP_OK && sticky == LCP_OK) {
-            sticky = r->status;
-            sticky_msg = lcp_last_error() ? lcp_last_error() : "request failed";
-          }
-          done.push_back(r);
-          completed++;
-        }
-        inflight[k] = inflight.back();
-        inflight.pop_back();
-        finished = true;
+        done.push_back(r);
+        completed++;
       }
-      if (finished) cv_done.notify_all();
-      if (to_launch.empty() && !finished) std::this_thread::sleep_for(std::chrono::microseconds(20));
+      cv_done.notify_all();
+      cv_work.notify_all();  // this structure may have more requests waiting
     }
   }
 };
@@ -183,7 +165,6 @@ lcp_status lcp_server_create(int32_t device, int32_t nslots, int32_t precision, 
     s->streams.push_back(stream);
     if ((st = lcp_ctx_set_stream(c, stream))) return st;
     if ((st = lcp_ctx_set_precision(c, precision))) return st;
-    s->free_slots.push_back(nslots - 1 - k);
   }
   {
     lcp_status st = lcp_ctx_create(device, &s->admin);
@@ -195,7 +176,7 @@ lcp_status lcp_server_create(int32_t device, int32_t nslots, int32_t precision, 
     return fail(LCP_ENOMEM, "pinned allocation failed");
   for (int k = 0; k < kEnergySlots; ++k) s->free_energy.push_back(s->energy_arena + (size_t)k * 8);
   lcp_server* raw = s.get();
-  s->worker = std::thread([raw]() { raw->run(); });
+  for (int k = 0; k < nslots; ++k) s->workers.emplace_back([raw, k]() { raw->run(k); });
   *out = s.release();
   return LCP_OK;
 }
@@ -207,7 +188,8 @@ void lcp_server_destroy(lcp_server* srv) {
     srv->stop = true;
   }
   srv->cv_work.notify_all();
-  if (srv->worker.joinable()) srv->worker.join();
+  for (auto& w : srv->workers)
+    if (w.joinable()) w.join();
   cudaSetDevice(srv->device);
   for (auto* r : srv->done) {
     if (r->done) cudaEventDestroy(r->done);

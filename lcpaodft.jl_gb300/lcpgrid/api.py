@@ -472,20 +472,25 @@ class GridStepJob:
         check(lib.lcp_job_footprint(self._h, ctypes.byref(out)))
         return int(out.value)
 
-    def _get(self, fn, n):
-        outs = [np.zeros(n) for _ in range(self.nspin)]
+    def _get(self, fn, n, out=None):
+        outs = out if out is not None else [np.zeros(n) for _ in range(self.nspin)]
+        for o in outs:
+            if o.dtype != np.float64 or o.size != n or not o.flags["C_CONTIGUOUS"]:
+                raise TypeError("output arrays must be C-contiguous float64 of the grid / H size")
         p, keep = dptrs(outs)
         check(fn(self.ctx._h, self._h, p))
         return outs
 
-    def density(self):
-        return self._get(lib.lcp_job_get_density, self.ucell.NN)
+    def density(self, out=None):
+        return self._get(lib.lcp_job_get_density, self.ucell.NN, out)
 
-    def hks(self):
-        return self._get(lib.lcp_job_get_hks, self.ucell.Total_Hsize)
+    def hks(self, out=None):
+        """H of the last step; `out` (one array per spin, e.g. in pinned memory)
+        receives it in place."""
+        return self._get(lib.lcp_job_get_hks, self.ucell.Total_Hsize, out)
 
-    def vpot(self):
-        return self._get(lib.lcp_job_get_vpot, self.ucell.NN)
+    def vpot(self, out=None):
+        return self._get(lib.lcp_job_get_vpot, self.ucell.NN, out)
 
     def __del__(self):
         try:
