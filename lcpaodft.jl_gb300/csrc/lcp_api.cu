@@ -12,8 +12,7 @@
 #include <string>
 #include <vector>
 
-#include "lcp_device.h"
-#include "lcp_internal.h"
+#include "lcp_api_state.h"
 
 using lcp::DevGeom;
 using lcp::DevPairs;
@@ -26,131 +25,6 @@ thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error_cstr() { return g_last_error.c_str(); }
 }  // namespace lcp
-
-namespace {
-
-lcp_status fail(lcp_status code, const std::string& msg) {
-  lcp::set_error(msg);
-  return code;
-}
-
-lcp_status cuda_fail(cudaError_t e, const char* where) {
-  return fail(e == cudaErrorMemoryAllocation ? LCP_ENOMEM : LCP_EDEVICE,
-              std::string(where) + ": " + cudaGetErrorString(e));
-}
-
-#define API_CUDA(expr, where)                       \
-  do {                                              \
-    cudaError_t _e = (expr);                        \
-    if (_e != cudaSuccess) return cuda_fail(_e, where); \
-  } while (0)
-
-// Owning device buffer.
-struct DBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  DBuf() = default;
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  ~DBuf() {
-    if (p) cudaFree(p);
-  }
-  cudaError_t ensure(size_t n) {
-    if (n <= bytes && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, n ? n : 16);
-    if (e == cudaSuccess) bytes = n;
-    return e;
-  }
-  template <class T>
-  T* as() const {
-    return reinterpret_cast<T*>(p);
-  }
-};
-
-template <class T>
-cudaError_t upload(DBuf& b, const std::vector<T>& v, cudaStream_t st) {
-  cudaError_t e = b.ensure(v.size() * sizeof(T));
-  if (e != cudaSuccess) return e;
-  if (v.empty()) return cudaSuccess;
-  e = cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return e;
-  return cudaStreamSynchronize(st);
-}
-
-int channels(int32_t spinpol) { return spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4); }
-
-}  // namespace
-
-struct lcp_ucell {
-  lcp::UCell u;
-};
-
-struct FftPlans {
-  cufftHandle fwd = 0, inv = 0;
-  bool ok = false;
-};
-
-struct lcp_ctx {
-  int device = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  int32_t precision = LCP_PREC_FP64;
-  int64_t launches = 0;
-  std::map<std::tuple<int, int, int>, FftPlans> plans;
-  // workspaces of the host-buffer entry points
-  DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
-  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale;
-  ~lcp_ctx() {
-    cudaSetDevice(device);
-    for (auto& kv : plans) {
-      if (kv.second.fwd) cufftDestroy(kv.second.fwd);
-      if (kv.second.inv) cufftDestroy(kv.second.inv);
-    }
-    if (own) cudaStreamDestroy(own);
-  }
-};
-
-struct lcp_orbs {
-  const lcp_ucell* ucell = nullptr;
-  int device = 0;
-  bool grad = false;
-  int max_no = 0;
-  DevGeom geom{};
-  DevPairs pairs{};
-  // device arrays
-  DBuf atv, gxyz, spe, sph_off, glist, clist, phi_off, numorbs;
-  DBuf species, radial;
-  DBuf phi, dphi[3], phi32;
-  DBuf p_atom, p_jatom, p_boffp, p_boffq, p_self, p_lensoff, p_g1, p_g2, it_pair, it_start, it_count;
-  int64_t table_elems = 0;
-  // brick tiling and split-BF16 tables of the tensor-core path (built on first use)
-  bool bricks_ready = false;
-  lcp::Bricks bricks;
-  lcp::TcBrickGeom bgeom{};
-  DBuf b_code, b_imgoff, b_imgblk, b_taboff, b_tabpair, b_tab, b_tabslot, b_slotbase, b_redoff, b_redslot;
-  DBuf b_subpair, b_subchunks, b_sbfold, b_sbchunks;  // sub-pairs and H sub-blocks (orbital chunks)
-  DBuf o_atom, o_jatom, o_boff, o_partner;  // ordered pair list
-  DBuf b_scale, b_tmp;                       // fixed-point scale of the tables: [S_phi, 1/S_phi]
-  double phi_scale = 1.0;
-};
-
-struct lcp_job {
-  const lcp_ucell* ucell = nullptr;
-  const lcp_orbs* orbs = nullptr;
-  int32_t spinpol = LCP_SPIN_OFF, xc = LCP_XC_LDA;
-  int nspin = 1;
-  int64_t nn = 0, hsize = 0;
-  double recvecs[9] = {};
-  DBuf dm[4], rho[4], hks[4], vpot[4];
-  DBuf aden, pcc, vna, dvh, real, spec, part, scal;
-  bool has_aden = false, has_pcc = false, has_vna = false;
-  FftPlans* plans = nullptr;
-};
-
-namespace {
 
 lcp_status get_plans(lcp_ctx* ctx, const int32_t* ng, FftPlans** out) {
   auto key = std::make_tuple((int)ng[0], (int)ng[1], (int)ng[2]);
@@ -362,7 +236,6 @@ lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const
   return LCP_OK;
 }
 
-}  // namespace
 
 
 extern "C" {

@@ -1,0 +1,142 @@
+// Internal state of the C ABI objects (contexts, cells, orbital tables, jobs)
+// shared by the translation units that orchestrate kernels.  Not part of the
+// public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "lcp_device.h"
+#include "lcp_internal.h"
+
+static inline lcp_status fail(lcp_status code, const std::string& msg) {
+  lcp::set_error(msg);
+  return code;
+}
+
+static inline lcp_status cuda_fail(cudaError_t e, const char* where) {
+  return fail(e == cudaErrorMemoryAllocation ? LCP_ENOMEM : LCP_EDEVICE,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define API_CUDA(expr, where)                       \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_fail(_e, where); \
+  } while (0)
+
+// Owning device buffer.
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+template <class T>
+cudaError_t upload(DBuf& b, const std::vector<T>& v, cudaStream_t st) {
+  cudaError_t e = b.ensure(v.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  e = cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
+}
+
+static inline int channels(int32_t spinpol) { return spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4); }
+
+struct lcp_ucell {
+  lcp::UCell u;
+};
+
+struct FftPlans {
+  cufftHandle fwd = 0, inv = 0;
+  bool ok = false;
+};
+
+struct lcp_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  int32_t precision = LCP_PREC_FP64;
+  int64_t launches = 0;
+  std::map<std::tuple<int, int, int>, FftPlans> plans;
+  // workspaces of the host-buffer entry points
+  DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
+  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale;
+  ~lcp_ctx() {
+    cudaSetDevice(device);
+    for (auto& kv : plans) {
+      if (kv.second.fwd) cufftDestroy(kv.second.fwd);
+      if (kv.second.inv) cufftDestroy(kv.second.inv);
+    }
+    if (own) cudaStreamDestroy(own);
+  }
+};
+
+struct lcp_orbs {
+  const lcp_ucell* ucell = nullptr;
+  int device = 0;
+  bool grad = false;
+  int max_no = 0;
+  lcp::DevGeom geom{};
+  lcp::DevPairs pairs{};
+  // device arrays
+  DBuf atv, gxyz, spe, sph_off, glist, clist, phi_off, numorbs;
+  DBuf species, radial;
+  DBuf phi, dphi[3], phi32;
+  DBuf p_atom, p_jatom, p_boffp, p_boffq, p_self, p_lensoff, p_g1, p_g2, it_pair, it_start, it_count;
+  int64_t table_elems = 0;
+  // brick tiling and split-BF16 tables of the tensor-core path (built on first use)
+  bool bricks_ready = false;
+  lcp::Bricks bricks;
+  lcp::TcBrickGeom bgeom{};
+  DBuf b_code, b_imgoff, b_imgblk, b_taboff, b_tabpair, b_tab, b_tabslot, b_slotbase, b_redoff, b_redslot;
+  DBuf b_subpair, b_subchunks, b_sbfold, b_sbchunks;  // sub-pairs and H sub-blocks (orbital chunks)
+  DBuf o_atom, o_jatom, o_boff, o_partner;  // ordered pair list
+  DBuf b_scale, b_tmp;                       // fixed-point scale of the tables: [S_phi, 1/S_phi]
+  double phi_scale = 1.0;
+};
+
+struct lcp_job {
+  const lcp_ucell* ucell = nullptr;
+  const lcp_orbs* orbs = nullptr;
+  int32_t spinpol = LCP_SPIN_OFF, xc = LCP_XC_LDA;
+  int nspin = 1;
+  int64_t nn = 0, hsize = 0;
+  double recvecs[9] = {};
+  DBuf dm[4], rho[4], hks[4], vpot[4];
+  DBuf aden, pcc, vna, dvh, real, spec, part, scal;
+  bool has_aden = false, has_pcc = false, has_vna = false;
+  FftPlans* plans = nullptr;
+};
+
+
+// helpers of lcp_api.cu used by the other orchestration files
+lcp_status get_plans(lcp_ctx* ctx, const int32_t* ng, FftPlans** out);
+lcp_status check_ctx(lcp_ctx* ctx);
+lcp_status check_pair(const lcp_ucell* ucell, const lcp_orbs* orbs);
+lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o);
+lcp_status device_status(lcp_ctx* ctx);

@@ -116,6 +116,70 @@ struct TcBrickGeom {
   const int64_t* tab_off;
   const int32_t* tab_pair;
 };
+// One cell of a tensor-core launch: its brick tiling and tables, and where the
+// step reads and writes.  A batch launch covers the bricks of several cells.
+struct TcCell {
+  int64_t nbricks, nblocks;
+  int32_t bdim[3], nb[3], ngrid[3];
+  int32_t npts;
+  const __nv_bfloat16* tab;    // part-major split-BF16 tables of the cell
+  const int64_t* img_off;      // [nbricks+1]
+  const int64_t* tab_off;      // [nbricks+1]
+  const int32_t* tab_pair;     // sub-pair tables (density)
+  const int32_t* tab_slot;     // slot tables (matrix elements)
+  const int64_t* slot_base;    // [nbricks+1]
+  double phi_scale;            // S_phi of the tables
+  const __nv_bfloat16* dsym;   // density: split D blocks, zero block at zero_pair
+  int64_t zero_pair;
+  double* rho;                 // density output (one spin channel)
+  const double* vpot;          // matrix elements: V (one channel)
+  float2* vw;                  // [nbricks * 128] per-brick V weights (workspace)
+  float* vscale;               // [nbricks]
+  float* scratch;              // partial blocks, slot_base-indexed
+};
+// Several cells in one launch: brick k of the launch is brick brick_local[k]
+// of cell brick_cell[k].  cells == nullptr: a single cell, passed by value.
+struct TcBatch {
+  int64_t nbricks;
+  int32_t ncells;
+  const TcCell* cells;
+  const int32_t* brick_cell;
+  const int64_t* brick_local;
+};
+TcCell tc_cell_of(const TcBrickGeom& bg, const __nv_bfloat16* tab);
+// Batched split D blocks: cell c's sub-pairs (and its zero block) at
+// start[c] .. start[c+1] of the launch's blocks.
+struct DsymCell {
+  int64_t nsub;
+  const int32_t* sub_pair;
+  const int32_t* sub_chunks;
+  const int32_t* pair_atom;
+  const int32_t* pair_jatom;
+  const int64_t* boff;
+  const int32_t* partner;
+  const int32_t* numorbs;
+  const double* dm;
+  __nv_bfloat16* out;
+};
+cudaError_t launch_dsym_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_blocks,
+                              const double* scale, cudaStream_t st);
+// Batched partial-block reduction: cell c's H sub-blocks at start[c] .. start[c+1].
+struct RedCell {
+  const int64_t* red_off;
+  const int64_t* red_slot;
+  const int32_t* sb_fold;
+  const int32_t* sb_chunks;
+  const float* scratch;
+  DevPairs pr;
+  const int32_t* numorbs;
+  double dv;
+  double* H;
+};
+cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, int64_t total,
+                                  cudaStream_t st);
+cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, const double* dscale, int* status,
+                                    cudaStream_t st);
+cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,
                                 cudaStream_t st);
 cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const int32_t* numorbs,

@@ -249,6 +249,35 @@ __global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t
 // k = orbital 16 cb + b' of its jatom; fixed-point with scale[0].  Dsym adds
 // the partner's transposed block, except on the diagonal chunks of a self
 // pair (which is its own partner).  Entry nsub is a zero block.
+__device__ __forceinline__ void dsym_entry(int64_t sp, int w, int64_t nsub, const int32_t* __restrict__ sub_pair,
+                                           const int32_t* __restrict__ sub_chunks,
+                                           const int32_t* __restrict__ pair_atom,
+                                           const int32_t* __restrict__ pair_jatom, const int64_t* __restrict__ boff,
+                                           const int32_t* __restrict__ partner, const int32_t* __restrict__ numorbs,
+                                           const double* __restrict__ dm, double inv, __nv_bfloat16* __restrict__ out) {
+  const int kh = w >> 7, nh = (w >> 6) & 1, rr = (w >> 3) & 7, cc = w & 7;
+  double v = 0.0;
+  if (sp < nsub) {
+    const int p = sub_pair[sp], ch = sub_chunks[sp];
+    const int ca = ch >> 8, cb = ch & 255;
+    const int a = ca * 16 + nh * 8 + rr, b = cb * 16 + kh * 8 + cc;
+    const int i = pair_atom[p], j = pair_jatom[p];
+    const int noi = numorbs[i], noj = numorbs[j];
+    if (a < noi && b < noj) {
+      v = dm[boff[p] + (int64_t)a * noj + b];
+      const int q = partner[p];
+      if (q != p || ca != cb) v += dm[boff[q] + (int64_t)b * noi + a];
+    }
+  }
+  __nv_bfloat16 h, mm, l;
+  const double x = v * inv;
+  const float xf = (float)x;
+  fx_split_f(xf, (float)(x - (double)xf), h, mm, l);
+  out[sp * kDsymElems + w] = h;
+  out[sp * kDsymElems + 256 + w] = mm;
+  out[sp * kDsymElems + 512 + w] = l;
+}
+
 __global__ void dsym_kernel(int64_t nsub, const int32_t* __restrict__ sub_pair, const int32_t* __restrict__ sub_chunks,
                             const int32_t* __restrict__ pair_atom, const int32_t* __restrict__ pair_jatom,
                             const int64_t* __restrict__ boff, const int32_t* __restrict__ partner,
@@ -256,30 +285,28 @@ __global__ void dsym_kernel(int64_t nsub, const int32_t* __restrict__ sub_pair, 
                             const double* __restrict__ scale, __nv_bfloat16* __restrict__ out) {
   const double inv = scale[1];
   const int64_t total = (nsub + 1) * 256;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    dsym_entry(e >> 8, (int)(e & 255), nsub, sub_pair, sub_chunks, pair_atom, pair_jatom, boff, partner, numorbs, dm,
+               inv, out);
+}
+
+// Batched: the split D blocks of several cells (each with its zero block),
+// cell c's entries at start[c] .. start[c+1] (in blocks) of the launch.
+__global__ void dsym_batch_kernel(int32_t ncells, const DsymCell* __restrict__ cells,
+                                  const int64_t* __restrict__ start, const double* __restrict__ scale) {
+  const double inv = scale[1];
+  const int64_t total = start[ncells] * 256;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t sp = e >> 8;
-    const int w = (int)(e & 255);
-    const int kh = w >> 7, nh = (w >> 6) & 1, rr = (w >> 3) & 7, cc = w & 7;
-    double v = 0.0;
-    if (sp < nsub) {
-      const int p = sub_pair[sp], ch = sub_chunks[sp];
-      const int ca = ch >> 8, cb = ch & 255;
-      const int a = ca * 16 + nh * 8 + rr, b = cb * 16 + kh * 8 + cc;
-      const int i = pair_atom[p], j = pair_jatom[p];
-      const int noi = numorbs[i], noj = numorbs[j];
-      if (a < noi && b < noj) {
-        v = dm[boff[p] + (int64_t)a * noj + b];
-        const int q = partner[p];
-        if (q != p || ca != cb) v += dm[boff[q] + (int64_t)b * noi + a];
-      }
+    const int64_t g = e >> 8;
+    int lo = 0, hi = ncells;  // cell with start[lo] <= g < start[lo+1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (start[mid] <= g) lo = mid;
+      else hi = mid;
     }
-    __nv_bfloat16 h, mm, l;
-    const double x = v * inv;
-    const float xf = (float)x;
-    fx_split_f(xf, (float)(x - (double)xf), h, mm, l);
-    out[sp * kDsymElems + w] = h;
-    out[sp * kDsymElems + 256 + w] = mm;
-    out[sp * kDsymElems + 512 + w] = l;
+    const DsymCell& c = cells[lo];
+    dsym_entry(g - start[lo], (int)(e & 255), c.nsub, c.sub_pair, c.sub_chunks, c.pair_atom, c.pair_jatom, c.boff,
+               c.partner, c.numorbs, c.dm, inv, c.out);
   }
 }
 
@@ -334,20 +361,22 @@ __device__ __forceinline__ void smem_point_row(const uint8_t* blk, int p, float*
 // ==========================================================================
 
 struct TcDensArgs {
-  int64_t nbricks, nblocks;
-  int32_t bdim[3], nb[3], ngrid[3];
-  int32_t npts;
-  int32_t zero_pair;
-  double phi_scale;      // S_phi
-  const double* dscale;  // [S_D, 1/S_D]
-  const int64_t* img_off;
-  const int64_t* tab_off;
-  const int32_t* tab_pair;
-  const __nv_bfloat16* tab;
-  const __nv_bfloat16* dsym;
-  double* rho;
+  TcCell cell0;          // the cell of a single-cell launch
+  TcBatch batch;         // or the cells of a batch
+  const double* dscale;  // [S_D, 1/S_D], one scale for every cell of the launch
   int* status;
 };
+
+// Cell and cell-local brick index of brick k of a launch.
+__device__ __forceinline__ const TcCell* tc_cell(const TcCell* c0, const TcBatch& b, int64_t k, int64_t& hb) {
+  if (!b.cells) {
+    hb = k;
+    return c0;
+  }
+  hb = b.brick_local[k];
+  return b.cells + b.brick_cell[k];
+}
+
 
 // Density kernel roles (320 threads, one CTA per SM, persistent over bricks):
 //   warp 0     table producer: per K step (brick, window, image t) three 4 KB
@@ -382,7 +411,7 @@ constexpr size_t kDSmem = kDSmemStages + (size_t)kDGatherWarps * kDMaxImages * k
 constexpr uint32_t kDBufCols = 256;               // TMEM columns per window buffer
 constexpr uint32_t kDCross = 128;                 // cross accumulator within a buffer
 
-__global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
+__global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constant__ TcDensArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint64_t full_bar[kDStages], empty_bar[kDStages], mdone_bar[kDStages], tempty_bar[2], drain_bar;
   __shared__ uint32_t tslot;
@@ -404,6 +433,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tslot;
+  const int64_t ntotal = args.batch.cells ? args.batch.nbricks : args.cell0.nbricks;
   auto give_up = [&]() {
     if (!abort_flag) atomicExch(args.status, LCP_ETIMEDOUT);
     abort_flag = 1;
@@ -412,9 +442,11 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
   if (warp == 0) {
     // ------------------------------------------------------------ table producer
     uint32_t it = 0;
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin) {
         for (int k = 0; k < m - c0; ++k, ++it) {
           const int t = m - 1 - k;
@@ -428,7 +460,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
             uint8_t* sA = smem + stage * kDStageBytes;
             tc::mbar_arrive_expect_tx(&full_bar[stage], kDStageA);
             for (int part = 0; part < 3; ++part)
-              tc::bulk_g2s(sA + part * 4096, args.tab + ((int64_t)part * args.nblocks + i0 + t) * kPart, 4096,
+              tc::bulk_g2s(sA + part * 4096, cl.tab + ((int64_t)part * cl.nblocks + i0 + t) * kPart, 4096,
                            &full_bar[stage]);
           }
           __syncwarp();
@@ -444,13 +476,15 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
     // ------------------------------------------------------------ D gatherers
     const int gw = warp - 6;
     int32_t* pair = reinterpret_cast<int32_t*>(smem + kDSmemStages) + gw * kDMaxImages * kDMaxImages;
-    const uint8_t* dsym = reinterpret_cast<const uint8_t*>(args.dsym);
     uint32_t it = 0;
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       if (m == 0) continue;
-      const int32_t* ptab = args.tab_pair + args.tab_off[hb];
+      const int32_t* ptab = cl.tab_pair + cl.tab_off[hb];
+      const uint8_t* dsym = reinterpret_cast<const uint8_t*>(cl.dsym);
       __syncwarp();
       for (int e = lane; e < m * m; e += 32) pair[e] = ptab[e];
       __syncwarp();
@@ -470,7 +504,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
             // 16-byte pieces: (image, part, kh, 16 x 16 B)
             const int si = c / 96, w = c - si * 96, part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
             int pr = pair[(c0 + si) * m + t];
-            if (pr < 0) pr = args.zero_pair;
+            if (pr < 0) pr = (int)cl.zero_pair;
             cp_async16(sB + part * (2 * kDBLbo) + kh * kDBLbo + si * 256 + q * 16,
                        dsym + (int64_t)pr * (kDsymElems * 2) + part * 512 + kh * 256 + q * 16);
           }
@@ -496,9 +530,11 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     uint32_t it = 0, win = 0;
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin, ++win) {
         const int c1 = min(c0 + kDWin, m);
         const uint32_t buf = win & 1, wuse = win >> 1;
@@ -556,11 +592,13 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
     // ------------------------------------------------------------ epilogue
     const uint32_t quarter = warp & 3;  // TMEM lanes [32 * quarter, 32 * quarter + 32)
     const int p = (int)quarter * 32 + lane;
-    const double out_scale = args.phi_scale * args.phi_scale * args.dscale[0];
+    const double dsc = args.dscale[0];
     uint32_t it = 0, win = 0, mpar = 0;  // mpar: phase bit of mdone_bar per stage
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       float acc_hi = 0.0f, acc_lo = 0.0f;
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin, ++win) {
         const int c1 = min(c0 + kDWin, m);
@@ -592,9 +630,9 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(TcDensArgs args) {
         if (lane == 0) tc::mbar_arrive(&tempty_bar[buf]);
       }
       if (abort_flag) break;
-      if (p < args.npts)
-        args.rho[brick_point_index(hb, p, args.bdim, args.nb, args.ngrid)] =
-            ((double)acc_hi + (double)acc_lo) * out_scale;
+      if (p < cl.npts)
+        cl.rho[brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid)] =
+            ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * dsc);
     }
   }
   tc::fence_before_sync();
@@ -658,32 +696,23 @@ constexpr size_t kHSmem = 3 * (size_t)kHABytes + (size_t)kHStages * 3 * kHBBytes
 constexpr uint32_t kHBufCols = 256, kHAccCols = 64;
 
 struct TcHamArgs {
-  int64_t nbricks, nblocks;
-  int32_t bdim[3], nb[3], ngrid[3];
-  int32_t npts;
-  double phi_scale;
-  const int64_t* img_off;
-  const int64_t* tab_off;
-  const int32_t* tab_slot;
-  const int64_t* slot_base;
-  const __nv_bfloat16* tab;
-  const float2* vw;     // per brick and point slot: V / S_V as FP32 hi + lo
-  const float* vscale;  // per brick: S_V * S_phi^2 (a power of two)
-  float* scratch;
+  TcCell cell0;
+  TcBatch batch;
   int* status;
 };
 
 // Per brick: S_V = power of two >= max|V| over the brick's points, and V / S_V
 // (exact) as an FP32 pair hi + lo, for the V-weighting inside the matrix
-// element kernel.  One block of 128 threads (point slots) per brick.
-__global__ void __launch_bounds__(128) vweight_kernel(int64_t nbricks, int3 bdim, int3 nb, int3 ngrid, int npts,
-                                                      const double* __restrict__ vpot, double phi2,
-                                                      float2* __restrict__ vw, float* __restrict__ vscale) {
+// element kernel; S_V * S_phi^2 per brick for its epilogue.  One block of 128
+// threads (point slots) per brick.
+__global__ void __launch_bounds__(128) vweight_kernel(const __grid_constant__ TcHamArgs args) {
   __shared__ unsigned long long smax[4];
   const int p = threadIdx.x, warp = p >> 5, lane = p & 31;
-  const int32_t bd[3] = {bdim.x, bdim.y, bdim.z}, nbb[3] = {nb.x, nb.y, nb.z}, ng[3] = {ngrid.x, ngrid.y, ngrid.z};
-  for (int64_t hb = blockIdx.x; hb < nbricks; hb += gridDim.x) {
-    const double v = p < npts ? vpot[brick_point_index(hb, p, bd, nbb, ng)] : 0.0;
+  const int64_t ntotal = args.batch.cells ? args.batch.nbricks : args.cell0.nbricks;
+  for (int64_t k = blockIdx.x; k < ntotal; k += gridDim.x) {
+    int64_t hb;
+    const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+    const double v = p < cl.npts ? cl.vpot[brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid)] : 0.0;
     // |v| as bits: non-negative doubles order like their bit patterns
     unsigned long long m = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
     for (int o = 16; o > 0; o >>= 1) {
@@ -698,13 +727,13 @@ __global__ void __launch_bounds__(128) vweight_kernel(int64_t nbricks, int3 bdim
     const double sv = pow2_from_exp(e);
     const double vs = v * pow2_from_exp(-e);  // exact: a power-of-two scaling
     const float vh = (float)vs;
-    vw[hb * 128 + p] = make_float2(vh, (float)(vs - (double)vh));
-    if (p == 0) vscale[hb] = (float)(sv * phi2);
+    cl.vw[hb * 128 + p] = make_float2(vh, (float)(vs - (double)vh));
+    if (p == 0) cl.vscale[hb] = (float)(sv * cl.phi_scale * cl.phi_scale);
     __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_kernel(TcHamArgs args) {
+__global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_kernel(const __grid_constant__ TcHamArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint64_t bfull_bar[kHStages], bready_bar[kHStages], bempty_bar[kHStages], tfull_bar[2], tempty_bar[2];
   __shared__ uint64_t afull_bar, afree_bar, drain_bar;
@@ -734,6 +763,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tslot;
+  const int64_t ntotal = args.batch.cells ? args.batch.nbricks : args.cell0.nbricks;
   auto give_up = [&]() {
     if (!abort_flag) atomicExch(args.status, LCP_ETIMEDOUT);
     abort_flag = 1;
@@ -743,7 +773,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     // ------------------------------------------------------------ producer
     uint32_t it = 0, grp = 0;
     // B tile `it` (images t0 .. t0+nt-1 of brick i0) into its stage
-    auto load_b = [&](int64_t i0, int t0, int nt) -> bool {
+    auto load_b = [&](const TcCell& cl, int64_t i0, int t0, int nt) -> bool {
       const int stage = (int)(it % kHStages);
       const uint32_t use = it / kHStages;
       if (use > 0 && !tc::mbar_wait_abortable(&bempty_bar[stage], (use - 1) & 1, &abort_flag)) return false;
@@ -751,20 +781,22 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
       if (lane == 0) {
         tc::mbar_arrive_expect_tx(&bfull_bar[stage], nt * 3 * kImgBytes);
         for (int part = 0; part < 3; ++part)
-          tc::bulk_g2s(sB + part * kHBBytes, args.tab + ((int64_t)part * args.nblocks + i0 + t0) * kPart,
+          tc::bulk_g2s(sB + part * kHBBytes, cl.tab + ((int64_t)part * cl.nblocks + i0 + t0) * kPart,
                        nt * kImgBytes, &bfull_bar[stage]);
       }
       __syncwarp();
       ++it;
       return true;
     };
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup, ++grp) {
         // the group's first B tile goes ahead of the A refill, which waits
         // for the previous group's MMAs
-        if (!load_b(i0, s0, min(kHWin, m - s0))) {
+        if (!load_b(cl, i0, s0, min(kHWin, m - s0))) {
           give_up();
           break;
         }
@@ -776,12 +808,12 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
         if (lane == 0) {
           tc::mbar_arrive_expect_tx(&afull_bar, na * 3 * kImgBytes);
           for (int part = 0; part < 3; ++part)
-            tc::bulk_g2s(sA + part * kHABytes, args.tab + ((int64_t)part * args.nblocks + i0 + s0) * kPart,
+            tc::bulk_g2s(sA + part * kHABytes, cl.tab + ((int64_t)part * cl.nblocks + i0 + s0) * kPart,
                          na * kImgBytes, &afull_bar);
         }
         __syncwarp();
         bool ok = true;
-        for (int t0 = s0 + kHWin; t0 < m && ok; t0 += kHWin) ok = load_b(i0, t0, min(kHWin, m - t0));
+        for (int t0 = s0 + kHWin; t0 < m && ok; t0 += kHWin) ok = load_b(cl, i0, t0, min(kHWin, m - t0));
         if (!ok) {
           give_up();
           break;
@@ -796,9 +828,11 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     uint32_t it = 0, grp = 0;
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup, ++grp) {
         if (!tc::mbar_wait_abortable(&afull_bar, grp & 1, &abort_flag)) {
           give_up();
@@ -862,11 +896,13 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     static_assert(32 * kHXformWarps == 256, "one transform thread per chunk of an image");
     const int pt = ((tt >> 3) & 15) * 8 + (tt & 7);  // its point slot
     uint32_t it = 0;
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       if (m == 0) continue;
-      const float2 w = args.vw[hb * 128 + pt];
+      const float2 w = cl.vw[hb * 128 + pt];
       const float vh = w.x, vl = w.y;
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
         for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
@@ -914,13 +950,15 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     const uint32_t quarter = warp & 3;
     const int row = (int)quarter * 32 + lane;  // TMEM lane = M row = (s image, orbital)
     uint32_t it = 0;
-    for (int64_t hb = blockIdx.x; hb < args.nbricks && !abort_flag; hb += gridDim.x) {
-      const int64_t i0 = args.img_off[hb];
-      const int m = (int)(args.img_off[hb + 1] - i0);
+    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+      int64_t hb;
+      const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
+      const int64_t i0 = cl.img_off[hb];
+      const int m = (int)(cl.img_off[hb + 1] - i0);
       if (m == 0) continue;
-      const int64_t tb = args.tab_off[hb];
-      const int64_t sbase = args.slot_base[hb];
-      const float out_scale = args.vscale[hb];  // S_V * S_phi^2, a power of two
+      const int64_t tb = cl.tab_off[hb];
+      const int64_t sbase = cl.slot_base[hb];
+      const float out_scale = cl.vscale[hb];  // S_V * S_phi^2, a power of two
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
         const int s = s0 + (row >> 4), a = row & 15;
         for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
@@ -929,7 +967,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
           int slot[kHWin];
 #pragma unroll
           for (int j = 0; j < kHWin; ++j)
-            slot[j] = (j < nt && s < m && s <= t0 + j) ? args.tab_slot[tb + s * m + t0 + j] : -1;
+            slot[j] = (j < nt && s < m && s <= t0 + j) ? cl.tab_slot[tb + s * m + t0 + j] : -1;
           if (!tc::mbar_wait_abortable(&tfull_bar[buf], (it >> 1) & 1, &abort_flag)) {
             give_up();
             break;
@@ -952,7 +990,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
                   o[c] = (__uint_as_float(y[0][c]) +
                           (__uint_as_float(y[1][c]) + (__uint_as_float(y[2][c]) + __uint_as_float(y[3][c])))) *
                          out_scale;
-                float4* dst = reinterpret_cast<float4*>(args.scratch + (sbase + slot[j]) * 256 + a * 16);
+                float4* dst = reinterpret_cast<float4*>(cl.scratch + (sbase + slot[j]) * 256 + a * 16);
                 dst[0] = make_float4(o[0], o[1], o[2], o[3]);
                 dst[1] = make_float4(o[4], o[5], o[6], o[7]);
                 dst[2] = make_float4(o[8], o[9], o[10], o[11]);
@@ -986,6 +1024,73 @@ __device__ __forceinline__ void ff_add8(float* hi, float* lo, float4 a, float4 b
   ff_add(hi[4], lo[4], b.x); ff_add(hi[5], lo[5], b.y); ff_add(hi[6], lo[6], b.z); ff_add(hi[7], lo[7], b.w);
 }
 
+__device__ __forceinline__ void h_reduce_block(int64_t u, const int64_t* __restrict__ red_off,
+                                               const int64_t* __restrict__ red_slot,
+                                               const int32_t* __restrict__ sb_fold,
+                                               const int32_t* __restrict__ sb_chunks,
+                                               const float* __restrict__ scratch, const DevPairs& pr,
+                                               const int32_t* __restrict__ numorbs, double dv, double* H,
+                                               int64_t* s_code, float (*s_part)[8][256]) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float dh[8], dl[8], th[8], tl[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) dh[i] = dl[i] = th[i] = tl[i] = 0.0f;
+  const int64_t k0 = red_off[u], k1 = red_off[u + 1];
+  for (int64_t kb = k0; kb < k1; kb += 256) {
+    const int n = (int)min((int64_t)256, k1 - kb);
+    __syncthreads();
+    if (tid < n) s_code[tid] = red_slot[kb + tid];
+    __syncthreads();
+    for (int j = warp; j < n; j += 32) {  // slots j, j+8, j+16, j+24 in flight together
+      float4 v[4][2];
+      int64_t c[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int jj = j + 8 * q;
+        c[q] = jj < n ? s_code[jj] : -1;
+        if (c[q] >= 0) {
+          const float4* src = reinterpret_cast<const float4*>(scratch + (c[q] >> 1) * 256) + lane * 2;
+          v[q][0] = __ldg(src);
+          v[q][1] = __ldg(src + 1);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (c[q] < 0) continue;
+        if (c[q] & 1) ff_add8(th, tl, v[q][0], v[q][1]);
+        else ff_add8(dh, dl, v[q][0], v[q][1]);
+      }
+    }
+  }
+  __syncthreads();  // the previous sub-block's readers of s_part are done
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    s_part[0][warp][lane * 8 + i] = dh[i];
+    s_part[1][warp][lane * 8 + i] = dl[i];
+    s_part[2][warp][lane * 8 + i] = th[i];
+    s_part[3][warp][lane * 8 + i] = tl[i];
+  }
+  __syncthreads();
+  const int a = tid >> 4, b = tid & 15, et = b * 16 + a;
+  float hi = 0.0f, lo = 0.0f;
+  for (int w = 0; w < 8; ++w) {
+    ff_add(hi, lo, s_part[0][w][tid]);
+    lo += s_part[1][w][tid];
+    ff_add(hi, lo, s_part[2][w][et]);
+    lo += s_part[3][w][et];
+  }
+  const double acc = (double)hi + (double)lo;
+  const int q = sb_fold[u], ch = sb_chunks[u];
+  const int ra = (ch >> 8) * 16 + a, rb = (ch & 255) * 16 + b;  // entry of the pair's block
+  const int i = pr.atom[q], jj = pr.jatom[q];
+  const int noi = numorbs[i], noj = numorbs[jj];
+  if (ra < noi && rb < noj) {
+    const double v = acc * dv;
+    H[pr.boff_p[q] + (int64_t)ra * noj + rb] = v;
+    if (!pr.self[q]) H[pr.boff_q[q] + (int64_t)rb * noi + ra] = v;
+  }
+}
+
 __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nsb, const int64_t* __restrict__ red_off,
                                                        const int64_t* __restrict__ red_slot,
                                                        const int32_t* __restrict__ sb_fold,
@@ -993,65 +1098,26 @@ __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nsb, const int64_
                                                        const float* __restrict__ scratch, DevPairs pr,
                                                        const int32_t* __restrict__ numorbs, double dv, double* H) {
   __shared__ int64_t s_code[256];
-  __shared__ float s_part[4][8][256];  // [own hi, own lo, partner hi, partner lo][warp][entry]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int64_t u = blockIdx.x; u < nsb; u += gridDim.x) {
-    float dh[8], dl[8], th[8], tl[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) dh[i] = dl[i] = th[i] = tl[i] = 0.0f;
-    const int64_t k0 = red_off[u], k1 = red_off[u + 1];
-    for (int64_t kb = k0; kb < k1; kb += 256) {
-      const int n = (int)min((int64_t)256, k1 - kb);
-      __syncthreads();
-      if (tid < n) s_code[tid] = red_slot[kb + tid];
-      __syncthreads();
-      for (int j = warp; j < n; j += 32) {  // slots j, j+8, j+16, j+24 in flight together
-        float4 v[4][2];
-        int64_t c[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int jj = j + 8 * q;
-          c[q] = jj < n ? s_code[jj] : -1;
-          if (c[q] >= 0) {
-            const float4* src = reinterpret_cast<const float4*>(scratch + (c[q] >> 1) * 256) + lane * 2;
-            v[q][0] = __ldg(src);
-            v[q][1] = __ldg(src + 1);
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          if (c[q] < 0) continue;
-          if (c[q] & 1) ff_add8(th, tl, v[q][0], v[q][1]);
-          else ff_add8(dh, dl, v[q][0], v[q][1]);
-        }
-      }
+  __shared__ float s_part[4][8][256];  // [direct hi, direct lo, transposed hi, transposed lo][warp][entry]
+  for (int64_t u = blockIdx.x; u < nsb; u += gridDim.x)
+    h_reduce_block(u, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H, s_code, s_part);
+}
+
+// Batched: the sub-blocks of several cells, cell c's at start[c] .. start[c+1].
+__global__ void __launch_bounds__(256) h_reduce_batch_kernel(int32_t ncells, const RedCell* __restrict__ cells,
+                                                             const int64_t* __restrict__ start) {
+  __shared__ int64_t s_code[256];
+  __shared__ float s_part[4][8][256];
+  for (int64_t g = blockIdx.x; g < start[ncells]; g += gridDim.x) {
+    int lo = 0, hi = ncells;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (start[mid] <= g) lo = mid;
+      else hi = mid;
     }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      s_part[0][warp][lane * 8 + i] = dh[i];
-      s_part[1][warp][lane * 8 + i] = dl[i];
-      s_part[2][warp][lane * 8 + i] = th[i];
-      s_part[3][warp][lane * 8 + i] = tl[i];
-    }
-    __syncthreads();
-    const int a = tid >> 4, b = tid & 15, et = b * 16 + a;
-    float hi = 0.0f, lo = 0.0f;
-    for (int w = 0; w < 8; ++w) {
-      ff_add(hi, lo, s_part[0][w][tid]);
-      lo += s_part[1][w][tid];
-      ff_add(hi, lo, s_part[2][w][et]);
-      lo += s_part[3][w][et];
-    }
-    const double acc = (double)hi + (double)lo;
-    const int q = sb_fold[u], ch = sb_chunks[u];
-    const int ra = (ch >> 8) * 16 + a, rb = (ch & 255) * 16 + b;  // entry of the pair's block
-    const int i = pr.atom[q], jj = pr.jatom[q];
-    const int noi = numorbs[i], noj = numorbs[jj];
-    if (ra < noi && rb < noj) {
-      const double v = acc * dv;
-      H[pr.boff_p[q] + (int64_t)ra * noj + rb] = v;
-      if (!pr.self[q]) H[pr.boff_q[q] + (int64_t)rb * noi + ra] = v;
-    }
+    const RedCell& c = cells[lo];
+    h_reduce_block(g - start[lo], c.red_off, c.red_slot, c.sb_fold, c.sb_chunks, c.scratch, c.pr, c.numorbs, c.dv,
+                   c.H, s_code, s_part);
   }
 }
 
@@ -1097,34 +1163,85 @@ cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* su
   return cudaGetLastError();
 }
 
-cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
-                              const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
-                              int* status, cudaStream_t st) {
-  if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
-  TcDensArgs a{};
-  a.nbricks = bg.nbricks;
-  a.nblocks = bg.nblocks;
+cudaError_t launch_dsym_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_blocks,
+                              const double* scale, cudaStream_t st) {
+  const int64_t total = total_blocks * 256;
+  if (total == 0) return cudaSuccess;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+  dsym_batch_kernel<<<blocks, 256, 0, st>>>(ncells, cells, start, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, int64_t total,
+                                  cudaStream_t st) {
+  if (total == 0) return cudaSuccess;
+  const int grid = (int)std::min<int64_t>(total, (int64_t)sm_count() * 8);
+  h_reduce_batch_kernel<<<grid, 256, 0, st>>>(ncells, cells, start);
+  return cudaGetLastError();
+}
+
+TcCell tc_cell_of(const TcBrickGeom& bg, const __nv_bfloat16* tab) {
+  TcCell c{};
+  c.nbricks = bg.nbricks;
+  c.nblocks = bg.nblocks;
   for (int d = 0; d < 3; ++d) {
-    a.bdim[d] = bg.bdim[d];
-    a.nb[d] = bg.nb[d];
-    a.ngrid[d] = bg.ngrid[d];
+    c.bdim[d] = bg.bdim[d];
+    c.nb[d] = bg.nb[d];
+    c.ngrid[d] = bg.ngrid[d];
   }
-  a.npts = bg.npts;
-  a.zero_pair = zero_pair;
-  a.phi_scale = phi_scale;
+  c.npts = bg.npts;
+  c.tab = tab;
+  c.img_off = bg.img_off;
+  c.tab_off = bg.tab_off;
+  c.tab_pair = bg.tab_pair;
+  return c;
+}
+
+static int tc_grid(const TcCell& cell0, const TcBatch& batch) {
+  const int64_t n = batch.cells ? batch.nbricks : cell0.nbricks;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(n, sm_count()));
+}
+
+cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, const double* dscale, int* status,
+                                    cudaStream_t st) {
+  TcDensArgs a{};
+  a.cell0 = cell0;
+  a.batch = batch;
   a.dscale = dscale;
-  a.img_off = bg.img_off;
-  a.tab_off = bg.tab_off;
-  a.tab_pair = bg.tab_pair;
-  a.tab = tab;
-  a.dsym = dsym;
-  a.rho = rho;
   a.status = status;
   // 512 TMEM columns per CTA: the shared-memory ring (> half an SM) keeps one CTA per SM
   static_assert(kDSmem > 120 * 1024, "one CTA per SM");
   LCP_CUDA_TRY(cudaFuncSetAttribute(density_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDSmem));
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(bg.nbricks, sm_count()));
-  density_tc_kernel<<<grid, 192 + 32 * kDGatherWarps, kDSmem, st>>>(a);
+  density_tc_kernel<<<tc_grid(cell0, batch), 192 + 32 * kDGatherWarps, kDSmem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
+                              const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
+                              int* status, cudaStream_t st) {
+  if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
+  TcCell c = tc_cell_of(bg, tab);
+  c.phi_scale = phi_scale;
+  c.dsym = dsym;
+  c.zero_pair = zero_pair;
+  c.rho = rho;
+  return launch_density_tc_batch(c, TcBatch{}, dscale, status, st);
+}
+
+cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st) {
+  TcHamArgs a{};
+  a.cell0 = cell0;
+  a.batch = batch;
+  a.status = status;
+  const int64_t n = batch.cells ? batch.nbricks : cell0.nbricks;
+  if (n > 0) {
+    const int vgrid = (int)std::min<int64_t>(n, (int64_t)sm_count() * 16);
+    vweight_kernel<<<vgrid, 128, 0, st>>>(a);
+    LCP_CUDA_TRY(cudaGetLastError());
+  }
+  LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
+  static_assert(kHSmem > 120 * 1024, "one CTA per SM");
+  hamiltonian_tc_kernel<<<tc_grid(cell0, batch), 192 + 32 * kHXformWarps, kHSmem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -1132,38 +1249,15 @@ cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot
                                   const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
                                   float* vscale, float* scratch, int* status, cudaStream_t st) {
   if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
-  TcHamArgs a{};
-  a.nbricks = bg.nbricks;
-  a.nblocks = bg.nblocks;
-  for (int d = 0; d < 3; ++d) {
-    a.bdim[d] = bg.bdim[d];
-    a.nb[d] = bg.nb[d];
-    a.ngrid[d] = bg.ngrid[d];
-  }
-  a.npts = bg.npts;
-  a.phi_scale = phi_scale;
-  a.img_off = bg.img_off;
-  a.tab_off = bg.tab_off;
-  a.tab_slot = tab_slot;
-  a.slot_base = slot_base;
-  a.tab = tab;
-  a.vw = vw;
-  a.vscale = vscale;
-  a.scratch = scratch;
-  a.status = status;
-  LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(bg.nbricks, sm_count()));
-  if (bg.nbricks > 0) {
-    const int vgrid = (int)std::min<int64_t>(bg.nbricks, (int64_t)sm_count() * 16);
-    vweight_kernel<<<vgrid, 128, 0, st>>>(bg.nbricks, make_int3(bg.bdim[0], bg.bdim[1], bg.bdim[2]),
-                                          make_int3(bg.nb[0], bg.nb[1], bg.nb[2]),
-                                          make_int3(bg.ngrid[0], bg.ngrid[1], bg.ngrid[2]), bg.npts, vpot,
-                                          phi_scale * phi_scale, vw, vscale);
-    LCP_CUDA_TRY(cudaGetLastError());
-  }
-  static_assert(kHSmem > 120 * 1024, "one CTA per SM");
-  hamiltonian_tc_kernel<<<grid, 192 + 32 * kHXformWarps, kHSmem, st>>>(a);
-  return cudaGetLastError();
+  TcCell c = tc_cell_of(bg, tab);
+  c.tab_slot = tab_slot;
+  c.slot_base = slot_base;
+  c.phi_scale = phi_scale;
+  c.vpot = vpot;
+  c.vw = vw;
+  c.vscale = vscale;
+  c.scratch = scratch;
+  return launch_hamiltonian_tc_batch(c, TcBatch{}, status, st);
 }
 
 cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* red_slot, const int32_t* sb_fold,
