@@ -112,9 +112,10 @@ enum {
 lcp_status lcp_ucell_get_int(const lcp_ucell* ucell, int32_t field, int64_t index,
                              int32_t* dst, int64_t count);
 lcp_status lcp_ucell_get_atv(const lcp_ucell* ucell, double* dst /* [ncell*3] */);
-/* Grid-brick tiling of the tensor-core path: info[12] = brick dims (3), bricks
+/* Grid-brick tiling of the tensor-core path: info[14] = brick dims (3), bricks
  * per axis (3), points per brick, bricks, table blocks, max atom images of a
- * brick, total images, image pairs that are neighbour pairs. */
+ * brick, total images, image pairs that are neighbour pairs, partial H blocks
+ * (FP32 scratch slots of 1 KB), split-D sub-pairs. */
 lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info);
 
 /* Calc_Ngrid(Ecut, Latvecs) -- src/utils/Calc_Ngrid.jl:1-76 */
@@ -263,6 +264,35 @@ lcp_status lcp_server_poll(lcp_server* srv, int32_t max, int32_t wait_ms, uint64
                            double* latency_ms, int32_t* n);
 /* out4 = submitted, completed, resident bytes, budget. */
 lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4);
+
+/* ---------------------------------------------------------------- batching */
+
+/* Batched grid step over the device-resident jobs of many cells (the
+ * spec batching form; the reference steps one cell at a time).  Each
+ * stage runs once for all cells: one persistent tensor-core launch over the
+ * bricks of every cell for the density and for the matrix elements, batched
+ * cuFFT plans per grid shape, tiled grid kernels and FP64 reductions over all
+ * cells.  The step is captured once as a CUDA graph and replayed.  Results
+ * land in the jobs' own buffers (read them with lcp_job_get_* /
+ * lcp_job_energies); each cell's density, H and energy sums are computed as
+ * in a single-cell split-BF16 step.  The jobs (same SpinPol and xc, split-BF16
+ * context) stay owned by the caller and must outlive the batch; their D is
+ * set with lcp_job_set_dm. */
+typedef struct lcp_batch lcp_batch;
+enum { LCP_BATCH_GRAPH = 0, LCP_BATCH_EAGER = 1 };
+lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, lcp_batch** out);
+void lcp_batch_destroy(lcp_batch* batch);
+/* One step of every cell on the context's stream (asynchronous).
+ * LCP_BATCH_GRAPH: replay the captured graph (the first call runs eagerly and
+ * captures); LCP_BATCH_EAGER: launch the kernels one by one. */
+lcp_status lcp_batch_step(lcp_ctx* ctx, lcp_batch* batch, int32_t mode);
+/* Waits for the stream; reports (and clears) a device-side timeout. */
+lcp_status lcp_batch_check_status(lcp_ctx* ctx, lcp_batch* batch);
+/* energies[5 * njobs]: each job's lcp_job_energies, in the batch's order. */
+lcp_status lcp_batch_energies(lcp_ctx* ctx, lcp_batch* batch, double* energies);
+/* out8 = cells, grid-shape groups, bricks, own kernels per step, workspace
+ * bytes, graph captured (0/1), H sub-blocks, split-D blocks. */
+lcp_status lcp_batch_info(const lcp_batch* batch, int64_t* out8);
 
 /* Split-BF16 density that allocates no device memory.  No counterpart in the
  * reference: it is for callers that cannot call cudaMalloc at call time --

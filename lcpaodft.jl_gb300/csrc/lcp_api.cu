@@ -238,6 +238,32 @@ lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const
 
 
 
+// The job's cell as a grid-step pass sees it (its own buffers).
+lcp::GridCell job_grid_cell(lcp_job* job) {
+  const lcp::UCell& u = job->ucell->u;
+  lcp::GridCell c{};
+  for (int d = 0; d < 3; ++d) c.ng[d] = u.ngrid[d];
+  c.nn = job->nn;
+  c.hsize = job->hsize;
+  for (int d = 0; d < 9; ++d) c.rv[d] = job->recvecs[d];
+  c.gridvol = u.gridvol;
+  c.aden = job->has_aden ? job->aden.as<double>() : nullptr;
+  c.pcc = job->has_pcc ? job->pcc.as<double>() : nullptr;
+  c.vna = job->has_vna ? job->vna.as<double>() : nullptr;
+  for (int s = 0; s < job->nspin && s < 2; ++s) {
+    c.rho[s] = job->rho[s].as<double>();
+    c.vpot[s] = job->vpot[s].as<double>();
+    c.dm[s] = job->dm[s].as<double>();
+    c.hks[s] = job->hks[s].as<double>();
+  }
+  c.real = job->real.as<double>();
+  c.spec = job->spec.p;
+  c.dvh = job->dvh.as<double>();
+  c.part = job->part.as<double>();
+  c.sums = job->scal.as<double>();
+  return c;
+}
+
 extern "C" {
 
 const char* lcp_last_error(void) { return lcp::last_error_cstr(); }
@@ -349,6 +375,8 @@ lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info) {
   for (auto v : b.tab_pair) paired += v >= 0;
   info[10] = (int64_t)b.img_block.size();
   info[11] = paired;
+  info[12] = b.slot_base.empty() ? 0 : b.slot_base.back();
+  info[13] = b.nsub;
   return LCP_OK;
 }
 
@@ -836,7 +864,7 @@ static lcp_status energy_host(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t
     API_CUDA(cudaMemcpyAsync(ctx->w_aux[2].p, dvhart, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
     d_vh = ctx->w_aux[2].as<double>();
   }
-  API_CUDA(ctx->w_part.ensure((size_t)lcp::kReduceBlocks * 3 * sizeof(double)), "alloc");
+  API_CUDA(ctx->w_part.ensure((size_t)std::max<int64_t>(lcp::red_tiles(nn), 1) * 3 * sizeof(double)), "alloc");
   API_CUDA(ctx->w_scal.ensure(8 * sizeof(double)), "alloc");
   API_CUDA(lcp::launch_energy_sums(xc, spinpol, nn, d_ad, d_pc, dr, d_vh, ctx->w_part.as<double>(),
                                    ctx->w_scal.as<double>(), ctx->stream),
@@ -921,7 +949,8 @@ lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* 
   API_CUDA(j->dvh.ensure(nn * sizeof(double)), "alloc");
   API_CUDA(j->real.ensure(nn * sizeof(double)), "alloc");
   API_CUDA(j->spec.ensure(nspec * 2 * sizeof(double)), "alloc");
-  API_CUDA(j->part.ensure((size_t)lcp::kReduceBlocks * 3 * sizeof(double)), "alloc");
+  API_CUDA(j->part.ensure((size_t)std::max<int64_t>({3 * lcp::red_tiles(nn), lcp::red_tiles(hs), 1}) * sizeof(double)),
+           "alloc");
   API_CUDA(j->scal.ensure(16 * sizeof(double)), "alloc");
   auto put = [&](DBuf& b, const double* src, bool& flag) -> cudaError_t {
     flag = src != nullptr;
@@ -953,21 +982,6 @@ lcp_status lcp_job_set_dm(lcp_ctx* ctx, lcp_job* job, const double* const* dm) {
   return LCP_OK;
 }
 
-__global__ void job_finish_kernel(const double* sc, double gridvol, int spinpol, double* out) {
-  // sc: [0..2] = (sum dRho*dVH, xc sum up, xc sum down), [3] = sum <D,H>
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const double eh1 = sc[0] * gridvol * 0.5;
-    const double x1 = sc[1] * gridvol;
-    const double x2 = spinpol == LCP_SPIN_OFF ? x1 : sc[2] * gridvol;
-    const double fs = spinpol == LCP_SPIN_OFF ? 2.0 : 1.0;
-    out[0] = eh1;
-    out[1] = x1;
-    out[2] = x2;
-    out[3] = sc[3];
-    out[4] = fs * sc[3] + eh1 + x1 + x2;
-  }
-}
-
 static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;
@@ -980,57 +994,47 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   cudaStream_t st = ctx->stream;
   const double* dm[4];
   double* rho[4];
-  const double* crho[4];
-  double* vp[4];
   const double* cvp[4];
   double* hk[4];
-  const double* chk[4];
   for (int c = 0; c < ns; ++c) {
     dm[c] = job->dm[c].as<double>();
     rho[c] = job->rho[c].as<double>();
-    crho[c] = rho[c];
-    vp[c] = job->vpot[c].as<double>();
-    cvp[c] = vp[c];
+    cvp[c] = job->vpot[c].as<double>();
     hk[c] = job->hks[c].as<double>();
-    chk[c] = hk[c];
   }
-  const double* ad = job->has_aden ? job->aden.as<double>() : nullptr;
-  const double* pc = job->has_pcc ? job->pcc.as<double>() : nullptr;
-  const double* na = job->has_vna ? job->vna.as<double>() : nullptr;
+  const lcp::GridCell gc = job_grid_cell(job);
+  const lcp::GridBatch one{};
   // 1. density
   mark(0);
   if ((s = density_device(ctx, job->orbs, ns, dm, rho, job->nn))) return s;
   mark(1);
   // 2. Poisson
-  API_CUDA(lcp::launch_poisson_prep(job->spinpol, job->nn, rho[0], ns > 1 ? rho[1] : nullptr, ad,
-                                    job->real.as<double>(), st),
-           "poisson_prep");
-  ctx->launches++;
+  API_CUDA(lcp::launch_poisson_prep_g(job->spinpol, gc, one, st), "poisson_prep");
   FftPlans* plans = nullptr;  // the executing context's plans (any context may run the job)
   if ((s = get_plans(ctx, u.ngrid, &plans))) return s;
-  if ((s = poisson_device(ctx, plans, u.ngrid, job->recvecs, job->real.as<double>(), job->spec.p,
-                          job->dvh.as<double>())))
-    return s;
+  if (cufftExecD2Z(plans->fwd, job->real.as<double>(), reinterpret_cast<cufftDoubleComplex*>(job->spec.p)) !=
+      CUFFT_SUCCESS)
+    return fail(LCP_EDEVICE, "cufftExecD2Z failed");
+  API_CUDA(lcp::launch_poisson_scale_g(gc, one, st), "poisson_scale");
+  if (cufftExecZ2D(plans->inv, reinterpret_cast<cufftDoubleComplex*>(job->spec.p), job->dvh.as<double>()) !=
+      CUFFT_SUCCESS)
+    return fail(LCP_EDEVICE, "cufftExecZ2D failed");
+  ctx->launches += 2;
   mark(2);
-  // 3. xc + potential, with the FP64 energy partial sums in the same pass
-  API_CUDA(lcp::launch_xc_vpot_energy(job->xc, job->spinpol, job->nn, ad, pc, crho, job->dvh.as<double>(), na, vp,
-                                      job->part.as<double>(), st),
-           "xc_vpot_energy");
+  // 3. xc + potential, with the FP64 energy tile partials in the same pass
+  API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, job->spinpol, gc, one, st), "xc_vpot_energy");
   ctx->launches++;
   mark(3);
-  // 4. FP64 energy terms: final reduction of the partial sums
-  API_CUDA(lcp::launch_finish_sums3(job->part.as<double>(), job->scal.as<double>(), st), "energy");
+  // 4. FP64 energy terms: the sums of the tile partials
+  API_CUDA(lcp::launch_grid_sums_g(gc, one, st), "energy");
   ctx->launches++;
   mark(4);
   // 5. grid matrix elements
   if ((s = hamiltonian_device(ctx, job->orbs, ns, cvp, hk, job->hsize))) return s;
   mark(5);
-  // 6. sum_s <D_s, H_s> and the job energy
-  API_CUDA(lcp::launch_dot_sum(ns, job->hsize, dm, chk, job->part.as<double>(), job->scal.as<double>() + 3, st), "dot");
+  // 6. sum_s <D_s, H_s> and the job energies
+  API_CUDA(lcp::launch_dot_energy_g(job->spinpol, ns, gc, one, one, st), "dot");
   ctx->launches += 2;
-  job_finish_kernel<<<1, 32, 0, st>>>(job->scal.as<double>(), u.gridvol, job->spinpol, job->scal.as<double>() + 8);
-  API_CUDA(cudaGetLastError(), "finish");
-  ctx->launches++;
   mark(6);
   return LCP_OK;
 }

@@ -140,3 +140,8 @@ lcp_status check_ctx(lcp_ctx* ctx);
 lcp_status check_pair(const lcp_ucell* ucell, const lcp_orbs* orbs);
 lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o);
 lcp_status device_status(lcp_ctx* ctx);
+lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const double* const* dm, double* const* rho,
+                          int64_t nn);
+lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const double* const* vpot,
+                              double* const* hks, int64_t hsize);
+lcp::GridCell job_grid_cell(lcp_job* job);

@@ -1,0 +1,444 @@
+// Batched SCF grid step: the device-resident jobs of many cells stepped
+// together.  Every stage runs once for all cells:
+//
+//   - the split-D blocks, their per-cell fixed-point scales, the density and
+//     the grid matrix elements each take one launch over the bricks (or
+//     blocks) of every cell.  The tensor-core kernels are persistent, with one
+//     CTA per SM walking a brick list that mixes the cells, heaviest bricks
+//     first;
+//   - Poisson runs batched cuFFT plans, one per grid shape, over contiguous
+//     per-shape buffers;
+//   - the pointwise grid kernels and the FP64 reductions run over tiles of
+//     every cell.  Their partition per cell is the one of a single-cell step,
+//     so a cell's energy sums are the same bits as when its job steps alone.
+//
+// The whole step is recorded once as a CUDA graph and replayed.
+// Everything a step touches is allocated at creation; results land in the
+// jobs' own buffers (density, potential, H, energies).
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#include "lcp_api_state.h"
+
+namespace {
+
+struct ShapeGroup {
+  int32_t ng[3];
+  std::vector<int> cells;  // batch cell indices, in order
+  int64_t nn = 0, nspec = 0;
+  cufftHandle fwd = 0, inv = 0;
+  DBuf real, spec;  // count * nn doubles, count * nspec complex
+};
+
+int64_t spec_len(const int32_t* ng) { return (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1); }
+
+}  // namespace
+
+struct lcp_batch {
+  int device = 0;
+  int32_t spinpol = LCP_SPIN_OFF, xc = LCP_XC_LDA, nspin = 1, ncells = 0;
+  std::vector<lcp_job*> jobs;
+  std::vector<std::unique_ptr<ShapeGroup>> groups;
+  DBuf fft_work;
+  // device tables (per spin channel where the pointers differ)
+  DBuf tc_cells[2], brick_cell, brick_local;
+  DBuf dsym_cells[2], dsym_start, abs_start;
+  DBuf red_cells[2], red_start;
+  DBuf grid_cells, pt_start, sp_start, h_start;
+  // workspaces
+  DBuf dsym, dscale, dtmp, vw, vscale, hscratch, status;
+  int64_t nbricks = 0, dsym_blocks = 0, abs_total = 0, nsb = 0, pt_tiles = 0, sp_tiles = 0, h_tiles = 0;
+  int64_t kernels_per_step = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~lcp_batch() {
+    cudaSetDevice(device);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& g : groups) {
+      if (g->fwd) cufftDestroy(g->fwd);
+      if (g->inv) cufftDestroy(g->inv);
+    }
+  }
+};
+
+namespace {
+
+template <class T>
+cudaError_t upload_pod(DBuf& b, const std::vector<T>& v) {
+  cudaError_t e = b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+std::vector<int64_t> prefix(const std::vector<int64_t>& counts) {
+  std::vector<int64_t> s(counts.size() + 1, 0);
+  for (size_t i = 0; i < counts.size(); ++i) s[i + 1] = s[i] + counts[i];
+  return s;
+}
+
+// Records one batched step on stream st.
+lcp_status record_step(lcp_batch* b, cudaStream_t st) {
+  const int32_t nc = b->ncells;
+  lcp::TcBatch tb{};
+  tb.nbricks = b->nbricks;
+  tb.ncells = nc;
+  tb.brick_cell = b->brick_cell.as<int32_t>();
+  tb.brick_local = b->brick_local.as<int64_t>();
+  const lcp::TcCell none{};
+  lcp::GridBatch pts{nc, b->grid_cells.as<lcp::GridCell>(), b->pt_start.as<int64_t>(), b->pt_tiles};
+  lcp::GridBatch sps{nc, b->grid_cells.as<lcp::GridCell>(), b->sp_start.as<int64_t>(), b->sp_tiles};
+  lcp::GridBatch hts{nc, b->grid_cells.as<lcp::GridCell>(), b->h_start.as<int64_t>(), b->h_tiles};
+  lcp::GridBatch per{nc, b->grid_cells.as<lcp::GridCell>(), nullptr, nc};
+  const lcp::GridCell gnone{};
+  int* status = b->status.as<int>();
+  // 1. density, per channel: D scales, split D blocks, the tensor-core pass
+  for (int c = 0; c < b->nspin; ++c) {
+    const lcp::DsymCell* dc = b->dsym_cells[c].as<lcp::DsymCell>();
+    // |D + D'^T| <= 2 max|D|: the fixed-point scale of the symmetrised blocks
+    API_CUDA(lcp::launch_absmax_scale_batch(nc, dc, b->abs_start.as<int64_t>(), b->abs_total, 2.0,
+                                            b->dtmp.as<unsigned long long>(), b->dscale.as<double>(), st),
+             "batch dm scale");
+    API_CUDA(lcp::launch_dsym_batch(nc, dc, b->dsym_start.as<int64_t>(), b->dsym_blocks, st), "batch dsym");
+    tb.cells = b->tc_cells[c].as<lcp::TcCell>();
+    API_CUDA(lcp::launch_density_tc_batch(none, tb, status, st), "batch density");
+  }
+  // 2. Poisson: sources, forward transforms per shape, 4 pi / G^2, inverse
+  API_CUDA(lcp::launch_poisson_prep_g(b->spinpol, gnone, pts, st), "batch poisson prep");
+  for (auto& g : b->groups)
+    if (cufftSetStream(g->fwd, st) != CUFFT_SUCCESS || cufftSetStream(g->inv, st) != CUFFT_SUCCESS)
+      return fail(LCP_EDEVICE, "cufftSetStream failed");
+  for (auto& g : b->groups)
+    if (cufftExecD2Z(g->fwd, g->real.as<double>(), g->spec.as<cufftDoubleComplex>()) != CUFFT_SUCCESS)
+      return fail(LCP_EDEVICE, "cufftExecD2Z (batched) failed");
+  API_CUDA(lcp::launch_poisson_scale_g(gnone, sps, st), "batch poisson scale");
+  for (auto& g : b->groups)
+    if (cufftExecZ2D(g->inv, g->spec.as<cufftDoubleComplex>(), g->real.as<double>()) != CUFFT_SUCCESS)
+      return fail(LCP_EDEVICE, "cufftExecZ2D (batched) failed");
+  // 3./4. xc + potential + energy partials, then the per-cell sums
+  API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, st), "batch xc");
+  API_CUDA(lcp::launch_grid_sums_g(gnone, per, st), "batch sums");
+  // 5. grid matrix elements, per channel
+  for (int c = 0; c < b->nspin; ++c) {
+    tb.cells = b->tc_cells[c].as<lcp::TcCell>();
+    API_CUDA(lcp::launch_hamiltonian_tc_batch(none, tb, status, st), "batch hamiltonian");
+    API_CUDA(lcp::launch_h_reduce_batch(nc, b->red_cells[c].as<lcp::RedCell>(), b->red_start.as<int64_t>(), b->nsb,
+                                        st),
+             "batch h_reduce");
+  }
+  // 6. <D,H> and the energies of every cell
+  API_CUDA(lcp::launch_dot_energy_g(b->spinpol, b->nspin, gnone, hts, per, st), "batch dot");
+  return LCP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, lcp_batch** out) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!jobs || !out || njobs <= 0) return fail(LCP_EINVAL, "lcp_batch_create: NULL argument or no jobs");
+  *out = nullptr;
+  if (ctx->precision != LCP_PREC_BF16X3)
+    return fail(LCP_ENOTSUP, "the batched step runs the split-BF16 contractions (precision bf16x3)");
+  std::unique_ptr<lcp_batch> b(new lcp_batch());
+  b->device = ctx->device;
+  b->ncells = njobs;
+  for (int k = 0; k < njobs; ++k) {
+    lcp_job* j = jobs[k];
+    if (!j) return fail(LCP_EINVAL, "lcp_batch_create: NULL job");
+    if (k == 0) {
+      b->spinpol = j->spinpol;
+      b->xc = j->xc;
+      b->nspin = j->nspin;
+    } else if (j->spinpol != b->spinpol || j->xc != b->xc) {
+      return fail(LCP_EINVAL, "lcp_batch_create: every job of a batch has the same SpinPol and xc");
+    }
+    if (j->orbs->device != ctx->device) return fail(LCP_EINVAL, "lcp_batch_create: job on another device");
+    for (int q = 0; q < k; ++q)
+      if (jobs[q] == j) return fail(LCP_EINVAL, "lcp_batch_create: a job appears twice");
+    if ((s = ensure_bricks(ctx, const_cast<lcp_orbs*>(j->orbs)))) return s;
+    b->jobs.push_back(j);
+  }
+  const int nc = njobs, ns = b->nspin;
+
+  // shape groups (first appearance order) and each cell's place in its group
+  std::map<std::tuple<int, int, int>, int> gidx;
+  std::vector<int> cell_group(nc), cell_slot(nc);
+  for (int k = 0; k < nc; ++k) {
+    const int32_t* ng = b->jobs[k]->ucell->u.ngrid;
+    auto key = std::make_tuple((int)ng[0], (int)ng[1], (int)ng[2]);
+    auto it = gidx.find(key);
+    if (it == gidx.end()) {
+      it = gidx.emplace(key, (int)b->groups.size()).first;
+      std::unique_ptr<ShapeGroup> g(new ShapeGroup());
+      for (int d = 0; d < 3; ++d) g->ng[d] = ng[d];
+      g->nn = (int64_t)ng[0] * ng[1] * ng[2];
+      g->nspec = spec_len(ng);
+      b->groups.push_back(std::move(g));
+    }
+    ShapeGroup& g = *b->groups[it->second];
+    cell_group[k] = it->second;
+    cell_slot[k] = (int)g.cells.size();
+    g.cells.push_back(k);
+  }
+  // batched plans sharing one work area (the groups run one after another)
+  size_t work = 0;
+  for (auto& gp : b->groups) {
+    ShapeGroup& g = *gp;
+    long long n[3] = {g.ng[0], g.ng[1], g.ng[2]};
+    const long long cnt = (long long)g.cells.size();
+    size_t w1 = 0, w2 = 0;
+    if (cufftCreate(&g.fwd) != CUFFT_SUCCESS || cufftCreate(&g.inv) != CUFFT_SUCCESS)
+      return fail(LCP_EDEVICE, "cufftCreate failed");
+    cufftSetAutoAllocation(g.fwd, 0);
+    cufftSetAutoAllocation(g.inv, 0);
+    if (cufftMakePlanMany64(g.fwd, 3, n, nullptr, 1, g.nn, nullptr, 1, g.nspec, CUFFT_D2Z, cnt, &w1) !=
+            CUFFT_SUCCESS ||
+        cufftMakePlanMany64(g.inv, 3, n, nullptr, 1, g.nspec, nullptr, 1, g.nn, CUFFT_Z2D, cnt, &w2) !=
+            CUFFT_SUCCESS)
+      return fail(LCP_EDEVICE, "batched cuFFT plan creation failed");
+    work = std::max(work, std::max(w1, w2));
+    API_CUDA(g.real.ensure((size_t)cnt * g.nn * sizeof(double)), "batch grid alloc");
+    API_CUDA(g.spec.ensure((size_t)cnt * g.nspec * 2 * sizeof(double)), "batch spectrum alloc");
+  }
+  API_CUDA(b->fft_work.ensure(std::max<size_t>(work, 16)), "cuFFT work area");
+  for (auto& g : b->groups) {
+    cufftSetWorkArea(g->fwd, b->fft_work.p);
+    cufftSetWorkArea(g->inv, b->fft_work.p);
+  }
+
+  // per-cell sizes and workspace offsets
+  std::vector<int64_t> nbr(nc), nsub1(nc), nslot(nc), nsbc(nc), ptt(nc), spt(nc), ht(nc), abt(nc);
+  for (int k = 0; k < nc; ++k) {
+    const lcp_job* j = b->jobs[k];
+    const lcp::Bricks& br = j->orbs->bricks;
+    nbr[k] = br.nbricks;
+    nsub1[k] = br.nsub + 1;
+    nslot[k] = br.slot_base.back();
+    nsbc[k] = (int64_t)br.sb_fold.size();
+    ptt[k] = lcp::red_tiles(j->nn);
+    spt[k] = lcp::red_tiles(spec_len(j->ucell->u.ngrid));
+    ht[k] = lcp::red_tiles(j->hsize);
+    abt[k] = lcp::abs_tiles(j->hsize);
+  }
+  const auto brick_off = prefix(nbr), dsym_off = prefix(nsub1), slot_off = prefix(nslot), sb_off = prefix(nsbc);
+  const auto pt_off = prefix(ptt), sp_off = prefix(spt), h_off = prefix(ht), ab_off = prefix(abt);
+  b->nbricks = brick_off[nc];
+  b->dsym_blocks = dsym_off[nc];
+  b->nsb = sb_off[nc];
+  b->pt_tiles = pt_off[nc];
+  b->sp_tiles = sp_off[nc];
+  b->h_tiles = h_off[nc];
+  b->abs_total = ab_off[nc];
+  API_CUDA(b->dsym.ensure((size_t)std::max<int64_t>(b->dsym_blocks, 1) * 768 * 2), "batch dsym alloc");
+  API_CUDA(b->dscale.ensure((size_t)nc * 2 * sizeof(double)), "alloc");
+  API_CUDA(b->dtmp.ensure((size_t)nc * sizeof(unsigned long long)), "alloc");
+  API_CUDA(b->vw.ensure((size_t)std::max<int64_t>(b->nbricks, 1) * 128 * sizeof(float2)), "batch V weight alloc");
+  API_CUDA(b->vscale.ensure((size_t)std::max<int64_t>(b->nbricks, 1) * sizeof(float)), "alloc");
+  API_CUDA(b->hscratch.ensure((size_t)std::max<int64_t>(slot_off[nc], 1) * 256 * sizeof(float)), "batch H scratch");
+  API_CUDA(b->status.ensure(sizeof(int)), "alloc");
+  API_CUDA(cudaMemset(b->status.p, 0, sizeof(int)), "memset");
+
+  // brick list: every cell's bricks, heaviest first (the persistent CTAs take
+  // bricks k, k + grid, ... so a descending order balances them); the order
+  // changes no result -- each brick writes its own points and partial blocks
+  {
+    std::vector<std::tuple<int64_t, int32_t, int64_t>> order;  // (-cost, cell, brick)
+    order.reserve(b->nbricks);
+    for (int k = 0; k < nc; ++k) {
+      const lcp::Bricks& br = b->jobs[k]->orbs->bricks;
+      for (int64_t hb = 0; hb < br.nbricks; ++hb) {
+        const int64_t m = br.img_off[hb + 1] - br.img_off[hb];
+        order.emplace_back(-(m * m + 8 * m), (int32_t)k, hb);
+      }
+    }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const auto& x, const auto& y) { return std::get<0>(x) < std::get<0>(y); });
+    std::vector<int32_t> bc(order.size());
+    std::vector<int64_t> bl(order.size());
+    for (size_t i = 0; i < order.size(); ++i) {
+      bc[i] = std::get<1>(order[i]);
+      bl[i] = std::get<2>(order[i]);
+    }
+    API_CUDA(upload_pod(b->brick_cell, bc), "upload");
+    API_CUDA(upload_pod(b->brick_local, bl), "upload");
+  }
+
+  // per-cell tables
+  std::vector<lcp::GridCell> gcs(nc);
+  for (int k = 0; k < nc; ++k) {
+    lcp_job* j = b->jobs[k];
+    ShapeGroup& g = *b->groups[cell_group[k]];
+    lcp::GridCell c = job_grid_cell(j);
+    c.real = g.real.as<double>() + (int64_t)cell_slot[k] * g.nn;
+    c.spec = g.spec.as<double>() + (int64_t)cell_slot[k] * g.nspec * 2;
+    c.dvh = c.real;  // the inverse transform writes back over the source
+    gcs[k] = c;
+  }
+  API_CUDA(upload_pod(b->grid_cells, gcs), "upload");
+  for (int ch = 0; ch < ns; ++ch) {
+    std::vector<lcp::TcCell> tcs(nc);
+    std::vector<lcp::DsymCell> dcs(nc);
+    std::vector<lcp::RedCell> rcs(nc);
+    for (int k = 0; k < nc; ++k) {
+      lcp_job* j = b->jobs[k];
+      const lcp_orbs* o = j->orbs;
+      const lcp::UCell& u = j->ucell->u;
+      __nv_bfloat16* dsym = b->dsym.as<__nv_bfloat16>() + dsym_off[k] * 768;
+      const double* dscale = b->dscale.as<double>() + 2 * k;
+      float* scratch = b->hscratch.as<float>() + slot_off[k] * 256;
+      lcp::TcCell t = lcp::tc_cell_of(o->bgeom, o->b_tab.as<__nv_bfloat16>());
+      t.phi_scale = o->phi_scale;
+      t.dsym = dsym;
+      t.zero_pair = o->bricks.nsub;
+      t.dscale = dscale;
+      t.rho = j->rho[ch].as<double>();
+      t.tab_slot = o->b_tabslot.as<int32_t>();
+      t.slot_base = o->b_slotbase.as<int64_t>();
+      t.vpot = j->vpot[ch].as<double>();
+      t.vw = b->vw.as<float2>() + brick_off[k] * 128;
+      t.vscale = b->vscale.as<float>() + brick_off[k];
+      t.scratch = scratch;
+      tcs[k] = t;
+      lcp::DsymCell d{};
+      d.nsub = o->bricks.nsub;
+      d.hsize = j->hsize;
+      d.scale = dscale;
+      d.sub_pair = o->b_subpair.as<int32_t>();
+      d.sub_chunks = o->b_subchunks.as<int32_t>();
+      d.pair_atom = o->o_atom.as<int32_t>();
+      d.pair_jatom = o->o_jatom.as<int32_t>();
+      d.boff = o->o_boff.as<int64_t>();
+      d.partner = o->o_partner.as<int32_t>();
+      d.numorbs = o->geom.numorbs;
+      d.dm = j->dm[ch].as<double>();
+      d.out = dsym;
+      dcs[k] = d;
+      lcp::RedCell r{};
+      r.red_off = o->b_redoff.as<int64_t>();
+      r.red_slot = o->b_redslot.as<int64_t>();
+      r.sb_fold = o->b_sbfold.as<int32_t>();
+      r.sb_chunks = o->b_sbchunks.as<int32_t>();
+      r.scratch = scratch;
+      r.pr = o->pairs;
+      r.numorbs = o->geom.numorbs;
+      r.dv = u.gridvol;
+      r.H = j->hks[ch].as<double>();
+      rcs[k] = r;
+    }
+    API_CUDA(upload_pod(b->tc_cells[ch], tcs), "upload");
+    API_CUDA(upload_pod(b->dsym_cells[ch], dcs), "upload");
+    API_CUDA(upload_pod(b->red_cells[ch], rcs), "upload");
+  }
+  API_CUDA(upload_pod(b->dsym_start, dsym_off), "upload");
+  API_CUDA(upload_pod(b->abs_start, ab_off), "upload");
+  API_CUDA(upload_pod(b->red_start, sb_off), "upload");
+  API_CUDA(upload_pod(b->pt_start, pt_off), "upload");
+  API_CUDA(upload_pod(b->sp_start, sp_off), "upload");
+  API_CUDA(upload_pod(b->h_start, h_off), "upload");
+  // our kernels per step: per channel absmax + pow2 + dsym + density + vweight
+  // + H + reduce; once prep, scale, xc, sums, dot, dot-finish
+  b->kernels_per_step = 7 * ns + 6;
+  API_CUDA(cudaDeviceSynchronize(), "batch create");
+  *out = b.release();
+  return LCP_OK;
+}
+
+void lcp_batch_destroy(lcp_batch* batch) { delete batch; }
+
+lcp_status lcp_batch_step(lcp_ctx* ctx, lcp_batch* b, int32_t mode) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!b) return fail(LCP_EINVAL, "NULL batch");
+  if (ctx->device != b->device) return fail(LCP_EINVAL, "batch on another device");
+  if (mode == LCP_BATCH_EAGER) {
+    if ((s = record_step(b, ctx->stream))) return s;
+  } else if (mode == LCP_BATCH_GRAPH) {
+    if (!b->exec) {
+      // the first step runs eagerly (module loading, kernel attributes), the
+      // capture of the second becomes the graph that every later step replays
+      if ((s = record_step(b, ctx->stream))) return s;
+      API_CUDA(cudaStreamSynchronize(ctx->stream), "batch warm-up");
+      cudaStream_t cap = nullptr;
+      API_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
+      cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        lcp_status rs = record_step(b, cap);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(cap, &g);
+        if (rs != LCP_OK) {
+          if (g) cudaGraphDestroy(g);
+          cudaStreamDestroy(cap);
+          return rs;
+        }
+        if (e == cudaSuccess) {
+          b->graph = g;
+          e = cudaGraphInstantiate(&b->exec, g, 0);
+        }
+      }
+      cudaStreamDestroy(cap);
+      API_CUDA(e, "batch graph capture");
+      ctx->launches += b->kernels_per_step;
+      return LCP_OK;
+    }
+    API_CUDA(cudaGraphLaunch(b->exec, ctx->stream), "cudaGraphLaunch");
+  } else {
+    return fail(LCP_EINVAL, "lcp_batch_step: mode is LCP_BATCH_GRAPH or LCP_BATCH_EAGER");
+  }
+  ctx->launches += b->kernels_per_step;
+  return LCP_OK;
+}
+
+lcp_status lcp_batch_check_status(lcp_ctx* ctx, lcp_batch* b) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!b) return fail(LCP_EINVAL, "NULL batch");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "batch status");
+  int st = 0;
+  API_CUDA(cudaMemcpy(&st, b->status.p, sizeof(int), cudaMemcpyDeviceToHost), "status");
+  if (st) {
+    cudaMemset(b->status.p, 0, sizeof(int));
+    return fail(st, "a device wait timed out (batched tensor-core step)");
+  }
+  return LCP_OK;
+}
+
+lcp_status lcp_batch_energies(lcp_ctx* ctx, lcp_batch* b, double* out) {
+  lcp_status s = lcp_batch_check_status(ctx, b);
+  if (s) return s;
+  if (!out) return fail(LCP_EINVAL, "NULL argument");
+  for (int k = 0; k < b->ncells; ++k)
+    API_CUDA(cudaMemcpyAsync(out + 5 * k, b->jobs[k]->scal.as<double>() + 8, 5 * sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "batch energies");
+  return LCP_OK;
+}
+
+lcp_status lcp_batch_info(const lcp_batch* b, int64_t* out8) {
+  if (!b || !out8) return fail(LCP_EINVAL, "NULL argument");
+  out8[0] = b->ncells;
+  out8[1] = (int64_t)b->groups.size();
+  out8[2] = b->nbricks;
+  out8[3] = b->kernels_per_step;
+  int64_t bytes = 0;
+  for (const DBuf* d : {&b->fft_work, &b->dsym, &b->vw, &b->vscale, &b->hscratch})
+    bytes += (int64_t)d->bytes;
+  for (auto& g : b->groups) bytes += (int64_t)(g->real.bytes + g->spec.bytes);
+  out8[4] = bytes;
+  out8[5] = b->exec ? 1 : 0;
+  out8[6] = b->nsb;
+  out8[7] = b->dsym_blocks;
+  return LCP_OK;
+}
+
+}  // extern "C"

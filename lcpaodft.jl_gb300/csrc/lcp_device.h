@@ -91,19 +91,55 @@ cudaError_t launch_xc_vpot(int xc, int spinpol, int64_t nn, const double* pcc,
                            double* const* vxc_out, double* const* vpot_out, cudaStream_t st);
 cudaError_t launch_vpot(int spinpol, int64_t nn, const double* dvh, const double* const* vxc,
                         const double* vna, double* const* vpot, cudaStream_t st);
-// Deterministic FP64 energy sums: out[0] = sum dRho*dVH, out[1..2] = xc sums.
+// Deterministic FP64 energy sums: out[0] = sum dRho*dVH, out[1..2] = xc sums;
+// partials: 3 * red_tiles(nn) doubles.
 cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* aden,
                                const double* pcc, const double* const* rho, const double* dvh,
                                double* partials, double* out, cudaStream_t st);
-// Job step: xc + potential + the energy partial sums in one pass (partials as
-// launch_energy_sums), then the final reduction of the three sums into out.
-cudaError_t launch_xc_vpot_energy(int xc, int spinpol, int64_t nn, const double* aden, const double* pcc,
-                                  const double* const* rho, const double* dvh, const double* vna,
-                                  double* const* vpot_out, double* partials, cudaStream_t st);
-cudaError_t launch_finish_sums3(const double* partials, double* out, cudaStream_t st);
-cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const double* const* b,
-                           double* partials, double* out, cudaStream_t st);
-constexpr int kReduceBlocks = 1024;
+// Reductions run over tiles of kRedTile elements, one block per tile.
+constexpr int kRedTile = 1024;
+__host__ __device__ inline int64_t red_tiles(int64_t n) { return n > 0 ? (n + kRedTile - 1) / kRedTile : 0; }
+
+// One cell of a grid-step pass: its grid, the fields it reads and writes, and
+// its reduction partials.  A launch covers one cell (passed by value) or a
+// batch of cells (a device table); a cell's results are the same bits either
+// way.
+struct GridCell {
+  int32_t ng[3];
+  int64_t nn, hsize;
+  double rv[9];          // reciprocal vectors (rows), 2*pi*inv(Latvecs')
+  double gridvol;
+  const double* aden;    // atomic density or nullptr
+  const double* pcc;     // partial core correction or nullptr
+  const double* vna;     // neutral-atom potential or nullptr
+  const double* rho[2];
+  double* real;          // Poisson source (nn)
+  void* spec;            // its half spectrum (ng0 * ng1 * (ng2/2+1) complex)
+  const double* dvh;     // Hartree potential (nn)
+  double* vpot[2];
+  const double* dm[2];
+  const double* hks[2];
+  double* part;          // tile partials: 3 * red_tiles(nn) and red_tiles(hsize) doubles
+  double* sums;          // [0..2] grid sums, [3] sum <D,H>, [8..12] the step's energies
+};
+// cells == nullptr: the single cell passed by value.  Otherwise block g of a
+// tiled launch belongs to the cell c with start[c] <= g < start[c+1], and a
+// per-cell launch has one block per cell.
+struct GridBatch {
+  int32_t ncells;
+  const GridCell* cells;
+  const int64_t* start;
+  int64_t nblocks;
+};
+cudaError_t launch_poisson_prep_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
+cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaStream_t st);
+// xc + potential + the energy-term tile partials in one pass (tiles of nn)
+cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
+// per cell: sums[0..2] from the energy partials
+cudaError_t launch_grid_sums_g(const GridCell& c0, const GridBatch& b, cudaStream_t st);
+// <D,H> tile partials (tiles of hsize), then per cell sums[3] and the energies
+cudaError_t launch_dot_energy_g(int spinpol, int nspin, const GridCell& c0, const GridBatch& tiles,
+                                const GridBatch& cells, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
 // Device copy of the brick tiling (see struct Bricks in lcp_internal.h).
 struct TcBrickGeom {
@@ -131,6 +167,7 @@ struct TcCell {
   double phi_scale;            // S_phi of the tables
   const __nv_bfloat16* dsym;   // density: split D blocks, zero block at zero_pair
   int64_t zero_pair;
+  const double* dscale;        // density: [S_D, 1/S_D] of the cell's D
   double* rho;                 // density output (one spin channel)
   const double* vpot;          // matrix elements: V (one channel)
   float2* vw;                  // [nbricks * 128] per-brick V weights (workspace)
@@ -150,7 +187,8 @@ TcCell tc_cell_of(const TcBrickGeom& bg, const __nv_bfloat16* tab);
 // Batched split D blocks: cell c's sub-pairs (and its zero block) at
 // start[c] .. start[c+1] of the launch's blocks.
 struct DsymCell {
-  int64_t nsub;
+  int64_t nsub, hsize;
+  const double* scale;  // [S_D, 1/S_D] of the cell
   const int32_t* sub_pair;
   const int32_t* sub_chunks;
   const int32_t* pair_atom;
@@ -162,7 +200,12 @@ struct DsymCell {
   __nv_bfloat16* out;
 };
 cudaError_t launch_dsym_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_blocks,
-                              const double* scale, cudaStream_t st);
+                              cudaStream_t st);
+// Per-cell fixed-point scale of D: scale[2c] = power of two >= factor * max|D_c|,
+// scale[2c+1] its inverse; start over abs_tiles(hsize) tiles per cell; tmp: ncells words.
+int64_t abs_tiles(int64_t n);
+cudaError_t launch_absmax_scale_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_tiles,
+                                      double factor, unsigned long long* tmp, double* scale, cudaStream_t st);
 // Batched partial-block reduction: cell c's H sub-blocks at start[c] .. start[c+1].
 struct RedCell {
   const int64_t* red_off;
@@ -177,8 +220,7 @@ struct RedCell {
 };
 cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, int64_t total,
                                   cudaStream_t st);
-cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, const double* dscale, int* status,
-                                    cudaStream_t st);
+cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,
                                 cudaStream_t st);

@@ -212,6 +212,13 @@ __global__ void vpot_kernel(VpotArgs a) {
 }
 
 // ------------------------------------------------------------ deterministic reductions
+//
+// Every reduction runs over fixed tiles of kRedTile points (or matrix
+// entries): one block per tile, thread t summing the tile's elements t,
+// t + 256, ... in order, then a fixed tree over the block; one block per cell
+// then sums the cell's tile partials the same way.  The partition depends only
+// on the cell's own sizes, so a cell's sums are the same bits whether it runs
+// alone or in a batch of cells.
 
 constexpr int kRedThreads = 256;
 
@@ -229,6 +236,36 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* out)
     for (int c = 0; c < NV; ++c) out[c] = sh[c][0];
 }
 
+// Cell and cell-local block of block g of a grid launch.
+__device__ __forceinline__ const GridCell& grid_cell(const GridCell& c0, const GridBatch& b, int64_t g, int64_t& lb) {
+  if (!b.cells) {
+    lb = g;
+    return c0;
+  }
+  int lo = 0, hi = b.ncells;  // cell with start[lo] <= g < start[lo+1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (b.start[mid] <= g) lo = mid;
+    else hi = mid;
+  }
+  lb = g - b.start[lo];
+  return b.cells[lo];
+}
+
+// Calc_EH1 (src/Energy.jl:655-666) and Calc_EXC1 (src/Energy.jl:669-700, with
+// Calc_Vxc_Grid switch 0 of src/XC/XC_Func.jl:164-189) terms of one point;
+// e is the xc energy density at the point's density.
+__device__ __forceinline__ void energy_terms(int xc, int spinpol, double r0, double r1, double ad, double pc,
+                                             double dvh, double e, double (&acc)[3]) {
+  const double drho = spinpol == LCP_SPIN_OFF ? 2 * (r0 - ad) : r0 + r1 - 2 * ad;
+  acc[0] += drho * dvh;
+  const double temp = ad + pc;
+  double eat, vat;
+  lda_ca(2 * temp, eat, vat);
+  acc[1] += (r0 + pc) * e - temp * eat;
+  if (xc != LCP_XC_LDA) acc[2] += (r1 + pc) * e - temp * eat;
+}
+
 struct EnergyArgs {
   int xc, spinpol;
   int64_t nn;
@@ -236,105 +273,165 @@ struct EnergyArgs {
   const double* pcc;
   const double* rho[2];
   const double* dvh;
-  double* partials;  // [kReduceBlocks][3]
+  double* partials;  // [red_tiles(nn)][3]
 };
 
-// Per-block partial sums of Calc_EH1 (src/Energy.jl:655-666) and Calc_EXC1
-// (src/Energy.jl:669-700, with Calc_Vxc_Grid switch 0 of src/XC/XC_Func.jl:164-189).
+// Per-tile partial sums of the energy terms (one block per tile).
 __global__ void __launch_bounds__(kRedThreads) energy_partials_kernel(EnergyArgs a) {
   double v[3] = {0, 0, 0};
-  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < a.nn; x += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t x0 = (int64_t)blockIdx.x * kRedTile, x1 = min(a.nn, x0 + kRedTile);
+  for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
     const double ad = a.aden ? a.aden[x] : 0.0;
     const double pc = a.pcc ? a.pcc[x] : 0.0;
-    const double drho = a.spinpol == LCP_SPIN_OFF ? 2 * (a.rho[0][x] - ad) : a.rho[0][x] + a.rho[1][x] - 2 * ad;
-    if (a.dvh) v[0] += drho * a.dvh[x];
-    const double temp = ad + pc;
-    double ea, va;
-    lda_ca(2 * temp, ea, va);
+    const double r0 = a.rho[0][x];
+    double e, vv, r1 = 0.0;
     if (a.xc == LCP_XC_LDA) {
-      double e, vv;
-      lda_ca(2 * (a.rho[0][x] + pc), e, vv);
-      v[1] += (a.rho[0][x] + pc) * e - temp * ea;
+      lda_ca(2 * (r0 + pc), e, vv);
     } else {
-      double e, vu, vd;
-      lsda_ca(a.rho[0][x] + pc, a.rho[1][x] + pc, e, vu, vd);
-      v[1] += (a.rho[0][x] + pc) * e - temp * ea;
-      v[2] += (a.rho[1][x] + pc) * e - temp * ea;
+      double vd;
+      r1 = a.rho[1][x];
+      lsda_ca(r0 + pc, r1 + pc, e, vv, vd);
     }
+    energy_terms(a.xc, a.spinpol, r0, r1, ad, pc, a.dvh ? a.dvh[x] : 0.0, e, v);
   }
   block_reduce_store<3>(v, a.partials + (size_t)blockIdx.x * 3);
 }
 
-// The job step's fused pass: Set_XC_Grid! + Set_Vpot_Grid! (as
-// xc_vpot_kernel) and the Calc_EH1 / Calc_EXC1 partial sums (as
-// energy_partials_kernel), evaluating the xc functional once per point.  The
-// partial sums run over the same points in the same order as
-// energy_partials_kernel, so the energies are bit-identical to it.
-__global__ void __launch_bounds__(kRedThreads) xc_vpot_energy_kernel(XcArgs a, EnergyArgs ea) {
-  double acc[3] = {0, 0, 0};
-  const int nv = a.spinpol == LCP_SPIN_OFF ? 1 : (a.spinpol == LCP_SPIN_ON ? 2 : 4);
-  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < a.nn; x += (int64_t)gridDim.x * blockDim.x) {
-    const double pc = a.pcc ? a.pcc[x] : 0.0;
-    const double r0 = a.rho[0][x];
-    double v[4] = {0, 0, 0, 0};
-    double e;
-    double r1 = 0.0;
-    if (a.xc == LCP_XC_LDA) {
-      lda_ca(2 * (r0 + pc), e, v[0]);
-    } else {
-      r1 = a.rho[1][x];
-      lsda_ca(r0 + pc, r1 + pc, e, v[0], v[1]);
-      if (a.spinpol == LCP_SPIN_NC) {
-        const double th = a.rho[2][x], ph = a.rho[3][x];
-        const double t0 = 0.5 * (v[0] + v[1]), t1 = 0.5 * (v[0] - v[1]);
-        v[3] = -t1 * sin(th) * sin(ph);
-        v[2] = t1 * sin(th) * cos(ph);
-        v[1] = t0 - t1 * cos(th);
-        v[0] = t0 + t1 * cos(th);
-      }
-    }
-    for (int c = 0; c < nv; ++c)
-      if (a.vxc[c]) a.vxc[c][x] = v[c];
-    const double dvh = a.dvh[x];
-    if (a.vpot[0]) {
-      const double na = a.vna ? a.vna[x] : 0.0;
-      for (int c = 0; c < nv; ++c) a.vpot[c][x] = c < 2 ? dvh + v[c] + na : v[c];
-    }
-    const double ad = ea.aden ? ea.aden[x] : 0.0;
-    const double drho = a.spinpol == LCP_SPIN_OFF ? 2 * (r0 - ad) : r0 + r1 - 2 * ad;
-    acc[0] += drho * dvh;
-    const double temp = ad + pc;
-    double eat, vat;
-    lda_ca(2 * temp, eat, vat);
-    acc[1] += (r0 + pc) * e - temp * eat;
-    if (a.xc != LCP_XC_LDA) acc[2] += (r1 + pc) * e - temp * eat;
-  }
-  block_reduce_store<3>(acc, ea.partials + (size_t)blockIdx.x * 3);
-}
-
 template <int NV>
-__global__ void __launch_bounds__(kRedThreads) finish_sums_kernel(const double* __restrict__ partials, int nblocks,
+__global__ void __launch_bounds__(kRedThreads) finish_sums_kernel(const double* __restrict__ partials, int64_t nblocks,
                                                                   double* out) {
   double v[NV];
   for (int c = 0; c < NV; ++c) v[c] = 0.0;
-  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-    for (int c = 0; c < NV; ++c) v[c] += partials[(size_t)b * NV + c];
+  for (int64_t b = threadIdx.x; b < nblocks; b += blockDim.x)
+    for (int c = 0; c < NV; ++c) v[c] += partials[b * NV + c];
   block_reduce_store<NV>(v, out);
 }
 
-struct DotArgs {
-  int nvec;
-  int64_t n;
-  const double* a[4];
-  const double* b[4];
-  double* partials;
+struct GridArgs {
+  GridCell cell0;
+  GridBatch batch;
+  int xc, spinpol, nspin;
 };
-__global__ void __launch_bounds__(kRedThreads) dot_partials_kernel(DotArgs d) {
+
+// Poisson source 2rho - 2rho_a / rho_up + rho_down - 2rho_a (as
+// poisson_prep_kernel), one tile of one cell per block.
+__global__ void __launch_bounds__(kRedThreads) poisson_prep_g_kernel(const __grid_constant__ GridArgs a) {
+  int64_t t;
+  const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
+  const int64_t x0 = t * kRedTile, x1 = min(c.nn, x0 + kRedTile);
+  const double* r0 = c.rho[0];
+  const double* r1 = c.rho[1];
+  const double* ad = c.aden;
+  for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
+    const double aa = ad ? ad[x] : 0.0;
+    c.real[x] = a.spinpol == LCP_SPIN_OFF ? 2 * r0[x] - 2 * aa : r0[x] + r1[x] - 2 * aa;
+  }
+}
+
+// 4*pi/|G|^2 scaling of the half spectrum (as poisson_scale_kernel), one
+// tile of one cell per block.
+__global__ void __launch_bounds__(kRedThreads) poisson_scale_g_kernel(const __grid_constant__ GridArgs a) {
+  int64_t t;
+  const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
+  const int ng[3] = {c.ng[0], c.ng[1], c.ng[2]};
+  double rv[9];
+  for (int d = 0; d < 9; ++d) rv[d] = c.rv[d];
+  const double inv_nn = 1.0 / ((double)ng[0] * ng[1] * ng[2]);
+  const int N1 = ng[0], N2 = ng[1], N3 = ng[2], H3 = N3 / 2 + 1;
+  const int64_t total = (int64_t)N1 * N2 * H3;
+  const int64_t x0 = t * kRedTile, x1 = min(total, x0 + kRedTile);
+  cuDoubleComplex* spec = reinterpret_cast<cuDoubleComplex*>(c.spec);
+  for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
+    const int k = (int)(x % H3);
+    const int64_t ij = x / H3;
+    const int j = (int)(ij % N2);
+    const int i = (int)(ij / N2);
+    double s;
+    if (i == 0 && j == 0 && k == 0) {
+      s = 0.0;
+    } else {
+      const int mi = (N1 - i) % N1, mj = (N2 - j) % N2, mk = (N3 - k) % N3;
+      s = 0.5 * (inv_g2_scale(i, j, k, ng, rv) + inv_g2_scale(mi, mj, mk, ng, rv)) * inv_nn;
+    }
+    const cuDoubleComplex v = spec[x];
+    spec[x] = make_cuDoubleComplex(v.x * s, v.y * s);
+  }
+}
+
+// The grid step's fused pass: Set_XC_Grid! + Set_Vpot_Grid! (as
+// xc_vpot_kernel) and the energy-term partial sums (as
+// energy_partials_kernel, over the same tiles in the same order, so the sums
+// are the same bits), evaluating the xc functional once per point.
+__global__ void __launch_bounds__(kRedThreads) xc_vpot_energy_g_kernel(const __grid_constant__ GridArgs a) {
+  int64_t t;
+  const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
+  const int64_t x0 = t * kRedTile, x1 = min(c.nn, x0 + kRedTile);
+  double acc[3] = {0, 0, 0};
+  const int nv = a.spinpol == LCP_SPIN_OFF ? 1 : 2;
+  for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
+    const double pc = c.pcc ? c.pcc[x] : 0.0;
+    const double r0 = c.rho[0][x];
+    double v[2] = {0, 0};
+    double e, r1 = 0.0;
+    if (a.xc == LCP_XC_LDA) {
+      lda_ca(2 * (r0 + pc), e, v[0]);
+    } else {
+      r1 = c.rho[1][x];
+      lsda_ca(r0 + pc, r1 + pc, e, v[0], v[1]);
+    }
+    const double dvh = c.dvh[x];
+    const double na = c.vna ? c.vna[x] : 0.0;
+    for (int s = 0; s < nv; ++s) c.vpot[s][x] = dvh + v[s] + na;
+    energy_terms(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, dvh, e, acc);
+  }
+  block_reduce_store<3>(acc, c.part + t * 3);
+}
+
+// Sums of each cell's energy tile partials: sums[0..2] (one block per cell).
+__global__ void __launch_bounds__(kRedThreads) grid_sums_g_kernel(const __grid_constant__ GridArgs a) {
+  const GridCell& c = a.batch.cells ? a.batch.cells[blockIdx.x] : a.cell0;
+  const int64_t nt = red_tiles(c.nn);
+  double v[3] = {0, 0, 0};
+  for (int64_t b = threadIdx.x; b < nt; b += blockDim.x)
+    for (int k = 0; k < 3; ++k) v[k] += c.part[b * 3 + k];
+  block_reduce_store<3>(v, c.sums);
+}
+
+// Tile partials of sum_s <D_s, H_s> (one block per tile of matrix entries).
+__global__ void __launch_bounds__(kRedThreads) dot_g_kernel(const __grid_constant__ GridArgs a) {
+  int64_t t;
+  const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
+  const int64_t x0 = t * kRedTile, x1 = min(c.hsize, x0 + kRedTile);
   double v[1] = {0.0};
-  for (int c = 0; c < d.nvec; ++c)
-    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < d.n; x += (int64_t)gridDim.x * blockDim.x)
-      v[0] += d.a[c][x] * d.b[c][x];
-  block_reduce_store<1>(v, d.partials + blockIdx.x);
+  for (int s = 0; s < a.nspin; ++s) {
+    const double* dm = c.dm[s];
+    const double* hk = c.hks[s];
+    for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) v[0] += dm[x] * hk[x];
+  }
+  block_reduce_store<1>(v, c.part + t);
+}
+
+// sums[3] = sum_s <D_s, H_s> and the step's energies (one block per cell):
+// sums[8..12] = E_H1, E_xc1 (up), E_xc1 (down), sum <D,H>,
+// f_s sum <D,H> + E_H1 + E_xc1, with f_s = 2 for SpinPol "off".
+__global__ void __launch_bounds__(kRedThreads) dot_energy_g_kernel(const __grid_constant__ GridArgs a) {
+  const GridCell& c = a.batch.cells ? a.batch.cells[blockIdx.x] : a.cell0;
+  const int64_t nt = red_tiles(c.hsize);
+  double v[1] = {0.0};
+  for (int64_t b = threadIdx.x; b < nt; b += blockDim.x) v[0] += c.part[b];
+  block_reduce_store<1>(v, c.sums + 3);
+  if (threadIdx.x == 0) {
+    double* sc = c.sums;
+    const double eh1 = sc[0] * c.gridvol * 0.5;
+    const double x1 = sc[1] * c.gridvol;
+    const double x2 = a.spinpol == LCP_SPIN_OFF ? x1 : sc[2] * c.gridvol;
+    const double fs = a.spinpol == LCP_SPIN_OFF ? 2.0 : 1.0;
+    sc[8] = eh1;
+    sc[9] = x1;
+    sc[10] = x2;
+    sc[11] = sc[3];
+    sc[12] = fs * sc[3] + eh1 + x1 + x2;
+  }
 }
 
 // FP64 FMA throughput probe: 8 independent dependency chains per thread.
@@ -422,52 +519,63 @@ cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* ad
   a.rho[1] = spinpol == LCP_SPIN_OFF ? nullptr : rho[1];
   a.dvh = dvh;
   a.partials = partials;
-  energy_partials_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(a);
+  const int64_t nt = red_tiles(nn);
+  energy_partials_kernel<<<(unsigned)nt, kRedThreads, 0, st>>>(a);
   LCP_CUDA_TRY(cudaGetLastError());
-  finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
+  finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, nt, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_xc_vpot_energy(int xc, int spinpol, int64_t nn, const double* aden, const double* pcc,
-                                  const double* const* rho, const double* dvh, const double* vna,
-                                  double* const* vpot_out, double* partials, cudaStream_t st) {
-  XcArgs a{};
+namespace {
+GridArgs grid_args(const GridCell& c0, const GridBatch& b, int xc, int spinpol, int nspin) {
+  GridArgs a;
+  a.cell0 = c0;
+  a.batch = b;
   a.xc = xc;
   a.spinpol = spinpol;
-  a.nn = nn;
-  a.pcc = pcc;
-  const int nr = spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4);
-  for (int c = 0; c < nr; ++c) {
-    a.rho[c] = rho[c];
-    a.vpot[c] = vpot_out[c];
-  }
-  a.dvh = dvh;
-  a.vna = vna;
-  EnergyArgs e{};
-  e.aden = aden;
-  e.partials = partials;
-  xc_vpot_energy_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(a, e);
+  a.nspin = nspin;
+  return a;
+}
+// blocks of a tiled launch: the batch's total, or the single cell's tiles
+unsigned tiled_blocks(const GridBatch& b, int64_t single) { return (unsigned)(b.cells ? b.nblocks : single); }
+unsigned cell_blocks(const GridBatch& b) { return (unsigned)(b.cells ? b.ncells : 1); }
+int64_t spec_size(const GridCell& c) { return (int64_t)c.ng[0] * c.ng[1] * (c.ng[2] / 2 + 1); }
+}  // namespace
+
+cudaError_t launch_poisson_prep_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st) {
+  const unsigned n = tiled_blocks(b, red_tiles(c0.nn));
+  if (n == 0) return cudaSuccess;
+  poisson_prep_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, 0, spinpol, 0));
   return cudaGetLastError();
 }
 
-cudaError_t launch_finish_sums3(const double* partials, double* out, cudaStream_t st) {
-  finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
+cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaStream_t st) {
+  const unsigned n = tiled_blocks(b, red_tiles(spec_size(c0)));
+  if (n == 0) return cudaSuccess;
+  poisson_scale_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, 0, 0, 0));
   return cudaGetLastError();
 }
 
-cudaError_t launch_dot_sum(int nvec, int64_t n, const double* const* a, const double* const* b, double* partials,
-                           double* out, cudaStream_t st) {
-  DotArgs d{};
-  d.nvec = nvec;
-  d.n = n;
-  for (int c = 0; c < nvec; ++c) {
-    d.a[c] = a[c];
-    d.b[c] = b[c];
+cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st) {
+  const unsigned n = tiled_blocks(b, red_tiles(c0.nn));
+  if (n == 0) return cudaSuccess;
+  xc_vpot_energy_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, xc, spinpol, 0));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_grid_sums_g(const GridCell& c0, const GridBatch& b, cudaStream_t st) {
+  grid_sums_g_kernel<<<cell_blocks(b), kRedThreads, 0, st>>>(grid_args(c0, b, 0, 0, 0));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dot_energy_g(int spinpol, int nspin, const GridCell& c0, const GridBatch& tiles,
+                                const GridBatch& cells, cudaStream_t st) {
+  const unsigned n = tiled_blocks(tiles, red_tiles(c0.hsize));
+  if (n > 0) {
+    dot_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, tiles, 0, spinpol, nspin));
+    LCP_CUDA_TRY(cudaGetLastError());
   }
-  d.partials = partials;
-  dot_partials_kernel<<<kReduceBlocks, kRedThreads, 0, st>>>(d);
-  LCP_CUDA_TRY(cudaGetLastError());
-  finish_sums_kernel<1><<<1, kRedThreads, 0, st>>>(partials, kReduceBlocks, out);
+  dot_energy_g_kernel<<<cell_blocks(cells), kRedThreads, 0, st>>>(grid_args(c0, cells, 0, spinpol, nspin));
   return cudaGetLastError();
 }
 

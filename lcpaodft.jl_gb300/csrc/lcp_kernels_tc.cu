@@ -212,6 +212,42 @@ __global__ void pow2_scale_kernel(const unsigned long long* mx, double factor, d
   }
 }
 
+// Batched: max |D| per cell over tiles of kAbsTile entries (block g: a tile
+// of the cell c with start[c] <= g < start[c+1]) into tmp[c].
+constexpr int kAbsTile = 4096;
+__global__ void absmax_batch_kernel(int32_t ncells, const DsymCell* __restrict__ cells,
+                                    const int64_t* __restrict__ start, unsigned long long* tmp) {
+  const int64_t g = blockIdx.x;
+  int lo = 0, hi = ncells;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (start[mid] <= g) lo = mid;
+    else hi = mid;
+  }
+  const DsymCell& c = cells[lo];
+  const int64_t x0 = (g - start[lo]) * kAbsTile, x1 = min(c.hsize, x0 + kAbsTile);
+  unsigned long long m = 0;
+  for (int64_t i = x0 + threadIdx.x; i < x1; i += blockDim.x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(c.dm[i]) & 0x7fffffffffffffffull;
+    m = b > m ? b : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(tmp + lo, m);
+}
+
+__global__ void pow2_scale_batch_kernel(int32_t ncells, const unsigned long long* __restrict__ mx, double factor,
+                                        double* scale) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncells) {
+    const double s = pow2_ceil(__longlong_as_double((long long)mx[c]) * factor);
+    scale[2 * c] = s;
+    scale[2 * c + 1] = 1.0 / s;
+  }
+}
+
 __global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t* __restrict__ phi_off,
                                    const int32_t* __restrict__ numorbs, const int64_t* __restrict__ sph_off,
                                    int natom, const int32_t* __restrict__ point_code, int64_t npoints,
@@ -293,8 +329,7 @@ __global__ void dsym_kernel(int64_t nsub, const int32_t* __restrict__ sub_pair, 
 // Batched: the split D blocks of several cells (each with its zero block),
 // cell c's entries at start[c] .. start[c+1] (in blocks) of the launch.
 __global__ void dsym_batch_kernel(int32_t ncells, const DsymCell* __restrict__ cells,
-                                  const int64_t* __restrict__ start, const double* __restrict__ scale) {
-  const double inv = scale[1];
+                                  const int64_t* __restrict__ start) {
   const int64_t total = start[ncells] * 256;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t g = e >> 8;
@@ -306,7 +341,7 @@ __global__ void dsym_batch_kernel(int32_t ncells, const DsymCell* __restrict__ c
     }
     const DsymCell& c = cells[lo];
     dsym_entry(g - start[lo], (int)(e & 255), c.nsub, c.sub_pair, c.sub_chunks, c.pair_atom, c.pair_jatom, c.boff,
-               c.partner, c.numorbs, c.dm, inv, c.out);
+               c.partner, c.numorbs, c.dm, c.scale[1], c.out);
   }
 }
 
@@ -363,7 +398,6 @@ __device__ __forceinline__ void smem_point_row(const uint8_t* blk, int p, float*
 struct TcDensArgs {
   TcCell cell0;          // the cell of a single-cell launch
   TcBatch batch;         // or the cells of a batch
-  const double* dscale;  // [S_D, 1/S_D], one scale for every cell of the launch
   int* status;
 };
 
@@ -592,7 +626,6 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
     // ------------------------------------------------------------ epilogue
     const uint32_t quarter = warp & 3;  // TMEM lanes [32 * quarter, 32 * quarter + 32)
     const int p = (int)quarter * 32 + lane;
-    const double dsc = args.dscale[0];
     uint32_t it = 0, win = 0, mpar = 0;  // mpar: phase bit of mdone_bar per stage
     for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
       int64_t hb;
@@ -632,7 +665,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
       if (abort_flag) break;
       if (p < cl.npts)
         cl.rho[brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid)] =
-            ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * dsc);
+            ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * cl.dscale[0]);
     }
   }
   tc::fence_before_sync();
@@ -1164,11 +1197,24 @@ cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* su
 }
 
 cudaError_t launch_dsym_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_blocks,
-                              const double* scale, cudaStream_t st) {
+                              cudaStream_t st) {
   const int64_t total = total_blocks * 256;
   if (total == 0) return cudaSuccess;
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
-  dsym_batch_kernel<<<blocks, 256, 0, st>>>(ncells, cells, start, scale);
+  dsym_batch_kernel<<<blocks, 256, 0, st>>>(ncells, cells, start);
+  return cudaGetLastError();
+}
+
+int64_t abs_tiles(int64_t n) { return (n + kAbsTile - 1) / kAbsTile; }
+
+cudaError_t launch_absmax_scale_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_tiles,
+                                      double factor, unsigned long long* tmp, double* scale, cudaStream_t st) {
+  LCP_CUDA_TRY(cudaMemsetAsync(tmp, 0, (size_t)ncells * sizeof(unsigned long long), st));
+  if (total_tiles > 0) {
+    absmax_batch_kernel<<<(unsigned)total_tiles, 256, 0, st>>>(ncells, cells, start, tmp);
+    LCP_CUDA_TRY(cudaGetLastError());
+  }
+  pow2_scale_batch_kernel<<<(ncells + 127) / 128, 128, 0, st>>>(ncells, tmp, factor, scale);
   return cudaGetLastError();
 }
 
@@ -1202,12 +1248,10 @@ static int tc_grid(const TcCell& cell0, const TcBatch& batch) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(n, sm_count()));
 }
 
-cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, const double* dscale, int* status,
-                                    cudaStream_t st) {
+cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st) {
   TcDensArgs a{};
   a.cell0 = cell0;
   a.batch = batch;
-  a.dscale = dscale;
   a.status = status;
   // 512 TMEM columns per CTA: the shared-memory ring (> half an SM) keeps one CTA per SM
   static_assert(kDSmem > 120 * 1024, "one CTA per SM");
@@ -1224,8 +1268,9 @@ cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, d
   c.phi_scale = phi_scale;
   c.dsym = dsym;
   c.zero_pair = zero_pair;
+  c.dscale = dscale;
   c.rho = rho;
-  return launch_density_tc_batch(c, TcBatch{}, dscale, status, st);
+  return launch_density_tc_batch(c, TcBatch{}, status, st);
 }
 
 cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st) {

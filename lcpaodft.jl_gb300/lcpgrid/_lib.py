@@ -101,6 +101,12 @@ _SIGS = {
     "lcp_server_submit": ([_vp, _i32, _ppd, ctypes.c_uint64], _i32),
     "lcp_server_poll": ([_vp, _i32, _i32, ctypes.POINTER(ctypes.c_uint64), _pd, _pd, ctypes.POINTER(_i32)], _i32),
     "lcp_server_stats": ([_vp, ctypes.POINTER(_i64)], _i32),
+    "lcp_batch_create": ([_vp, _i32, ctypes.POINTER(_vp), ctypes.POINTER(_vp)], _i32),
+    "lcp_batch_destroy": ([_vp], None),
+    "lcp_batch_step": ([_vp, _vp, _i32], _i32),
+    "lcp_batch_check_status": ([_vp, _vp], _i32),
+    "lcp_batch_energies": ([_vp, _vp, _pd], _i32),
+    "lcp_batch_info": ([_vp, ctypes.POINTER(_i64)], _i32),
     "lcp_job_get_density": ([_vp, _vp, _ppd], _i32),
     "lcp_job_get_hks": ([_vp, _vp, _ppd], _i32),
     "lcp_job_get_vpot": ([_vp, _vp, _ppd], _i32),

@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib
 from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 
-__all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Server",
+__all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Batch", "Server",
            "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "Solve_Poisson", "Solve_Poisson_xyz",
            "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
            "Calc_MatrixElements_dVH_Vxc_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
@@ -178,11 +178,11 @@ class UCell:
 
     def brick_info(self):
         """Grid-brick tiling of the tensor-core path."""
-        out = (ctypes.c_int64 * 12)()
+        out = (ctypes.c_int64 * 14)()
         check(lib.lcp_ucell_get_bricks(self._h, out))
         v = list(out)
         return {"bdim": v[0:3], "nbricks_axis": v[3:6], "points": v[6], "bricks": v[7], "blocks": v[8],
-                "max_images": v[9], "images": v[10], "paired": v[11]}
+                "max_images": v[9], "images": v[10], "paired": v[11], "h_slots": v[12], "sub_pairs": v[13]}
 
     def Recvecs(self):
         """2*pi*inv(Latvecs') (src/Mixing/DFT_Mixing.jl:91)."""
@@ -497,6 +497,58 @@ class GridStepJob:
             if getattr(self, "_h", None):
                 lib.lcp_job_destroy(self._h)
                 self._h = None
+        except Exception:
+            pass
+
+
+class Batch:
+    """Batched grid step over the device-resident jobs of many cells
+    (lcp_batch_*): one persistent tensor-core launch per contraction over the
+    bricks of every cell, batched FFTs per grid shape, tiled grid kernels over
+    all cells, replayed as one CUDA graph.  Results land in the jobs (read
+    them with job.energies() / job.hks() / job.density())."""
+
+    GRAPH, EAGER = 0, 1
+
+    def __init__(self, jobs):
+        self.jobs = list(jobs)  # the batch reads their buffers: keep them alive
+        if not self.jobs:
+            raise ValueError("a batch needs at least one job")
+        self.ctx = self.jobs[0].ctx
+        arr = (ctypes.c_void_p * len(self.jobs))(*[j._h.value for j in self.jobs])
+        h = ctypes.c_void_p()
+        check(lib.lcp_batch_create(self.ctx._h, len(self.jobs), arr, ctypes.byref(h)))
+        self._h = h
+
+    def step(self, graph=True):
+        check(lib.lcp_batch_step(self.ctx._h, self._h, self.GRAPH if graph else self.EAGER))
+
+    def check_status(self):
+        check(lib.lcp_batch_check_status(self.ctx._h, self._h))
+
+    def energies(self):
+        """[njobs, 5]: each job's energies (as GridStepJob.energies)."""
+        out = np.zeros(5 * len(self.jobs))
+        check(lib.lcp_batch_energies(self.ctx._h, self._h, dptr(out)))
+        return out.reshape(-1, 5)
+
+    def info(self):
+        """dict: cells, shape groups, bricks, kernels per step, workspace bytes,
+        graph captured, H sub-blocks, split-D blocks."""
+        out = (ctypes.c_int64 * 8)()
+        check(lib.lcp_batch_info(self._h, out))
+        keys = ("cells", "shape_groups", "bricks", "kernels_per_step", "workspace_bytes", "graph", "h_subblocks",
+                "dsym_blocks")
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib.lcp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

@@ -9,6 +9,12 @@
   smooth cutoff at 7 bohr) tabulated on a 1000-point log mesh, grid 96^3,
   PSD density matrix with trace 256, smooth V_na with |G| < 3 bohr^-1 and
   amplitude 0.5 Ha.
+* ``batch_pool``: the batching form -- independent cells of 2-64 atoms with
+  1-3 species (cutoffs from {6, 7, 8, 9} bohr, 4/9/13/18 orbitals),
+  cubic lattice constants of 4-12 A, random positions at least 3.5 bohr
+  apart, grids from Calc_Ngrid at 150 Ry (24^3-96^3).
+* ``serving_pool``: the serving form -- random Si-density cells of 2-216
+  atoms (log-uniform) with the 64-atom workload's species.
 
 Everything is generated from a seed with numpy; nothing is read from disk.
 """
@@ -192,5 +198,85 @@ def serving_pool(nstruct=24, seed=777, nmin=2, nmax=216):
         out.append({"name": "rand%d_%d" % (natom, k), "latvecs": lat, "gxyz": pos, "natom": natom,
                     "atom2spe": [1] * natom, "cut": [7.0] * natom, "ngrid": ngrid, "origin": [0.0, 0.0, 0.0],
                     "numorbs": [pao.Spe_Total_NumOrbs] * natom, "paos": [pao],
+                    "vna_seed": seed + 1000 + k, "dm_seed": seed + 2000 + k, "trace": 2.0 * natom})
+    return out
+
+
+def calc_ngrid(ecut, latvecs):
+    """Calc_Ngrid (src/utils/Calc_Ngrid.jl:1-76): per axis the 2^p 3^q 5^r 7^s
+    nearest in log to |det L| sqrt(Ecut) / (pi |a_j x a_k|)."""
+    L = np.asarray(latvecs, float)
+    temp = abs(np.linalg.det(L)) / math.pi * math.sqrt(ecut)
+    out = []
+    for d in range(3):
+        lgn = math.log(temp / np.linalg.norm(np.cross(L[(d + 1) % 3], L[(d + 2) % 3])))
+        best, bk = 1e10, 1
+        l2, l3, l5, l7 = (math.log(x) for x in (2, 3, 5, 7))
+        for p in range(int(math.ceil(lgn / l2)) + 1):
+            for q in range(int(math.ceil((lgn - p * l2) / l3)) + 1):
+                for r in range(int(math.ceil((lgn - p * l2 - q * l3) / l5)) + 1):
+                    for t in range(int(math.ceil((lgn - p * l2 - q * l3 - r * l5) / l7)) + 1):
+                        lg = p * l2 + q * l3 + r * l5 + t * l7
+                        if abs(lg - lgn) < best:
+                            best, bk = abs(lg - lgn), 2 ** p * 3 ** q * 5 ** r * 7 ** t
+        out.append(bk)
+    return tuple(out)
+
+
+BATCH_CUTOFFS = (6.0, 7.0, 8.0, 9.0)
+BATCH_BASES = {4: (1, 1, 0), 9: (1, 1, 1), 13: (2, 2, 1), 18: (2, 2, 2)}  # orbitals: (s, p, d) radial functions
+
+
+def _place(rng, natom, side, min_sep, tries=20000):
+    pos = []
+    for _ in range(natom):
+        for _try in range(tries):
+            x = rng.uniform(0, side, size=3)
+            if all(((x - y) - side * np.round((x - y) / side)) @ ((x - y) - side * np.round((x - y) / side))
+                   >= min_sep * min_sep for y in pos):
+                pos.append(x)
+                break
+        else:
+            return None
+    return np.array(pos)
+
+
+def batch_pool(ncells=256, seed=4242, nmin=2, nmax=64, min_sep=3.5, ecut=150.0, amax_ang=12.0):
+    """Cells of the batching form.  Per cell: natom ~ U{nmin..nmax}, 1-3
+    species each with a cutoff from BATCH_CUTOFFS and a basis from
+    BATCH_BASES (synthetic radial functions), atoms assigned species
+    uniformly; a cubic lattice constant ~ U[a0, amax_ang] A with a0 = max(4 A, the
+    side at which the spheres of radius min_sep/2 fill 20% of the cell),
+    random positions at least min_sep bohr apart (the box is redrawn larger
+    when placement fails); grid Calc_Ngrid(ecut); a PSD D with trace
+    2 * natom and a smooth V_na."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(ncells):
+        natom = int(rng.integers(nmin, nmax + 1))
+        nspe = int(rng.integers(1, 4))
+        species = []
+        for s_ in range(nspe):
+            rc = float(BATCH_CUTOFFS[rng.integers(len(BATCH_CUTOFFS))])
+            no = list(BATCH_BASES)[rng.integers(len(BATCH_BASES))]
+            nb = BATCH_BASES[no]
+            max_l = 2 if nb[2] else 1
+            species.append(synthetic_species(int(rng.integers(1 << 30)), max_l=max_l,
+                                             num_basis=nb[:max_l + 1], rc=rc))
+        a2s = [int(x) + 1 for x in rng.integers(0, nspe, size=natom)]
+        a0 = max(4.0 * ANG_TO_BOHR, (natom * (4.0 / 3.0) * math.pi * (min_sep / 2) ** 3 / 0.2) ** (1.0 / 3.0))
+        side = rng.uniform(a0, max(a0, amax_ang * ANG_TO_BOHR))
+        cell_rng = np.random.default_rng(int(rng.integers(1 << 30)))
+        while True:
+            pos = _place(cell_rng, natom, side, min_sep)
+            if pos is not None:
+                break
+            side *= 1.05
+        lat = np.eye(3) * side
+        ngrid = calc_ngrid(ecut, lat)
+        out.append({"name": "cell%d_%datoms_%dspe" % (k, natom, nspe), "latvecs": lat, "gxyz": pos,
+                    "natom": natom, "atom2spe": a2s, "cut": [species[s - 1].Spe_Atom_Cut1 for s in a2s],
+                    "ngrid": ngrid, "origin": [0.0, 0.0, 0.0],
+                    "numorbs": [species[s - 1].Spe_Total_NumOrbs for s in a2s], "paos": species,
                     "vna_seed": seed + 1000 + k, "dm_seed": seed + 2000 + k, "trace": 2.0 * natom})
     return out

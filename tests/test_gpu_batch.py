@@ -1,0 +1,126 @@
+"""Batched grid step (lcp_batch_*): many cells' device-resident jobs stepped
+together -- one tensor-core launch per contraction over every cell's bricks,
+batched FFTs per grid shape, tiled grid kernels over all cells, CUDA-graph
+replay.  Each cell's results must match its job stepped alone."""
+import numpy as np
+import pytest
+
+import lcpgrid as L
+
+pytestmark = pytest.mark.gpu
+
+
+def _cells(ctx, spin="off", n_pool=6, seed=91):
+    """Small cells of the batching form (1-3 species, cutoffs 6-9 bohr,
+    4/9/13/18 orbitals, grids from Calc_Ngrid at 150 Ry) plus two cells that
+    share a grid shape (batched FFT plan with two transforms)."""
+    from helpers import product_pao, si2_cell
+    from lcpgrid.workloads import batch_pool, psd_density_matrices, smooth_vna
+    cells = []
+    for c in batch_pool(n_pool, seed=seed, nmax=10, amax_ang=7.0):
+        u = L.UCell(2 if spin == "on" else 1, c["latvecs"], c["natom"], c["atom2spe"], c["gxyz"], c["cut"],
+                    c["ngrid"], c["origin"], Total_NumOrbs=c["numorbs"])
+        cells.append((u, L.Set_Orbitals_Grid(c["paos"], u, ctx)))
+    lat, pos, ng = si2_cell()
+    for scale in (1.0, 1.01):
+        u = L.UCell(2 if spin == "on" else 1, lat, 2, [1, 1], pos * scale, [7.0, 7.0], ng, [0, 0, 0],
+                    Total_NumOrbs=[13, 13])
+        cells.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx)))
+    jobs = []
+    nspin = 2 if spin == "on" else 1
+    for k, (u, orbs) in enumerate(cells):
+        vna = smooth_vna(u.Ngrid, u.Latvecs, 300 + k)
+        job = L.GridStepJob(u, orbs, spin, "LDA" if spin == "off" else "LSDA", None, None, vna)
+        dm = psd_density_matrices(u, 400 + k, nspin=nspin, trace=2.0 * u.Natom)
+        job.set_dm(dm)
+        jobs.append(job)
+    return jobs
+
+
+def _alone(jobs):
+    out = []
+    for job in jobs:
+        job.step()
+        out.append((job.energies(), [x.copy() for x in job.density()], [x.copy() for x in job.hks()]))
+    return out
+
+
+def _compare(jobs, ref, exact_density=True):
+    for job, (e, rho, hks) in zip(jobs, ref):
+        for a, b in zip(job.density(), rho):
+            if exact_density:
+                np.testing.assert_array_equal(a, b)  # same kernels, same per-cell D scale
+        for a, b in zip(job.hks(), hks):
+            # V differs from the single-cell step only by the batched FFT's rounding
+            np.testing.assert_allclose(a, b, rtol=0, atol=1e-12 * max(1.0, np.abs(b).max()))
+        np.testing.assert_allclose(job.energies(), e, rtol=1e-11, atol=1e-12)
+
+
+@pytest.mark.parametrize("spin", ["off", "on"])
+def test_batch_matches_alone(spin):
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, spin)
+    ref = _alone(jobs)
+    b = L.Batch(jobs)
+    info = b.info()
+    assert info["cells"] == len(jobs) and info["shape_groups"] < len(jobs)
+    b.step(graph=False)
+    b.check_status()
+    _compare(jobs, ref)
+    en = b.energies()
+    np.testing.assert_array_equal(en, np.array([j.energies() for j in jobs]))
+    b.close()
+
+
+def test_batch_graph_replay():
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, "off", n_pool=4, seed=17)
+    b = L.Batch(jobs)
+    b.step(graph=False)
+    eager = b.energies().copy()
+    h_eager = [j.hks()[0].copy() for j in jobs]
+    for _ in range(3):  # the first call runs and captures, the others replay
+        b.step(graph=True)
+        np.testing.assert_array_equal(b.energies(), eager)
+    assert b.info()["graph"] == 1
+    for j, h in zip(jobs, h_eager):
+        np.testing.assert_array_equal(j.hks()[0], h)
+    # a new D reaches the graph through the jobs' device buffers
+    from lcpgrid.workloads import psd_density_matrices
+    j0 = jobs[0]
+    j0.set_dm(psd_density_matrices(j0.ucell, 999, trace=2.0 * j0.ucell.Natom))
+    b.step(graph=True)
+    e_new = b.energies()
+    assert not np.array_equal(e_new[0], eager[0])
+    np.testing.assert_array_equal(e_new[1:], eager[1:])
+    j0.step()
+    np.testing.assert_allclose(j0.energies(), e_new[0], rtol=1e-11, atol=1e-12)
+    b.close()
+
+
+def test_batch_energy_within_tolerance_of_fp64():
+    """Split-BF16 batch vs the FP64 per-cell step: <= 1 uHa/atom."""
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, "off", n_pool=4, seed=23)
+    b = L.Batch(jobs)
+    b.step(graph=True)
+    e_batch = b.energies()
+    ctx.set_precision("fp64")
+    for k, job in enumerate(jobs):
+        job.step()
+        e64 = job.energies()
+        assert abs(e_batch[k, 4] - e64[4]) / job.ucell.Natom <= 1e-6, (k, e_batch[k], e64)
+    b.close()
+
+
+def test_batch_rejects_mixed_and_fp64():
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, "off", n_pool=1, seed=5)
+    jobs_on = _cells(ctx, "on", n_pool=1, seed=5)
+    with pytest.raises(L.LCPError):
+        L.Batch([jobs[0], jobs_on[0]])
+    with pytest.raises(L.LCPError):
+        L.Batch([jobs[0], jobs[0]])
+    ctx.set_precision("fp64")
+    with pytest.raises(L.LCPError):
+        L.Batch(jobs)
