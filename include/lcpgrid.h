@@ -117,6 +117,12 @@ lcp_status lcp_ucell_get_atv(const lcp_ucell* ucell, double* dst /* [ncell*3] */
  * brick, total images, image pairs that are neighbour pairs, partial H blocks
  * (FP32 scratch slots of 1 KB), split-D sub-pairs. */
 lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info);
+/* Brick shapes (sides <= 8, 16..128 points; the last brick of an axis is
+ * ragged where the side does not divide Ngrid) ranked by the predicted cost
+ * of the tensor-core passes: up to `max` shapes (3 ints each) and their costs
+ * (arbitrary units; may be NULL). */
+lcp_status lcp_brick_shape_candidates(const lcp_ucell* ucell, int32_t max, int32_t* shapes, double* cost,
+                                      int32_t* n);
 
 /* Calc_Ngrid(Ecut, Latvecs) -- src/utils/Calc_Ngrid.jl:1-76 */
 lcp_status lcp_calc_ngrid(double ecut, const double* latvecs, int32_t* ngrid_out);
@@ -265,6 +271,24 @@ lcp_status lcp_server_poll(lcp_server* srv, int32_t max, int32_t wait_ms, uint64
 /* out4 = submitted, completed, resident bytes, budget. */
 lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4);
 
+/* ---------------------------------------------------------------- brick tiling of the split-BF16 path */
+
+/* Sets the brick shape of the orbitals' split-BF16 tables (shape NULL or
+ * {0,0,0}: the predicted best); the tables are rebuilt on next use. */
+lcp_status lcp_orbs_set_brick_shape(lcp_ctx* ctx, lcp_orbs* orbs, const int32_t* shape);
+/* The brick shape in use (builds the tables if needed). */
+lcp_status lcp_orbs_get_brick_shape(lcp_ctx* ctx, lcp_orbs* orbs, int32_t* shape);
+/* Autotuner: times the density and matrix-element passes on the device for
+ * the `ncand` best predicted shapes (skipping shapes whose bricks see more
+ * atom images than the kernels hold) and keeps the fastest; shape_out[3] and
+ * ms_out (its time for one density + one H pass) may be NULL. */
+lcp_status lcp_orbs_autotune_bricks(lcp_ctx* ctx, lcp_orbs* orbs, int32_t ncand, int32_t* shape_out,
+                                    double* ms_out);
+/* Builds the split-BF16 tables, then frees the FP64 (and FP32, gradient)
+ * orbital tables: the orbitals then serve the split-BF16 path only (other
+ * precisions, downloads and shape changes return LCP_ESTATE). */
+lcp_status lcp_orbs_release_fp64(lcp_ctx* ctx, lcp_orbs* orbs);
+
 /* ---------------------------------------------------------------- batching */
 
 /* Batched grid step over the device-resident jobs of many cells (the
@@ -280,7 +304,11 @@ lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4);
  * set with lcp_job_set_dm. */
 typedef struct lcp_batch lcp_batch;
 enum { LCP_BATCH_GRAPH = 0, LCP_BATCH_EAGER = 1 };
-lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, lcp_batch** out);
+/* scratch_bytes: budget for the FP32 partial H blocks (1 KB each) that the
+ * matrix-element pass keeps until their reduction; the cells are taken in
+ * waves that fit it, one launch per wave (0: no limit, one wave). */
+lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes,
+                            lcp_batch** out);
 void lcp_batch_destroy(lcp_batch* batch);
 /* One step of every cell on the context's stream (asynchronous).
  * LCP_BATCH_GRAPH: replay the captured graph (the first call runs eagerly and
@@ -291,7 +319,7 @@ lcp_status lcp_batch_check_status(lcp_ctx* ctx, lcp_batch* batch);
 /* energies[5 * njobs]: each job's lcp_job_energies, in the batch's order. */
 lcp_status lcp_batch_energies(lcp_ctx* ctx, lcp_batch* batch, double* energies);
 /* out8 = cells, grid-shape groups, bricks, own kernels per step, workspace
- * bytes, graph captured (0/1), H sub-blocks, split-D blocks. */
+ * bytes, graph captured (0/1), H sub-blocks, waves of the H pass. */
 lcp_status lcp_batch_info(const lcp_batch* batch, int64_t* out8);
 
 /* Split-BF16 density that allocates no device memory.  No counterpart in the

@@ -4,6 +4,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -69,6 +70,7 @@ lcp_status check_pair(const lcp_ucell* ucell, const lcp_orbs* orbs) {
 
 lcp_status ensure_phi32(lcp_ctx* ctx, lcp_orbs* o) {
   if (o->phi32.p) return LCP_OK;
+  if (o->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released");
   API_CUDA(o->phi32.ensure(o->table_elems * sizeof(float)), "phi32 alloc");
   API_CUDA(lcp::launch_convert_f32(o->phi.as<double>(), o->phi32.as<float>(), o->table_elems, ctx->stream),
            "convert_f32");
@@ -80,13 +82,15 @@ lcp_status ensure_phi32(lcp_ctx* ctx, lcp_orbs* o) {
 // tensor-core path, built once per tabulation.
 lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   if (o->bricks_ready) return LCP_OK;
+  if (o->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released");
   const lcp::UCell& u = o->ucell->u;
   lcp::Bricks& b = o->bricks;
-  std::string err = lcp::build_bricks(u, b);
+  std::string err = lcp::build_bricks(u, b, o->brick_shape[0] > 0 ? o->brick_shape : nullptr);
   if (!err.empty()) return fail(LCP_EINVAL, err);
-  if (b.max_images > 64)
+  if (b.max_images > lcp::kMaxBrickImages)
     return fail(LCP_ENOTSUP, "a grid brick is touched by " + std::to_string(b.max_images) +
-                                 " atom images (16-orbital chunks); the tensor-core path supports 64");
+                                 " atom images (16-orbital chunks); the tensor-core path supports " +
+                                 std::to_string(lcp::kMaxBrickImages));
   cudaStream_t st = ctx->stream;
   API_CUDA(upload(o->b_code, b.point_code, st), "upload");
   API_CUDA(upload(o->b_imgoff, b.img_off, st), "upload");
@@ -137,6 +141,22 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   return LCP_OK;
 }
 
+namespace {
+void drop_bricks(lcp_orbs* o) {
+  o->bricks_ready = false;
+  o->bricks = lcp::Bricks();
+  for (DBuf* d : {&o->b_code, &o->b_imgoff, &o->b_imgblk, &o->b_taboff, &o->b_tabpair, &o->b_tab, &o->b_tabslot,
+                  &o->b_slotbase, &o->b_redoff, &o->b_redslot, &o->b_subpair, &o->b_subchunks, &o->b_sbfold,
+                  &o->b_sbchunks})
+    d->release();
+}
+
+__global__ void fill_kernel(double* x, int64_t n, double v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+}  // namespace
+
 lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, const double* const* dm,
                              double* const* rho) {
   lcp_orbs* o = const_cast<lcp_orbs*>(orbs_c);
@@ -170,6 +190,7 @@ lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const d
                           int64_t nn) {
   int prec = ctx->precision;
   if (prec == LCP_PREC_BF16X3) return density_tc_device(ctx, orbs, nspin, dm, rho);
+  if (orbs->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released (split-BF16 only)");
   for (int s = 0; s < nspin; ++s) API_CUDA(cudaMemsetAsync(rho[s], 0, nn * sizeof(double), ctx->stream), "memset");
   if (prec == LCP_PREC_FP32) {
     lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
@@ -224,6 +245,7 @@ lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const
                               double* const* hks, int64_t hsize) {
   int prec = ctx->precision;
   if (prec == LCP_PREC_BF16X3) return hamiltonian_tc_device(ctx, orbs, nch, vpot, hks);
+  if (orbs->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released (split-BF16 only)");
   for (int c = 0; c < nch; ++c) API_CUDA(cudaMemsetAsync(hks[c], 0, hsize * sizeof(double), ctx->stream), "memset");
   if (prec == LCP_PREC_FP32) {
     lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
@@ -377,6 +399,20 @@ lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info) {
   info[11] = paired;
   info[12] = b.slot_base.empty() ? 0 : b.slot_base.back();
   info[13] = b.nsub;
+  return LCP_OK;
+}
+
+lcp_status lcp_brick_shape_candidates(const lcp_ucell* ucell, int32_t max, int32_t* shapes, double* cost,
+                                      int32_t* n) {
+  if (!ucell || !shapes || !n || max < 0) return fail(LCP_EINVAL, "NULL argument");
+  std::vector<double> c;
+  auto cand = lcp::brick_shape_candidates(ucell->u, &c);
+  const int k = (int)std::min<size_t>(cand.size(), (size_t)max);
+  for (int i = 0; i < k; ++i) {
+    for (int d = 0; d < 3; ++d) shapes[3 * i + d] = cand[i][d];
+    if (cost) cost[i] = c[i];
+  }
+  *n = k;
   return LCP_OK;
 }
 
@@ -628,6 +664,116 @@ void lcp_orbs_destroy(lcp_orbs* orbs) {
   delete orbs;
 }
 
+
+lcp_status lcp_orbs_set_brick_shape(lcp_ctx* ctx, lcp_orbs* orbs, const int32_t* shape) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!orbs) return fail(LCP_EINVAL, "NULL orbs");
+  int32_t sh[3] = {0, 0, 0};
+  if (shape && shape[0] > 0) {
+    const int32_t* ng = orbs->ucell->u.ngrid;
+    for (int d = 0; d < 3; ++d) {
+      if (shape[d] < 1 || shape[d] > 8 || shape[d] > ng[d]) return fail(LCP_EINVAL, "brick sides are 1..min(8, Ngrid)");
+      sh[d] = shape[d];
+    }
+    if (sh[0] * sh[1] * sh[2] > 128) return fail(LCP_EINVAL, "a brick holds at most 128 points");
+  }
+  if (orbs->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "set brick shape");
+  std::memcpy(orbs->brick_shape, sh, sizeof(sh));
+  drop_bricks(orbs);
+  return LCP_OK;
+}
+
+lcp_status lcp_orbs_get_brick_shape(lcp_ctx* ctx, lcp_orbs* orbs, int32_t* shape) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!orbs || !shape) return fail(LCP_EINVAL, "NULL argument");
+  if ((s = ensure_bricks(ctx, orbs))) return s;
+  for (int d = 0; d < 3; ++d) shape[d] = orbs->bricks.bdim[d];
+  return LCP_OK;
+}
+
+lcp_status lcp_orbs_release_fp64(lcp_ctx* ctx, lcp_orbs* orbs) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!orbs) return fail(LCP_EINVAL, "NULL orbs");
+  if ((s = ensure_bricks(ctx, orbs))) return s;
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "release");
+  for (DBuf* d : {&orbs->phi, &orbs->dphi[0], &orbs->dphi[1], &orbs->dphi[2], &orbs->phi32}) d->release();
+  orbs->phi_released = true;
+  return LCP_OK;
+}
+
+lcp_status lcp_orbs_autotune_bricks(lcp_ctx* ctx, lcp_orbs* orbs, int32_t ncand, int32_t* shape_out,
+                                    double* ms_out) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!orbs || ncand < 1) return fail(LCP_EINVAL, "lcp_orbs_autotune_bricks: NULL orbs or ncand < 1");
+  if (orbs->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released");
+  const lcp::UCell& u = orbs->ucell->u;
+  auto cand = lcp::brick_shape_candidates(u, nullptr);
+  // D = V = 1: the passes' work does not depend on the values
+  DBuf dm, vp, rho, hk;
+  API_CUDA(dm.ensure(u.total_hsize * sizeof(double)), "alloc");
+  API_CUDA(hk.ensure(u.total_hsize * sizeof(double)), "alloc");
+  API_CUDA(vp.ensure(u.nn() * sizeof(double)), "alloc");
+  API_CUDA(rho.ensure(u.nn() * sizeof(double)), "alloc");
+  fill_kernel<<<1024, 256, 0, ctx->stream>>>(dm.as<double>(), u.total_hsize, 1.0);
+  fill_kernel<<<1024, 256, 0, ctx->stream>>>(vp.as<double>(), u.nn(), 1.0);
+  API_CUDA(cudaGetLastError(), "fill");
+  const double* cdm[1] = {dm.as<double>()};
+  double* prho[1] = {rho.as<double>()};
+  const double* cvp[1] = {vp.as<double>()};
+  double* phk[1] = {hk.as<double>()};
+  cudaEvent_t e0, e1;
+  API_CUDA(cudaEventCreate(&e0), "event");
+  API_CUDA(cudaEventCreate(&e1), "event");
+  double best_ms = 1e30;
+  std::array<int32_t, 3> best{0, 0, 0};
+  int tried = 0;
+  for (size_t i = 0; i < cand.size() && tried < ncand && s == LCP_OK; ++i) {
+    std::memcpy(orbs->brick_shape, cand[i].data(), sizeof(int32_t) * 3);
+    drop_bricks(orbs);
+    lcp_status bs = ensure_bricks(ctx, orbs);
+    if (bs == LCP_ENOTSUP) continue;  // too many images per brick for this shape
+    if ((s = bs)) break;
+    ++tried;
+    double ms = 1e30;
+    for (int rep = 0; rep < 4 && s == LCP_OK; ++rep) {  // the first run warms up
+      cudaEventRecord(e0, ctx->stream);
+      if ((s = density_tc_device(ctx, orbs, 1, cdm, prho))) break;
+      if ((s = hamiltonian_tc_device(ctx, orbs, 1, cvp, phk))) break;
+      cudaEventRecord(e1, ctx->stream);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) {
+        s = cuda_fail(e, "autotune");
+        break;
+      }
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0) ms = std::min(ms, (double)t);
+    }
+    if (s == LCP_OK && (s = device_status(ctx)) == LCP_OK && ms < best_ms) {
+      best_ms = ms;
+      best = cand[i];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s) return s;
+  if (tried == 0) return fail(LCP_ENOTSUP, "no brick shape keeps the atom images per brick within the limit");
+  if (std::memcmp(orbs->bricks.bdim, best.data(), sizeof(int32_t) * 3) != 0 || !orbs->bricks_ready) {
+    std::memcpy(orbs->brick_shape, best.data(), sizeof(int32_t) * 3);
+    drop_bricks(orbs);
+    if ((s = ensure_bricks(ctx, orbs))) return s;
+  }
+  if (shape_out)
+    for (int d = 0; d < 3; ++d) shape_out[d] = best[d];
+  if (ms_out) *ms_out = best_ms;
+  return LCP_OK;
+}
+
 lcp_status lcp_orbs_download(lcp_ctx* ctx, const lcp_orbs* orbs, int32_t component, int32_t atom, double* dst,
                              int64_t count) {
   lcp_status s = check_ctx(ctx);
@@ -641,6 +787,7 @@ lcp_status lcp_orbs_download(lcp_ctx* ctx, const lcp_orbs* orbs, int32_t compone
   if (count != n) return fail(LCP_EINVAL, "count must be GridN*NumOrbs = " + std::to_string(n));
   int64_t off = 0;
   for (int a = 0; a < atom; ++a) off += (u.sphere_off[a + 1] - u.sphere_off[a]) * (int64_t)u.numorbs[a];
+  if (orbs->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released");
   const DBuf& b = component == 0 ? orbs->phi : orbs->dphi[component - 1];
   API_CUDA(cudaMemcpyAsync(dst, b.as<double>() + off, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
            "download");

@@ -49,6 +49,11 @@ struct DBuf {
     if (e == cudaSuccess) bytes = n;
     return e;
   }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
   template <class T>
   T* as() const {
     return reinterpret_cast<T*>(p);
@@ -111,6 +116,8 @@ struct lcp_orbs {
   int64_t table_elems = 0;
   // brick tiling and split-BF16 tables of the tensor-core path (built on first use)
   bool bricks_ready = false;
+  int32_t brick_shape[3] = {0, 0, 0};  // requested brick shape, {0,0,0}: the predicted best
+  bool phi_released = false;           // FP64/FP32 tables freed (split-BF16 tables only)
   lcp::Bricks bricks;
   lcp::TcBrickGeom bgeom{};
   DBuf b_code, b_imgoff, b_imgblk, b_taboff, b_tabpair, b_tab, b_tabslot, b_slotbase, b_redoff, b_redslot;

@@ -12,6 +12,11 @@
 //     every cell.  Their partition per cell is the one of a single-cell step,
 //     so a cell's energy sums are the same bits as when its job steps alone.
 //
+// The matrix-element pass keeps one FP32 partial block per (brick, image
+// pair) until its reduction; under a byte budget for those blocks the cells
+// are taken in waves (consecutive cells whose blocks fit), one persistent
+// launch and one reduction per wave over a shared scratch area.
+//
 // The whole step is recorded once as a CUDA graph and replayed.
 // Everything a step touches is allocated at creation; results land in the
 // jobs' own buffers (density, potential, H, energies).
@@ -39,6 +44,13 @@ struct ShapeGroup {
 
 int64_t spec_len(const int32_t* ng) { return (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1); }
 
+// Cells [c0, c1) of the matrix-element pass that share the scratch area.
+struct Wave {
+  int c0 = 0, c1 = 0;
+  int64_t nbricks = 0, brick_off = 0;  // its brick list in hbrick_*
+  int64_t nsb = 0;                     // H sub-blocks of its cells
+};
+
 }  // namespace
 
 struct lcp_batch {
@@ -49,8 +61,10 @@ struct lcp_batch {
   DBuf fft_work;
   // device tables (per spin channel where the pointers differ)
   DBuf tc_cells[2], brick_cell, brick_local;
+  std::vector<Wave> waves;
+  DBuf hbrick_cell, hbrick_local, wred_start;  // per-wave brick lists and reduction starts
   DBuf dsym_cells[2], dsym_start, abs_start;
-  DBuf red_cells[2], red_start;
+  DBuf red_cells[2];
   DBuf grid_cells, pt_start, sp_start, h_start;
   // workspaces
   DBuf dsym, dscale, dtmp, vw, vscale, hscratch, status;
@@ -93,6 +107,7 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
   tb.brick_cell = b->brick_cell.as<int32_t>();
   tb.brick_local = b->brick_local.as<int64_t>();
   const lcp::TcCell none{};
+  const int64_t* wstart = b->wred_start.as<int64_t>();
   lcp::GridBatch pts{nc, b->grid_cells.as<lcp::GridCell>(), b->pt_start.as<int64_t>(), b->pt_tiles};
   lcp::GridBatch sps{nc, b->grid_cells.as<lcp::GridCell>(), b->sp_start.as<int64_t>(), b->sp_tiles};
   lcp::GridBatch hts{nc, b->grid_cells.as<lcp::GridCell>(), b->h_start.as<int64_t>(), b->h_tiles};
@@ -125,14 +140,21 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
   // 3./4. xc + potential + energy partials, then the per-cell sums
   API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, st), "batch xc");
   API_CUDA(lcp::launch_grid_sums_g(gnone, per, st), "batch sums");
-  // 5. grid matrix elements, per channel
-  for (int c = 0; c < b->nspin; ++c) {
-    tb.cells = b->tc_cells[c].as<lcp::TcCell>();
-    API_CUDA(lcp::launch_hamiltonian_tc_batch(none, tb, status, st), "batch hamiltonian");
-    API_CUDA(lcp::launch_h_reduce_batch(nc, b->red_cells[c].as<lcp::RedCell>(), b->red_start.as<int64_t>(), b->nsb,
-                                        st),
-             "batch h_reduce");
-  }
+  // 5. grid matrix elements, per channel and wave
+  for (int c = 0; c < b->nspin; ++c)
+    for (size_t w = 0; w < b->waves.size(); ++w) {
+      const Wave& wv = b->waves[w];
+      lcp::TcBatch hb{};
+      hb.nbricks = wv.nbricks;
+      hb.ncells = nc;
+      hb.cells = b->tc_cells[c].as<lcp::TcCell>();
+      hb.brick_cell = b->hbrick_cell.as<int32_t>() + wv.brick_off;
+      hb.brick_local = b->hbrick_local.as<int64_t>() + wv.brick_off;
+      API_CUDA(lcp::launch_hamiltonian_tc_batch(none, hb, status, st), "batch hamiltonian");
+      API_CUDA(lcp::launch_h_reduce_batch(wv.c1 - wv.c0, b->red_cells[c].as<lcp::RedCell>() + wv.c0,
+                                          wstart + wv.c0 + (int64_t)w, wv.nsb, st),
+               "batch h_reduce");
+    }
   // 6. <D,H> and the energies of every cell
   API_CUDA(lcp::launch_dot_energy_g(b->spinpol, b->nspin, gnone, hts, per, st), "batch dot");
   return LCP_OK;
@@ -142,10 +164,12 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
 
 extern "C" {
 
-lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, lcp_batch** out) {
+lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes,
+                            lcp_batch** out) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;
-  if (!jobs || !out || njobs <= 0) return fail(LCP_EINVAL, "lcp_batch_create: NULL argument or no jobs");
+  if (!jobs || !out || njobs <= 0 || scratch_bytes < 0)
+    return fail(LCP_EINVAL, "lcp_batch_create: NULL argument, no jobs or a negative budget");
   *out = nullptr;
   if (ctx->precision != LCP_PREC_BF16X3)
     return fail(LCP_ENOTSUP, "the batched step runs the split-BF16 contractions (precision bf16x3)");
@@ -230,7 +254,7 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, l
     ht[k] = lcp::red_tiles(j->hsize);
     abt[k] = lcp::abs_tiles(j->hsize);
   }
-  const auto brick_off = prefix(nbr), dsym_off = prefix(nsub1), slot_off = prefix(nslot), sb_off = prefix(nsbc);
+  const auto brick_off = prefix(nbr), dsym_off = prefix(nsub1), sb_off = prefix(nsbc);
   const auto pt_off = prefix(ptt), sp_off = prefix(spt), h_off = prefix(ht), ab_off = prefix(abt);
   b->nbricks = brick_off[nc];
   b->dsym_blocks = dsym_off[nc];
@@ -244,7 +268,28 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, l
   API_CUDA(b->dtmp.ensure((size_t)nc * sizeof(unsigned long long)), "alloc");
   API_CUDA(b->vw.ensure((size_t)std::max<int64_t>(b->nbricks, 1) * 128 * sizeof(float2)), "batch V weight alloc");
   API_CUDA(b->vscale.ensure((size_t)std::max<int64_t>(b->nbricks, 1) * sizeof(float)), "alloc");
-  API_CUDA(b->hscratch.ensure((size_t)std::max<int64_t>(slot_off[nc], 1) * 256 * sizeof(float)), "batch H scratch");
+  // waves of consecutive cells whose partial H blocks fit the budget
+  std::vector<int64_t> wslot(nc);  // first scratch slot of each cell within its wave
+  {
+    const int64_t cap = scratch_bytes > 0 ? scratch_bytes / 1024 : INT64_MAX;  // 1 KB per partial block
+    Wave cur;
+    int64_t used = 0, most = 0;
+    for (int k = 0; k < nc; ++k) {
+      if (k > cur.c0 && used + nslot[k] > cap) {
+        cur.c1 = k;
+        b->waves.push_back(cur);
+        cur = Wave();
+        cur.c0 = k;
+        used = 0;
+      }
+      wslot[k] = used;
+      used += nslot[k];
+      most = std::max(most, used);
+    }
+    cur.c1 = nc;
+    b->waves.push_back(cur);
+    API_CUDA(b->hscratch.ensure((size_t)std::max<int64_t>(most, 1) * 256 * sizeof(float)), "batch H scratch");
+  }
   API_CUDA(b->status.ensure(sizeof(int)), "alloc");
   API_CUDA(cudaMemset(b->status.p, 0, sizeof(int)), "memset");
 
@@ -252,25 +297,43 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, l
   // bricks k, k + grid, ... so a descending order balances them); the order
   // changes no result -- each brick writes its own points and partial blocks
   {
-    std::vector<std::tuple<int64_t, int32_t, int64_t>> order;  // (-cost, cell, brick)
-    order.reserve(b->nbricks);
-    for (int k = 0; k < nc; ++k) {
-      const lcp::Bricks& br = b->jobs[k]->orbs->bricks;
-      for (int64_t hb = 0; hb < br.nbricks; ++hb) {
-        const int64_t m = br.img_off[hb + 1] - br.img_off[hb];
-        order.emplace_back(-(m * m + 8 * m), (int32_t)k, hb);
+    auto sorted_bricks = [&](int c0, int c1, std::vector<int32_t>& bc, std::vector<int64_t>& bl) {
+      std::vector<std::tuple<int64_t, int32_t, int64_t>> order;  // (-cost, cell, brick)
+      for (int k = c0; k < c1; ++k) {
+        const lcp::Bricks& br = b->jobs[k]->orbs->bricks;
+        for (int64_t hb = 0; hb < br.nbricks; ++hb) {
+          const int64_t m = br.img_off[hb + 1] - br.img_off[hb];
+          order.emplace_back(-(m * m + 8 * m), (int32_t)k, hb);
+        }
       }
-    }
-    std::stable_sort(order.begin(), order.end(),
-                     [](const auto& x, const auto& y) { return std::get<0>(x) < std::get<0>(y); });
-    std::vector<int32_t> bc(order.size());
-    std::vector<int64_t> bl(order.size());
-    for (size_t i = 0; i < order.size(); ++i) {
-      bc[i] = std::get<1>(order[i]);
-      bl[i] = std::get<2>(order[i]);
+      std::stable_sort(order.begin(), order.end(),
+                       [](const auto& x, const auto& y) { return std::get<0>(x) < std::get<0>(y); });
+      for (auto& o : order) {
+        bc.push_back(std::get<1>(o));
+        bl.push_back(std::get<2>(o));
+      }
+    };
+    std::vector<int32_t> bc, hbc;
+    std::vector<int64_t> bl, hbl, wst;
+    sorted_bricks(0, nc, bc, bl);
+    for (Wave& w : b->waves) {
+      w.brick_off = (int64_t)hbc.size();
+      sorted_bricks(w.c0, w.c1, hbc, hbl);
+      w.nbricks = (int64_t)hbc.size() - w.brick_off;
+      // reduction starts of the wave's cells, rebased: wst[c0 + w .. c1 + w]
+      int64_t acc = 0;
+      for (int k = w.c0; k < w.c1; ++k) {
+        wst.push_back(acc);
+        acc += nsbc[k];
+      }
+      wst.push_back(acc);
+      w.nsb = acc;
     }
     API_CUDA(upload_pod(b->brick_cell, bc), "upload");
     API_CUDA(upload_pod(b->brick_local, bl), "upload");
+    API_CUDA(upload_pod(b->hbrick_cell, hbc), "upload");
+    API_CUDA(upload_pod(b->hbrick_local, hbl), "upload");
+    API_CUDA(upload_pod(b->wred_start, wst), "upload");
   }
 
   // per-cell tables
@@ -295,7 +358,7 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, l
       const lcp::UCell& u = j->ucell->u;
       __nv_bfloat16* dsym = b->dsym.as<__nv_bfloat16>() + dsym_off[k] * 768;
       const double* dscale = b->dscale.as<double>() + 2 * k;
-      float* scratch = b->hscratch.as<float>() + slot_off[k] * 256;
+      float* scratch = b->hscratch.as<float>() + wslot[k] * 256;
       lcp::TcCell t = lcp::tc_cell_of(o->bgeom, o->b_tab.as<__nv_bfloat16>());
       t.phi_scale = o->phi_scale;
       t.dsym = dsym;
@@ -341,13 +404,13 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, l
   }
   API_CUDA(upload_pod(b->dsym_start, dsym_off), "upload");
   API_CUDA(upload_pod(b->abs_start, ab_off), "upload");
-  API_CUDA(upload_pod(b->red_start, sb_off), "upload");
   API_CUDA(upload_pod(b->pt_start, pt_off), "upload");
   API_CUDA(upload_pod(b->sp_start, sp_off), "upload");
   API_CUDA(upload_pod(b->h_start, h_off), "upload");
-  // our kernels per step: per channel absmax + pow2 + dsym + density + vweight
-  // + H + reduce; once prep, scale, xc, sums, dot, dot-finish
-  b->kernels_per_step = 7 * ns + 6;
+  // our kernels per step: per channel absmax + pow2 + dsym + density, per
+  // channel and wave vweight + H + reduce; once prep, scale, xc, sums, dot,
+  // dot-finish
+  b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 6;
   API_CUDA(cudaDeviceSynchronize(), "batch create");
   *out = b.release();
   return LCP_OK;
@@ -437,7 +500,7 @@ lcp_status lcp_batch_info(const lcp_batch* b, int64_t* out8) {
   out8[4] = bytes;
   out8[5] = b->exec ? 1 : 0;
   out8[6] = b->nsb;
-  out8[7] = b->dsym_blocks;
+  out8[7] = (int64_t)b->waves.size();
   return LCP_OK;
 }
 

@@ -4,6 +4,7 @@
 // geometry.  Floating-point expressions are evaluated in the reference's
 // order so that sphere membership at R == rc resolves the same way.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -466,33 +467,80 @@ std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t 
   return "";
 }
 
-std::string build_bricks(const UCell& u, Bricks& b) {
-  // brick shape: divisors of Ngrid up to 8 per axis, the largest point count
-  // <= 128, then the most cubic, then the longest innermost side
-  int best[3] = {1, 1, 1};
-  long best_score = -1;
-  for (int b0 = 1; b0 <= 8; ++b0) {
-    if (u.ngrid[0] % b0) continue;
-    for (int b1 = 1; b1 <= 8; ++b1) {
-      if (u.ngrid[1] % b1) continue;
-      for (int b2 = 1; b2 <= 8; ++b2) {
-        if (u.ngrid[2] % b2) continue;
-        int prod = b0 * b1 * b2;
-        if (prod > 128) continue;
-        int mx = std::max(b0, std::max(b1, b2)), mn = std::min(b0, std::min(b1, b2));
-        long score = (long)prod * 10000 - (mx - mn) * 10 + b2;
-        if (score > best_score) {
-          best_score = score;
-          best[0] = b0;
-          best[1] = b1;
-          best[2] = b2;
-        }
-      }
-    }
+// Predicted cost (arbitrary units) of grid bricks of shape bd: each brick
+// costs kBrick, each (brick, 16-orbital sub-image) block kImage and each pair
+// of sub-images of a brick kPair (the tensor-core passes are one K step per
+// image pair and window, plus per-image table traffic).  The blocks of an atom
+// are estimated as the volume of its cutoff sphere grown by a brick (Steiner
+// formula for a box) over the average brick volume.
+double brick_shape_cost(const UCell& u, const int32_t* bd) {
+  constexpr double kBrick = 2.0, kImage = 1.0, kPair = 0.125, kPi = 3.14159265358979323846;
+  double L[3], nbr = 1.0, vcell;
+  for (int d = 0; d < 3; ++d) {
+    const double len = std::sqrt(u.lat[d][0] * u.lat[d][0] + u.lat[d][1] * u.lat[d][1] + u.lat[d][2] * u.lat[d][2]);
+    L[d] = len / u.ngrid[d] * bd[d];
+    nbr *= (double)((u.ngrid[d] + bd[d] - 1) / bd[d]);
   }
+  vcell = std::fabs(u.lat[0][0] * (u.lat[1][1] * u.lat[2][2] - u.lat[1][2] * u.lat[2][1]) -
+                    u.lat[0][1] * (u.lat[1][0] * u.lat[2][2] - u.lat[1][2] * u.lat[2][0]) +
+                    u.lat[0][2] * (u.lat[1][0] * u.lat[2][1] - u.lat[1][1] * u.lat[2][0]));
+  const double veff = vcell / nbr;
+  const double s2 = L[0] * L[1] + L[1] * L[2] + L[0] * L[2], s1 = L[0] + L[1] + L[2], v3 = L[0] * L[1] * L[2];
+  double blocks = 0.0;
+  for (int a = 0; a < u.natom; ++a) {
+    const int nch = (u.numorbs[a] + 15) / 16;
+    const double r = u.cut[a];
+    blocks += nch * (v3 + 2 * r * s2 + kPi * r * r * s1 + 4.0 / 3.0 * kPi * r * r * r) / veff;
+  }
+  const double m = blocks / nbr;
+  return nbr * (kBrick + kImage * m + kPair * m * m);
+}
+
+std::vector<std::array<int32_t, 3>> brick_shape_candidates(const UCell& u, std::vector<double>* costs) {
+  std::vector<std::pair<double, std::array<int32_t, 3>>> all;
+  for (int b0 = 1; b0 <= 8; ++b0)
+    for (int b1 = 1; b1 <= 8; ++b1)
+      for (int b2 = 1; b2 <= 8; ++b2) {
+        const int prod = b0 * b1 * b2;
+        if (prod > 128 || prod < 16 || b0 > u.ngrid[0] || b1 > u.ngrid[1] || b2 > u.ngrid[2]) continue;
+        const int32_t bd[3] = {b0, b1, b2};
+        all.push_back({brick_shape_cost(u, bd), {b0, b1, b2}});
+      }
+  std::stable_sort(all.begin(), all.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+  std::vector<std::array<int32_t, 3>> out;
+  if (costs) costs->clear();
+  for (auto& c : all) {
+    out.push_back(c.second);
+    if (costs) costs->push_back(c.first);
+  }
+  return out;
+}
+
+std::string build_bricks(const UCell& u, Bricks& b, const int32_t* shape) {
+  if (!shape || shape[0] <= 0) {
+    // the predicted best shape whose bricks stay within kMaxBrickImages
+    // sub-images (a smaller brick touches fewer atom images)
+    const auto cand = brick_shape_candidates(u, nullptr);
+    if (cand.empty()) return "no brick shape fits the grid";
+    std::string err;
+    const size_t tries = std::min<size_t>(cand.size(), 8);
+    for (size_t i = 0; i < tries; ++i) {
+      err = build_bricks(u, b, cand[i].data());
+      if (!err.empty() || b.max_images <= kMaxBrickImages) return err;
+    }
+    return err;
+  }
+  int best[3];
+  for (int d = 0; d < 3; ++d) {
+    if (shape[d] < 1 || shape[d] > u.ngrid[d]) return "brick shape out of range";
+    best[d] = shape[d];
+  }
+  if (best[0] * best[1] * best[2] > 128) return "a brick holds at most 128 points";
+  // bricks tile each period of the grid from 0; the last brick of an axis is
+  // ragged when the brick side does not divide Ngrid
   for (int d = 0; d < 3; ++d) {
     b.bdim[d] = best[d];
-    b.nb[d] = u.ngrid[d] / best[d];
+    b.nb[d] = (u.ngrid[d] + best[d] - 1) / best[d];
   }
   b.npts = best[0] * best[1] * best[2];
   b.nbricks = (int64_t)b.nb[0] * b.nb[1] * b.nb[2];
@@ -512,7 +560,20 @@ std::string build_bricks(const UCell& u, Bricks& b) {
     for (int64_t k = u.sphere_off[a]; k < u.sphere_off[a + 1]; ++k) {
       int x, y, z;
       unrolled(u, u.glist[k], u.clist[k], x, y, z);
-      int c0 = floordiv(x, b.bdim[0]), c1 = floordiv(y, b.bdim[1]), c2 = floordiv(z, b.bdim[2]);
+      // period R and home brick h per axis: c = R * nb + h
+      int l0, l1, l2, c0, c1, c2;
+      {
+        const int xs[3] = {x, y, z};
+        int ls[3], cs[3];
+        for (int d = 0; d < 3; ++d) {
+          const int R = floordiv(xs[d], u.ngrid[d]);
+          const int g = xs[d] - R * u.ngrid[d];
+          const int h = g / b.bdim[d];
+          ls[d] = g - h * b.bdim[d];
+          cs[d] = R * b.nb[d] + h;
+        }
+        l0 = ls[0], l1 = ls[1], l2 = ls[2], c0 = cs[0], c1 = cs[1], c2 = cs[2];
+      }
       auto key = std::make_tuple(c0, c1, c2);
       auto it = blocks.find(key);
       int32_t blk;
@@ -528,8 +589,7 @@ std::string build_bricks(const UCell& u, Bricks& b) {
       } else {
         blk = it->second;
       }
-      int l0 = x - c0 * b.bdim[0], l1 = y - c1 * b.bdim[1], l2 = z - c2 * b.bdim[2];
-      int slot = (l0 * b.bdim[1] + l1) * b.bdim[2] + l2;
+      const int slot = (l0 * b.bdim[1] + l1) * b.bdim[2] + l2;
       b.point_code[k] = blk * 128 + slot;
     }
   }

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "lcpgrid.h"
@@ -64,7 +65,8 @@ struct UCell {
 };
 
 // Grid bricks for the tensor-core contractions.  The home cell is tiled by
-// bricks of bdim points (bdim[d] divides Ngrid[d], at most 128 points); the
+// bricks of bdim points (at most 128; the last brick of an axis is ragged
+// when bdim[d] does not divide Ngrid[d], its slots past the grid empty); the
 // point slot of a brick-local coordinate l is (l0*bdim1 + l1)*bdim2 + l2.
 // Each atom's sphere is covered by "blocks": the bricks of the unrolled
 // lattice it touches, each holding 16 of the atom's orbitals on the brick's
@@ -103,7 +105,14 @@ struct Bricks {
   std::vector<int64_t> red_off;      // [nsb+1] CSR of slots per sub-block
   std::vector<int64_t> red_slot;     // global slot * 2 + (1 if the slot enters transposed)
 };
-std::string build_bricks(const UCell& u, Bricks& b);
+// Bricks of the given shape (ragged at the upper edge of an axis whose
+// Ngrid the side does not divide); shape == nullptr or shape[0] <= 0: the
+// predicted best shape with at most kMaxBrickImages sub-images per brick.
+constexpr int kMaxBrickImages = 64;
+std::string build_bricks(const UCell& u, Bricks& b, const int32_t* shape = nullptr);
+// Brick shapes (sides <= 8, 16..128 points) ranked by predicted cost.
+double brick_shape_cost(const UCell& u, const int32_t* bd);
+std::vector<std::array<int32_t, 3>> brick_shape_candidates(const UCell& u, std::vector<double>* costs);
 
 // Builds everything above; returns an error message or "".
 std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,

@@ -345,11 +345,14 @@ __global__ void dsym_batch_kernel(int32_t ncells, const DsymCell* __restrict__ c
   }
 }
 
+// Grid index of slot p of home brick hb, or -1 for a slot of a ragged brick
+// that lies past the grid.
 __device__ __forceinline__ int64_t brick_point_index(int64_t hb, int p, const int32_t* bdim, const int32_t* nb,
                                                      const int32_t* ngrid) {
   const int l2 = p % bdim[2], l1 = (p / bdim[2]) % bdim[1], l0 = p / (bdim[1] * bdim[2]);
   const int64_t h2 = hb % nb[2], h1 = (hb / nb[2]) % nb[1], h0 = hb / ((int64_t)nb[1] * nb[2]);
   const int64_t x = h0 * bdim[0] + l0, y = h1 * bdim[1] + l1, z = h2 * bdim[2] + l2;
+  if (x >= ngrid[0] || y >= ngrid[1] || z >= ngrid[2]) return -1;
   return (x * ngrid[1] + y) * ngrid[2] + z;
 }
 
@@ -663,9 +666,8 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
         if (lane == 0) tc::mbar_arrive(&tempty_bar[buf]);
       }
       if (abort_flag) break;
-      if (p < cl.npts)
-        cl.rho[brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid)] =
-            ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * cl.dscale[0]);
+      const int64_t gi = p < cl.npts ? brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid) : -1;
+      if (gi >= 0) cl.rho[gi] = ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * cl.dscale[0]);
     }
   }
   tc::fence_before_sync();
@@ -745,7 +747,8 @@ __global__ void __launch_bounds__(128) vweight_kernel(const __grid_constant__ Tc
   for (int64_t k = blockIdx.x; k < ntotal; k += gridDim.x) {
     int64_t hb;
     const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
-    const double v = p < cl.npts ? cl.vpot[brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid)] : 0.0;
+    const int64_t gi = p < cl.npts ? brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid) : -1;
+    const double v = gi >= 0 ? cl.vpot[gi] : 0.0;
     // |v| as bits: non-negative doubles order like their bit patterns
     unsigned long long m = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
     for (int o = 16; o > 0; o >>= 1) {

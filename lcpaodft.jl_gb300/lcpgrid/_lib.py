@@ -101,7 +101,12 @@ _SIGS = {
     "lcp_server_submit": ([_vp, _i32, _ppd, ctypes.c_uint64], _i32),
     "lcp_server_poll": ([_vp, _i32, _i32, ctypes.POINTER(ctypes.c_uint64), _pd, _pd, ctypes.POINTER(_i32)], _i32),
     "lcp_server_stats": ([_vp, ctypes.POINTER(_i64)], _i32),
-    "lcp_batch_create": ([_vp, _i32, ctypes.POINTER(_vp), ctypes.POINTER(_vp)], _i32),
+    "lcp_brick_shape_candidates": ([_vp, _i32, ctypes.POINTER(_i32), _pd, ctypes.POINTER(_i32)], _i32),
+    "lcp_orbs_set_brick_shape": ([_vp, _vp, ctypes.POINTER(_i32)], _i32),
+    "lcp_orbs_get_brick_shape": ([_vp, _vp, ctypes.POINTER(_i32)], _i32),
+    "lcp_orbs_autotune_bricks": ([_vp, _vp, _i32, ctypes.POINTER(_i32), _pd], _i32),
+    "lcp_orbs_release_fp64": ([_vp, _vp], _i32),
+    "lcp_batch_create": ([_vp, _i32, ctypes.POINTER(_vp), _i64, ctypes.POINTER(_vp)], _i32),
     "lcp_batch_destroy": ([_vp], None),
     "lcp_batch_step": ([_vp, _vp, _i32], _i32),
     "lcp_batch_check_status": ([_vp, _vp], _i32),

@@ -176,6 +176,14 @@ class UCell:
     def NN(self):
         return int(np.prod(self.Ngrid))
 
+    def brick_shape_candidates(self, max_shapes=8):
+        """[(shape, predicted cost)] best first."""
+        sh = np.zeros(3 * max_shapes, dtype=np.int32)
+        cost = np.zeros(max_shapes)
+        n = ctypes.c_int32()
+        check(lib.lcp_brick_shape_candidates(self._h, int(max_shapes), iptr(sh), dptr(cost), ctypes.byref(n)))
+        return [(tuple(int(x) for x in sh[3 * k:3 * k + 3]), float(cost[k])) for k in range(n.value)]
+
     def brick_info(self):
         """Grid-brick tiling of the tensor-core path."""
         out = (ctypes.c_int64 * 14)()
@@ -223,6 +231,28 @@ class DeviceOrbitalsGrid:
 
     def __getitem__(self, atom):
         return self.data(atom)
+
+    def set_brick_shape(self, shape=None):
+        """Brick shape of the split-BF16 tables (None: the predicted best)."""
+        sh = np.zeros(3, dtype=np.int32) if shape is None else np.asarray(shape, dtype=np.int32)
+        check(lib.lcp_orbs_set_brick_shape(self.ctx._h, self._h, iptr(sh)))
+
+    def brick_shape(self):
+        sh = np.zeros(3, dtype=np.int32)
+        check(lib.lcp_orbs_get_brick_shape(self.ctx._h, self._h, iptr(sh)))
+        return tuple(int(x) for x in sh)
+
+    def autotune_bricks(self, ncand=3):
+        """Times the split-BF16 passes for the ncand best predicted brick
+        shapes and keeps the fastest: (shape, ms per density + H pass)."""
+        sh = np.zeros(3, dtype=np.int32)
+        ms = ctypes.c_double()
+        check(lib.lcp_orbs_autotune_bricks(self.ctx._h, self._h, int(ncand), iptr(sh), ctypes.byref(ms)))
+        return tuple(int(x) for x in sh), float(ms.value)
+
+    def release_fp64(self):
+        """Keep only the split-BF16 tables (frees the FP64 tables)."""
+        check(lib.lcp_orbs_release_fp64(self.ctx._h, self._h))
 
     def __del__(self):
         try:
@@ -466,6 +496,11 @@ class GridStepJob:
         check(lib.lcp_job_energies(self.ctx._h, self._h, dptr(out)))
         return out
 
+    def prepare(self):
+        """Builds what the context's precision needs of the orbital tables
+        (split-BF16 brick tables, FP32 copy) ahead of the first step."""
+        check(lib.lcp_job_prepare(self.ctx._h, self._h))
+
     def footprint(self):
         """Device bytes of the job and its orbital tables."""
         out = ctypes.c_int64()
@@ -510,14 +545,16 @@ class Batch:
 
     GRAPH, EAGER = 0, 1
 
-    def __init__(self, jobs):
+    def __init__(self, jobs, scratch_bytes=0):
+        """scratch_bytes: budget of the partial H blocks (0: none); the cells
+        are then stepped in waves of the matrix-element pass."""
         self.jobs = list(jobs)  # the batch reads their buffers: keep them alive
         if not self.jobs:
             raise ValueError("a batch needs at least one job")
         self.ctx = self.jobs[0].ctx
         arr = (ctypes.c_void_p * len(self.jobs))(*[j._h.value for j in self.jobs])
         h = ctypes.c_void_p()
-        check(lib.lcp_batch_create(self.ctx._h, len(self.jobs), arr, ctypes.byref(h)))
+        check(lib.lcp_batch_create(self.ctx._h, len(self.jobs), arr, int(scratch_bytes), ctypes.byref(h)))
         self._h = h
 
     def step(self, graph=True):
@@ -534,11 +571,11 @@ class Batch:
 
     def info(self):
         """dict: cells, shape groups, bricks, kernels per step, workspace bytes,
-        graph captured, H sub-blocks, split-D blocks."""
+        graph captured, H sub-blocks, waves of the H pass."""
         out = (ctypes.c_int64 * 8)()
         check(lib.lcp_batch_info(self._h, out))
         keys = ("cells", "shape_groups", "bricks", "kernels_per_step", "workspace_bytes", "graph", "h_subblocks",
-                "dsym_blocks")
+                "waves")
         return {k: int(v) for k, v in zip(keys, out)}
 
     def close(self):

@@ -124,3 +124,22 @@ def test_batch_rejects_mixed_and_fp64():
     ctx.set_precision("fp64")
     with pytest.raises(L.LCPError):
         L.Batch(jobs)
+
+
+def test_batch_waves_same_bits():
+    """A scratch budget that splits the matrix-element pass into waves
+    changes no bit of the results."""
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, "off", n_pool=5, seed=29)
+    b1 = L.Batch(jobs)
+    b1.step(graph=True)
+    e1 = b1.energies().copy()
+    h1 = [j.hks()[0].copy() for j in jobs]
+    b1.close()
+    b2 = L.Batch(jobs, scratch_bytes=1)  # every cell a wave of its own
+    assert b2.info()["waves"] == len(jobs)
+    b2.step(graph=True)
+    np.testing.assert_array_equal(b2.energies(), e1)
+    for j, h in zip(jobs, h1):
+        np.testing.assert_array_equal(j.hks()[0], h)
+    b2.close()

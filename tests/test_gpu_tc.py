@@ -146,7 +146,7 @@ def test_job_energy_bf16x3_si64(ctx):
     assert abs(E["bf16x3"] - E["fp64"]) / u.Natom <= 1e-6, E
 
 
-def _mixed_cell(ctx, nrep=1):
+def _mixed_cell(ctx, nrep=1, ngrid=(44, 40, 48)):
     """Three species of 18 (s2p2d2: two 16-orbital chunks), 13 and 4 orbitals,
     cutoffs 8 / 7 / 6 bohr, seeded positions in a 11 x 10 x 12 bohr box."""
     from lcpgrid.workloads import synthetic_species
@@ -155,7 +155,7 @@ def _mixed_cell(ctx, nrep=1):
             synthetic_species(13, max_l=1, num_basis=(1, 1), rc=6.0)]
     lat = np.diag([11.0, 10.0, 12.0])
     pos = np.array([[1.0, 2.0, 3.0], [5.5, 6.0, 8.5], [8.0, 1.5, 6.0]])
-    u = L.UCell(1, lat, 3, [1, 2, 3], pos, [8.0, 7.0, 6.0], (44, 40, 48), [0, 0, 0], Total_NumOrbs=[18, 13, 4])
+    u = L.UCell(1, lat, 3, [1, 2, 3], pos, [8.0, 7.0, 6.0], ngrid, [0, 0, 0], Total_NumOrbs=[18, 13, 4])
     return u, L.Set_Orbitals_Grid(paos, u, ctx)
 
 
@@ -179,3 +179,63 @@ def test_orbital_chunks_density_and_h(ctx):
     assert np.max(np.abs(htc - h64)) <= H_TOL * np.max(np.abs(h64))
     dm = psd_dm(u, 32)[0]
     assert abs(np.dot(dm, htc) - np.dot(dm, h64)) <= SUM_TOL * np.sum(np.abs(dm * h64))
+
+
+def _check_vs_fp64(ctx, u, orbs, seed):
+    from test_gpu_parity import psd_dm
+    dm = psd_dm(u, seed)
+    r64 = _density(ctx, u, orbs, dm, "fp64")[0]
+    rtc = _density(ctx, u, orbs, dm, "bf16x3")[0]
+    assert np.max(np.abs(rtc - r64)) <= RHO_TOL * np.max(np.abs(r64))
+    assert abs(rtc.sum() - r64.sum()) <= SUM_TOL * abs(r64.sum())
+    vp = [np.random.default_rng(seed).normal(size=u.NN)]
+    h64 = _hks(ctx, u, orbs, vp, "fp64")[0]
+    htc = _hks(ctx, u, orbs, vp, "bf16x3")[0]
+    assert np.max(np.abs(htc - h64)) <= H_TOL * np.max(np.abs(h64))
+    return rtc, htc
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 8), (8, 4, 4), (5, 6, 4), (3, 7, 5), None])
+def test_ragged_bricks(ctx, shape):
+    """Brick sides that do not divide Ngrid (45 x 42 x 49): the last brick of
+    an axis is ragged, its slots past the grid empty; split-BF16 vs FP64."""
+    u, orbs = _mixed_cell(ctx, ngrid=(45, 42, 49))
+    ctx.set_precision("bf16x3")
+    try:
+        orbs.set_brick_shape(shape)
+        got = orbs.brick_shape()
+    finally:
+        ctx.set_precision("fp64")
+    if shape is not None:
+        assert got == tuple(shape)
+    else:
+        assert got == u.brick_shape_candidates(1)[0][0]
+    _check_vs_fp64(ctx, u, orbs, 61)
+
+
+def test_autotune_and_release_fp64(ctx):
+    """The measured brick-shape autotuner keeps one of the predicted best
+    shapes; after the FP64 tables are released the split-BF16 path gives the
+    same bits and the FP64 path refuses."""
+    from test_gpu_parity import psd_dm
+    u, orbs = _mixed_cell(ctx, ngrid=(45, 42, 49))
+    cands = [c[0] for c in u.brick_shape_candidates(8)]
+    ctx.set_precision("bf16x3")
+    try:
+        shape, ms = orbs.autotune_bricks(3)
+        assert shape in cands[:8] and ms > 0
+        assert orbs.brick_shape() == shape
+    finally:
+        ctx.set_precision("fp64")
+    rtc, htc = _check_vs_fp64(ctx, u, orbs, 62)
+    ctx.set_precision("bf16x3")
+    try:
+        orbs.release_fp64()
+    finally:
+        ctx.set_precision("fp64")
+    dm = psd_dm(u, 62)
+    np.testing.assert_array_equal(_density(ctx, u, orbs, dm, "bf16x3")[0], rtc)
+    with pytest.raises(L.LCPError):
+        _density(ctx, u, orbs, dm, "fp64")
+    with pytest.raises(L.LCPError):
+        orbs.set_brick_shape((4, 4, 8))
