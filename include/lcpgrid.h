@@ -314,6 +314,9 @@ void lcp_batch_destroy(lcp_batch* batch);
  * LCP_BATCH_GRAPH: replay the captured graph (the first call runs eagerly and
  * captures); LCP_BATCH_EAGER: launch the kernels one by one. */
 lcp_status lcp_batch_step(lcp_ctx* ctx, lcp_batch* batch, int32_t mode);
+/* One eager step with CUDA events between its stages (synchronises):
+ * stage_ms[6] as lcp_job_step_timed, for all cells together. */
+lcp_status lcp_batch_step_timed(lcp_ctx* ctx, lcp_batch* batch, double* stage_ms);
 /* Waits for the stream; reports (and clears) a device-side timeout. */
 lcp_status lcp_batch_check_status(lcp_ctx* ctx, lcp_batch* batch);
 /* energies[5 * njobs]: each job's lcp_job_energies, in the batch's order. */

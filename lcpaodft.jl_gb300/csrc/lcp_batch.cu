@@ -98,8 +98,12 @@ std::vector<int64_t> prefix(const std::vector<int64_t>& counts) {
   return s;
 }
 
-// Records one batched step on stream st.
-lcp_status record_step(lcp_batch* b, cudaStream_t st) {
+// Records one batched step on stream st (with events ev[0..6] at the stage
+// boundaries when ev is given).
+lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+  auto mark = [&](int k) {
+    if (ev) cudaEventRecord(ev[k], st);
+  };
   const int32_t nc = b->ncells;
   lcp::TcBatch tb{};
   tb.nbricks = b->nbricks;
@@ -115,6 +119,7 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
   const lcp::GridCell gnone{};
   int* status = b->status.as<int>();
   // 1. density, per channel: D scales, split D blocks, the tensor-core pass
+  mark(0);
   for (int c = 0; c < b->nspin; ++c) {
     const lcp::DsymCell* dc = b->dsym_cells[c].as<lcp::DsymCell>();
     // |D + D'^T| <= 2 max|D|: the fixed-point scale of the symmetrised blocks
@@ -126,6 +131,7 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
     API_CUDA(lcp::launch_density_tc_batch(none, tb, status, st), "batch density");
   }
   // 2. Poisson: sources, forward transforms per shape, 4 pi / G^2, inverse
+  mark(1);
   API_CUDA(lcp::launch_poisson_prep_g(b->spinpol, gnone, pts, st), "batch poisson prep");
   for (auto& g : b->groups)
     if (cufftSetStream(g->fwd, st) != CUFFT_SUCCESS || cufftSetStream(g->inv, st) != CUFFT_SUCCESS)
@@ -138,8 +144,11 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
     if (cufftExecZ2D(g->inv, g->spec.as<cufftDoubleComplex>(), g->real.as<double>()) != CUFFT_SUCCESS)
       return fail(LCP_EDEVICE, "cufftExecZ2D (batched) failed");
   // 3./4. xc + potential + energy partials, then the per-cell sums
+  mark(2);
   API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, st), "batch xc");
+  mark(3);
   API_CUDA(lcp::launch_grid_sums_g(gnone, per, st), "batch sums");
+  mark(4);
   // 5. grid matrix elements, per channel and wave
   for (int c = 0; c < b->nspin; ++c)
     for (size_t w = 0; w < b->waves.size(); ++w) {
@@ -156,7 +165,9 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st) {
                "batch h_reduce");
     }
   // 6. <D,H> and the energies of every cell
+  mark(5);
   API_CUDA(lcp::launch_dot_energy_g(b->spinpol, b->nspin, gnone, hts, per, st), "batch dot");
+  mark(6);
   return LCP_OK;
 }
 
@@ -459,6 +470,28 @@ lcp_status lcp_batch_step(lcp_ctx* ctx, lcp_batch* b, int32_t mode) {
   }
   ctx->launches += b->kernels_per_step;
   return LCP_OK;
+}
+
+lcp_status lcp_batch_step_timed(lcp_ctx* ctx, lcp_batch* b, double* stage_ms) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!b || !stage_ms) return fail(LCP_EINVAL, "NULL argument");
+  if (ctx->device != b->device) return fail(LCP_EINVAL, "batch on another device");
+  cudaEvent_t ev[7];
+  for (int k = 0; k < 7; ++k) API_CUDA(cudaEventCreate(&ev[k]), "cudaEventCreate");
+  s = record_step(b, ctx->stream, ev);
+  if (s == LCP_OK) {
+    ctx->launches += b->kernels_per_step;
+    cudaError_t e = cudaEventSynchronize(ev[6]);
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+      float ms = 0.f;
+      e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      stage_ms[k] = ms;
+    }
+    if (e != cudaSuccess) s = cuda_fail(e, "stage timing");
+  }
+  for (int k = 0; k < 7; ++k) cudaEventDestroy(ev[k]);
+  return s;
 }
 
 lcp_status lcp_batch_check_status(lcp_ctx* ctx, lcp_batch* b) {

@@ -520,13 +520,18 @@ std::string build_bricks(const UCell& u, Bricks& b, const int32_t* shape) {
   if (!shape || shape[0] <= 0) {
     // the predicted best shape whose bricks stay within kMaxBrickImages
     // sub-images (a smaller brick touches fewer atom images)
+    // (after a shape overflows, only shapes of fewer points are tried)
     const auto cand = brick_shape_candidates(u, nullptr);
     if (cand.empty()) return "no brick shape fits the grid";
     std::string err;
-    const size_t tries = std::min<size_t>(cand.size(), 8);
-    for (size_t i = 0; i < tries; ++i) {
+    int limit = 129, tries = 0;
+    for (size_t i = 0; i < cand.size() && tries < 12; ++i) {
+      const int prod = cand[i][0] * cand[i][1] * cand[i][2];
+      if (prod >= limit) continue;
+      ++tries;
       err = build_bricks(u, b, cand[i].data());
       if (!err.empty() || b.max_images <= kMaxBrickImages) return err;
+      limit = prod;
     }
     return err;
   }

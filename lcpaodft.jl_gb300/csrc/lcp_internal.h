@@ -107,8 +107,10 @@ struct Bricks {
 };
 // Bricks of the given shape (ragged at the upper edge of an axis whose
 // Ngrid the side does not divide); shape == nullptr or shape[0] <= 0: the
-// predicted best shape with at most kMaxBrickImages sub-images per brick.
-constexpr int kMaxBrickImages = 64;
+// predicted best shape with at most kMaxBrickImages sub-images per brick
+// (the kernels take any count; the bound keeps a brick's m x m pair tables
+// small).
+constexpr int kMaxBrickImages = 512;
 std::string build_bricks(const UCell& u, Bricks& b, const int32_t* shape = nullptr);
 // Brick shapes (sides <= 8, 16..128 points) ranked by predicted cost.
 double brick_shape_cost(const UCell& u, const int32_t* bd);

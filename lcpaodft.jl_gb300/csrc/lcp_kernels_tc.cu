@@ -440,10 +440,11 @@ constexpr int kDStageA = 3 * 4096;                // table block: hi, mid, lo
 constexpr int kDStageB = 3 * 2 * kDBLbo;          // Dsym pieces: (part, kh) x LBO
 constexpr int kDStageBytes = kDStageA + kDStageB;  // 24 KB
 constexpr size_t kDSmemStages = (size_t)kDStages * kDStageBytes;
-constexpr int kDMaxImages = 64;                   // sub-images per brick (checked at launch)
+constexpr int kDMaxImages = 64;                   // bricks of up to this many sub-images: pair table in smem
 constexpr int kDLag = 2;                          // K steps whose D pieces may still be in flight
 constexpr int kDGatherWarps = 4;                  // warps gathering D pieces (cp.async)
-// dynamic shared memory: the stages, then each gatherer's copy of the brick's pair table
+// dynamic shared memory: the stages, then each gatherer's copy of the brick's
+// pair table (larger bricks read theirs from global memory)
 constexpr size_t kDSmem = kDSmemStages + (size_t)kDGatherWarps * kDMaxImages * kDMaxImages * sizeof(int32_t);
 constexpr uint32_t kDBufCols = 256;               // TMEM columns per window buffer
 constexpr uint32_t kDCross = 128;                 // cross accumulator within a buffer
@@ -522,9 +523,13 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
       if (m == 0) continue;
       const int32_t* ptab = cl.tab_pair + cl.tab_off[hb];
       const uint8_t* dsym = reinterpret_cast<const uint8_t*>(cl.dsym);
-      __syncwarp();
-      for (int e = lane; e < m * m; e += 32) pair[e] = ptab[e];
-      __syncwarp();
+      const int32_t* prow = ptab;  // pair table of the brick: the smem copy when it fits
+      if (m <= kDMaxImages) {
+        __syncwarp();
+        for (int e = lane; e < m * m; e += 32) pair[e] = ptab[e];
+        __syncwarp();
+        prow = pair;
+      }
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin) {
         const int c1 = min(c0 + kDWin, m);
         for (int k = 0; k < m - c0; ++k, ++it) {
@@ -540,7 +545,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
           for (int c = gw * 32 + lane; c < nimg * 96; c += kDGatherWarps * 32) {
             // 16-byte pieces: (image, part, kh, 16 x 16 B)
             const int si = c / 96, w = c - si * 96, part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
-            int pr = pair[(c0 + si) * m + t];
+            int pr = prow[(c0 + si) * m + t];
             if (pr < 0) pr = (int)cl.zero_pair;
             cp_async16(sB + part * (2 * kDBLbo) + kh * kDBLbo + si * 256 + q * 16,
                        dsym + (int64_t)pr * (kDsymElems * 2) + part * 512 + kh * 256 + q * 16);
@@ -1266,7 +1271,6 @@ cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, i
 cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
                               const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
                               int* status, cudaStream_t st) {
-  if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
   TcCell c = tc_cell_of(bg, tab);
   c.phi_scale = phi_scale;
   c.dsym = dsym;
@@ -1296,7 +1300,6 @@ cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batc
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
                                   const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
                                   float* vscale, float* scratch, int* status, cudaStream_t st) {
-  if (bg.max_images > kDMaxImages) return cudaErrorInvalidValue;
   TcCell c = tc_cell_of(bg, tab);
   c.tab_slot = tab_slot;
   c.slot_base = slot_base;

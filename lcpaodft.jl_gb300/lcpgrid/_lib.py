@@ -110,6 +110,7 @@ _SIGS = {
     "lcp_batch_destroy": ([_vp], None),
     "lcp_batch_step": ([_vp, _vp, _i32], _i32),
     "lcp_batch_check_status": ([_vp, _vp], _i32),
+    "lcp_batch_step_timed": ([_vp, _vp, _pd], _i32),
     "lcp_batch_energies": ([_vp, _vp, _pd], _i32),
     "lcp_batch_info": ([_vp, ctypes.POINTER(_i64)], _i32),
     "lcp_job_get_density": ([_vp, _vp, _ppd], _i32),

@@ -480,8 +480,9 @@ class GridStepJob:
         p, keep = dptrs([_f64(DM[c]) for c in range(self.nspin)])
         check(lib.lcp_job_set_dm(self.ctx._h, self._h, p))
 
-    def step(self):
-        check(lib.lcp_job_step(self.ctx._h, self._h))
+    def step(self, ctx=None):
+        """One step on `ctx` (default: the context of the job's orbitals)."""
+        check(lib.lcp_job_step((ctx or self.ctx)._h, self._h))
 
     def step_timed(self):
         """One step with per-stage CUDA-event times (ms): density, Poisson,
@@ -545,13 +546,14 @@ class Batch:
 
     GRAPH, EAGER = 0, 1
 
-    def __init__(self, jobs, scratch_bytes=0):
+    def __init__(self, jobs, scratch_bytes=0, ctx=None):
         """scratch_bytes: budget of the partial H blocks (0: none); the cells
-        are then stepped in waves of the matrix-element pass."""
+        are then stepped in waves of the matrix-element pass.  ctx: the
+        split-BF16 context that steps the batch (default: the first job's)."""
         self.jobs = list(jobs)  # the batch reads their buffers: keep them alive
         if not self.jobs:
             raise ValueError("a batch needs at least one job")
-        self.ctx = self.jobs[0].ctx
+        self.ctx = ctx if ctx is not None else self.jobs[0].ctx
         arr = (ctypes.c_void_p * len(self.jobs))(*[j._h.value for j in self.jobs])
         h = ctypes.c_void_p()
         check(lib.lcp_batch_create(self.ctx._h, len(self.jobs), arr, int(scratch_bytes), ctypes.byref(h)))
@@ -559,6 +561,13 @@ class Batch:
 
     def step(self, graph=True):
         check(lib.lcp_batch_step(self.ctx._h, self._h, self.GRAPH if graph else self.EAGER))
+
+    def step_timed(self):
+        """One eager step with per-stage CUDA-event times (ms), as
+        GridStepJob.step_timed, for all cells together."""
+        out = np.zeros(6)
+        check(lib.lcp_batch_step_timed(self.ctx._h, self._h, dptr(out)))
+        return out
 
     def check_status(self):
         check(lib.lcp_batch_check_status(self.ctx._h, self._h))

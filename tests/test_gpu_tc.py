@@ -239,3 +239,18 @@ def test_autotune_and_release_fp64(ctx):
         _density(ctx, u, orbs, dm, "fp64")
     with pytest.raises(L.LCPError):
         orbs.set_brick_shape((4, 4, 8))
+
+
+def test_bricks_of_many_images(ctx):
+    """A dense cell of 18-orbital atoms with 9-bohr cutoffs: bricks touched by
+    more than 64 sub-images (the density kernel then reads the brick's pair
+    table from global memory instead of its shared-memory copy)."""
+    from lcpgrid.workloads import _place, synthetic_species
+    pao = synthetic_species(21, max_l=2, num_basis=(2, 2, 2), rc=9.0)
+    side = 12.0
+    pos = _place(np.random.default_rng(4), 16, side, 3.5)
+    u = L.UCell(1, np.eye(3) * side, 16, [1] * 16, pos, [9.0] * 16, (48, 48, 48), [0, 0, 0],
+                Total_NumOrbs=[18] * 16)
+    assert u.brick_info()["max_images"] > 64
+    orbs = L.Set_Orbitals_Grid([pao], u, ctx)
+    _check_vs_fp64(ctx, u, orbs, 63)
