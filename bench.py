@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32", "fp64"])
-    ap.add_argument("--workload", default="si64", choices=["si64", "si8"])
+    ap.add_argument("--workload", default="si64", choices=["si64", "si8", "mx2"])
     ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 drop-in form")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--serve-fp64-requests", type=int, default=60)
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
     ap.add_argument("--batching", action="store_true", help="run the batching form instead of the step bench")
+    ap.add_argument("--no-batching", action="store_true", help="skip the batching section of the step bench line")
     ap.add_argument("--batch-cells", type=int, default=256)
     ap.add_argument("--batch-seed", type=int, default=4242)
     ap.add_argument("--batch-threads", type=int, default=16, help="host threads building the cells")
@@ -248,21 +249,24 @@ def build_workload(ctx, wl):
     import lcpgrid as L
     from lcpgrid.workloads import psd_density_matrices, smooth_vna
     t0 = time.perf_counter()
-    u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+    nspin = 2 if wl.get("spinpol", "off") == "on" else 1
+    u = L.UCell(nspin, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
                 Total_NumOrbs=wl["numorbs"])
     t_geom = time.perf_counter() - t0
     t0 = time.perf_counter()
     orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx)
     t_tab = time.perf_counter() - t0
-    dm = psd_density_matrices(u, wl["dm_seed"], trace=wl["trace"])
+    dm = psd_density_matrices(u, wl["dm_seed"], nspin=nspin, trace=wl["trace"])
     vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
     return u, orbs, dm, vna, t_geom, t_tab
 
 
 def workload(args):
-    from lcpgrid.workloads import si64_workload
+    from lcpgrid.workloads import mx2_monolayer, si64_workload
     if args.workload == "si8":
         return si64_workload(nrep=1, ngrid=(48, 48, 48))
+    if args.workload == "mx2":
+        return mx2_monolayer()
     return si64_workload()
 
 
@@ -287,12 +291,14 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
 
     # FP64 reference energy of this step (the drop-in), for the error of other forms
-    job = L.GridStepJob(u, orbs, "off", "LDA", None, None, vna)
+    spin = wl.get("spinpol", "off")
+    nspin = len(dm)
+    job = L.GridStepJob(u, orbs, spin, "LDA" if spin == "off" else "LSDA", None, None, vna)
     job.set_dm(dm)
     ctx.set_precision("fp64")
     job.step()
     e_fp64 = job.energies()
-    h_fp64 = job.hks()[0]
+    h_fp64 = [h.copy() for h in job.hks()]
     fp64_ms = None
     if args.precision != "fp64" and args.fp64_steps > 0:
         fe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -335,23 +341,26 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     e_now = job.energies()
-    h_now = job.hks()[0]
+    h_now = job.hks()
 
     # e2e through the public API: pinned host D in, H and energies out, every step
-    pin_dm = torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True)
-    pin_dm.numpy()[:] = dm[0]
-    pin_h = torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True)
+    pin_dm = [torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True) for _ in range(nspin)]
+    for c in range(nspin):
+        pin_dm[c].numpy()[:] = dm[c]
+    pin_h = [torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True) for _ in range(nspin)]
     e2e_n = max(1, args.e2e_steps)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_n):
-        job.set_dm([pin_dm.numpy()])
+        job.set_dm([x.numpy() for x in pin_dm])
         job.step()
-        job.hks(out=[pin_h.numpy()])
+        job.hks(out=[x.numpy() for x in pin_h])
         e2e_e = job.energies()
     e2e_s = (time.perf_counter() - t0) / e2e_n
 
     dens_flops, ham_flops = pair_work(u)
+    dens_flops *= nspin  # the stages cover every spin channel
+    ham_flops *= nspin
     peaks, psrc = measured_peaks()
     # dominant kernel: the larger of the two pair contractions
     names = ["density", "poisson", "xc_vpot", "energy_sums", "hamiltonian", "dot_finish"]
@@ -387,19 +396,24 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {"fp64": "f64", "fp32": "f32", "bf16x3": "bf16x3/f32-acc"}[args.precision],
         "data": "synthetic (seeded: Gaussian radial functions, PSD D, smooth V_na)",
-        "config": {"workload": wl["name"], "atoms": wl["natom"], "orbitals_per_atom": wl["numorbs"][0],
+        "config": {"workload": wl["name"], "atoms": wl["natom"], "orbitals_per_atom": sorted(set(wl["numorbs"])),
                    "ngrid": list(wl["ngrid"]), "pairs": int(u.Nloop), "folded_pairs": int(u.n_unique),
-                   "lens_points": int(u.sum_numolg), "precision": args.precision, "spinpol": "off", "xc": "LDA",
+                   "lens_points": int(u.sum_numolg), "precision": args.precision, "spinpol": spin,
+                   "xc": "LDA" if spin == "off" else "LSDA",
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (phi tables %.0f MB)" % (u.sum_gridn * 13 * 8 / 1e6)},
+                   "l2": "inputs larger than L2 (phi tables %.0f MB)"
+                         % (sum(np.asarray(u.GridN_Atom, float) * np.asarray(wl["numorbs"])) * 8 / 1e6)},
         "stage_ms": dict(zip(names, [float(x) for x in stages])),
         "setup_s": {"ucell_host": t_geom, "tabulation": t_tab},
         "roofline": roof,
-        "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(u.Total_Hsize * 8),
-                "d2h_bytes_per_step": int(u.Total_Hsize * 8 + 40), "ms_per_step": e2e_s * 1e3},
+        "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(nspin * u.Total_Hsize * 8),
+                "d2h_bytes_per_step": int(nspin * u.Total_Hsize * 8 + 40), "ms_per_step": e2e_s * 1e3},
         "energy": {"E_grid": float(e_now[4]), "E_grid_fp64": float(e_fp64[4]),
                    "err_per_atom_uHa": abs(float(e_now[4] - e_fp64[4])) / wl["natom"] * 1e6,
-                   "max_abs_dH": float(np.max(np.abs(h_now - h_fp64)))},
+                   "rel_err": abs(float(e_now[4] - e_fp64[4])) / abs(float(e_fp64[4])),
+                   "max_abs_dH": float(max(np.max(np.abs(a - b)) for a, b in zip(h_now, h_fp64))),
+                   "terms": ["E_H1", "E_xc1 up", "E_xc1 down", "sum <D,H>", "E_grid"],
+                   "terms_this_form": [float(x) for x in e_now], "terms_fp64": [float(x) for x in e_fp64]},
         "fp64_dropin": None if fp64_ms is None else {
             "ms_per_step": fp64_ms, "steps": args.fp64_steps, "speedup_of_this_form": fp64_ms / ms_step},
         "clocks": clk,
@@ -412,7 +426,18 @@ def run_ours(args):
             line["serving"] = serving(args)
         except Exception as exc:  # the serving run must not hide the step line
             line["serving"] = {"error": repr(exc)}
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_batching and world == 1:
+        # the batching form on the same GPU: 256 mixed cells in one batched step
+        try:
+            del job
+            torch.cuda.synchronize()
+            line["batching"] = batching(args)
+        except Exception as exc:  # the batching run must not hide the step line
+            line["batching"] = {"error": repr(exc)}
+    if rank == 0 and not args.no_cpu_baseline and len(wl["paos"]) > 1:
+        line["cpu_baseline"] = {"value": None, "note": "the CPU baseline is timed on the one-species 64-atom cell "
+                                                       "(the default workload)"}
+    elif rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(wl, u, args.cpu_seconds, all_cores=True)
         except Exception as exc:  # the baseline must not hide the GPU line
@@ -692,10 +717,12 @@ def batching(args):
         e64 = np.array([jobs[k].energies() for k in ks])
         ctx.set_precision("bf16x3")
         err = np.abs(e_batch[ks, 4] - e64[:, 4]) / np.array([pool[k]["natom"] for k in ks]) * 1e6
+        rel = np.abs(e_batch[ks, 4] - e64[:, 4]) / np.abs(e64[:, 4])
         # the batch's per-cell time on the same cells, by their share of the pair work
         fp64 = {"cells": len(ks), "ms_all_sample_cells": float(f_ms[0]),
                 "ms_per_cell": float(f_ms[0]) / len(ks),
-                "max_err_per_atom_uHa": float(err.max()), "mean_err_per_atom_uHa": float(err.mean())}
+                "max_err_per_atom_uHa": float(err.max()), "mean_err_per_atom_uHa": float(err.mean()),
+                "max_rel_err": float(rel.max())}
 
     dens = ham = 0.0
     for u in ucells:

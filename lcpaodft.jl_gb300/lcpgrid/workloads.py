@@ -13,6 +13,10 @@
   1-3 species (cutoffs from {6, 7, 8, 9} bohr, 4/9/13/18 orbitals),
   cubic lattice constants of 4-12 A, random positions at least 3.5 bohr
   apart, grids from Calc_Ngrid at 150 Ry (24^3-96^3).
+* ``mx2_monolayer``: the large spin-polarised cell -- a 12 x 12 MX2
+  monolayer (trigonal prismatic, a = 3.19 A, 20 A of vacuum), 144 metal atoms
+  of 18 orbitals (rc 8) and 288 chalcogens of 13 (rc 7), grid 216 x 216 x 320,
+  LSDA with two PSD spin density matrices.
 * ``serving_pool``: the serving form -- random Si-density cells of 2-216
   atoms (log-uniform) with the 64-atom workload's species.
 
@@ -280,3 +284,41 @@ def batch_pool(ncells=256, seed=4242, nmin=2, nmax=64, min_sep=3.5, ecut=150.0, 
                     "numorbs": [species[s - 1].Spe_Total_NumOrbs for s in a2s], "paos": species,
                     "vna_seed": seed + 1000 + k, "dm_seed": seed + 2000 + k, "trace": 2.0 * natom})
     return out
+
+
+def mx2_monolayer(seed=555, nrep=12, a_ang=3.19, vacuum_ang=20.0, xx_ang=3.13, ngrid=(216, 216, 320)):
+    """The 12 x 12 MX2 monolayer: hexagonal cell a1 = a (1, 0, 0), a2 = a (1/2,
+    sqrt(3)/2, 0) repeated nrep x nrep, c = vacuum + the X-X layer thickness;
+    metal at in-plane fraction (0, 0) of each primitive cell, chalcogens at
+    (1/3, 2/3) at +-xx/2 about the metal plane (trigonal prismatic).  Species:
+    metal s2p2d2 (18 orbitals, rc 8), chalcogen s2p2d1 (13 orbitals, rc 7),
+    synthetic radial functions.  Two PSD spin density matrices of trace
+    3 * natom each (up and down)."""
+    a = a_ang * ANG_TO_BOHR
+    c = (vacuum_ang + xx_ang) * ANG_TO_BOHR
+    a1 = np.array([a, 0.0, 0.0])
+    a2 = np.array([a / 2, a * math.sqrt(3) / 2, 0.0])
+    lat = np.array([nrep * a1, nrep * a2, [0.0, 0.0, c]])
+    z0 = c / 2
+    dz = xx_ang * ANG_TO_BOHR / 2
+    pos, spe = [], []
+    for i in range(nrep):
+        for j in range(nrep):
+            o = i * a1 + j * a2
+            pos.append(o + [0, 0, z0])
+            spe.append(1)
+            x = o + a1 / 3.0 + 2.0 * a2 / 3.0  # in-plane fraction (1/3, 2/3)
+            pos.append(x + [0, 0, z0 + dz])
+            spe.append(2)
+            pos.append(x + [0, 0, z0 - dz])
+            spe.append(2)
+    paos = [synthetic_species(seed, max_l=2, num_basis=(2, 2, 2), rc=8.0),
+            synthetic_species(seed + 1, max_l=2, num_basis=(2, 2, 1), rc=7.0)]
+    natom = len(pos)
+    return {
+        "name": "mx2_%dx%d_%dx%dx%d" % (nrep, nrep, *ngrid),
+        "latvecs": lat, "gxyz": np.array(pos), "natom": natom, "atom2spe": spe,
+        "cut": [8.0 if t == 1 else 7.0 for t in spe], "ngrid": tuple(ngrid), "origin": [0.0, 0.0, 0.0],
+        "numorbs": [18 if t == 1 else 13 for t in spe], "paos": paos, "spinpol": "on",
+        "vna_seed": seed + 2, "dm_seed": seed + 3, "trace": 3.0 * natom,
+    }
