@@ -158,3 +158,25 @@ def test_batch_waves_same_bits():
     for j, h in zip(jobs, h1):
         np.testing.assert_array_equal(j.hks()[0], h)
     b2.close()
+
+
+def test_batch_isolates_a_bad_cell():
+    """A NaN in one cell's D poisons that cell's results only: every other
+    cell of the batch keeps the same bits as in a clean batch."""
+    from lcpgrid.workloads import psd_density_matrices
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, "off", n_pool=4, seed=41)
+    b = L.Batch(jobs)
+    b.step(graph=True)
+    clean = b.energies().copy()
+    bad = 2
+    dm = psd_density_matrices(jobs[bad].ucell, 7, trace=2.0 * jobs[bad].ucell.Natom)
+    dm[0][5] = np.nan
+    jobs[bad].set_dm(dm)
+    b.step(graph=True)
+    b.check_status()  # a NaN input is not a device error
+    got = b.energies()
+    assert np.isnan(got[bad]).any()
+    others = [k for k in range(len(jobs)) if k != bad]
+    np.testing.assert_array_equal(got[others], clean[others])
+    b.close()
