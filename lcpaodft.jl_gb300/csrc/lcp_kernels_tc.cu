@@ -415,11 +415,11 @@ __device__ __forceinline__ const TcCell* tc_cell(const TcCell* c0, const TcBatch
 }
 
 
-// Density kernel roles (320 threads, one CTA per SM, persistent over bricks):
+// Density kernel roles (448 threads, one CTA per SM, persistent over bricks):
 //   warp 0     table producer: per K step (brick, window, image t) three 4 KB
 //              bulk copies of t's table block (operand A), completing as
 //              transactions on full[stage] of a ring of kDStages stages;
-//   warps 6-9  D gatherers: the Dsym(s, t) pieces of the window (operand B)
+//   warps 6-13 D gatherers: the Dsym(s, t) pieces of the window (operand B)
 //              as 16-byte cp.async copies (one warp's cp.async issue costs
 //              ~35 cycles, a small bulk copy ~70, whatever its size), each
 //              warp publishing its share on full[stage] kDLag steps later,
@@ -434,22 +434,20 @@ __device__ __forceinline__ const TcCell* tc_cell(const TcCell* c0, const TcBatch
 //              window it frees the TMEM buffer, after a brick it writes rho.
 // Every wait is bounded; a timeout sets *status and stops all roles.
 constexpr int kDWin = 8;                          // images s per window (N <= 128)
-constexpr int kDStages = 6;
+constexpr int kDStages = 8;
 constexpr uint32_t kDBLbo = kDWin * 2 * 128;      // B: [part][kh][n-group][8 n][8 k]
 constexpr int kDStageA = 3 * 4096;                // table block: hi, mid, lo
 constexpr int kDStageB = 3 * 2 * kDBLbo;          // Dsym pieces: (part, kh) x LBO
 constexpr int kDStageBytes = kDStageA + kDStageB;  // 24 KB
 constexpr size_t kDSmemStages = (size_t)kDStages * kDStageBytes;
-constexpr int kDMaxImages = 64;                   // bricks of up to this many sub-images: pair table in smem
 constexpr int kDLag = 2;                          // K steps whose D pieces may still be in flight
-constexpr int kDGatherWarps = 4;                  // warps gathering D pieces (cp.async)
-// dynamic shared memory: the stages, then each gatherer's copy of the brick's
-// pair table (larger bricks read theirs from global memory)
-constexpr size_t kDSmem = kDSmemStages + (size_t)kDGatherWarps * kDMaxImages * kDMaxImages * sizeof(int32_t);
+constexpr int kDGatherWarps = 8;                  // warps gathering D pieces (cp.async)
+constexpr int kDPieces = (kDWin * 96 + kDGatherWarps * 32 - 1) / (kDGatherWarps * 32);  // per thread and step
+constexpr size_t kDSmem = kDSmemStages;            // 192 KB
 constexpr uint32_t kDBufCols = 256;               // TMEM columns per window buffer
 constexpr uint32_t kDCross = 128;                 // cross accumulator within a buffer
 
-__global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constant__ TcDensArgs args) {
+__global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel(const __grid_constant__ TcDensArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint64_t full_bar[kDStages], empty_bar[kDStages], mdone_bar[kDStages], tempty_bar[2], drain_bar;
   __shared__ uint32_t tslot;
@@ -513,7 +511,6 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
   } else if (warp >= 6) {
     // ------------------------------------------------------------ D gatherers
     const int gw = warp - 6;
-    int32_t* pair = reinterpret_cast<int32_t*>(smem + kDSmemStages) + gw * kDMaxImages * kDMaxImages;
     uint32_t it = 0;
     for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
       int64_t hb;
@@ -523,13 +520,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
       if (m == 0) continue;
       const int32_t* ptab = cl.tab_pair + cl.tab_off[hb];
       const uint8_t* dsym = reinterpret_cast<const uint8_t*>(cl.dsym);
-      const int32_t* prow = ptab;  // pair table of the brick: the smem copy when it fits
-      if (m <= kDMaxImages) {
-        __syncwarp();
-        for (int e = lane; e < m * m; e += 32) pair[e] = ptab[e];
-        __syncwarp();
-        prow = pair;
-      }
+      const int32_t* prow = ptab;  // the brick's m x m pair table, read through L1
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin) {
         const int c1 = min(c0 + kDWin, m);
         for (int k = 0; k < m - c0; ++k, ++it) {
@@ -542,13 +533,24 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
             break;
           }
           uint8_t* sB = smem + stage * kDStageBytes + kDStageA;
-          for (int c = gw * 32 + lane; c < nimg * 96; c += kDGatherWarps * 32) {
-            // 16-byte pieces: (image, part, kh, 16 x 16 B)
-            const int si = c / 96, w = c - si * 96, part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
-            int pr = prow[(c0 + si) * m + t];
-            if (pr < 0) pr = (int)cl.zero_pair;
-            cp_async16(sB + part * (2 * kDBLbo) + kh * kDBLbo + si * 256 + q * 16,
-                       dsym + (int64_t)pr * (kDsymElems * 2) + part * 512 + kh * 256 + q * 16);
+          // 16-byte pieces (image, part, kh, 16 x 16 B), at most kDPieces per
+          // thread: every pair index first, then the copies (a load between
+          // two copies would wait for the copy, as both touch shared memory)
+          int pr[kDPieces];
+#pragma unroll
+          for (int r = 0; r < kDPieces; ++r) {
+            const int c = gw * 32 + lane + r * kDGatherWarps * 32;
+            pr[r] = c < nimg * 96 ? prow[(c0 + c / 96) * m + t] : 0;
+          }
+#pragma unroll
+          for (int r = 0; r < kDPieces; ++r) {
+            const int c = gw * 32 + lane + r * kDGatherWarps * 32;
+            if (c < nimg * 96) {
+              const int si = c / 96, w = c - si * 96, part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
+              const int64_t pp = pr[r] < 0 ? cl.zero_pair : pr[r];
+              cp_async16(sB + part * (2 * kDBLbo) + kh * kDBLbo + si * 256 + q * 16,
+                         dsym + pp * (kDsymElems * 2) + part * 512 + kh * 256 + q * 16);
+            }
           }
           cp_async_commit();
           if (it >= (uint32_t)kDLag) {
@@ -580,7 +582,7 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin, ++win) {
         const int c1 = min(c0 + kDWin, m);
         const uint32_t buf = win & 1, wuse = win >> 1;
-        if (wuse > 0 && !tc::mbar_wait_abortable(&tempty_bar[buf], (wuse - 1) & 1, &abort_flag)) {
+        if (wuse > 0 && !tc::mbar_wait_warp(&tempty_bar[buf], (wuse - 1) & 1, &abort_flag)) {
           give_up();
           break;
         }
@@ -590,19 +592,25 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
           const int t = m - 1 - k;
           const int nimg = min(t, c1 - 1) - c0 + 1;
           const int stage = (int)(it % kDStages);
-          if (!tc::mbar_wait_abortable(&full_bar[stage], (it / kDStages) & 1, &abort_flag)) {
+          if (!tc::mbar_wait_warp(&full_bar[stage], (it / kDStages) & 1, &abort_flag)) {
             give_up();
             break;
           }
           tc::fence_after_sync();
-          if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16_f32(128, 16 * nimg, 0, 0);
-            const uint32_t a0 = tc::smem_u32(smem + stage * kDStageBytes), b0 = a0 + kDStageA;
-            const uint64_t dah = tc::smem_desc(a0, kALbo, kASbo), dam = tc::smem_desc(a0 + 4096, kALbo, kASbo),
-                           dal = tc::smem_desc(a0 + 8192, kALbo, kASbo);
-            const uint64_t dbh = tc::smem_desc(b0, kDBLbo, 128), dbm = tc::smem_desc(b0 + 2 * kDBLbo, kDBLbo, 128),
-                           dbl = tc::smem_desc(b0 + 4 * kDBLbo, kDBLbo, 128);
-            const uint32_t acc = k > 0 ? 1u : 0u;
+          // Descriptors are formed by the whole warp (warp-uniform values)
+          // and the lane elected by elect.sync issues: with the MMAs inside a
+          // lane-0 branch instead, each issue cost ~115 cycles whatever its N
+          // (measured), about twice the tensor core's own time.  elect.sync
+          // elects the same lane every time, so the commits below track
+          // every MMA of this warp.
+          const uint32_t idesc = tc::idesc_bf16_f32(128, 16 * nimg, 0, 0);
+          const uint32_t a0 = tc::smem_u32(smem + stage * kDStageBytes), b0 = a0 + kDStageA;
+          const uint64_t dah = tc::smem_desc(a0, kALbo, kASbo), dam = tc::smem_desc(a0 + 4096, kALbo, kASbo),
+                         dal = tc::smem_desc(a0 + 8192, kALbo, kASbo);
+          const uint64_t dbh = tc::smem_desc(b0, kDBLbo, 128), dbm = tc::smem_desc(b0 + 2 * kDBLbo, kDBLbo, 128),
+                         dbl = tc::smem_desc(b0 + 4 * kDBLbo, kDBLbo, 128);
+          const uint32_t acc = k > 0 ? 1u : 0u;
+          if (tc::elect_one()) {
             tc::mma_bf16(d0, dah, dbh, idesc, acc);
             tc::mma_bf16(d1, dah, dbm, idesc, acc);
             tc::mma_bf16(d1, dam, dbh, idesc, 1u);
@@ -624,8 +632,8 @@ __global__ void __launch_bounds__(320, 1) density_tc_kernel(const __grid_constan
         }
       }
     }
-    // every MMA issued by this thread has finished before TMEM is released
-    if (lane == 0) {
+    // every MMA issued by the elected thread has finished before TMEM is released
+    if (tc::elect_one()) {
       tc::mma_commit(&drain_bar);
       if (!tc::mbar_wait(&drain_bar, 0, 1u << 24)) give_up();
     }
@@ -875,58 +883,63 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
       const int64_t i0 = cl.img_off[hb];
       const int m = (int)(cl.img_off[hb + 1] - i0);
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup, ++grp) {
-        if (!tc::mbar_wait_abortable(&afull_bar, grp & 1, &abort_flag)) {
+        if (!tc::mbar_wait_warp(&afull_bar, grp & 1, &abort_flag)) {
           give_up();
           break;
         }
         for (int t0 = s0; t0 < m; t0 += kHWin, ++it) {
           const int stage = (int)(it % kHStages);
           const uint32_t buf = it & 1, tuse = it >> 1;
-          if (tuse > 0 && !tc::mbar_wait_abortable(&tempty_bar[buf], (tuse - 1) & 1, &abort_flag)) {
+          if (tuse > 0 && !tc::mbar_wait_warp(&tempty_bar[buf], (tuse - 1) & 1, &abort_flag)) {
             give_up();
             break;
           }
-          if (!tc::mbar_wait_abortable(&bready_bar[stage], (it / kHStages) & 1, &abort_flag)) {
+          if (!tc::mbar_wait_warp(&bready_bar[stage], (it / kHStages) & 1, &abort_flag)) {
             give_up();
             break;
           }
           tc::fence_after_sync();
-          if (lane == 0) {
-            // B parts stacked along N: the stage is [hi | mid | lo] x kHWin images,
-            // one MN-major operand of N = 3 * 16 * kHWin with uniform SBO.  Image
-            // slots beyond the tile hold stale data and feed only unused columns.
-            const uint32_t idesc3 = tc::idesc_bf16_f32(128, 3 * 16 * kHWin, 1, 1);
-            const uint32_t idesc2 = tc::idesc_bf16_f32(128, 2 * 16 * kHWin, 1, 1);
-            const uint32_t idesc1 = tc::idesc_bf16_f32(128, 16 * kHWin, 1, 1);
-            const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB0 + stage * 3 * kHBBytes);
-            const uint32_t d0 = tmem + buf * kHBufCols;
-            for (int ks = 0; ks < 8; ++ks) {
-              const uint32_t ko = ks * 256;
-              const uint64_t dah = tc::smem_desc(a0 + ko, 128, 2048),
-                             dam = tc::smem_desc(a0 + kHABytes + ko, 128, 2048),
-                             dal = tc::smem_desc(a0 + 2 * kHABytes + ko, 128, 2048);
-              const uint64_t dbh = tc::smem_desc(b0 + ko, 128, 2048),  // [hi | mid | lo] from here
-                             dbl = tc::smem_desc(b0 + 2 * kHBBytes + ko, 128, 2048);
-              // Accumulator k (quantum 2^-(14+8k)) at columns d0 + 64k: a product
-              // of parts (i, j) lands in accumulator i + j when the MMA with
-              // A part i starts at column d0 + 64 i.  lo*lo shares the last one.
-              const uint32_t acc = ks > 0 ? 1u : 0u;
+          // B parts stacked along N: the stage is [hi | mid | lo] x kHWin images,
+          // one MN-major operand of N = 3 * 16 * kHWin with uniform SBO.  Image
+          // slots beyond the tile hold stale data and feed only unused columns.
+          // Descriptors are warp-uniform; the lane elected by elect.sync (the
+          // same lane every time) issues and commits.
+          const uint32_t idesc3 = tc::idesc_bf16_f32(128, 3 * 16 * kHWin, 1, 1);
+          const uint32_t idesc2 = tc::idesc_bf16_f32(128, 2 * 16 * kHWin, 1, 1);
+          const uint32_t idesc1 = tc::idesc_bf16_f32(128, 16 * kHWin, 1, 1);
+          const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB0 + stage * 3 * kHBBytes);
+          const uint32_t d0 = tmem + buf * kHBufCols;
+#pragma unroll
+          for (int ks = 0; ks < 8; ++ks) {
+            const uint32_t ko = ks * 256;
+            const uint64_t dah = tc::smem_desc(a0 + ko, 128, 2048),
+                           dam = tc::smem_desc(a0 + kHABytes + ko, 128, 2048),
+                           dal = tc::smem_desc(a0 + 2 * kHABytes + ko, 128, 2048);
+            const uint64_t dbh = tc::smem_desc(b0 + ko, 128, 2048),  // [hi | mid | lo] from here
+                           dbl = tc::smem_desc(b0 + 2 * kHBBytes + ko, 128, 2048);
+            // Accumulator k (quantum 2^-(14+8k)) at columns d0 + 64k: a product
+            // of parts (i, j) lands in accumulator i + j when the MMA with
+            // A part i starts at column d0 + 64 i.  lo*lo shares the last one.
+            const uint32_t acc = ks > 0 ? 1u : 0u;
+            if (tc::elect_one()) {
               tc::mma_bf16(d0 + 3 * kHAccCols, dal, dbl, idesc1, acc);  // lo*lo (first write of acc 3)
               tc::mma_bf16(d0, dah, dbh, idesc3, acc);                   // hi * [hi, mid, lo] -> acc 0, 1, 2
               tc::mma_bf16(d0 + kHAccCols, dam, dbh, idesc3, 1u);        // mid * [hi, mid, lo] -> acc 1, 2, 3
               tc::mma_bf16(d0 + 2 * kHAccCols, dal, dbh, idesc2, 1u);    // lo * [hi, mid] -> acc 2, 3
             }
+          }
+          if (tc::elect_one()) {
             tc::mma_commit(&bempty_bar[stage]);
             tc::mma_commit(&tfull_bar[buf]);
           }
           __syncwarp();
         }
         if (abort_flag) break;
-        if (lane == 0) tc::mma_commit(&afree_bar);  // the A region may be refilled
+        if (tc::elect_one()) tc::mma_commit(&afree_bar);  // the A region may be refilled
         __syncwarp();
       }
     }
-    if (lane == 0) {
+    if (tc::elect_one()) {
       tc::mma_commit(&drain_bar);
       if (!tc::mbar_wait(&drain_bar, 0, 1u << 24)) give_up();
     }

@@ -68,6 +68,18 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 // ---------------------------------------------------------------- MMA
 
+// One lane of the converged warp, chosen by elect.sync; for the same member
+// mask it is the same lane every time.
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred = 0;
+  asm volatile(
+      "{\n\t.reg .pred P;\n\t"
+      "elect.sync _|P, 0xffffffff;\n\t"
+      "selp.u32 %0, 1, 0, P;\n\t}"
+      : "=r"(pred));
+  return pred != 0;
+}
+
 // D[tmem] (+)= A[smem] * B[smem]; issued by a single thread.
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
                                          uint32_t accumulate) {
@@ -125,6 +137,12 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint64_t* mbar, uint32_t par
     if ((i & 63u) == 63u && *abort) return false;
   }
   return false;
+}
+
+// The abortable wait with one outcome for the whole warp (for warps that
+// then issue through elect.sync, which needs the converged warp).
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* mbar, uint32_t parity, const volatile int* abort) {
+  return __all_sync(0xffffffffu, mbar_wait_abortable(mbar, parity, abort)) != 0;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
