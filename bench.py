@@ -31,10 +31,10 @@ for _p in (ROOT, PKG):
 
 METRIC = "ms per SCF grid step & jobs/s (p50/p99) split-BF16 vs FP64, <=1uHa/atom err"
 # DRAM bytes per table block of one split-BF16 stage launch (ncu, 8-atom 48^3
-# cell: density_tc_kernel 149.7 + 3.5 MB; hamiltonian_tc_kernel 150.0 + 55.2 MB
+# cell: density_tc_kernel 149.7 + 3.3 MB; hamiltonian_tc_kernel 150.1 + 55.9 MB
 # and h_reduce_kernel 93.6 + 3.2 MB, over 12076 blocks)
-TRAFFIC_PER_BLOCK = {"density": (149.71e6 + 3.51e6) / 12076,
-                     "hamiltonian": (150.05e6 + 55.20e6 + 93.62e6 + 3.18e6) / 12076}
+TRAFFIC_PER_BLOCK = {"density": (149.69e6 + 3.33e6) / 12076,
+                     "hamiltonian": (150.05e6 + 55.90e6 + 93.62e6 + 3.18e6) / 12076}
 UNIT = "grid steps/s"
 
 
