@@ -280,6 +280,7 @@ lcp::GridCell job_grid_cell(lcp_job* job) {
   }
   c.real = job->real.as<double>();
   c.spec = job->spec.p;
+  c.pfac = job->pfac.as<double>();
   c.dvh = job->dvh.as<double>();
   c.part = job->part.as<double>();
   c.sums = job->scal.as<double>();
@@ -1099,6 +1100,8 @@ lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* 
   API_CUDA(j->part.ensure((size_t)std::max<int64_t>({3 * lcp::red_tiles(nn), lcp::red_tiles(hs), 1}) * sizeof(double)),
            "alloc");
   API_CUDA(j->scal.ensure(16 * sizeof(double)), "alloc");
+  API_CUDA(j->pfac.ensure(nspec * sizeof(double)), "alloc");
+  API_CUDA(lcp::launch_poisson_table(u.ngrid, j->recvecs, j->pfac.as<double>(), ctx->stream), "poisson table");
   auto put = [&](DBuf& b, const double* src, bool& flag) -> cudaError_t {
     flag = src != nullptr;
     if (!src) return cudaSuccess;
@@ -1237,7 +1240,8 @@ lcp_status lcp_job_footprint(const lcp_job* job, int64_t* bytes) {
     add(job->hks[c]);
     add(job->vpot[c]);
   }
-  for (const DBuf* d : {&job->aden, &job->pcc, &job->vna, &job->dvh, &job->real, &job->spec, &job->part, &job->scal})
+  for (const DBuf* d : {&job->aden, &job->pcc, &job->vna, &job->dvh, &job->real, &job->spec, &job->part, &job->scal,
+                        &job->pfac})
     add(*d);
   const lcp_orbs* o = job->orbs;
   for (const DBuf* d : {&o->atv, &o->gxyz, &o->spe, &o->sph_off, &o->glist, &o->clist, &o->phi_off, &o->numorbs,

@@ -136,6 +136,7 @@ struct lcp_job {
   double recvecs[9] = {};
   DBuf dm[4], rho[4], hks[4], vpot[4];
   DBuf aden, pcc, vna, dvh, real, spec, part, scal;
+  DBuf pfac;  // Poisson factors of the half spectrum, tabulated at creation
   bool has_aden = false, has_pcc = false, has_vna = false;
   FftPlans* plans = nullptr;
 };

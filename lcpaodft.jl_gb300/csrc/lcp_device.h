@@ -115,6 +115,7 @@ struct GridCell {
   const double* rho[2];
   double* real;          // Poisson source (nn)
   void* spec;            // its half spectrum (ng0 * ng1 * (ng2/2+1) complex)
+  const double* pfac;    // tabulated Poisson factors of the half spectrum, or nullptr
   const double* dvh;     // Hartree potential (nn)
   double* vpot[2];
   const double* dm[2];
@@ -133,6 +134,8 @@ struct GridBatch {
 };
 cudaError_t launch_poisson_prep_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
 cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaStream_t st);
+// The Poisson factors of a grid (ng0 * ng1 * (ng2/2+1) doubles), for GridCell::pfac.
+cudaError_t launch_poisson_table(const int32_t* ngrid, const double* recvecs, double* out, cudaStream_t st);
 // xc + potential + the energy-term tile partials in one pass (tiles of nn)
 cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
 // per cell: sums[0..2] from the energy partials

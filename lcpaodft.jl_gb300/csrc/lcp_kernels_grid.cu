@@ -82,21 +82,26 @@ __device__ __forceinline__ void lda_ca(double den, double& exc, double& vxc) {
     vxc = 0.0;
     return;
   }
+  // The reference's expressions with the divisions by rs, sqrt(rs) and the
+  // correlation denominator each taken once as a reciprocal (FP64 division is
+  // a multi-instruction sequence on this GPU's narrow FP64 pipe).
   const double coe = 0.6203504908994;
   const double rs = coe * rcbrt(den);
-  const double tmp0 = 0.458165293632163 / rs;
-  const double Ex = -tmp0, dEx = tmp0 / rs;
+  const double irs = 1.0 / rs;
+  const double tmp0 = 0.458165293632163 * irs;
+  const double Ex = -tmp0, dEx = tmp0 * irs;
   double Ec, dEc;
   if (rs >= 1.0) {
-    const double t = sqrt(rs);
+    const double it = rsqrt(rs), t = rs * it;
     const double dum = 1.0 + 1.0529 * t + 0.3334 * rs;
-    const double t1 = 0.1423 / dum;
+    const double idum = 1.0 / dum;
+    const double t1 = 0.1423 * idum;
     Ec = -t1;
-    dEc = t1 / dum * (0.52645 / t + 0.3334);
+    dEc = t1 * idum * (0.52645 * it + 0.3334);
   } else {
     const double lr = log(rs);
     Ec = -0.0480 + 0.0311 * lr + rs * (0.0020 * lr - 0.0116);
-    dEc = 0.0311 / rs + 0.0020 * lr - 0.0096;
+    dEc = 0.0311 * irs + 0.0020 * lr - 0.0096;
   }
   exc = Ex + Ec;
   vxc = Ex + Ec - 1.0 / 3.0 * rs * (dEx + dEc);
@@ -330,29 +335,49 @@ __global__ void __launch_bounds__(kRedThreads) poisson_prep_g_kernel(const __gri
 
 // 4*pi/|G|^2 scaling of the half spectrum (as poisson_scale_kernel), one
 // tile of one cell per block.
+// The scale of half-spectrum element x of a cell (as poisson_scale_kernel).
+__device__ __forceinline__ double poisson_factor(int64_t x, const int* ng, const double* rv, double inv_nn) {
+  const int N1 = ng[0], N2 = ng[1], N3 = ng[2], H3 = N3 / 2 + 1;
+  const int k = (int)(x % H3);
+  const int64_t ij = x / H3;
+  const int j = (int)(ij % N2);
+  const int i = (int)(ij / N2);
+  if (i == 0 && j == 0 && k == 0) return 0.0;
+  const int mi = (N1 - i) % N1, mj = (N2 - j) % N2, mk = (N3 - k) % N3;
+  return 0.5 * (inv_g2_scale(i, j, k, ng, rv) + inv_g2_scale(mi, mj, mk, ng, rv)) * inv_nn;
+}
+
+// A cell's Poisson factors, tabulated once: the step's scaling pass is then
+// a streaming multiply instead of FP64 divisions per element.
+__global__ void __launch_bounds__(kRedThreads) poisson_table_kernel(PoissonArgs a, double* __restrict__ out) {
+  const int64_t total = (int64_t)a.ng[0] * a.ng[1] * (a.ng[2] / 2 + 1);
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x)
+    out[x] = poisson_factor(x, a.ng, a.rv, a.inv_nn);
+}
+
 __global__ void __launch_bounds__(kRedThreads) poisson_scale_g_kernel(const __grid_constant__ GridArgs a) {
   int64_t t;
   const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
+  if (c.pfac) {  // tabulated factors
+    const int64_t total = (int64_t)c.ng[0] * c.ng[1] * (c.ng[2] / 2 + 1);
+    const int64_t x0 = t * kRedTile, x1 = min(total, x0 + kRedTile);
+    double2* spec = reinterpret_cast<double2*>(c.spec);
+    for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
+      const double f = c.pfac[x];
+      const double2 v = spec[x];
+      spec[x] = make_double2(v.x * f, v.y * f);
+    }
+    return;
+  }
   const int ng[3] = {c.ng[0], c.ng[1], c.ng[2]};
   double rv[9];
   for (int d = 0; d < 9; ++d) rv[d] = c.rv[d];
   const double inv_nn = 1.0 / ((double)ng[0] * ng[1] * ng[2]);
-  const int N1 = ng[0], N2 = ng[1], N3 = ng[2], H3 = N3 / 2 + 1;
-  const int64_t total = (int64_t)N1 * N2 * H3;
+  const int64_t total = (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1);
   const int64_t x0 = t * kRedTile, x1 = min(total, x0 + kRedTile);
   cuDoubleComplex* spec = reinterpret_cast<cuDoubleComplex*>(c.spec);
   for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
-    const int k = (int)(x % H3);
-    const int64_t ij = x / H3;
-    const int j = (int)(ij % N2);
-    const int i = (int)(ij / N2);
-    double s;
-    if (i == 0 && j == 0 && k == 0) {
-      s = 0.0;
-    } else {
-      const int mi = (N1 - i) % N1, mj = (N2 - j) % N2, mk = (N3 - k) % N3;
-      s = 0.5 * (inv_g2_scale(i, j, k, ng, rv) + inv_g2_scale(mi, mj, mk, ng, rv)) * inv_nn;
-    }
+    const double s = poisson_factor(x, ng, rv, inv_nn);
     const cuDoubleComplex v = spec[x];
     spec[x] = make_cuDoubleComplex(v.x * s, v.y * s);
   }
@@ -546,6 +571,16 @@ cudaError_t launch_poisson_prep_g(int spinpol, const GridCell& c0, const GridBat
   const unsigned n = tiled_blocks(b, red_tiles(c0.nn));
   if (n == 0) return cudaSuccess;
   poisson_prep_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, 0, spinpol, 0));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_table(const int32_t* ngrid, const double* recvecs, double* out, cudaStream_t st) {
+  PoissonArgs a;
+  for (int d = 0; d < 3; ++d) a.ng[d] = ngrid[d];
+  for (int d = 0; d < 9; ++d) a.rv[d] = recvecs[d];
+  a.inv_nn = 1.0 / ((double)ngrid[0] * ngrid[1] * ngrid[2]);
+  const int64_t total = (int64_t)ngrid[0] * ngrid[1] * (ngrid[2] / 2 + 1);
+  poisson_table_kernel<<<grid_blocks(total, kRedThreads), kRedThreads, 0, st>>>(a, out);
   return cudaGetLastError();
 }
 
