@@ -185,6 +185,18 @@ lcp_status lcp_set_vpot_grid(lcp_ctx* ctx, int32_t spinpol, int64_t nn, const do
 lcp_status lcp_calc_matrix_elements(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
                                     int32_t spinpol, const double* const* vpot, double* const* hks);
 
+/* Force3_nospin / Force3_spin / Force3_nc (src/Force.jl:405-566 with
+ * _Calc_Force3_Blocked_Kernel!, src/Force.jl:3344-3394): the grid force term
+ * force[atom*3 + xyz] (Natom x 3, row-major), in FP64 whatever the context's
+ * precision.  vpot[c] (NN doubles) are the channels' potentials as the
+ * reference passes them -- off: Vpot; on: Vpot up, down; nc: dVHart + Vxc1,
+ * dVHart + Vxc2, Vxc3, Vxc4 -- and dm[c] the flat pair-block density
+ * matrices.  The orbitals must carry gradient tables (tabulated with
+ * grad = 1, Set_dOrbitals_Grid), else LCP_ESTATE.  Like the reference, the
+ * term is the energy's gradient (f_s d<D,H>/dR with V fixed). */
+lcp_status lcp_calc_force3(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs, int32_t spinpol,
+                           const double* const* vpot, const double* const* dm, double* force);
+
 /* Calc_EH1 (src/Energy.jl:655-666) and Calc_EXC1 (src/Energy.jl:669-700). */
 lcp_status lcp_calc_eh1(lcp_ctx* ctx, int32_t spinpol, int64_t nn, double gridvol,
                         const double* adensity, const double* const* density,

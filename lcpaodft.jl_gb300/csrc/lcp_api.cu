@@ -619,6 +619,24 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
   API_CUDA(upload(o->it_pair, ip, st), "upload");
   API_CUDA(upload(o->it_start, is, st), "upload");
   API_CUDA(upload(o->it_count, ic, st), "upload");
+  if (o->grad) {
+    // the force term's per-atom entries: item k's kept orientation goes to
+    // its pair's atom, the partner orientation to the neighbour atom
+    std::vector<int64_t> cnt(u.natom + 1, 0), code;
+    for (size_t k = 0; k < ip.size(); ++k) {
+      cnt[pa[ip[k]] + 1]++;
+      if (!pself[ip[k]]) cnt[pj[ip[k]] + 1]++;
+    }
+    for (int a = 0; a < u.natom; ++a) cnt[a + 1] += cnt[a];
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    code.resize(cnt[u.natom]);
+    for (size_t k = 0; k < ip.size(); ++k) {
+      code[fill[pa[ip[k]]]++] = (int64_t)k * 2;
+      if (!pself[ip[k]]) code[fill[pj[ip[k]]]++] = (int64_t)k * 2 + 1;
+    }
+    API_CUDA(upload(o->f_off, cnt, st), "upload");
+    API_CUDA(upload(o->f_code, code, st), "upload");
+  }
   DevPairs& pr = o->pairs;
   pr.nu = nu;
   pr.atom = o->p_atom.as<int32_t>();
@@ -853,6 +871,52 @@ lcp_status lcp_calc_matrix_elements(lcp_ctx* ctx, const lcp_ucell* ucell, const 
 }
 
 // ---------------------------------------------------------------- Poisson / xc / energies (host buffers)
+
+lcp_status lcp_calc_force3(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs, int32_t spinpol,
+                           const double* const* vpot, const double* const* dm, double* force) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if ((s = check_pair(ucell, orbs))) return s;
+  if (!vpot || !dm || !force) return fail(LCP_EINVAL, "NULL argument");
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "SpinPol must be off, on or nc");
+  if (!orbs->grad)
+    return fail(LCP_ESTATE, "the force term needs the gradient tables: tabulate with Set_dOrbitals_Grid");
+  if (orbs->phi_released) return fail(LCP_ESTATE, "the FP64 orbital tables were released");
+  const lcp::UCell& u = ucell->u;
+  const int nch = channels(spinpol);
+  const double coef[3][4] = {{4, 0, 0, 0}, {2, 2, 0, 0}, {2, 2, 4, -4}};  // src/Force.jl:443-445, 491-493, 554-556
+  const double* w = coef[spinpol == LCP_SPIN_OFF ? 0 : (spinpol == LCP_SPIN_ON ? 1 : 2)];
+  const int64_t nn = u.nn(), hs = u.total_hsize;
+  const double* dv[4];
+  const double* dd[4];
+  for (int c = 0; c < nch; ++c) {
+    if (!vpot[c] || !dm[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(ctx->w_aux[c].ensure(hs * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, vpot[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+    API_CUDA(cudaMemcpyAsync(ctx->w_aux[c].p, dm[c], hs * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+    dv[c] = ctx->w_in[c].as<double>();
+    dd[c] = ctx->w_aux[c].as<double>();
+  }
+  const int64_t nitems = orbs->pairs.nitems;
+  API_CUDA(ctx->w_part.ensure((size_t)std::max<int64_t>(nitems, 1) * 6 * sizeof(double)), "alloc");
+  API_CUDA(ctx->w_out[0].ensure((size_t)std::max(u.natom, 1) * 3 * sizeof(double)), "alloc");
+  const double* dphi[3] = {orbs->dphi[0].as<double>(), orbs->dphi[1].as<double>(), orbs->dphi[2].as<double>()};
+  API_CUDA(lcp::launch_force3_pairs(orbs->geom, orbs->pairs, nch, orbs->phi.as<double>(), dphi, dv, dd, w,
+                                    ctx->w_part.as<double>(), orbs->max_no, ctx->stream),
+           "force3");
+  API_CUDA(lcp::launch_force3_reduce(u.natom, orbs->f_off.as<int64_t>(), orbs->f_code.as<int64_t>(),
+                                     ctx->w_part.as<double>(), u.gridvol, ctx->w_out[0].as<double>(), ctx->stream),
+           "force3 reduce");
+  ctx->launches += 2;
+  API_CUDA(cudaMemcpyAsync(force, ctx->w_out[0].p, (size_t)u.natom * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream),
+           "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "force3");
+  return LCP_OK;
+}
 
 static lcp_status check_grid(const int32_t* ng) {
   if (!ng) return fail(LCP_EINVAL, "NULL Ngrid");
@@ -1247,7 +1311,7 @@ lcp_status lcp_job_footprint(const lcp_job* job, int64_t* bytes) {
   for (const DBuf* d : {&o->atv, &o->gxyz, &o->spe, &o->sph_off, &o->glist, &o->clist, &o->phi_off, &o->numorbs,
                         &o->species, &o->radial, &o->phi, &o->dphi[0], &o->dphi[1], &o->dphi[2], &o->phi32,
                         &o->p_atom, &o->p_jatom, &o->p_boffp, &o->p_boffq, &o->p_self, &o->p_lensoff, &o->p_g1,
-                        &o->p_g2, &o->it_pair, &o->it_start, &o->it_count, &o->b_code, &o->b_imgoff, &o->b_imgblk,
+                        &o->p_g2, &o->it_pair, &o->it_start, &o->it_count, &o->f_off, &o->f_code, &o->b_code, &o->b_imgoff, &o->b_imgblk,
                         &o->b_taboff, &o->b_tabpair, &o->b_tab, &o->b_tabslot, &o->b_slotbase, &o->b_redoff,
                         &o->b_redslot, &o->b_subpair, &o->b_subchunks, &o->b_sbfold, &o->b_sbchunks, &o->o_atom,
                         &o->o_jatom, &o->o_boff, &o->o_partner, &o->b_scale, &o->b_tmp})

@@ -113,6 +113,7 @@ struct lcp_orbs {
   DBuf species, radial;
   DBuf phi, dphi[3], phi32;
   DBuf p_atom, p_jatom, p_boffp, p_boffq, p_self, p_lensoff, p_g1, p_g2, it_pair, it_start, it_count;
+  DBuf f_off, f_code;  // per atom, its work-item halves (item * 2 + orientation) for the force term
   int64_t table_elems = 0;
   // brick tiling and split-BF16 tables of the tensor-core path (built on first use)
   bool bricks_ready = false;

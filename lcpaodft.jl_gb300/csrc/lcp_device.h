@@ -81,6 +81,15 @@ cudaError_t launch_hamiltonian_pairs(int prec, const DevGeom& g, const DevPairs&
                                      const double* const* vpot, double* const* hks, int max_no,
                                      cudaStream_t st);
 
+// grid force term (FP64): per work item the six sums of both orientations
+// (partials: 6 * nitems doubles), then per atom the sum of its entries
+// (item * 2 + orientation) times gridvol into force[natom][3]
+cudaError_t launch_force3_pairs(const DevGeom& g, const DevPairs& pr, int nch, const double* phi,
+                                const double* const* dphi, const double* const* vpot, const double* const* dm,
+                                const double* coef, double* partials, int max_no, cudaStream_t st);
+cudaError_t launch_force3_reduce(int natom, const int64_t* off, const int64_t* code, const double* partials,
+                                 double gridvol, double* force, cudaStream_t st);
+
 // grid kernels
 cudaError_t launch_poisson_prep(int spinpol, int64_t nn, const double* rho0, const double* rho1,
                                 const double* aden, double* out, cudaStream_t st);

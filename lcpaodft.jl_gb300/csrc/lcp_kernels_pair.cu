@@ -203,6 +203,146 @@ cudaError_t run_density(const DevGeom& g, const DevPairs& pr, int nspin, const T
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- grid force term
+
+// Force3 (src/Force.jl:405-566, 3344-3394): for every ordered pair (i, j, R)
+// the sum over its lens points of V(p) grad phi_i(p) . D_(i,j,R) phi_j(p),
+// weighted per channel.  Each folded pair item gives both orientations: the
+// kept one to atom i, the partner (j, i, -R) over the same points to atom j
+// (once for a pair that is its own partner).  Per item a fixed-order block
+// sum of the six components; force3_reduce_kernel then adds each atom's item
+// sums in item order (deterministic, no atomics).
+struct Coef4 {
+  double w[4];
+};
+
+template <int NOMAX>
+__global__ void __launch_bounds__(kPairThreads) force3_pairs_kernel(DevGeom g, DevPairs pr, int nch,
+                                                                    const double* __restrict__ phi,
+                                                                    const double* __restrict__ dpx,
+                                                                    const double* __restrict__ dpy,
+                                                                    const double* __restrict__ dpz, Ptr4 vpot,
+                                                                    Ptr4 dm, Coef4 w, double* __restrict__ out) {
+  extern __shared__ double fsm[];
+  double* Dp = fsm;                          // [nch][a][b]: kept pair's block
+  double* Dq = fsm + nch * NOMAX * NOMAX;    // [nch][b][a]: partner's block
+  __shared__ double red[6][kPairThreads];
+  for (int64_t item = blockIdx.x; item < pr.nitems; item += gridDim.x) {
+    const int64_t q = pr.item_pair[item];
+    const int i = pr.atom[q], j = pr.jatom[q];
+    const int noi = g.numorbs[i], noj = g.numorbs[j];
+    const int64_t bp = pr.boff_p[q], bq = pr.boff_q[q];
+    const bool self = pr.self[q] != 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < NOMAX * NOMAX; e += blockDim.x) {
+      const int a = e / NOMAX, b = e - a * NOMAX;
+      for (int c = 0; c < nch; ++c) {
+        Dp[c * NOMAX * NOMAX + a * NOMAX + b] = (a < noi && b < noj) ? dm.c[c][bp + (int64_t)a * noj + b] : 0.0;
+        Dq[c * NOMAX * NOMAX + b * NOMAX + a] =
+            (a < noi && b < noj && !self) ? dm.c[c][bq + (int64_t)b * noi + a] : 0.0;
+      }
+    }
+    __syncthreads();
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const int64_t start = pr.item_start[item];
+    const int count = pr.item_count[item];
+    const int64_t oi = g.phi_off[i], oj = g.phi_off[j];
+    const int32_t* gl_i = g.glist + g.sph_off[i];
+    for (int pt = threadIdx.x; pt < count; pt += blockDim.x) {
+      const int64_t k = start + pt;
+      const int64_t r1 = oi + (int64_t)pr.g1[k] * noi, r2 = oj + (int64_t)pr.g2[k] * noj;
+      double pi[NOMAX], pj[NOMAX];
+#pragma unroll
+      for (int a = 0; a < NOMAX; ++a) pi[a] = a < noi ? ldg(phi + r1 + a) : 0.0;
+#pragma unroll
+      for (int b = 0; b < NOMAX; ++b) pj[b] = b < noj ? ldg(phi + r2 + b) : 0.0;
+      const int gidx = gl_i[pr.g1[k]];
+      for (int c = 0; c < nch; ++c) {
+        const double v = w.w[c] * ldg(vpot.c[c] + gidx);
+        double sx = 0, sy = 0, sz = 0;
+        for (int a = 0; a < noi; ++a) {  // grad phi_i . D_p phi_j
+          double t = 0;
+#pragma unroll
+          for (int b = 0; b < NOMAX; ++b) t += Dp[c * NOMAX * NOMAX + a * NOMAX + b] * pj[b];
+          sx += ldg(dpx + r1 + a) * t;
+          sy += ldg(dpy + r1 + a) * t;
+          sz += ldg(dpz + r1 + a) * t;
+        }
+        acc[0] += v * sx;
+        acc[1] += v * sy;
+        acc[2] += v * sz;
+        if (!self) {
+          double ux = 0, uy = 0, uz = 0;
+          for (int b = 0; b < noj; ++b) {  // grad phi_j . D_q phi_i
+            double t = 0;
+#pragma unroll
+            for (int a = 0; a < NOMAX; ++a) t += Dq[c * NOMAX * NOMAX + b * NOMAX + a] * pi[a];
+            ux += ldg(dpx + r2 + b) * t;
+            uy += ldg(dpy + r2 + b) * t;
+            uz += ldg(dpz + r2 + b) * t;
+          }
+          acc[3] += v * ux;
+          acc[4] += v * uy;
+          acc[5] += v * uz;
+        }
+      }
+    }
+    for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int s2 = kPairThreads / 2; s2 > 0; s2 >>= 1) {
+      if (threadIdx.x < s2)
+        for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s2];
+      __syncthreads();
+    }
+    if (threadIdx.x < 6) out[item * 6 + threadIdx.x] = red[threadIdx.x][0];
+  }
+}
+
+// force[atom][x,y,z] = gridvol * sum over the atom's entries (item * 2 + half)
+// of the item sums, in entry order (one block per atom).
+__global__ void __launch_bounds__(kPairThreads) force3_reduce_kernel(int natom, const int64_t* __restrict__ off,
+                                                                     const int64_t* __restrict__ code,
+                                                                     const double* __restrict__ part, double gridvol,
+                                                                     double* __restrict__ force) {
+  __shared__ double red[3][kPairThreads];
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    double v[3] = {0, 0, 0};
+    for (int64_t e = off[atom] + threadIdx.x; e < off[atom + 1]; e += blockDim.x) {
+      const int64_t c = code[e];
+      const double* src = part + (c >> 1) * 6 + (c & 1) * 3;
+      for (int k = 0; k < 3; ++k) v[k] += src[k];
+    }
+    __syncthreads();
+    for (int k = 0; k < 3; ++k) red[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int s2 = kPairThreads / 2; s2 > 0; s2 >>= 1) {
+      if (threadIdx.x < s2)
+        for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s2];
+      __syncthreads();
+    }
+    if (threadIdx.x < 3) force[atom * 3 + threadIdx.x] = red[threadIdx.x][0] * gridvol;
+  }
+}
+
+template <int NOMAX>
+cudaError_t run_force3(const DevGeom& g, const DevPairs& pr, int nch, const double* phi, const double* const* dphi,
+                       const double* const* vp, const double* const* dm, const double* coef, double* part,
+                       cudaStream_t st) {
+  Ptr4 v{}, d{};
+  Coef4 w{};
+  for (int c = 0; c < nch; ++c) {
+    v.c[c] = vp[c];
+    d.c[c] = dm[c];
+    w.w[c] = coef[c];
+  }
+  const size_t smem = (size_t)2 * nch * NOMAX * NOMAX * sizeof(double);
+  LCP_CUDA_TRY(cudaFuncSetAttribute(force3_pairs_kernel<NOMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+  force3_pairs_kernel<NOMAX><<<persistent_blocks(pr.nitems, 4), kPairThreads, smem, st>>>(
+      g, pr, nch, phi, dphi[0], dphi[1], dphi[2], v, d, w, part);
+  return cudaGetLastError();
+}
+
 template <typename T, int NOMAX>
 cudaError_t run_hamiltonian(const DevGeom& g, const DevPairs& pr, int nch, const T* phi, const double* const* vp,
                             double* const* h, cudaStream_t st) {
@@ -232,6 +372,21 @@ cudaError_t launch_density_pairs(int prec, const DevGeom& g, const DevPairs& pr,
   }
   if (max_no <= 16) return run_density<double, 16>(g, pr, nspin, phi64, dm, rho, st);
   return run_density<double, 32>(g, pr, nspin, phi64, dm, rho, st);
+}
+
+cudaError_t launch_force3_pairs(const DevGeom& g, const DevPairs& pr, int nch, const double* phi,
+                                const double* const* dphi, const double* const* vpot, const double* const* dm,
+                                const double* coef, double* partials, int max_no, cudaStream_t st) {
+  if (pr.nitems == 0) return cudaSuccess;
+  if (max_no <= 16) return run_force3<16>(g, pr, nch, phi, dphi, vpot, dm, coef, partials, st);
+  return run_force3<32>(g, pr, nch, phi, dphi, vpot, dm, coef, partials, st);
+}
+
+cudaError_t launch_force3_reduce(int natom, const int64_t* off, const int64_t* code, const double* partials,
+                                 double gridvol, double* force, cudaStream_t st) {
+  if (natom == 0) return cudaSuccess;
+  force3_reduce_kernel<<<natom, kPairThreads, 0, st>>>(natom, off, code, partials, gridvol, force);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_hamiltonian_pairs(int prec, const DevGeom& g, const DevPairs& pr, int nch, const double* phi64,

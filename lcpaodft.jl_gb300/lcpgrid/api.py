@@ -15,7 +15,7 @@ from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 __all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Batch", "Server",
            "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "Solve_Poisson", "Solve_Poisson_xyz",
            "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
-           "Calc_MatrixElements_dVH_Vxc_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
+           "Calc_MatrixElements_dVH_Vxc_nc", "Force3_nospin", "Force3_spin", "Force3_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
 
 
 def _f64(a):
@@ -421,6 +421,36 @@ def Calc_MatrixElements_dVH_Vxc_on(ucell, Orbs_Grid, Vpot_Grid, MPI_Hks):
 def Calc_MatrixElements_dVH_Vxc_nc(ucell, Orbs_Grid, Vpot_Grid, MPI_Hks):
     """src/Hamiltonian.jl:327-380."""
     _matrix_elements("nc", ucell, Orbs_Grid, Vpot_Grid, MPI_Hks)
+
+
+def _force3(spin, pao, Orbs_Grid, Vpot, DM, ucell):
+    """The reference tabulates the gradient tables inside Force3; here they
+    come with Orbs_Grid when it was made by Set_dOrbitals_Grid, else they are
+    tabulated (on Orbs_Grid's context) for this call."""
+    orbs = Orbs_Grid if getattr(Orbs_Grid, "with_grad", False) else Set_dOrbitals_Grid(pao, ucell, Orbs_Grid.ctx)
+    n = _lib.NCHAN[spin]
+    vp, keep_v = dptrs([_f64(Vpot[c]) for c in range(n)])
+    dp, keep_d = dptrs([_f64(DM[c]) for c in range(n)])
+    out = np.zeros((ucell.Natom, 3))
+    check(lib.lcp_calc_force3(orbs.ctx._h, ucell._h, orbs._h, _lib.SPIN[spin], vp, dp, dptr(out)))
+    return out
+
+
+def Force3_nospin(pao, Orbs_Grid, Vpot_Grid, DM, ucell):
+    """src/Force.jl:405-446: VpotForce [Natom, 3]; DM as flat pair blocks."""
+    return _force3("off", pao, Orbs_Grid, Vpot_Grid, DM, ucell)
+
+
+def Force3_spin(pao, Orbs_Grid, Vpot_Grid, DM, ucell):
+    """src/Force.jl:449-499."""
+    return _force3("on", pao, Orbs_Grid, Vpot_Grid, DM, ucell)
+
+
+def Force3_nc(pao, Orbs_Grid, dVHart_Grid, Vxc_Grid, DM, ucell):
+    """src/Force.jl:502-566: Vpot1 = dVHart + Vxc1, Vpot2 = dVHart + Vxc2."""
+    dv = _f64(dVHart_Grid)
+    V = [dv + _f64(Vxc_Grid[0]), dv + _f64(Vxc_Grid[1]), _f64(Vxc_Grid[2]), _f64(Vxc_Grid[3])]
+    return _force3("nc", pao, Orbs_Grid, V, DM, ucell)
 
 
 def Calc_EH1(SpinPol, GridVol, ADensity_Grid, Density_Grid, dVHart_Grid, ctx=None):

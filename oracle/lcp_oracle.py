@@ -867,6 +867,39 @@ def calc_matrix_elements(ucell, orbs, vpot, nchannels):
 # Poisson, xc, potentials, energies
 
 
+def calc_force3(spinpol, ucell, orbs, dorbs, vpot, dm):
+    """Grid force term: Force3_nospin / Force3_spin / Force3_nc
+    (src/Force.jl:405-566) with _Calc_Force3_Blocked_Kernel!
+    (src/Force.jl:3344-3394).  For every ordered pair (atom, jatom, R) of the
+    neighbour list, in list order, the sum over the overlap points of
+    V(p) * (d phi_atom(p) . D_pair phi_jatom(p)); the channel sums are
+    weighted (off: 4; on: 2, 2; nc: 2, 2, 4, -4) and scaled by GridVol.
+
+    ``vpot`` holds the channels' potentials as the reference passes them (off:
+    [Vpot]; on: [Vpot_up, Vpot_down]; nc: [dVH + Vxc1, dVH + Vxc2, Vxc3,
+    Vxc4]); ``dm`` the flat pair-block density matrices per channel;
+    ``dorbs`` the gradient tables of set_dorbitals_grid.  Returns [Natom, 3]."""
+    coef = {"off": [4.0], "on": [2.0, 2.0], "nc": [2.0, 2.0, 4.0, -4.0]}[spinpol]
+    F = np.zeros((ucell.Natom, 3))
+    for loop, (atom, jatom, _) in enumerate(ucell.pairs):
+        a, b = atom - 1, jatom - 1
+        no0, no1 = int(ucell.Total_NumOrbs[a]), int(ucell.Total_NumOrbs[b])
+        off = int(ucell.block_offset[loop])
+        g1 = ucell.MPI_GListTAtoms1[loop]
+        g2 = ucell.MPI_GListTAtoms2[loop]
+        if g1.size == 0:
+            continue
+        gidx = ucell.GridListAtom[a][g1]
+        for c, w in enumerate(coef):
+            D = dm[c][off:off + no0 * no1].reshape(no0, no1)   # [ist, jst]
+            P = D @ orbs[b][:, g2]                              # :3371-3373
+            V = vpot[c][gidx]
+            for k in range(3):
+                local = np.einsum("op,op->p", dorbs[k][a][:, g1], P)  # :3380-3386
+                F[a, k] += w * float(np.sum(V * local)) * ucell.GridVol
+    return F
+
+
 def set_density_xyz(spinpol, ngrid, density, adensity):
     """src/Poisson.jl:10-26."""
     if spinpol == "off":
