@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--serving", action="store_true", help="run the serving form instead of the step bench")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section of the step bench line")
+    ap.add_argument("--no-force", action="store_true", help="skip the grid force term section of the step bench line")
     ap.add_argument("--serve-structures", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-rate", type=float, default=400.0, help="offered Poisson rate, jobs/s")
@@ -149,6 +150,46 @@ def pair_work(ucell):
     dens = float(np.sum(w * olg * (2 * no[a] * no[b] + 2 * no[a])))
     ham = float(np.sum(w * olg * (2 * no[a] * no[b] + no[a])))
     return dens, ham
+
+
+def force_work(ucell):
+    """Algorithmic flops of the grid force term: per ordered pair and lens
+    point, D phi_j (2 NO_i NO_j) and the three gradient dot products (6 NO_i)."""
+    import numpy as np
+    no = np.asarray(ucell.Total_NumOrbs, dtype=np.float64)
+    a = ucell.MPI_atom - 1
+    b = ucell.MPI_natn - 1
+    olg = ucell.MPI_NumOLG.astype(np.float64)
+    return float(np.sum(olg * (2 * no[a] * no[b] + 6 * no[a])))
+
+
+def force3_section(wl, u, dm, vna, reps=5):
+    """Force3 (FP64) on the step's cell: gradient tables, then the call as the
+    reference makes it (host V and D in, forces out), timed end to end."""
+    import numpy as np
+
+    import lcpgrid as L
+    ctx = L.Context(0)
+    t0 = time.perf_counter()
+    orbs = L.Set_dOrbitals_Grid(wl["paos"], u, ctx)
+    ctx.synchronize()
+    t_tab = time.perf_counter() - t0
+    V = [np.asarray(vna, dtype=np.float64)] * len(dm)
+    fn = L.Force3_nospin if len(dm) == 1 else L.Force3_spin
+    F = fn(wl["paos"], orbs, V, dm, u)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        F = fn(wl["paos"], orbs, V, dm, u)
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    flops = force_work(u) * len(dm)
+    fp64 = ctx.probe_fp64_tflops()
+    ach = flops / (ms * 1e-3) / 1e12
+    return {"ms_per_call": ms, "calls": reps, "gradient_tabulation_s": t_tab,
+            "max_abs_force": float(np.max(np.abs(F))),
+            "roofline": {"bound": "fp64-alu", "achieved": ach, "peak": fp64, "unit": "TFLOP/s", "frac": ach / fp64,
+                         "peak_source": "probe: FP64 FMA loop on this GPU",
+                         "note": "end to end: includes the host copies of V and D (%.0f MB)"
+                                 % (len(dm) * (u.NN + u.Total_Hsize) * 8 / 1e6)}}
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)
@@ -420,6 +461,11 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "gpu_launches_note": "library kernels per timed region; cuFFT adds 2 FFT launches per step",
     }
+    if rank == 0 and not args.no_force and world == 1:
+        try:
+            line["force3"] = force3_section(wl, u, dm, vna)
+        except Exception as exc:  # the force section must not hide the step line
+            line["force3"] = {"error": repr(exc)}
     if rank == 0 and not args.no_serving and world == 1:
         # the serving form on the same GPU: Poisson stream of mixed-size structures
         try:
