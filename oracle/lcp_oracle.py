@@ -1087,13 +1087,17 @@ def calc_eh1(spinpol, gridvol, adensity, density, dvhart):
     return e * gridvol * 0.5
 
 
-def calc_exc1(spinpol, xc_type, gridvol, adensity, pcc, density):
+def calc_exc1(spinpol, xc_type, gridvol, adensity, pcc, density, ngrid=None, latvecs=None):
     """src/Energy.jl:669-700 with Calc_Vxc_Grid switch 0 (src/XC/XC_Func.jl:164-189).
 
     Returns the two-entry EXC vector; for "off" the caller sets EXC[2]=EXC[1]
-    (src/Energy.jl:646-648)."""
+    (src/Energy.jl:646-648).  GGA_PBE needs the grid (``ngrid``, ``latvecs``)
+    for its gradient stencil."""
     if xc_type == "LDA":
         eps = [lda_ca(2 * (density[0] + pcc), 0)]
+    elif xc_type == "GGA_PBE":
+        dc = calc_diff_coef(glatvecs_of(latvecs, ngrid))
+        eps = calc_vxc_grid_gga(spinpol, ngrid, pcc, density, dc)
     else:
         u, d = lsda_ca(density[0] + pcc, density[1] + pcc, 0)
         eps = [u, d]
@@ -1106,7 +1110,277 @@ def calc_exc1(spinpol, xc_type, gridvol, adensity, pcc, density):
     return exc
 
 
-def grid_energy(spinpol, ucell, dm, H, eh1, exc):
+# --------------------------------------------------------------------------
+# GGA-PBE: pointwise kernel (src/XC/XC_PBE.jl) and the 27-point gradient
+# stencil (src/XC/GGA_PBE.jl), vectorised over grid points.
+
+DEN_MIN = 1.0e-14  # src/LCPAODFT.jl:71 (also the local den_min of src/XC/XC_PBE.jl)
+
+
+def pw92c(d1, d2):
+    """XC_PW92C (src/XC/XC_PBE.jl:1-126): returns (Ec, Vc1, Vc2, d1, d2), the
+    densities as the function leaves them (it resets both to den_min/2 where
+    their sum is <= den_min)."""
+    d1 = np.array(d1, dtype=np.float64, copy=True)
+    d2 = np.array(d2, dtype=np.float64, copy=True)
+    dtot = d1 + d2
+    low = dtot <= DEN_MIN
+    d1[low] = 0.5e-14
+    d2[low] = 0.5e-14
+    dtot = np.where(low, DEN_MIN, dtot)
+    rs = np.where(low, 6203.504908994, 0.6203504908994 * dtot ** (-1 / 3))
+    tmp0 = 1.0 / dtot
+    zeta = tmp0 * (d1 - d2)
+    zeta = np.where(zeta > 0.99, 0.99, zeta)
+    zeta = np.where(zeta < -1.0, -0.99, zeta)
+    drsdd = -(1 / 3) * rs * tmp0
+    dzdd1 = tmp0 * (1 - zeta)
+    dzdd2 = tmp0 * (-1 - zeta)
+    srs = np.sqrt(rs)
+
+    def g(A, a1, b1, b2, b3, b4):
+        b = b1 * srs + rs * (b2 + b3 * srs + b4 * rs)
+        dbdrs = b1 * 0.5 / srs + b2 + b3 * 1.5 * srs + b4 * 2 * rs
+        c = 1 + 1 / (2 * A * b)
+        dcdrs = -(c - 1) * dbdrs / b
+        dum = np.log(c)
+        dum1 = 1 + a1 * rs
+        return -2 * A * dum1 * dum, -2 * A * (a1 * dum + dum1 * dcdrs / c)
+
+    G0, dG0 = g(0.0310910, 0.2137000, 7.5957000, 3.5876000, 1.6382000, 0.4929400)
+    G1, dG1 = g(0.0155450, 0.2054800, 14.1189000, 6.1977000, 3.3662000, 0.6251700)
+    G2, dG2 = g(0.0168870, 0.1112500, 10.3570000, 3.6231000, 0.8802600, 0.4967100)
+    c = 1.92366105093154
+    fpp0 = 1.70992093416137
+    tmp1 = np.cbrt(1 + zeta)
+    tmp2 = np.cbrt(1 - zeta)
+    f = (tmp1 ** 4 + tmp2 ** 4 - 2) * c
+    dfdz = (4 / 3) * (tmp1 - tmp2) * c
+    z3 = zeta ** 3
+    z4 = z3 * zeta
+    Ec = G0 - G2 * f / fpp0 * (1 - z4) + (G1 - G0) * f * z4
+    dEcdrs = dG0 - dG2 * f / fpp0 * (1 - z4) + (dG1 - dG0) * f * z4
+    dEcdz = -G2 / fpp0 * (dfdz * (1 - z4) - f * 4 * z3) + (G1 - G0) * (dfdz * z4 + f * 4 * z3)
+    dum = dEcdrs * drsdd
+    Vc1 = Ec + dtot * (dum + dEcdz * dzdd1)
+    Vc2 = Ec + dtot * (dum + dEcdz * dzdd2)
+    return Ec, Vc1, Vc2, d1, d2
+
+
+def xc_ex_unpolarised(ds):
+    """XC_EX with NSP = 1 (src/XC/XC_PBE.jl:132-184): returns (EX1, VX1)."""
+    D = np.maximum(ds, DEN_MIN)
+    RS = 0.6203504908994 * D ** (-0.333333333333333)
+    VXP = -0.610887057710857 / RS
+    return 0.75 * VXP, VXP
+
+
+def xc_pbe(ed, gdens):
+    """XC_PBE! (src/XC/XC_PBE.jl:187-476), vectorised.
+
+    ``ed`` = (rho_up, rho_down) arrays, ``gdens`` = the six gradient arrays
+    (d/dx, d/dy, d/dz of up, then of down).  Returns (Exc[2], DEXDD[2],
+    DECDD[2], DEXDGD[6], DECDGD[6]) as lists of arrays, in the reference's
+    output order."""
+    THD = 1 / 3
+    beta = 0.06672455060314922
+    gamma = (1 - math.log(2)) / (PI * PI)
+    kappa = 0.8040
+    mu = beta * PI * PI / 3
+    GD_min = 1e-14
+    d1 = np.maximum(0.5 * DEN_MIN, np.asarray(ed[0], dtype=np.float64))
+    d2 = np.maximum(0.5 * DEN_MIN, np.asarray(ed[1], dtype=np.float64))
+    dt = d1 + d2
+    g = [np.asarray(x, dtype=np.float64) for x in gdens]
+    GDT = [g[0] + g[3], g[1] + g[4], g[2] + g[5]]
+    GDM = [np.sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]),
+           np.sqrt(g[3] * g[3] + g[4] * g[4] + g[5] * g[5])]
+    GDMT = np.maximum(GD_min, np.sqrt(GDT[0] * GDT[0] + GDT[1] * GDT[1] + GDT[2] * GDT[2]))
+
+    # local correlation; XC_PW92C writes the densities back (:15-24)
+    Ec_unif, Vc1_unif, Vc2_unif, d1, d2 = pw92c(d1, d2)
+
+    # correlation energy (:241-267)
+    kF = np.cbrt(3 * PI * PI * dt)
+    ks = np.sqrt(4 * kF / PI)
+    zeta = (d1 - d2) / dt
+    zeta = np.where(zeta > 0.99, 0.99, zeta)
+    zeta = np.where(zeta < -1.0, -0.99, zeta)
+    phi = 0.5 * ((1 + zeta) ** (2 / 3) + (1 - zeta) ** (2 / 3))
+    t = GDMT / (2 * phi * ks * dt)
+    f1 = Ec_unif / (gamma * phi ** 3)
+    f2 = np.exp(-f1)
+    A = beta / gamma / (f2 - 1)
+    f3 = t * t + A * t ** 4
+    f4 = beta / gamma * f3 / (1 + A * f3)
+    H = gamma * phi ** 3 * np.log(1 + f4)
+    Fc = Ec_unif + H
+
+    # correlation derivatives (:273-342)
+    DKFDD = 1 / 3 * kF / dt
+    DKSDD = 0.5 * ks * DKFDD / kF
+    DPDZ = 0.5 * 2 / 3 * (1 / np.cbrt(1 + zeta) - 1 / np.cbrt(1 - zeta))
+    DFCDD = []
+    for Vc_unif, DZDD in ((Vc1_unif, 1 / dt - zeta / dt), (Vc2_unif, -1 / dt - zeta / dt)):
+        DECUDD = (Vc_unif - Ec_unif) / dt
+        DPDD = DPDZ * DZDD
+        DTDD = (-t) * (DPDD / phi + DKSDD / ks + 1 / dt)
+        DF1DD = f1 * (DECUDD / Ec_unif - 3 * DPDD / phi)
+        DF2DD = -f2 * DF1DD
+        DADD = -A * DF2DD / (f2 - 1)
+        DF3DD = (2 * t + 4 * A * t ** 3) * DTDD + DADD * t ** 4
+        DF4DD = f4 * (DF3DD / f3 - (DADD * f3 + A * DF3DD) / (1 + A * f3))
+        DHDD = 3 * H * DPDD / phi + gamma * phi ** 3 * DF4DD / (1 + f4)
+        DFCDD.append(Vc_unif + H + dt * DHDD)
+    DFCDGD = []
+    for x in range(3):
+        DTDGD = (t / GDMT) * GDT[x] / GDMT
+        DF3DGD = DTDGD * (2.0 * t + 4.0 * A * t * t * t)
+        DF4DGD = f4 * DF3DGD * (1.0 / f3 - A / (1.0 + A * f3))
+        DHDGD = gamma * phi * phi * phi * DF4DGD / (1.0 + f4)
+        DFCDGD.append(dt * DHDGD)
+
+    # exchange, spin by spin (:348-451)
+    Fx = np.zeros_like(dt)
+    DFXDD = []
+    DFXDGD = []
+    for ds_, gdm, gs in ((d1, GDM[0], g[0:3]), (d2, GDM[1], g[3:6])):
+        DS = np.maximum(DEN_MIN, 2 * ds_)
+        GDMS = np.maximum(GD_min, 2 * gdm)
+        KFS = np.cbrt(3 * PI * PI * DS)
+        s = GDMS / (2 * KFS * DS)
+        f1x = 1 + mu * s * s / kappa
+        f = 1 + kappa - kappa / f1x
+        Ex_unif, Vx1_unif = xc_ex_unpolarised(DS)
+        Fx = Fx + DS * Ex_unif * f
+        DKFDDx = THD * KFS / DS
+        DSDD = s * (-(DKFDDx / KFS) - 1 / DS)
+        DF1DD = 2 * (f1x - 1) * DSDD / s
+        DFDD = kappa * DF1DD / (f1x * f1x)
+        DFXDD.append(Vx1_unif * f + DS * Ex_unif * DFDD)
+        for x in range(3):
+            GDS = 2 * gs[x]
+            DSDGD = (s / GDMS) * GDS / GDMS
+            DF1DGD = 2 * mu * s * DSDGD / kappa
+            DFDGD = kappa * DF1DGD / (f1x * f1x)
+            DFXDGD.append(DS * Ex_unif * DFDGD)
+    Fx = 0.5 * Fx / dt
+    return [Fx, Fc], DFXDD, DFCDD, DFXDGD, DFCDGD + DFCDGD
+
+
+def calc_diff_coef(glatvecs):
+    """Calc_Diff_Coef (src/XC/GGA_PBE.jl:1-39): the x, y, z first-derivative
+    weights of the tri-quadratic fit through the 27 neighbours
+    (i1, j1, k1) in -1..1 (k1 fastest), as a (3, 27) array."""
+    gL = np.asarray(glatvecs, dtype=np.float64)
+    M = np.zeros((27, 27))
+    p = 0
+    for i1 in (-1, 0, 1):
+        for j1 in (-1, 0, 1):
+            for k1 in (-1, 0, 1):
+                x, y, z = i1 * gL[0] + j1 * gL[1] + k1 * gL[2]
+                q = 0
+                for i2 in range(3):
+                    for j2 in range(3):
+                        for k2 in range(3):
+                            M[p, q] = x ** i2 * y ** j2 * z ** k2
+                            q += 1
+                p += 1
+    inv = np.linalg.inv(M)
+    # rows 10, 4, 2 (1-based) of the inverse: the x, y, z monomial coefficients
+    return np.stack([inv[9], inv[3], inv[1]])
+
+
+def _stencil(ngrid, f, coef):
+    """sum_p coef[p] * f[neighbour p] with periodic wrap (transform2primcell,
+    src/XC/GGA_PBE.jl:42-50); the neighbour order is i1, j1, k1 in -1..1, k1
+    fastest, as in src/XC/GGA_PBE.jl:77-90."""
+    a = np.asarray(f, dtype=np.float64).reshape(ngrid)
+    out = np.zeros(a.shape)
+    p = 0
+    for i1 in (-1, 0, 1):
+        for j1 in (-1, 0, 1):
+            for k1 in (-1, 0, 1):
+                out += coef[p] * np.roll(a, shift=(-i1, -j1, -k1), axis=(0, 1, 2))
+                p += 1
+    return out.ravel()
+
+
+def _gga_spin_densities(spinpol, density):
+    """(ED up, ED down) before the PCC is added and the centre-point test value
+    (2 rho for "off", rho_up + rho_down otherwise)."""
+    if spinpol == "off":
+        r = np.asarray(density[0], dtype=np.float64)
+        return r, r, 2 * r
+    r0 = np.asarray(density[0], dtype=np.float64)
+    r1 = np.asarray(density[1], dtype=np.float64)
+    return r0, r1, r0 + r1
+
+
+def set_ddensity_grid(spinpol, ngrid, density, pcc, diff_coef):
+    """Set_dDensity_Grid! (src/XC/GGA_PBE.jl:53-159): per spin, the three
+    gradient components of rho_s + pcc, zero where the centre test value is
+    <= den_min.  Returns [spin][xyz] arrays (one spin for "off")."""
+    r0, r1, test = _gga_spin_densities(spinpol, density)
+    pc = np.zeros_like(r0) if pcc is None else np.asarray(pcc, dtype=np.float64)
+    on = DEN_MIN < test
+    out = []
+    for r in ((r0,) if spinpol == "off" else (r0, r1)):
+        out.append([np.where(on, _stencil(ngrid, r + pc, diff_coef[a]), 0.0) for a in range(3)])
+    return out
+
+
+def _gga_gdens(spinpol, dden):
+    up = dden[0]
+    dn = dden[0] if spinpol == "off" else dden[1]
+    return [up[0], up[1], up[2], dn[0], dn[1], dn[2]]
+
+
+def set_xc_grid_gga(spinpol, ngrid, pcc, density, diff_coef):
+    """Set_XC_Grid!(xc_func::XC_GGA_PBE, ...) (src/XC/XC_Func.jl:148-160):
+    Set_dDensity_Grid! then Set_Vxc_GGA_PBE! (src/XC/GGA_PBE.jl:162-193,
+    274-462).  Returns (Vxc_Grid, dDensity_Grid, dEXC_dGD)."""
+    r0, r1, test = _gga_spin_densities(spinpol, density)
+    pc = np.zeros_like(r0) if pcc is None else np.asarray(pcc, dtype=np.float64)
+    dden = set_ddensity_grid(spinpol, ngrid, density, pcc, diff_coef)
+    # pointwise pass: 2 ED >= den_min ("off", :301) / ED1 + ED2 > den_min (:393)
+    act = test >= DEN_MIN if spinpol == "off" else test > DEN_MIN
+    _, dexdd, decdd, dexdgd, decdgd = xc_pbe((r0 + pc, r1 + pc), _gga_gdens(spinpol, dden))
+    ns = 1 if spinpol == "off" else 2
+    vxc = [np.where(act, dexdd[s] + decdd[s], 0.0) for s in range(ns)]
+    dexc = [[np.where(act, dexdgd[3 * s + a] + decdgd[3 * s + a], 0.0) for a in range(3)] for s in range(ns)]
+    # divergence pass: centre test value > den_min (:328, :426)
+    on = test > DEN_MIN
+    for s in range(ns):
+        tmp = _stencil(ngrid, dexc[s][0], diff_coef[0])
+        tmp = tmp + _stencil(ngrid, dexc[s][1], diff_coef[1])
+        tmp = tmp + _stencil(ngrid, dexc[s][2], diff_coef[2])
+        vxc[s] = np.where(on, vxc[s] - tmp, vxc[s])
+    if spinpol == "nc":
+        tmp0 = 0.5 * (vxc[0] + vxc[1])
+        tmp1 = 0.5 * (vxc[0] - vxc[1])
+        th, ph = np.asarray(density[2]), np.asarray(density[3])
+        vxc = [tmp0 + np.cos(th) * tmp1, tmp0 - np.cos(th) * tmp1,
+               -tmp1 * np.sin(th) * np.cos(ph), -tmp1 * np.sin(th) * np.sin(ph)]
+    return vxc, dden, dexc
+
+
+def calc_vxc_grid_gga(spinpol, ngrid, pcc, density, diff_coef):
+    """_Calc_Vxc_Grid_GGA! (src/XC/XC_Func.jl:193-215 with the five-argument
+    _Set_Vxc_GGA_PBE_* of src/XC/GGA_PBE.jl:196-271): the PBE energy per
+    particle Exc[1] + Exc[2] where the centre test value is > den_min, else 0;
+    the same array for both spins."""
+    r0, r1, test = _gga_spin_densities(spinpol, density)
+    pc = np.zeros_like(r0) if pcc is None else np.asarray(pcc, dtype=np.float64)
+    dden = set_ddensity_grid(spinpol, ngrid, density, pcc, diff_coef)
+    exc = xc_pbe((r0 + pc, r1 + pc), _gga_gdens(spinpol, dden))[0]
+    e = np.where(test > DEN_MIN, exc[0] + exc[1], 0.0)
+    return [e] if spinpol == "off" else [e, e.copy()]
+
+
+def glatvecs_of(latvecs, ngrid):
+    """gtv of Calc_EXC1 (src/Energy.jl:676-679): Latvecs rows / Ngrid."""
+    return _glatvecs(latvecs, ngrid)
     """Job energy scalar: f_s * sum_s <D_s, H^grid_s> + E_H1 + E_xc1, with f_s = 2
     for "off" (as src/Energy.jl:475-505 doubles the kinetic term) and
     E_xc1 = EXC[1] + EXC[2] with EXC[2] = EXC[1] for "off" (src/Energy.jl:646-648)."""

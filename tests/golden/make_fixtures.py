@@ -5,7 +5,7 @@ This script is run once, in a checkout that has the reference project
 
 * ``golden_vectors.json`` -- the numeric expectations written inline in the
   reference's own unit tests (``test/test_UCell.jl``, ``test_Set_Orbs_Grid.jl``,
-  ``test_Poisson.jl``, ``test_LDA_CA.jl``, ``test_LSDA_CA.jl``,
+  ``test_Poisson.jl``, ``test_LDA_CA.jl``, ``test_LSDA_CA.jl``, ``test_XC_PBE.jl``,
   ``test_Set_XC_Grid.jl``, ``test_Set_AdenPCC_Grid.jl``, ``test_Calc_Ngrid.jl``,
   ``test_Read_PAO.jl``).  The Julia test files are read as text; the array
   literals after ``≈`` / ``==`` are parsed as JSON.  Nothing is executed.
@@ -112,6 +112,22 @@ def parse_lsda(ref):
                 res.setdefault(str(switch), {})[m.group(1)] = json.loads(m.group(2))
     return {"up": [0.1 * i for i in range(1, 11)],
             "down": [0.1 * i - 0.1 for i in range(1, 11)], "switch": res}
+
+
+def parse_xc_pbe(ref):
+    """Inputs and expected outputs of the pointwise PBE kernel (test/test_XC_PBE.jl)."""
+    path = os.path.join(ref, "test/test_XC_PBE.jl")
+    res = {}
+    with open(path) as f:
+        for line in f:
+            line = line.strip()
+            m = re.match(r"(ED|GDENS) = (\[.*\])$", line)
+            if m:
+                res[m.group(1)] = json.loads(m.group(2))
+            m = re.match(r"@test (Exc|DEXDD|DECDD|DEXDGD|DECDGD) ≈ (.*)$", line)
+            if m:
+                res[m.group(1)] = json.loads(m.group(2))
+    return res
 
 
 def _testsets(path):
@@ -243,6 +259,7 @@ def main():
         "poisson_si_3x3x3": parse_poisson(ref),
         "lda_ca": parse_lda(ref),
         "lsda_ca": parse_lsda(ref),
+        "xc_pbe": parse_xc_pbe(ref),
         "xc_grid": parse_xc_grid(ref),
         "adenpcc": parse_adenpcc(ref),
         "calc_ngrid": parse_ngrid(ref),
