@@ -42,7 +42,7 @@ enum {
 };
 
 enum { LCP_SPIN_OFF = 0, LCP_SPIN_ON = 1, LCP_SPIN_NC = 2 };
-enum { LCP_XC_LDA = 0, LCP_XC_LSDA = 1 };
+enum { LCP_XC_LDA = 0, LCP_XC_LSDA = 1, LCP_XC_GGA_PBE = 2 };
 /* arithmetic of the pair contractions (density assembly, grid H) */
 enum { LCP_PREC_FP64 = 0, LCP_PREC_FP32 = 1, LCP_PREC_BF16X3 = 2 };
 
@@ -174,6 +174,23 @@ lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn
                            const double* pcc, const double* const* density_grid,
                            double* const* vxc_grid);
 
+/* Calc_Diff_Coef(gLatvecs) (src/XC/GGA_PBE.jl:1-39), the Diff_Coef of
+ * XC_Func("GGA_PBE", ...) (src/XC/XC_Func.jl:87-104): diff_coef[3*27] = the
+ * x, y, z gradient weights of the 27-point stencil for the grid vectors
+ * glatvecs (3x3 row-major, row i = Latvecs row i / Ngrid[i]).  Host only. */
+lcp_status lcp_calc_diff_coef(const double* glatvecs, double* diff_coef);
+
+/* Set_XC_Grid!(xc_func::XC_GGA_PBE, PCCDensity_Grid, Density_Grid)
+ * (src/XC/XC_Func.jl:148-160): Set_dDensity_Grid! then Set_Vxc_GGA_PBE!
+ * (src/XC/GGA_PBE.jl:53-193, 274-462) on the Ngrid grid.  vxc_grid: 1 ("off"),
+ * 2 ("on") or 4 ("nc", which also reads Density_Grid[3:4]) channels.
+ * ddensity_grid and dexc_dgd (each NULL, or 3 pointers per spin, [spin][xyz],
+ * one spin for "off", two otherwise) receive xc_func.dDensity_Grid and
+ * xc_func.dEXC_dGD.  pcc may be NULL (zero). */
+lcp_status lcp_set_xc_grid_gga(lcp_ctx* ctx, int32_t spinpol, const int32_t* ngrid, const double* diff_coef,
+                               const double* pcc, const double* const* density_grid, double* const* vxc_grid,
+                               double* const* ddensity_grid, double* const* dexc_dgd);
+
 /* Set_Vpot_Grid!(xc_func, dVHart_Grid, Vpot_Grid) (src/Matrix/Set_Vpot_Grid.jl:1-19);
  * vna (may be NULL) is added to the spin-diagonal channels. */
 lcp_status lcp_set_vpot_grid(lcp_ctx* ctx, int32_t spinpol, int64_t nn, const double* dvhart,
@@ -204,13 +221,21 @@ lcp_status lcp_calc_eh1(lcp_ctx* ctx, int32_t spinpol, int64_t nn, double gridvo
 lcp_status lcp_calc_exc1(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn, double gridvol,
                          const double* adensity, const double* pcc,
                          const double* const* density, double* exc /* [2] */);
+/* Calc_EXC1(SpinPol, xc_type, system_grid, ...) (src/Energy.jl:669-700) with the
+ * system grid given as Ngrid and Latvecs (3x3 row-major; GridVol = |det| / NN):
+ * every xc type, GGA_PBE included (its energy per particle needs the gradient
+ * stencil, src/XC/XC_Func.jl:193-215). */
+lcp_status lcp_calc_exc1_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, const int32_t* ngrid,
+                              const double* latvecs, double gridvol, const double* adensity, const double* pcc,
+                              const double* const* density, double* exc /* [2] */);
 
 /* ---------------------------------------------------------------- device-resident step */
 
 /* One SCF grid step with all state on the device: density from D, Poisson,
  * xc, potential (+ optional V_na), grid H and the FP64 energy terms.  The
  * inputs adensity/pcc/vna (NN doubles each, may be NULL = zero) are copied at
- * creation. */
+ * creation.  xc: LDA ("off"), LSDA ("on") or GGA_PBE (either; its gradient
+ * stencil comes from the cell's Latvecs and Ngrid). */
 lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
                           int32_t spinpol, int32_t xc, const double* adensity,
                           const double* pcc, const double* vna, lcp_job** out);

@@ -284,7 +284,17 @@ lcp::GridCell job_grid_cell(lcp_job* job) {
   c.dvh = job->dvh.as<double>();
   c.part = job->part.as<double>();
   c.sums = job->scal.as<double>();
+  if (job->xc == LCP_XC_GGA_PBE) {
+    c.dcoef = job->dcoef.as<double>();
+    c.dexc = job->dexc.as<double>();
+  }
   return c;
+}
+
+// gLatvecs: Latvecs rows / Ngrid (src/Energy.jl:676-679)
+static void grid_vectors(const double* lat, const int32_t* ngrid, double gtv[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int d = 0; d < 3; ++d) gtv[i][d] = lat[i * 3 + d] / ngrid[i];
 }
 
 extern "C" {
@@ -985,6 +995,7 @@ lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn
                            const double* const* density_grid, double* const* vxc_grid) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;
+  if (xc == LCP_XC_GGA_PBE) return fail(LCP_EINVAL, "GGA_PBE needs the grid: use lcp_set_xc_grid_gga");
   if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA) return fail(LCP_EINVAL, "please check xc_type name");
   if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol name");
   if ((xc == LCP_XC_LDA) != (spinpol == LCP_SPIN_OFF)) return fail(LCP_EINVAL, "please check xc_type and SpinPol");
@@ -1012,6 +1023,97 @@ lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn
   for (int c = 0; c < nr; ++c)
     API_CUDA(cudaMemcpyAsync(vxc_grid[c], dv[c], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
   API_CUDA(cudaStreamSynchronize(ctx->stream), "xc");
+  return LCP_OK;
+}
+
+lcp_status lcp_calc_diff_coef(const double* glatvecs, double* diff_coef) {
+  if (!glatvecs || !diff_coef) return fail(LCP_EINVAL, "NULL argument");
+  double gtv[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int d = 0; d < 3; ++d) gtv[i][d] = glatvecs[i * 3 + d];
+  if (!lcp::calc_diff_coef(gtv, diff_coef)) return fail(LCP_EINVAL, "singular gradient stencil (check gLatvecs)");
+  return LCP_OK;
+}
+
+// Uploads the GGA inputs into the context's workspaces and fills the cell:
+// rho (1 or 2 spins; "nc" angles into w_in[2..3]), pcc, the stencil weights,
+// the dE/d(grad rho) scratch and, if wanted, the gradient output.
+static lcp_status gga_cell_host(lcp_ctx* ctx, int32_t spinpol, const int32_t* ngrid, const double* dc,
+                                const double* pcc, const double* const* density, bool want_dden, lcp::GridCell& c) {
+  const int64_t nn = (int64_t)ngrid[0] * ngrid[1] * ngrid[2];
+  const int nin = spinpol == LCP_SPIN_OFF ? 1 : (spinpol == LCP_SPIN_ON ? 2 : 4);
+  const int ns = spinpol == LCP_SPIN_OFF ? 1 : 2;
+  c = lcp::GridCell{};
+  for (int d = 0; d < 3; ++d) c.ng[d] = ngrid[d];
+  c.nn = nn;
+  for (int k = 0; k < nin; ++k) {
+    if (!density[k]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[k].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[k].p, density[k], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+  }
+  for (int k = 0; k < ns; ++k) {
+    c.rho[k] = ctx->w_in[k].as<double>();
+    API_CUDA(ctx->w_out[k].ensure(nn * sizeof(double)), "alloc");
+    c.vpot[k] = ctx->w_out[k].as<double>();
+  }
+  if (pcc) {
+    API_CUDA(ctx->w_b.ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_b.p, pcc, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    c.pcc = ctx->w_b.as<double>();
+  }
+  API_CUDA(ctx->w_a.ensure(81 * sizeof(double)), "alloc");
+  API_CUDA(cudaMemcpyAsync(ctx->w_a.p, dc, 81 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  c.dcoef = ctx->w_a.as<double>();
+  API_CUDA(ctx->w_aux[0].ensure((size_t)3 * ns * nn * sizeof(double)), "alloc");
+  c.dexc = ctx->w_aux[0].as<double>();
+  if (want_dden) {
+    API_CUDA(ctx->w_aux[1].ensure((size_t)3 * ns * nn * sizeof(double)), "alloc");
+    c.dden = ctx->w_aux[1].as<double>();
+  }
+  return LCP_OK;
+}
+
+lcp_status lcp_set_xc_grid_gga(lcp_ctx* ctx, int32_t spinpol, const int32_t* ngrid, const double* diff_coef,
+                               const double* pcc, const double* const* density_grid, double* const* vxc_grid,
+                               double* const* ddensity_grid, double* const* dexc_dgd) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol name");
+  if (!ngrid || !diff_coef || !density_grid || !vxc_grid) return fail(LCP_EINVAL, "NULL argument");
+  if (ngrid[0] <= 0 || ngrid[1] <= 0 || ngrid[2] <= 0) return fail(LCP_EINVAL, "Ngrid must be positive");
+  const int64_t nn = (int64_t)ngrid[0] * ngrid[1] * ngrid[2];
+  const int ns = spinpol == LCP_SPIN_OFF ? 1 : 2;
+  const int nv = channels(spinpol);
+  for (int k = 0; k < nv; ++k)
+    if (!vxc_grid[k]) return fail(LCP_EINVAL, "NULL channel");
+  lcp::GridCell c;
+  if ((s = gga_cell_host(ctx, spinpol, ngrid, diff_coef, pcc, density_grid, ddensity_grid != nullptr, c))) return s;
+  API_CUDA(lcp::launch_gga_g(spinpol, c, lcp::GridBatch{}, true, ctx->stream), "gga");
+  ctx->launches += 2;
+  if (spinpol == LCP_SPIN_NC) {
+    for (int k = 2; k < 4; ++k) API_CUDA(ctx->w_out[k].ensure(nn * sizeof(double)), "alloc");
+    double* o[4] = {ctx->w_out[0].as<double>(), ctx->w_out[1].as<double>(), ctx->w_out[2].as<double>(),
+                    ctx->w_out[3].as<double>()};
+    API_CUDA(lcp::launch_gga_nc_rotate(nn, o[0], o[1], ctx->w_in[2].as<double>(), ctx->w_in[3].as<double>(), o,
+                                       ctx->stream),
+             "gga nc");
+    ctx->launches++;
+  }
+  for (int k = 0; k < nv; ++k)
+    API_CUDA(cudaMemcpyAsync(vxc_grid[k], ctx->w_out[k].p, nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H");
+  for (int k = 0; k < 3 * ns; ++k) {
+    if (ddensity_grid && ddensity_grid[k])
+      API_CUDA(cudaMemcpyAsync(ddensity_grid[k], c.dden + k * nn, nn * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->stream),
+               "D2H");
+    if (dexc_dgd && dexc_dgd[k])
+      API_CUDA(cudaMemcpyAsync(dexc_dgd[k], c.dexc + k * nn, nn * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->stream),
+               "D2H");
+  }
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "gga");
   return LCP_OK;
 }
 
@@ -1105,11 +1207,51 @@ lcp_status lcp_calc_exc1(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn, 
                          const double* pcc, const double* const* density, double* exc) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;
+  if (xc == LCP_XC_GGA_PBE) return fail(LCP_EINVAL, "GGA_PBE needs the grid: use lcp_calc_exc1_grid");
   if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA) return fail(LCP_EINVAL, "please check xc_type");
   if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol");
   if (nn <= 0 || !density || !exc) return fail(LCP_EINVAL, "NULL argument");
   double out[3];
   if ((s = energy_host(ctx, xc, spinpol, nn, adensity, pcc, density, nullptr, out))) return s;
+  exc[0] = out[1] * gridvol;
+  exc[1] = out[2] * gridvol;
+  return LCP_OK;
+}
+
+lcp_status lcp_calc_exc1_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, const int32_t* ngrid, const double* latvecs,
+                              double gridvol, const double* adensity, const double* pcc, const double* const* density,
+                              double* exc) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!ngrid || !density || !exc) return fail(LCP_EINVAL, "NULL argument");
+  if (ngrid[0] <= 0 || ngrid[1] <= 0 || ngrid[2] <= 0) return fail(LCP_EINVAL, "Ngrid must be positive");
+  const int64_t nn = (int64_t)ngrid[0] * ngrid[1] * ngrid[2];
+  if (xc != LCP_XC_GGA_PBE) return lcp_calc_exc1(ctx, xc, spinpol, nn, gridvol, adensity, pcc, density, exc);
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol");
+  if (!latvecs) return fail(LCP_EINVAL, "NULL argument");
+  double gtv[3][3], dc[81];
+  grid_vectors(latvecs, ngrid, gtv);
+  if (!lcp::calc_diff_coef(gtv, dc)) return fail(LCP_EINVAL, "singular gradient stencil (check Latvecs)");
+  // Calc_EXC1 reads the two collinear spins only, also for "nc"
+  const int32_t sp = spinpol == LCP_SPIN_OFF ? LCP_SPIN_OFF : LCP_SPIN_ON;
+  lcp::GridCell c;
+  if ((s = gga_cell_host(ctx, sp, ngrid, dc, pcc, density, false, c))) return s;
+  if (adensity) {
+    API_CUDA(ctx->w_aux[2].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_aux[2].p, adensity, nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+    c.aden = ctx->w_aux[2].as<double>();
+  }
+  API_CUDA(ctx->w_part.ensure((size_t)std::max<int64_t>(lcp::red_tiles(nn), 1) * 3 * sizeof(double)), "alloc");
+  API_CUDA(ctx->w_scal.ensure(16 * sizeof(double)), "alloc");
+  c.part = ctx->w_part.as<double>();
+  c.sums = ctx->w_scal.as<double>();
+  API_CUDA(lcp::launch_gga_g(sp, c, lcp::GridBatch{}, false, ctx->stream), "gga energy");
+  API_CUDA(lcp::launch_grid_sums_g(c, lcp::GridBatch{}, ctx->stream), "gga energy sums");
+  ctx->launches += 2;
+  double out[3];
+  API_CUDA(cudaMemcpyAsync(out, ctx->w_scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "gga energy");
   exc[0] = out[1] * gridvol;
   exc[1] = out[2] * gridvol;
   return LCP_OK;
@@ -1126,7 +1268,9 @@ lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* 
   *out = nullptr;
   if (spinpol != LCP_SPIN_OFF && spinpol != LCP_SPIN_ON)
     return fail(LCP_ENOTSUP, "the device-resident step supports SpinPol off/on");
-  if ((xc == LCP_XC_LDA) != (spinpol == LCP_SPIN_OFF)) return fail(LCP_EINVAL, "please check xc_type and SpinPol");
+  if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA && xc != LCP_XC_GGA_PBE) return fail(LCP_EINVAL, "please check xc_type");
+  if (xc != LCP_XC_GGA_PBE && (xc == LCP_XC_LDA) != (spinpol == LCP_SPIN_OFF))
+    return fail(LCP_EINVAL, "please check xc_type and SpinPol");
   const lcp::UCell& u = ucell->u;
   std::unique_ptr<lcp_job> j(new lcp_job());
   j->ucell = ucell;
@@ -1166,6 +1310,15 @@ lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* 
   API_CUDA(j->scal.ensure(16 * sizeof(double)), "alloc");
   API_CUDA(j->pfac.ensure(nspec * sizeof(double)), "alloc");
   API_CUDA(lcp::launch_poisson_table(u.ngrid, j->recvecs, j->pfac.as<double>(), ctx->stream), "poisson table");
+  if (xc == LCP_XC_GGA_PBE) {
+    double gtv[3][3], dc[81];
+    grid_vectors(&u.lat[0][0], u.ngrid, gtv);
+    if (!lcp::calc_diff_coef(gtv, dc)) return fail(LCP_EINVAL, "singular gradient stencil (check Latvecs)");
+    API_CUDA(j->dcoef.ensure(81 * sizeof(double)), "alloc");
+    API_CUDA(j->dexc.ensure((size_t)3 * j->nspin * nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(j->dcoef.p, dc, sizeof dc, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    API_CUDA(cudaStreamSynchronize(ctx->stream), "H2D");  // dc is a stack buffer
+  }
   auto put = [&](DBuf& b, const double* src, bool& flag) -> cudaError_t {
     flag = src != nullptr;
     if (!src) return cudaSuccess;
@@ -1236,8 +1389,13 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   ctx->launches += 2;
   mark(2);
   // 3. xc + potential, with the FP64 energy tile partials in the same pass
-  API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, job->spinpol, gc, one, st), "xc_vpot_energy");
-  ctx->launches++;
+  if (job->xc == LCP_XC_GGA_PBE) {
+    API_CUDA(lcp::launch_gga_g(job->spinpol, gc, one, true, st), "gga");
+    ctx->launches += 2;
+  } else {
+    API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, job->spinpol, gc, one, st), "xc_vpot_energy");
+    ctx->launches++;
+  }
   mark(3);
   // 4. FP64 energy terms: the sums of the tile partials
   API_CUDA(lcp::launch_grid_sums_g(gc, one, st), "energy");
@@ -1305,7 +1463,7 @@ lcp_status lcp_job_footprint(const lcp_job* job, int64_t* bytes) {
     add(job->vpot[c]);
   }
   for (const DBuf* d : {&job->aden, &job->pcc, &job->vna, &job->dvh, &job->real, &job->spec, &job->part, &job->scal,
-                        &job->pfac})
+                        &job->pfac, &job->dcoef, &job->dexc})
     add(*d);
   const lcp_orbs* o = job->orbs;
   for (const DBuf* d : {&o->atv, &o->gxyz, &o->spe, &o->sph_off, &o->glist, &o->clist, &o->phi_off, &o->numorbs,

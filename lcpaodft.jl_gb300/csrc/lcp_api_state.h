@@ -138,6 +138,7 @@ struct lcp_job {
   DBuf dm[4], rho[4], hks[4], vpot[4];
   DBuf aden, pcc, vna, dvh, real, spec, part, scal;
   DBuf pfac;  // Poisson factors of the half spectrum, tabulated at creation
+  DBuf dcoef, dexc;  // GGA_PBE: stencil weights [3][27] and dE/d(grad rho) [spin][xyz][nn]
   bool has_aden = false, has_pcc = false, has_vna = false;
   FftPlans* plans = nullptr;
 };

@@ -145,7 +145,10 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
       return fail(LCP_EDEVICE, "cufftExecZ2D (batched) failed");
   // 3./4. xc + potential + energy partials, then the per-cell sums
   mark(2);
-  API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, st), "batch xc");
+  if (b->xc == LCP_XC_GGA_PBE)
+    API_CUDA(lcp::launch_gga_g(b->spinpol, gnone, pts, true, st), "batch gga");
+  else
+    API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, st), "batch xc");
   mark(3);
   API_CUDA(lcp::launch_grid_sums_g(gnone, per, st), "batch sums");
   mark(4);
@@ -420,8 +423,8 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
   API_CUDA(upload_pod(b->h_start, h_off), "upload");
   // our kernels per step: per channel absmax + pow2 + dsym + density, per
   // channel and wave vweight + H + reduce; once prep, scale, xc, sums, dot,
-  // dot-finish
-  b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 6;
+  // dot-finish (GGA-PBE: xc is two passes)
+  b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 6 + (b->xc == LCP_XC_GGA_PBE ? 1 : 0);
   API_CUDA(cudaDeviceSynchronize(), "batch create");
   *out = b.release();
   return LCP_OK;

@@ -131,6 +131,10 @@ struct GridCell {
   const double* hks[2];
   double* part;          // tile partials: 3 * red_tiles(nn) and red_tiles(hsize) doubles
   double* sums;          // [0..2] grid sums, [3] sum <D,H>, [8..12] the step's energies
+  // GGA-PBE only (nullptr otherwise)
+  const double* dcoef;   // gradient stencil weights [3][27] (Calc_Diff_Coef)
+  double* dexc;          // dE/d(grad rho) scratch: [spin][xyz][nn]
+  double* dden;          // optional output: grad(rho + pcc) as [spin][xyz][nn]
 };
 // cells == nullptr: the single cell passed by value.  Otherwise block g of a
 // tiled launch belongs to the cell c with start[c] <= g < start[c+1], and a
@@ -147,6 +151,14 @@ cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaS
 cudaError_t launch_poisson_table(const int32_t* ngrid, const double* recvecs, double* out, cudaStream_t st);
 // xc + potential + the energy-term tile partials in one pass (tiles of nn)
 cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
+// GGA-PBE pass of the grid step (cells with dcoef/dexc set): gradient + PBE
+// (+ energy tile partials where part is set), then, if potential, the
+// divergence term and, where dvh is set, vpot = dVHart + vxc + V_na (without
+// dvh, vpot receives vxc).  spinpol "off" or "on".
+cudaError_t launch_gga_g(int spinpol, const GridCell& c0, const GridBatch& b, bool potential, cudaStream_t st);
+// The "nc" rotation of GGA potentials into four channels (out[0..1] may be vu/vd).
+cudaError_t launch_gga_nc_rotate(int64_t nn, const double* vu, const double* vd, const double* theta,
+                                 const double* phi, double* const* out, cudaStream_t st);
 // per cell: sums[0..2] from the energy partials
 cudaError_t launch_grid_sums_g(const GridCell& c0, const GridBatch& b, cudaStream_t st);
 // <D,H> tile partials (tiles of hsize), then per cell sums[3] and the energies

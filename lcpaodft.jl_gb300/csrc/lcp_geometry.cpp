@@ -736,4 +736,55 @@ std::string build_bricks(const UCell& u, Bricks& b, const int32_t* shape) {
   return "";
 }
 
+// Row q of inv(M), M[p][q] = x_p^i2 y_p^j2 z_p^k2 with q = 9 i2 + 3 j2 + k2 and
+// p = 9 (i1+1) + 3 (j1+1) + (k1+1), holds the coefficient of monomial q of
+// the fit as weights on the 27 values; rows 9, 3, 1 (the reference's 10, 4, 2)
+// are the x, y and z monomials, i.e. the gradient at the centre.  Gauss-Jordan
+// elimination with partial pivoting on [M | I].
+bool calc_diff_coef(const double gtv[3][3], double out[81]) {
+  constexpr int N = 27;
+  std::vector<double> a((size_t)N * 2 * N, 0.0);
+  auto A = [&](int r, int c) -> double& { return a[(size_t)r * 2 * N + c]; };
+  int p = 0;
+  for (int i1 = -1; i1 <= 1; ++i1)
+    for (int j1 = -1; j1 <= 1; ++j1)
+      for (int k1 = -1; k1 <= 1; ++k1, ++p) {
+        double r[3];
+        for (int d = 0; d < 3; ++d) r[d] = i1 * gtv[0][d] + j1 * gtv[1][d] + k1 * gtv[2][d];
+        int q = 0;
+        for (int i2 = 0; i2 <= 2; ++i2)
+          for (int j2 = 0; j2 <= 2; ++j2)
+            for (int k2 = 0; k2 <= 2; ++k2, ++q) {
+              double m = 1.0;
+              for (int e = 0; e < i2; ++e) m *= r[0];
+              double my = 1.0;
+              for (int e = 0; e < j2; ++e) my *= r[1];
+              double mz = 1.0;
+              for (int e = 0; e < k2; ++e) mz *= r[2];
+              A(p, q) = m * my * mz;
+            }
+        A(p, N + p) = 1.0;
+      }
+  for (int c = 0; c < N; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < N; ++r)
+      if (std::fabs(A(r, c)) > std::fabs(A(piv, c))) piv = r;
+    if (!(std::fabs(A(piv, c)) > 0.0)) return false;
+    if (piv != c)
+      for (int k = 0; k < 2 * N; ++k) std::swap(A(c, k), A(piv, k));
+    const double inv = 1.0 / A(c, c);
+    for (int k = 0; k < 2 * N; ++k) A(c, k) *= inv;
+    for (int r = 0; r < N; ++r) {
+      if (r == c) continue;
+      const double f = A(r, c);
+      if (f == 0.0) continue;
+      for (int k = 0; k < 2 * N; ++k) A(r, k) -= f * A(c, k);
+    }
+  }
+  const int rows[3] = {9, 3, 1};
+  for (int d = 0; d < 3; ++d)
+    for (int k = 0; k < N; ++k) out[d * N + k] = A(rows[d], N + k);
+  return true;
+}
+
 }  // namespace lcp

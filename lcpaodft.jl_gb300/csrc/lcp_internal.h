@@ -127,4 +127,9 @@ void pair_overlap(const UCell& u, int32_t pair, std::vector<int32_t>& g1, std::v
 
 void set_error(const std::string& msg);
 
+// Calc_Diff_Coef (src/XC/GGA_PBE.jl:1-39): the x, y, z first-derivative
+// weights [3][27] of the tri-quadratic fit through the 27 neighbours of a grid
+// point, for grid vectors gtv (rows).  False if the fit matrix is singular.
+bool calc_diff_coef(const double gtv[3][3], double out[81]);
+
 }  // namespace lcp

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(_HERE, "liblcpgrid.so")
 LCP_OK, LCP_EINVAL, LCP_ENOMEM, LCP_EDEVICE, LCP_ETIMEDOUT, LCP_ENOTSUP, LCP_ESTATE = range(7)
 SPIN = {"off": 0, "on": 1, "nc": 2}
 NCHAN = {"off": 1, "on": 2, "nc": 4}
-XC = {"LDA": 0, "LSDA": 1}
+XC = {"LDA": 0, "LSDA": 1, "GGA_PBE": 2}
 PREC = {"fp64": 0, "fp32": 1, "bf16x3": 2}
 
 F_FNAN, F_NATN, F_NCN, F_GRIDN_ATOM, F_GRIDLIST, F_CELLLIST = 0, 1, 2, 3, 4, 5
@@ -80,6 +80,9 @@ _SIGS = {
     "lcp_solve_poisson": ([_vp, _pi32, _pd, _i32, _ppd, _pd, _pd], _i32),
     "lcp_solve_poisson_xyz": ([_vp, _pi32, _pd, _pd, _pd], _i32),
     "lcp_set_xc_grid": ([_vp, _i32, _i32, _i64, _pd, _ppd, _ppd], _i32),
+    "lcp_calc_diff_coef": ([_pd, _pd], _i32),
+    "lcp_set_xc_grid_gga": ([_vp, _i32, _pi32, _pd, _pd, _ppd, _ppd, _ppd, _ppd], _i32),
+    "lcp_calc_exc1_grid": ([_vp, _i32, _i32, _pi32, _pd, _dbl, _pd, _pd, _ppd, _pd], _i32),
     "lcp_set_vpot_grid": ([_vp, _i32, _i64, _pd, _ppd, _pd, _ppd], _i32),
     "lcp_calc_matrix_elements": ([_vp, _vp, _vp, _i32, _ppd, _ppd], _i32),
     "lcp_calc_eh1": ([_vp, _i32, _i64, _dbl, _pd, _ppd, _pd, _pd], _i32),

@@ -14,7 +14,7 @@ from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 
 __all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Batch", "Server",
            "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "Solve_Poisson", "Solve_Poisson_xyz",
-           "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
+           "Calc_Diff_Coef", "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
            "Calc_MatrixElements_dVH_Vxc_nc", "Force3_nospin", "Force3_spin", "Force3_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
 
 
@@ -352,19 +352,35 @@ def Solve_Poisson_xyz(Ngrid, Recvecs, Density_xyz, dVHart_Grid, ctx=None):
     check(lib.lcp_solve_poisson_xyz(ctx._h, iptr(ng), dptr(_f64(Recvecs)), dptr(src), dptr(dVHart_Grid)))
 
 
-class XC_Func:
-    """``XC_Func(xc_type, SpinPol, Nspin, Ngrid)`` for LDA/LSDA
-    (src/XC/XC_Func.jl:47-108)."""
+def _xc_name(xc_type):
+    """xc_type spellings accepted by the reference (src/DFT_Setup.jl:436-447)."""
+    x = xc_type.strip().upper().replace("-", "_")
+    if x in ("GGA", "PBE"):
+        x = "GGA_PBE"
+    if x not in _lib.XC:
+        raise LCPError(_lib.LCP_EINVAL, "please check xc_type name")
+    return x
 
-    def __init__(self, xc_type, SpinPol, Nspin, Ngrid):
-        xc = xc_type.upper()
+
+def Calc_Diff_Coef(gLatvecs):
+    """``Calc_Diff_Coef(gLatvecs)`` (src/XC/GGA_PBE.jl:1-39): the x, y, z
+    weights of the 27-point gradient stencil, as three length-27 arrays."""
+    out = np.zeros(81)
+    check(lib.lcp_calc_diff_coef(dptr(_f64(gLatvecs).reshape(3, 3)), dptr(out)))
+    return [out[0:27].copy(), out[27:54].copy(), out[54:81].copy()]
+
+
+class XC_Func:
+    """``XC_Func(xc_type, SpinPol, Nspin, Ngrid, gLatvecs)``
+    (src/XC/XC_Func.jl:47-108).  GGA_PBE needs gLatvecs (rows Latvecs[i] /
+    Ngrid[i]) for its Diff_Coef and carries dDensity_Grid and dEXC_dGD."""
+
+    def __init__(self, xc_type, SpinPol, Nspin, Ngrid, gLatvecs=None):
+        xc = _xc_name(xc_type)
         sp = SpinPol.lower()
-        if xc not in ("LDA", "LSDA"):
-            raise LCPError(_lib.LCP_ENOTSUP if xc.replace("-", "_") == "GGA_PBE" else _lib.LCP_EINVAL,
-                           "please check xc_type name")
         if sp not in _lib.SPIN:
             raise LCPError(_lib.LCP_EINVAL, "please check SpinPol name")
-        if (xc == "LDA") != (sp == "off"):
+        if xc == "LDA" and sp != "off" or xc == "LSDA" and sp == "off":
             raise LCPError(_lib.LCP_EINVAL, "please check xc_type and SpinPol")
         self.xc_type = xc
         self.SpinPol = sp
@@ -372,10 +388,18 @@ class XC_Func:
         self.Ngrid = tuple(int(x) for x in Ngrid)
         nn = int(np.prod(self.Ngrid))
         self.Vxc_Grid = [np.zeros(nn) for _ in range(_lib.NCHAN[sp])]
+        if xc == "GGA_PBE":
+            if gLatvecs is None:
+                raise LCPError(_lib.LCP_EINVAL, "GGA_PBE needs gLatvecs")
+            self.Diff_Coef = Calc_Diff_Coef(gLatvecs)
+            ns = max(self.Nspin, 1 if sp == "off" else 2)
+            self.dDensity_Grid = [[np.zeros(nn) for _ in range(3)] for _ in range(ns)]
+            self.dEXC_dGD = [[np.zeros(nn) for _ in range(3)] for _ in range(ns)]
 
 
 def Set_XC_Grid(xc_func, PCCDensity_Grid, Density_Grid, ctx=None):
-    """``Set_XC_Grid!`` (src/XC/XC_Func.jl:111-145): fills xc_func.Vxc_Grid."""
+    """``Set_XC_Grid!`` (src/XC/XC_Func.jl:111-160): fills xc_func.Vxc_Grid
+    (and, for GGA_PBE, xc_func.dDensity_Grid and xc_func.dEXC_dGD)."""
     ctx = ctx or default_context()
     n = _lib.NCHAN[xc_func.SpinPol]
     nn = int(np.prod(xc_func.Ngrid))
@@ -383,6 +407,15 @@ def Set_XC_Grid(xc_func, PCCDensity_Grid, Density_Grid, ctx=None):
     pr, k1 = dptrs(rho)
     pv, k2 = dptrs(xc_func.Vxc_Grid)
     pcc = None if PCCDensity_Grid is None else _f64(PCCDensity_Grid)
+    if xc_func.xc_type == "GGA_PBE":
+        ns = 1 if xc_func.SpinPol == "off" else 2
+        ng = np.array(xc_func.Ngrid, dtype=np.int32)
+        dc = _f64(np.concatenate(xc_func.Diff_Coef))
+        pd, k3 = dptrs([xc_func.dDensity_Grid[s][a] for s in range(ns) for a in range(3)])
+        pe, k4 = dptrs([xc_func.dEXC_dGD[s][a] for s in range(ns) for a in range(3)])
+        check(lib.lcp_set_xc_grid_gga(ctx._h, _lib.SPIN[xc_func.SpinPol], iptr(ng), dptr(dc), dptr(pcc), pr, pv,
+                                      pd, pe))
+        return
     check(lib.lcp_set_xc_grid(ctx._h, _lib.XC[xc_func.xc_type], _lib.SPIN[xc_func.SpinPol], nn, dptr(pcc), pr, pv))
 
 
@@ -468,7 +501,8 @@ def Calc_EH1(SpinPol, GridVol, ADensity_Grid, Density_Grid, dVHart_Grid, ctx=Non
 
 
 def Calc_EXC1(SpinPol, xc_type, system_grid, ADensity_Grid, PCCDensity_Grid, Density_Grid, ctx=None):
-    """src/Energy.jl:669-700; ``system_grid`` supplies GridVol (a UCell works)."""
+    """src/Energy.jl:669-700; ``system_grid`` supplies GridVol, and for
+    GGA_PBE also Ngrid and Latvecs (a UCell works)."""
     ctx = ctx or default_context()
     s = _spin(SpinPol)
     nr = 1 if s == "off" else 2
@@ -477,7 +511,14 @@ def Calc_EXC1(SpinPol, xc_type, system_grid, ADensity_Grid, PCCDensity_Grid, Den
     out = np.zeros(2)
     ad = None if ADensity_Grid is None else _f64(ADensity_Grid)
     pcc = None if PCCDensity_Grid is None else _f64(PCCDensity_Grid)
-    check(lib.lcp_calc_exc1(ctx._h, _lib.XC[xc_type.upper()], _lib.SPIN[s], rho[0].size, float(system_grid.GridVol),
+    xc = _xc_name(xc_type)
+    if xc == "GGA_PBE":
+        ng = np.array(system_grid.Ngrid, dtype=np.int32)
+        lat = _f64(system_grid.Latvecs).reshape(3, 3)
+        check(lib.lcp_calc_exc1_grid(ctx._h, _lib.XC[xc], _lib.SPIN[s], iptr(ng), dptr(lat),
+                                     float(system_grid.GridVol), dptr(ad), dptr(pcc), pr, dptr(out)))
+        return out
+    check(lib.lcp_calc_exc1(ctx._h, _lib.XC[xc], _lib.SPIN[s], rho[0].size, float(system_grid.GridVol),
                             dptr(ad), dptr(pcc), pr, dptr(out)))
     return out
 
@@ -502,7 +543,7 @@ class GridStepJob:
         keep = [None if x is None else _f64(x) for x in (ADensity_Grid, PCCDensity_Grid, Vna_Grid)]
         h = ctypes.c_void_p()
         check(lib.lcp_job_create(self.ctx._h, ucell._h, Orbs_Grid._h, _lib.SPIN[self.SpinPol],
-                                 _lib.XC[xc_type.upper()], dptr(keep[0]), dptr(keep[1]), dptr(keep[2]),
+                                 _lib.XC[_xc_name(xc_type)], dptr(keep[0]), dptr(keep[1]), dptr(keep[2]),
                                  ctypes.byref(h)))
         self._h = h
 

@@ -1381,6 +1381,9 @@ def calc_vxc_grid_gga(spinpol, ngrid, pcc, density, diff_coef):
 def glatvecs_of(latvecs, ngrid):
     """gtv of Calc_EXC1 (src/Energy.jl:676-679): Latvecs rows / Ngrid."""
     return _glatvecs(latvecs, ngrid)
+
+
+def grid_energy(spinpol, ucell, dm, H, eh1, exc):
     """Job energy scalar: f_s * sum_s <D_s, H^grid_s> + E_H1 + E_xc1, with f_s = 2
     for "off" (as src/Energy.jl:475-505 doubles the kinetic term) and
     E_xc1 = EXC[1] + EXC[2] with EXC[2] = EXC[1] for "off" (src/Energy.jl:646-648)."""

@@ -10,7 +10,7 @@ import lcpgrid as L
 pytestmark = pytest.mark.gpu
 
 
-def _cells(ctx, spin="off", n_pool=6, seed=91):
+def _cells(ctx, spin="off", n_pool=6, seed=91, xc=None):
     """Small cells of the batching form (1-3 species, cutoffs 6-9 bohr,
     4/9/13/18 orbitals, grids from Calc_Ngrid at 150 Ry) plus two cells that
     share a grid shape (batched FFT plan with two transforms)."""
@@ -30,7 +30,7 @@ def _cells(ctx, spin="off", n_pool=6, seed=91):
     nspin = 2 if spin == "on" else 1
     for k, (u, orbs) in enumerate(cells):
         vna = smooth_vna(u.Ngrid, u.Latvecs, 300 + k)
-        job = L.GridStepJob(u, orbs, spin, "LDA" if spin == "off" else "LSDA", None, None, vna)
+        job = L.GridStepJob(u, orbs, spin, xc or ("LDA" if spin == "off" else "LSDA"), None, None, vna)
         dm = psd_density_matrices(u, 400 + k, nspin=nspin, trace=2.0 * u.Natom)
         job.set_dm(dm)
         jobs.append(job)
@@ -69,6 +69,20 @@ def test_batch_matches_alone(spin):
     _compare(jobs, ref)
     en = b.energies()
     np.testing.assert_array_equal(en, np.array([j.energies() for j in jobs]))
+    b.close()
+
+
+@pytest.mark.parametrize("spin", ["off", "on"])
+def test_batch_gga_matches_alone(spin):
+    """GGA-PBE cells: the gradient/PBE and divergence passes run tiled over
+    every cell of the batch."""
+    ctx = L.Context(0, precision="bf16x3")
+    jobs = _cells(ctx, spin, n_pool=4, seed=23, xc="GGA_PBE")
+    ref = _alone(jobs)
+    b = L.Batch(jobs)
+    b.step(graph=False)
+    b.check_status()
+    _compare(jobs, ref)
     b.close()
 
 

@@ -129,15 +129,16 @@ def test_hamiltonian_bf16x3_si64(ctx):
     assert abs(etc - e64) <= SUM_TOL * abs(e64), (etc, e64)
 
 
-def test_job_energy_bf16x3_si64(ctx):
-    """Grid energy of one full step (rho, Poisson, LDA, H, energies) on the
+@pytest.mark.parametrize("xc", ["LDA", "GGA_PBE"])
+def test_job_energy_bf16x3_si64(ctx, xc):
+    """Grid energy of one full step (rho, Poisson, xc, H, energies) on the
     64-atom 96^3 cell: split-BF16 contractions vs FP64, <= 1 uHa/atom."""
     u, orbs, dm, vna = _si64(ctx)
     E = {}
     for prec in ("fp64", "bf16x3"):
         ctx.set_precision(prec)
         try:
-            job = L.GridStepJob(u, orbs, "off", "LDA", None, None, vna)
+            job = L.GridStepJob(u, orbs, "off", xc, None, None, vna)
             job.set_dm(dm)
             job.step()
             E[prec] = job.energies()[4]
