@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--serving", action="store_true", help="run the serving form instead of the step bench")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section of the step bench line")
     ap.add_argument("--no-force", action="store_true", help="skip the grid force term section of the step bench line")
+    ap.add_argument("--no-gga", action="store_true", help="skip the GGA-PBE section of the step bench line")
     ap.add_argument("--serve-structures", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-rate", type=float, default=400.0, help="offered Poisson rate, jobs/s")
@@ -190,6 +191,49 @@ def force3_section(wl, u, dm, vna, reps=5):
                          "peak_source": "probe: FP64 FMA loop on this GPU",
                          "note": "end to end: includes the host copies of V and D (%.0f MB)"
                                  % (len(dm) * (u.NN + u.Total_Hsize) * 8 / 1e6)}}
+
+
+def gga_section(wl, u, orbs, dm, vna, steps=10):
+    """The same step with GGA-PBE as its xc (the gradient stencil + PBE pass
+    and the divergence pass replace the LDA pass), split-BF16 and FP64, and
+    the oracle's GGA pass on the same density for the CPU side."""
+    import numpy as np
+
+    import lcpgrid as L
+    from oracle import lcp_oracle as O
+    spin = wl.get("spinpol", "off")
+    out = {}
+    rho = None
+    ctx = orbs.ctx
+    keep = ctx.precision
+    try:
+        for prec in ("bf16x3", "fp64"):
+            ctx.set_precision(prec)
+            job = L.GridStepJob(u, orbs, spin, "GGA_PBE", None, None, vna)
+            job.set_dm(dm)
+            for _ in range(3):
+                job.step()
+            st = np.array([job.step_timed() for _ in range(steps if prec == "bf16x3" else 2)])
+            med = np.median(st, axis=0)
+            out[prec] = {"ms_per_step": float(med.sum()), "xc_pass_ms": float(med[2]),
+                         "stage_ms": [float(x) for x in med], "E_grid": float(job.energies()[4])}
+            if prec == "fp64":
+                rho = [x.copy() for x in job.density()]
+    finally:
+        ctx.set_precision(keep)
+    out["err_per_atom_uHa"] = abs(out["bf16x3"]["E_grid"] - out["fp64"]["E_grid"]) / wl["natom"] * 1e6
+    out["points_per_s_xc_pass"] = float(u.NN / (out["bf16x3"]["xc_pass_ms"] * 1e-3))
+    # the oracle's GGA pass (gradient, PBE, divergence) on one thread, same grid
+    gl = O.glatvecs_of(np.asarray(wl["latvecs"], dtype=np.float64), u.Ngrid)
+    t0 = time.perf_counter()
+    O.set_xc_grid_gga(spin, u.Ngrid, None, rho, O.calc_diff_coef(gl))
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": cpu_s * 1e3, "unit": "ms per GGA xc pass", "cores": 1, "kind": "port",
+                           "sample": "the oracle's gradient + PBE + divergence pass on the same %dx%dx%d density"
+                                     % tuple(u.Ngrid)}
+    out["roofline"] = {"bound": "fp64-alu", "note": "the PBE pass issues FP64 instructions at 87% of the FP64 "
+                       "pipe's peak and the divergence pass at 76% (ncu); DRAM traffic is a few bytes per point"}
+    return out
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)
@@ -466,6 +510,11 @@ def run_ours(args):
             line["force3"] = force3_section(wl, u, dm, vna)
         except Exception as exc:  # the force section must not hide the step line
             line["force3"] = {"error": repr(exc)}
+    if rank == 0 and not args.no_gga and world == 1:
+        try:
+            line["gga_pbe"] = gga_section(wl, u, orbs, dm, vna)
+        except Exception as exc:  # the GGA section must not hide the step line
+            line["gga_pbe"] = {"error": repr(exc)}
     if rank == 0 and not args.no_serving and world == 1:
         # the serving form on the same GPU: Poisson stream of mixed-size structures
         try:

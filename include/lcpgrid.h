@@ -174,6 +174,12 @@ lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn
                            const double* pcc, const double* const* density_grid,
                            double* const* vxc_grid);
 
+/* diagonalize_nc_density!(Density_Grid) (src/Matrix/Set_Density_Grid.jl:243-261):
+ * the four "nc" channels (Re11, Re22, Re12, Im12), host arrays of nn doubles,
+ * become (Nup, Ndown, theta, phi) in place (EulerAngle_Spin,
+ * src/utils/EulerAngle_Spin.jl:1-6). */
+lcp_status lcp_diagonalize_nc_density(lcp_ctx* ctx, int64_t nn, double* const* density_grid);
+
 /* Calc_Diff_Coef(gLatvecs) (src/XC/GGA_PBE.jl:1-39), the Diff_Coef of
  * XC_Func("GGA_PBE", ...) (src/XC/XC_Func.jl:87-104): diff_coef[3*27] = the
  * x, y, z gradient weights of the 27-point stencil for the grid vectors
@@ -234,8 +240,11 @@ lcp_status lcp_calc_exc1_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, const i
 /* One SCF grid step with all state on the device: density from D, Poisson,
  * xc, potential (+ optional V_na), grid H and the FP64 energy terms.  The
  * inputs adensity/pcc/vna (NN doubles each, may be NULL = zero) are copied at
- * creation.  xc: LDA ("off"), LSDA ("on") or GGA_PBE (either; its gradient
- * stencil comes from the cell's Latvecs and Ngrid). */
+ * creation.  xc: LDA ("off"), LSDA ("on", "nc") or GGA_PBE (any; its
+ * gradient stencil comes from the cell's Latvecs and Ngrid).  "nc" carries
+ * four DM/density/potential/H channels: the density is diagonalized
+ * (diagonalize_nc_density!) before Poisson and xc, as src/KSsolve_SCF.jl:252-255
+ * does, and the xc potentials are rotated into the four channels. */
 lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
                           int32_t spinpol, int32_t xc, const double* adensity,
                           const double* pcc, const double* vna, lcp_job** out);

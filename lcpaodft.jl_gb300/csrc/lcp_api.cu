@@ -272,7 +272,7 @@ lcp::GridCell job_grid_cell(lcp_job* job) {
   c.aden = job->has_aden ? job->aden.as<double>() : nullptr;
   c.pcc = job->has_pcc ? job->pcc.as<double>() : nullptr;
   c.vna = job->has_vna ? job->vna.as<double>() : nullptr;
-  for (int s = 0; s < job->nspin && s < 2; ++s) {
+  for (int s = 0; s < job->nspin && s < 4; ++s) {
     c.rho[s] = job->rho[s].as<double>();
     c.vpot[s] = job->vpot[s].as<double>();
     c.dm[s] = job->dm[s].as<double>();
@@ -1026,6 +1026,26 @@ lcp_status lcp_set_xc_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, int64_t nn
   return LCP_OK;
 }
 
+lcp_status lcp_diagonalize_nc_density(lcp_ctx* ctx, int64_t nn, double* const* density_grid) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (nn <= 0 || !density_grid) return fail(LCP_EINVAL, "NULL argument");
+  double* d[4];
+  for (int c = 0; c < 4; ++c) {
+    if (!density_grid[c]) return fail(LCP_EINVAL, "NULL channel");
+    API_CUDA(ctx->w_in[c].ensure(nn * sizeof(double)), "alloc");
+    API_CUDA(cudaMemcpyAsync(ctx->w_in[c].p, density_grid[c], nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+             "H2D");
+    d[c] = ctx->w_in[c].as<double>();
+  }
+  API_CUDA(lcp::launch_nc_diagonalize(nn, d, ctx->stream), "nc diagonalize");
+  ctx->launches++;
+  for (int c = 0; c < 4; ++c)
+    API_CUDA(cudaMemcpyAsync(density_grid[c], d[c], nn * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "nc diagonalize");
+  return LCP_OK;
+}
+
 lcp_status lcp_calc_diff_coef(const double* glatvecs, double* diff_coef) {
   if (!glatvecs || !diff_coef) return fail(LCP_EINVAL, "NULL argument");
   double gtv[3][3];
@@ -1095,8 +1115,8 @@ lcp_status lcp_set_xc_grid_gga(lcp_ctx* ctx, int32_t spinpol, const int32_t* ngr
     for (int k = 2; k < 4; ++k) API_CUDA(ctx->w_out[k].ensure(nn * sizeof(double)), "alloc");
     double* o[4] = {ctx->w_out[0].as<double>(), ctx->w_out[1].as<double>(), ctx->w_out[2].as<double>(),
                     ctx->w_out[3].as<double>()};
-    API_CUDA(lcp::launch_gga_nc_rotate(nn, o[0], o[1], ctx->w_in[2].as<double>(), ctx->w_in[3].as<double>(), o,
-                                       ctx->stream),
+    API_CUDA(lcp::launch_nc_rotate(nn, o[0], o[1], ctx->w_in[2].as<double>(), ctx->w_in[3].as<double>(), -1.0, o,
+                                   ctx->stream),
              "gga nc");
     ctx->launches++;
   }
@@ -1266,8 +1286,7 @@ lcp_status lcp_job_create(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* 
   if ((s = check_pair(ucell, orbs))) return s;
   if (!out) return fail(LCP_EINVAL, "NULL argument");
   *out = nullptr;
-  if (spinpol != LCP_SPIN_OFF && spinpol != LCP_SPIN_ON)
-    return fail(LCP_ENOTSUP, "the device-resident step supports SpinPol off/on");
+  if (spinpol < LCP_SPIN_OFF || spinpol > LCP_SPIN_NC) return fail(LCP_EINVAL, "please check SpinPol");
   if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA && xc != LCP_XC_GGA_PBE) return fail(LCP_EINVAL, "please check xc_type");
   if (xc != LCP_XC_GGA_PBE && (xc == LCP_XC_LDA) != (spinpol == LCP_SPIN_OFF))
     return fail(LCP_EINVAL, "please check xc_type and SpinPol");
@@ -1374,6 +1393,11 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   // 1. density
   mark(0);
   if ((s = density_device(ctx, job->orbs, ns, dm, rho, job->nn))) return s;
+  if (job->spinpol == LCP_SPIN_NC) {
+    // diagonalize_nc_density! (src/KSsolve_SCF.jl:252-255): rho[0..3] become Nup, Ndown, theta, phi
+    API_CUDA(lcp::launch_nc_diagonalize(job->nn, rho, st), "nc diagonalize");
+    ctx->launches++;
+  }
   mark(1);
   // 2. Poisson
   API_CUDA(lcp::launch_poisson_prep_g(job->spinpol, gc, one, st), "poisson_prep");
@@ -1389,11 +1413,22 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   ctx->launches += 2;
   mark(2);
   // 3. xc + potential, with the FP64 energy tile partials in the same pass
+  // ("nc": the collinear pass on (Nup, Ndown), then the rotation into four channels)
+  const int32_t sp_xc = job->spinpol == LCP_SPIN_NC ? LCP_SPIN_ON : job->spinpol;
   if (job->xc == LCP_XC_GGA_PBE) {
-    API_CUDA(lcp::launch_gga_g(job->spinpol, gc, one, true, st), "gga");
+    API_CUDA(lcp::launch_gga_g(sp_xc, gc, one, true, st), "gga");
     ctx->launches += 2;
   } else {
-    API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, job->spinpol, gc, one, st), "xc_vpot_energy");
+    API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, sp_xc, gc, one, st), "xc_vpot_energy");
+    ctx->launches++;
+  }
+  if (job->spinpol == LCP_SPIN_NC) {
+    // dVHart + V_na is common to both diagonal channels and drops out of tmp1
+    double* vp[4] = {job->vpot[0].as<double>(), job->vpot[1].as<double>(), job->vpot[2].as<double>(),
+                     job->vpot[3].as<double>()};
+    API_CUDA(lcp::launch_nc_rotate(job->nn, vp[0], vp[1], rho[2], rho[3], job->xc == LCP_XC_GGA_PBE ? -1.0 : 1.0, vp,
+                                   st),
+             "nc rotate");
     ctx->launches++;
   }
   mark(3);

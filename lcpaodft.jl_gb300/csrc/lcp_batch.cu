@@ -193,6 +193,7 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
   for (int k = 0; k < njobs; ++k) {
     lcp_job* j = jobs[k];
     if (!j) return fail(LCP_EINVAL, "lcp_batch_create: NULL job");
+    if (j->spinpol == LCP_SPIN_NC) return fail(LCP_ENOTSUP, "the batched step supports SpinPol off/on");
     if (k == 0) {
       b->spinpol = j->spinpol;
       b->xc = j->xc;

@@ -121,14 +121,14 @@ struct GridCell {
   const double* aden;    // atomic density or nullptr
   const double* pcc;     // partial core correction or nullptr
   const double* vna;     // neutral-atom potential or nullptr
-  const double* rho[2];
+  const double* rho[4];  // [2..3]: the "nc" angles theta, phi after diagonalize_nc_density!
   double* real;          // Poisson source (nn)
   void* spec;            // its half spectrum (ng0 * ng1 * (ng2/2+1) complex)
   const double* pfac;    // tabulated Poisson factors of the half spectrum, or nullptr
   const double* dvh;     // Hartree potential (nn)
-  double* vpot[2];
-  const double* dm[2];
-  const double* hks[2];
+  double* vpot[4];
+  const double* dm[4];
+  const double* hks[4];
   double* part;          // tile partials: 3 * red_tiles(nn) and red_tiles(hsize) doubles
   double* sums;          // [0..2] grid sums, [3] sum <D,H>, [8..12] the step's energies
   // GGA-PBE only (nullptr otherwise)
@@ -156,9 +156,14 @@ cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, con
 // divergence term and, where dvh is set, vpot = dVHart + vxc + V_na (without
 // dvh, vpot receives vxc).  spinpol "off" or "on".
 cudaError_t launch_gga_g(int spinpol, const GridCell& c0, const GridBatch& b, bool potential, cudaStream_t st);
-// The "nc" rotation of GGA potentials into four channels (out[0..1] may be vu/vd).
-cudaError_t launch_gga_nc_rotate(int64_t nn, const double* vu, const double* vd, const double* theta,
-                                 const double* phi, double* const* out, cudaStream_t st);
+// "nc": diagonalize_nc_density! in place, (Re11, Re22, Re12, Im12) -> (Nup,
+// Ndown, theta, phi), and the rotation of collinear potentials (vu, vd) into
+// the four channels by the local angles; out[0..1] may be vu/vd.  sign3 is the
+// sign of the third channel's tmp1 sin(theta) cos(phi): +1 for LDA/LSDA
+// (src/XC/XC_Func.jl:130-142), -1 for GGA-PBE (src/XC/GGA_PBE.jl:174-192).
+cudaError_t launch_nc_diagonalize(int64_t nn, double* const* rho, cudaStream_t st);
+cudaError_t launch_nc_rotate(int64_t nn, const double* vu, const double* vd, const double* theta, const double* phi,
+                             double sign3, double* const* out, cudaStream_t st);
 // per cell: sums[0..2] from the energy partials
 cudaError_t launch_grid_sums_g(const GridCell& c0, const GridBatch& b, cudaStream_t st);
 // <D,H> tile partials (tiles of hsize), then per cell sums[3] and the energies

@@ -394,25 +394,6 @@ __global__ void __launch_bounds__(kRedThreads) gga_div_g_kernel(const __grid_con
   }
 }
 
-// "nc" (src/XC/GGA_PBE.jl:174-192): rotate the up/down potentials by the
-// local spin angles into the four channels.
-// Each point's inputs are read before its outputs are written, so o0/o1 may
-// be the vu/vd buffers.
-__global__ void gga_nc_rotate_kernel(int64_t nn, const double* vu, const double* vd, const double* theta,
-                                     const double* phi, double* o0, double* o1, double* o2, double* o3) {
-  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nn; x += (int64_t)gridDim.x * blockDim.x) {
-    const double tmp0 = 0.5 * (vu[x] + vd[x]);
-    const double tmp1 = 0.5 * (vu[x] - vd[x]);
-    double sit, cot, sip, cop;
-    sincos(theta[x], &sit, &cot);
-    sincos(phi[x], &sip, &cop);
-    o3[x] = -tmp1 * sit * sip;
-    o2[x] = -tmp1 * sit * cop;
-    o1[x] = tmp0 - cot * tmp1;
-    o0[x] = tmp0 + cot * tmp1;
-  }
-}
-
 }  // namespace
 
 cudaError_t launch_gga_g(int spinpol, const GridCell& c0, const GridBatch& b, bool potential, cudaStream_t st) {
@@ -431,13 +412,6 @@ cudaError_t launch_gga_g(int spinpol, const GridCell& c0, const GridBatch& b, bo
     LCP_CUDA_TRY(cudaGetLastError());
     if (potential) gga_div_g_kernel<false><<<(unsigned)n, kRedThreads, 0, st>>>(a);
   }
-  return cudaGetLastError();
-}
-
-cudaError_t launch_gga_nc_rotate(int64_t nn, const double* vu, const double* vd, const double* theta,
-                                 const double* phi, double* const* out, cudaStream_t st) {
-  const int64_t b = std::max<int64_t>(1, std::min<int64_t>((nn + 255) / 256, 152 * 32));
-  gga_nc_rotate_kernel<<<(unsigned)b, 256, 0, st>>>(nn, vu, vd, theta, phi, out[0], out[1], out[2], out[3]);
   return cudaGetLastError();
 }
 

@@ -185,6 +185,57 @@ __global__ void vpot_kernel(VpotArgs a) {
   }
 }
 
+// ------------------------------------------------------------ "nc" channels
+
+// diagonalize_nc_density! (src/Matrix/Set_Density_Grid.jl:243-261): per point
+// EulerAngle_Spin (src/utils/EulerAngle_Spin.jl:1-6) of the spin density
+// matrix, through xyz_to_spherical (src/utils/xyz_to_spherical.jl:1-31) of
+// (2 Re12, -2 Im12, Re11 - Re22).
+__global__ void nc_diagonalize_kernel(int64_t nn, double* __restrict__ d0, double* __restrict__ d1,
+                                      double* __restrict__ d2, double* __restrict__ d3) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+    const double re11 = d0[i], re22 = d1[i], re12 = d2[i], im12 = d3[i];
+    const double x = 2 * re12, y = -2 * im12, z = re11 - re22;
+    // each product and sum rounded on its own (no FMA contraction), as the
+    // reference evaluates them: theta = acos(z/r) amplifies a 1-ulp change
+    // of r near the poles to ~1e-8
+    const double dum = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+    const double r = sqrt(__dadd_rn(dum, __dmul_rn(z, z)));
+    const double r1 = sqrt(dum);
+    double theta = 0.5 * kPi, phi = 0.0;
+    if (1e-14 <= r) {
+      const double c = r < fabs(z) ? (z > 0 ? 1.0 : (z < 0 ? -1.0 : 0.0)) : z / r;
+      theta = acos(c);
+      if (1e-14 <= r1) {
+        const double sy = r1 < fabs(y) ? (y > 0 ? 1.0 : (y < 0 ? -1.0 : 0.0)) : y / r1;
+        phi = x >= 0.0 ? asin(sy) : kPi - asin(sy);
+      }
+    }
+    d0[i] = 0.5 * __dadd_rn(__dadd_rn(re11, re22), r);
+    d1[i] = 0.5 * __dadd_rn(__dadd_rn(re11, re22), -r);
+    d2[i] = theta;
+    d3[i] = phi;
+  }
+}
+
+// The "nc" potentials from the collinear pair (vu, vd) and the local angles;
+// each point's inputs are read before its outputs are written, so out[0..1]
+// may be the vu/vd buffers.
+__global__ void nc_rotate_kernel(int64_t nn, const double* vu, const double* vd, const double* theta,
+                                 const double* phi, double sign3, double* o0, double* o1, double* o2, double* o3) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nn; x += (int64_t)gridDim.x * blockDim.x) {
+    const double tmp0 = 0.5 * (vu[x] + vd[x]);
+    const double tmp1 = 0.5 * (vu[x] - vd[x]);
+    double sit, cot, sip, cop;
+    sincos(theta[x], &sit, &cot);
+    sincos(phi[x], &sip, &cop);
+    o3[x] = -tmp1 * sit * sip;
+    o2[x] = sign3 * tmp1 * sit * cop;
+    o1[x] = tmp0 - cot * tmp1;
+    o0[x] = tmp0 + cot * tmp1;
+  }
+}
+
 struct EnergyArgs {
   int xc, spinpol;
   int64_t nn;
@@ -462,6 +513,18 @@ cudaError_t launch_energy_sums(int xc, int spinpol, int64_t nn, const double* ad
   energy_partials_kernel<<<(unsigned)nt, kRedThreads, 0, st>>>(a);
   LCP_CUDA_TRY(cudaGetLastError());
   finish_sums_kernel<3><<<1, kRedThreads, 0, st>>>(partials, nt, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nc_diagonalize(int64_t nn, double* const* rho, cudaStream_t st) {
+  nc_diagonalize_kernel<<<grid_blocks(nn, 256), 256, 0, st>>>(nn, rho[0], rho[1], rho[2], rho[3]);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nc_rotate(int64_t nn, const double* vu, const double* vd, const double* theta, const double* phi,
+                             double sign3, double* const* out, cudaStream_t st) {
+  nc_rotate_kernel<<<grid_blocks(nn, 256), 256, 0, st>>>(nn, vu, vd, theta, phi, sign3, out[0], out[1], out[2],
+                                                         out[3]);
   return cudaGetLastError();
 }
 

@@ -80,6 +80,7 @@ _SIGS = {
     "lcp_solve_poisson": ([_vp, _pi32, _pd, _i32, _ppd, _pd, _pd], _i32),
     "lcp_solve_poisson_xyz": ([_vp, _pi32, _pd, _pd, _pd], _i32),
     "lcp_set_xc_grid": ([_vp, _i32, _i32, _i64, _pd, _ppd, _ppd], _i32),
+    "lcp_diagonalize_nc_density": ([_vp, _i64, _ppd], _i32),
     "lcp_calc_diff_coef": ([_pd, _pd], _i32),
     "lcp_set_xc_grid_gga": ([_vp, _i32, _pi32, _pd, _pd, _ppd, _ppd, _ppd, _ppd], _i32),
     "lcp_calc_exc1_grid": ([_vp, _i32, _i32, _pi32, _pd, _dbl, _pd, _pd, _ppd, _pd], _i32),

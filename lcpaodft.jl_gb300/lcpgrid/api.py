@@ -13,7 +13,7 @@ from . import _lib
 from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 
 __all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Batch", "Server",
-           "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "Solve_Poisson", "Solve_Poisson_xyz",
+           "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "diagonalize_nc_density", "Solve_Poisson", "Solve_Poisson_xyz",
            "Calc_Diff_Coef", "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
            "Calc_MatrixElements_dVH_Vxc_nc", "Force3_nospin", "Force3_spin", "Force3_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
 
@@ -318,6 +318,21 @@ def Set_Density_Grid(SpinPol, ucell, Orbs_Grid, DM, Density_Grid):
     pdm, k1 = dptrs(dm)
     pr, k2 = dptrs([Density_Grid[c] for c in range(n)])
     check(lib.lcp_set_density_grid(Orbs_Grid.ctx._h, ucell._h, Orbs_Grid._h, _lib.SPIN[s], pdm, pr))
+
+
+def diagonalize_nc_density(Density_Grid, ctx=None):
+    """``diagonalize_nc_density!`` (src/Matrix/Set_Density_Grid.jl:243-261):
+    the four "nc" channels (Re11, Re22, Re12, Im12) become (Nup, Ndown,
+    theta, phi) in place."""
+    ctx = ctx or default_context()
+    for c in range(4):
+        if Density_Grid[c].dtype != np.float64 or not Density_Grid[c].flags["C_CONTIGUOUS"]:
+            raise TypeError("Density_Grid must hold C-contiguous float64 arrays")
+    nn = Density_Grid[0].size
+    if any(Density_Grid[c].size != nn for c in range(4)):
+        raise LCPError(_lib.LCP_EINVAL, "Density_Grid channels differ in size")
+    p, keep = dptrs([Density_Grid[c] for c in range(4)])
+    check(lib.lcp_diagonalize_nc_density(ctx._h, nn, p))
 
 
 class Rhor_Mixing:

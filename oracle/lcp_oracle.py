@@ -1053,6 +1053,15 @@ def lsda_ca(up, down, switch):
     return o1, o2
 
 
+def diagonalize_nc_density(density):
+    """diagonalize_nc_density! (src/Matrix/Set_Density_Grid.jl:243-261) with
+    EulerAngle_Spin (src/utils/EulerAngle_Spin.jl:1-6): (Re11, Re22, Re12,
+    Im12) -> (Nup, Ndown, theta, phi), returned as new arrays."""
+    re11, re22, re12, im12 = (np.asarray(d, dtype=np.float64) for d in density[:4])
+    r, theta, ph = xyz_to_spherical(2 * re12, -2 * im12, re11 - re22)
+    return [0.5 * (re11 + re22 + r), 0.5 * (re11 + re22 - r), theta, ph]
+
+
 def set_xc_grid(xc_type, spinpol, pcc, density):
     """V_xc on the grid (src/XC/XC_Func.jl:111-145)."""
     if xc_type == "LDA":
@@ -1384,11 +1393,12 @@ def glatvecs_of(latvecs, ngrid):
 
 
 def grid_energy(spinpol, ucell, dm, H, eh1, exc):
-    """Job energy scalar: f_s * sum_s <D_s, H^grid_s> + E_H1 + E_xc1, with f_s = 2
+    """Job energy scalar: f_s * sum_s <D_s, H^grid_s> + E_H1 + E_xc1 (the sum over
+    all channels, four for "nc"), with f_s = 2
     for "off" (as src/Energy.jl:475-505 doubles the kinetic term) and
     E_xc1 = EXC[1] + EXC[2] with EXC[2] = EXC[1] for "off" (src/Energy.jl:646-648)."""
     fs = 2.0 if spinpol == "off" else 1.0
-    nspin = 1 if spinpol == "off" else 2
+    nspin = {"off": 1, "on": 2, "nc": 4}[spinpol]
     e_dh = sum(float(np.dot(dm[s], H[s])) for s in range(nspin))
     e_xc = exc[0] + (exc[0] if spinpol == "off" else exc[1])
     return fs * e_dh + eh1 + e_xc

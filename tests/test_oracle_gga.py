@@ -120,3 +120,24 @@ def test_exc1_gga_matches_energy():
     temp = aden + pcc
     want = (_energy("on", dc, pcc, dens) - 2 * np.sum(temp * o.lda_ca(2 * temp, 0))) * gridvol
     assert abs(exc[0] + exc[1] - want) <= 1e-12 * abs(want)
+
+
+def test_diagonalize_nc_density_invariants():
+    """Nup, Ndown are the eigenvalues of the 2x2 spin density matrix
+    [[Re11, Re12 + i Im12], [Re12 - i Im12, Re22]] and the angles give its
+    spin direction (2 Re12, -2 Im12, Re11 - Re22) / r."""
+    rng = np.random.default_rng(6)
+    n = 500
+    d = [rng.uniform(0, 0.3, n), rng.uniform(0, 0.3, n), rng.normal(0, 0.05, n), rng.normal(0, 0.05, n)]
+    d[2][:5] = 0.0
+    d[3][:5] = 0.0  # collinear points: phi = 0
+    d[0][5:8] = d[1][5:8]
+    d[2][5:8] = 0.0
+    d[3][5:8] = 0.0  # no spin at all: r = 0, theta = pi/2, phi = 0
+    nu, nd, th, ph = o.diagonalize_nc_density(d)
+    np.testing.assert_allclose(nu + nd, d[0] + d[1], rtol=1e-14)
+    np.testing.assert_allclose(nu * nd, d[0] * d[1] - d[2] ** 2 - d[3] ** 2, rtol=1e-12, atol=1e-16)
+    r = nu - nd
+    m = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)])
+    np.testing.assert_allclose(m, np.stack([2 * d[2], -2 * d[3], d[0] - d[1]]), atol=1e-14)
+    assert np.all(ph[:5] == 0.0) and np.all(th[5:8] == 0.5 * np.pi) and np.all(ph[5:8] == 0.0)
