@@ -124,6 +124,17 @@ lcp_status lcp_ucell_get_bricks(const lcp_ucell* ucell, int64_t* info);
 lcp_status lcp_brick_shape_candidates(const lcp_ucell* ucell, int32_t max, int32_t* shapes, double* cost,
                                       int32_t* n);
 
+/* UCell(...) with Calc_AtomsGrid and Calc_AtomOverlap_Grid (src/UCell.jl:297-516)
+ * run on the context's GPU: the same object as lcp_ucell_create, with the
+ * same lists bit for bit.  LCP_ENOTSUP when an atom's grid box reaches image
+ * cells outside -CpyCell..CpyCell-1 (where the reference's Find_CGrids!
+ * leaves its table or takes its out-of-range branch); lcp_ucell_create
+ * handles those cells. */
+lcp_status lcp_ucell_create_device(lcp_ctx* ctx, int32_t nspin, const double* latvecs, int32_t natom,
+                                   const int32_t* atom2spe, const double* gxyz, const double* atoms_cut1,
+                                   const int32_t* ngrid, const double* grid_origin, const int32_t* total_numorbs,
+                                   lcp_ucell** out);
+
 /* Calc_Ngrid(Ecut, Latvecs) -- src/utils/Calc_Ngrid.jl:1-76 */
 lcp_status lcp_calc_ngrid(double ecut, const double* latvecs, int32_t* ngrid_out);
 
@@ -150,6 +161,27 @@ void lcp_orbs_destroy(lcp_orbs* orbs);
  * PackedOrbitalsGrid.data[atom]).  component: 0 = phi, 1..3 = d/dx, d/dy, d/dz. */
 lcp_status lcp_orbs_download(lcp_ctx* ctx, const lcp_orbs* orbs, int32_t component,
                              int32_t atom, double* dst, int64_t count);
+
+/* A radial table on a log mesh, as KumoF reads it (src/utils/KumoF.jl). */
+typedef struct {
+  int32_t num_mesh;  /* mesh points (>= 8) */
+  const double* xv;  /* log radii (Spe_PAO_XV / Spe_VPS_XV) */
+  const double* rv;  /* radii (Spe_PAO_RV / Spe_VPS_RV) */
+  const double* yv;  /* values in the (num_mesh + 4)-long layout (Spe_Atomic_Den / Spe_Atomic_PCC) */
+} lcp_radial;
+
+/* Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, ucell)
+ * (src/Matrix/Set_AdenPCC_Grid.jl:1-142) on the device: the atomic density,
+ * the partial-core density and the initial Density_Grid (1, 2 or 4 channels).
+ * init_atoms_nspin[atom*2 + {0,1}] = (Nu, Nd); init_atoms_angle[atom*2 + {0,1}]
+ * = (theta, phi), read for "nc" only (may be NULL otherwise).  atomic_den[spe]
+ * and atomic_pcc[spe] are the species' tables (atom2spe, 1-based).  Outputs
+ * are host arrays of NN doubles; every point sums its atoms' terms in the
+ * reference's order. */
+lcp_status lcp_set_adenpcc_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t spinpol,
+                                const double* init_atoms_nspin, const double* init_atoms_angle, int32_t nspecies,
+                                const lcp_radial* atomic_den, const lcp_radial* atomic_pcc, double* adensity_grid,
+                                double* pccdensity_grid, double* const* density_grid);
 
 /* Set_Density_Grid!(SpinPol, ucell, Orbs_Grid, DM, Density_Grid)
  * (src/Matrix/Set_Density_Grid.jl:1-304).  dm[s]: Total_Hsize doubles;

@@ -104,12 +104,11 @@ struct AtomSphere {
   bool any = false;
 };
 
-// Calc_AtomsGrid for one atom (src/UCell.jl:333-400).  `carry` is the Cxyz
-// left by the previous atom (Find_CGrids! keeps it across calls).
-void atom_sphere(const UCell& u, int a, const double carry[3], AtomSphere& out) {
-  const int N1 = u.ngrid[0], N2 = u.ngrid[1], N3 = u.ngrid[2];
-  const int C = u.cpycell;
-  const int n = 2 * C + 1;
+}  // namespace
+
+// The grid-index box [nmin, nmax] that Calc_AtomsGrid scans for one atom
+// (src/UCell.jl:333-364).
+void atom_box(const UCell& u, int a, int nmin[3], int nmax[3]) {
   double gT[3][3], grec[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) gT[i][j] = u.glat[j][i];
@@ -120,7 +119,6 @@ void atom_sphere(const UCell& u, int a, const double carry[3], AtomSphere& out) 
   const double Gx = u.gxyz[a * 3], Gy = u.gxyz[a * 3 + 1], Gz = u.gxyz[a * 3 + 2];
   const double* L = &u.lat[0][0];
   double rc5 = u.cut[a] + 0.5;
-  int nmin[3], nmax[3];
   for (int k = 0; k < 3; ++k) {
     int i = kindex[k][0], j = kindex[k][1];
     double vx = L[i * 3 + 1] * L[j * 3 + 2] - L[i * 3 + 2] * L[j * 3 + 1];
@@ -138,6 +136,19 @@ void atom_sphere(const UCell& u, int a, const double carry[3], AtomSphere& out) 
     nmin[k] = (int)std::trunc((cx * grec[k][0] + cy * grec[k][1] + cz * grec[k][2]) * 0.5 / kPi);
     if (nmax[k] < nmin[k]) std::swap(nmin[k], nmax[k]);
   }
+}
+
+namespace {
+
+// Calc_AtomsGrid for one atom (src/UCell.jl:333-400).  `carry` is the Cxyz
+// left by the previous atom (Find_CGrids! keeps it across calls).
+void atom_sphere(const UCell& u, int a, const double carry[3], AtomSphere& out) {
+  const int N1 = u.ngrid[0], N2 = u.ngrid[1], N3 = u.ngrid[2];
+  const int C = u.cpycell;
+  const int n = 2 * C + 1;
+  const double Gx = u.gxyz[a * 3], Gy = u.gxyz[a * 3 + 1], Gz = u.gxyz[a * 3 + 2];
+  int nmin[3], nmax[3];
+  atom_box(u, a, nmin, nmax);
   const double rcut = u.cut[a];
   double c[3] = {carry[0], carry[1], carry[2]};
   bool seen_in = false;
@@ -295,9 +306,12 @@ void pair_overlap(const UCell& u, int32_t pair, std::vector<int32_t>& g1, std::v
   overlap_with_lut(u, lut, pair, g1, g2);
 }
 
-std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,
-                        const int32_t* atom2spe, const double* gxyz, const double* cut,
-                        const int32_t* ngrid, const double* origin, const int32_t* numorbs) {
+// Everything of UCell(...) but the sphere and overlap lists: checks, CpyCell
+// and image cells, neighbour lists, the pair list with its DM/H block offsets
+// and partners.
+std::string build_ucell_head(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,
+                             const int32_t* atom2spe, const double* gxyz, const double* cut,
+                             const int32_t* ngrid, const double* origin, const int32_t* numorbs) {
   if (natom <= 0) return "Natom must be positive";
   if (nspin != 1 && nspin != 2 && nspin != 4) return "Nspin must be 1, 2 or 4";
   for (int d = 0; d < 3; ++d)
@@ -367,35 +381,6 @@ std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t 
     u.fnan[a] = (int32_t)u.natn[a].size() - 1;
   }
 
-  // Calc_AtomsGrid (src/UCell.jl:297-411).  Atoms are independent unless an
-  // image cell falls outside +-CpyCell before the first in-range point, when
-  // the previous atom's stale Cxyz matters; then redo sequentially.
-  std::vector<AtomSphere> sph(natom);
-  const double zero3[3] = {0, 0, 0};
-  parallel_for(natom, [&](int64_t a, int) { atom_sphere(u, (int)a, zero3, sph[a]); });
-  bool need_seq = false;
-  for (int a = 1; a < natom; ++a)
-    if (sph[a].out_before_first_in) need_seq = true;
-  if (need_seq) {
-    double carry[3] = {0, 0, 0};
-    for (int a = 0; a < natom; ++a) {
-      AtomSphere s;
-      atom_sphere(u, a, carry, s);
-      if (s.any)
-        for (int d = 0; d < 3; ++d) carry[d] = s.last_c[d];
-      sph[a] = std::move(s);
-    }
-  }
-  u.sphere_off.assign(natom + 1, 0);
-  for (int a = 0; a < natom; ++a) u.sphere_off[a + 1] = u.sphere_off[a] + (int64_t)sph[a].gl.size();
-  u.glist.resize(u.sphere_off[natom]);
-  u.clist.resize(u.sphere_off[natom]);
-  for (int a = 0; a < natom; ++a) {
-    std::copy(sph[a].gl.begin(), sph[a].gl.end(), u.glist.begin() + u.sphere_off[a]);
-    std::copy(sph[a].cl.begin(), sph[a].cl.end(), u.clist.begin() + u.sphere_off[a]);
-  }
-  sph.clear();
-
   // flattened pair list and DM/H block offsets (src/UCell.jl:82-128)
   u.pair_atom.clear();
   u.pair_jatom.clear();
@@ -436,13 +421,52 @@ std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t 
   for (int p = 0; p < u.nloop; ++p)
     if (u.partner[p] < 0) return "neighbour list is not symmetric";
 
-  // exact overlap lists of the kept orientation of each folded pair
+  // the kept orientation of each folded pair
   u.uniq_pair.clear();
   for (int p = 0; p < u.nloop; ++p)
     if (p <= u.partner[p]) u.uniq_pair.push_back(p);
+  return "";
+}
+
+// Calc_AtomsGrid (src/UCell.jl:297-411): the sphere lists.
+void build_spheres_host(UCell& u) {
+  const int natom = u.natom;
+  // Atoms are independent unless an image cell falls outside +-CpyCell before
+  // the first in-range point, when the previous atom's stale Cxyz matters;
+  // then redo sequentially.
+  std::vector<AtomSphere> sph(natom);
+  const double zero3[3] = {0, 0, 0};
+  parallel_for(natom, [&](int64_t a, int) { atom_sphere(u, (int)a, zero3, sph[a]); });
+  bool need_seq = false;
+  for (int a = 1; a < natom; ++a)
+    if (sph[a].out_before_first_in) need_seq = true;
+  if (need_seq) {
+    double carry[3] = {0, 0, 0};
+    for (int a = 0; a < natom; ++a) {
+      AtomSphere s;
+      atom_sphere(u, a, carry, s);
+      if (s.any)
+        for (int d = 0; d < 3; ++d) carry[d] = s.last_c[d];
+      sph[a] = std::move(s);
+    }
+  }
+  u.sphere_off.assign(natom + 1, 0);
+  for (int a = 0; a < natom; ++a) u.sphere_off[a + 1] = u.sphere_off[a] + (int64_t)sph[a].gl.size();
+  u.glist.resize(u.sphere_off[natom]);
+  u.clist.resize(u.sphere_off[natom]);
+  for (int a = 0; a < natom; ++a) {
+    std::copy(sph[a].gl.begin(), sph[a].gl.end(), u.glist.begin() + u.sphere_off[a]);
+    std::copy(sph[a].cl.begin(), sph[a].cl.end(), u.clist.begin() + u.sphere_off[a]);
+  }
+  sph.clear();
+}
+
+// Calc_AtomOverlap_Grid (src/UCell.jl:425-516): the exact overlap lists of the
+// kept orientation of each folded pair, and NumOLG of every pair.
+void build_overlaps_host(UCell& u) {
+  const int natom = u.natom;
   const int64_t nu = (int64_t)u.uniq_pair.size();
   std::vector<std::vector<int32_t>> ug1(nu), ug2(nu);
-  std::vector<int32_t> uniq_of_atom_first(natom + 1, 0);
   // group folded pairs by their atom so that one lookup table serves a group
   std::vector<std::vector<int64_t>> by_atom(natom);
   for (int64_t q = 0; q < nu; ++q) by_atom[u.pair_atom[u.uniq_pair[q]]].push_back(q);
@@ -464,6 +488,15 @@ std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t 
     u.numolg[p] = (int64_t)ug1[q].size();
     u.numolg[u.partner[p]] = (int64_t)ug1[q].size();
   }
+}
+
+std::string build_ucell(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,
+                        const int32_t* atom2spe, const double* gxyz, const double* cut,
+                        const int32_t* ngrid, const double* origin, const int32_t* numorbs) {
+  std::string e = build_ucell_head(u, nspin, latvecs, natom, atom2spe, gxyz, cut, ngrid, origin, numorbs);
+  if (!e.empty()) return e;
+  build_spheres_host(u);
+  build_overlaps_host(u);
   return "";
 }
 

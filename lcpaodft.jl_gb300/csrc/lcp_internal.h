@@ -127,6 +127,17 @@ void pair_overlap(const UCell& u, int32_t pair, std::vector<int32_t>& g1, std::v
 
 void set_error(const std::string& msg);
 
+// The parts of UCell(...): build_ucell = build_ucell_head (checks, image
+// cells, neighbour and pair lists), then the sphere lists (Calc_AtomsGrid)
+// and the overlap lists (Calc_AtomOverlap_Grid), on the host or the device.
+std::string build_ucell_head(UCell& u, int32_t nspin, const double* latvecs, int32_t natom,
+                             const int32_t* atom2spe, const double* gxyz, const double* cut,
+                             const int32_t* ngrid, const double* origin, const int32_t* numorbs);
+void build_spheres_host(UCell& u);
+void build_overlaps_host(UCell& u);
+// The grid-index box [nmin, nmax] Calc_AtomsGrid scans for atom a.
+void atom_box(const UCell& u, int a, int nmin[3], int nmax[3]);
+
 // Calc_Diff_Coef (src/XC/GGA_PBE.jl:1-39): the x, y, z first-derivative
 // weights [3][27] of the tri-quadratic fit through the 27 neighbours of a grid
 // point, for grid vectors gtv (rows).  False if the fit matrix is singular.

@@ -35,6 +35,11 @@ class lcp_pao(ctypes.Structure):
                 ("rv", ctypes.POINTER(ctypes.c_double)), ("rwf", ctypes.POINTER(ctypes.c_double))]
 
 
+class lcp_radial(ctypes.Structure):
+    _fields_ = [("num_mesh", ctypes.c_int32), ("xv", ctypes.POINTER(ctypes.c_double)),
+                ("rv", ctypes.POINTER(ctypes.c_double)), ("yv", ctypes.POINTER(ctypes.c_double))]
+
+
 class lcp_ucell_info(ctypes.Structure):
     _fields_ = [("cpycell", ctypes.c_int32), ("natom", ctypes.c_int32), ("nloop", ctypes.c_int32),
                 ("ncell", ctypes.c_int32), ("ngrid", ctypes.c_int32 * 3), ("max_numorbs", ctypes.c_int32),
@@ -60,6 +65,10 @@ _SIGS = {
     "lcp_last_error": ([], ctypes.c_char_p),
     "lcp_version": ([], ctypes.c_char_p),
     "lcp_ucell_create": ([_i32, _pd, _i32, _pi32, _pd, _pd, _pi32, _pd, _pi32, ctypes.POINTER(_vp)], _i32),
+    "lcp_ucell_create_device": ([_vp, _i32, _pd, _i32, _pi32, _pd, _pd, _pi32, _pd, _pi32, ctypes.POINTER(_vp)],
+                                _i32),
+    "lcp_set_adenpcc_grid": ([_vp, _vp, _i32, _pd, _pd, _i32, ctypes.POINTER(lcp_radial),
+                              ctypes.POINTER(lcp_radial), _pd, _pd, _ppd], _i32),
     "lcp_ucell_destroy": ([_vp], None),
     "lcp_ucell_get_info": ([_vp, ctypes.POINTER(lcp_ucell_info)], _i32),
     "lcp_ucell_get_int": ([_vp, _i32, _i64, _pi32, _i64], _i32),

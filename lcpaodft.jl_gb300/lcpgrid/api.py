@@ -13,7 +13,7 @@ from . import _lib
 from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 
 __all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Batch", "Server",
-           "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_Density_Grid", "diagonalize_nc_density", "Solve_Poisson", "Solve_Poisson_xyz",
+           "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_AdenPCC_Grid", "Set_Density_Grid", "diagonalize_nc_density", "Solve_Poisson", "Solve_Poisson_xyz",
            "Calc_Diff_Coef", "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
            "Calc_MatrixElements_dVH_Vxc_nc", "Force3_nospin", "Force3_spin", "Force3_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
 
@@ -89,13 +89,17 @@ def default_context(device=0):
 
 class UCell:
     """``UCell(Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin; Total_NumOrbs)``
-    (src/UCell.jl:210-294), built by the library on the host.
+    (src/UCell.jl:210-294), built by the library: on the host, or with
+    ``device=True`` its sphere and overlap lists on the GPU of ``ctx`` (the
+    same lists bit for bit; LCPError LCP_ENOTSUP for cells whose atoms' grid
+    boxes reach image cells outside -CpyCell..CpyCell-1).
 
     Lists are exposed with the reference's names: GridN_Atom, GridListAtom,
     CellListAtom (per atom), FNAN, natn, ncn, MPI_atom/MPI_natn/MPI_ncn,
     MPI_NumOLG and MPI_GListTAtoms1/2 (per pair)."""
 
-    def __init__(self, Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin, Total_NumOrbs=None):
+    def __init__(self, Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin, Total_NumOrbs=None,
+                 device=False, ctx=None):
         self.Latvecs = _f64(Latvecs).reshape(3, 3)
         self.Natom = int(Natom)
         self.atom2spe = np.ascontiguousarray(atom2spe, dtype=np.int32)
@@ -110,9 +114,12 @@ class UCell:
             raise LCPError(_lib.LCP_EINVAL, "per-atom arrays must have Natom entries")
         h = ctypes.c_void_p()
         ng = np.array(self.Ngrid, dtype=np.int32)
-        check(lib.lcp_ucell_create(self.Nspin, dptr(self.Latvecs), self.Natom, iptr(self.atom2spe), dptr(self.Gxyz),
-                                   dptr(self.Atoms_Cut1), iptr(ng), dptr(self.Grid_Origin), iptr(self.Total_NumOrbs),
-                                   ctypes.byref(h)))
+        args = (self.Nspin, dptr(self.Latvecs), self.Natom, iptr(self.atom2spe), dptr(self.Gxyz),
+                dptr(self.Atoms_Cut1), iptr(ng), dptr(self.Grid_Origin), iptr(self.Total_NumOrbs), ctypes.byref(h))
+        if device:
+            check(lib.lcp_ucell_create_device((ctx or default_context())._h, *args))
+        else:
+            check(lib.lcp_ucell_create(*args))
         self._h = h
         info = _lib.lcp_ucell_info()
         check(lib.lcp_ucell_get_info(self._h, ctypes.byref(info)))
@@ -333,6 +340,39 @@ def diagonalize_nc_density(Density_Grid, ctx=None):
         raise LCPError(_lib.LCP_EINVAL, "Density_Grid channels differ in size")
     p, keep = dptrs([Density_Grid[c] for c in range(4)])
     check(lib.lcp_diagonalize_nc_density(ctx._h, nn, p))
+
+
+def _radial(xv, rv, yv, keep):
+    arrs = [_f64(xv), _f64(rv), _f64(yv)]
+    if arrs[2].size != arrs[0].size + 4 or arrs[1].size != arrs[0].size:
+        raise LCPError(_lib.LCP_EINVAL, "radial table sizes: xv and rv n, values n + 4")
+    keep.extend(arrs)
+    return _lib.lcp_radial(arrs[0].size, dptr(arrs[0]), dptr(arrs[1]), dptr(arrs[2]))
+
+
+def Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, ucell, ctx=None):
+    """``Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, ucell)``
+    (src/Matrix/Set_AdenPCC_Grid.jl:1-142) on the GPU: returns (ADensity_Grid,
+    PCCDensity_Grid, Density_Grid).  ``pao[spe]`` carries Spe_PAO_XV,
+    Spe_PAO_RV and Spe_Atomic_Den; ``pspot[spe]`` Spe_VPS_XV, Spe_VPS_RV and
+    Spe_Atomic_PCC (``PCC`` objects)."""
+    ctx = ctx or default_context()
+    s = _spin(SpinPol)
+    keep = []
+    den = (_lib.lcp_radial * len(pao))(*[_radial(p.Spe_PAO_XV, p.Spe_PAO_RV, p.Spe_Atomic_Den, keep) for p in pao])
+    pcc = (_lib.lcp_radial * len(pspot))(*[_radial(p.Spe_VPS_XV, p.Spe_VPS_RV, p.Spe_Atomic_PCC, keep)
+                                           for p in pspot])
+    nsp = _f64([[float(x[0]), float(x[1])] for x in Init_Atoms_Nspin])
+    ang = _f64([[float(x[0]), float(x[1])] for x in Init_Atoms_Angle]) if Init_Atoms_Angle is not None else None
+    if nsp.shape != (ucell.Natom, 2) or (ang is not None and ang.shape != (ucell.Natom, 2)):
+        raise LCPError(_lib.LCP_EINVAL, "Init_Atoms_Nspin / Init_Atoms_Angle need Natom entries")
+    nn = ucell.NN
+    ad, pc = np.zeros(nn), np.zeros(nn)
+    dens = [np.zeros(nn) for _ in range(_lib.NCHAN[s])]
+    pr, k2 = dptrs(dens)
+    check(lib.lcp_set_adenpcc_grid(ctx._h, ucell._h, _lib.SPIN[s], dptr(nsp), dptr(ang), len(pao), den, pcc,
+                                   dptr(ad), dptr(pc), pr))
+    return ad, pc, dens
 
 
 class Rhor_Mixing:

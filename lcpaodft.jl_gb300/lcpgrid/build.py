@@ -49,7 +49,9 @@ def _compile(src, nvcc, verbose):
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
     else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I", INCLUDE, "-I", CSRC,
+        # no FMA contraction: the sphere lists' distance tests round like the
+        # reference's and the device build's
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-pthread", "-I", INCLUDE, "-I", CSRC,
                "-I", os.path.join(_cuda_root(nvcc), "include"), "-c", src, "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     return src, obj, res
@@ -60,7 +62,7 @@ def build(verbose=False, force=False):
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(INCLUDE, "lcpgrid.h"))
     newest = max(os.path.getmtime(p) for p in srcs + headers + [__file__])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > newest:
