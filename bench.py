@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section of the step bench line")
     ap.add_argument("--no-force", action="store_true", help="skip the grid force term section of the step bench line")
     ap.add_argument("--no-gga", action="store_true", help="skip the GGA-PBE section of the step bench line")
+    ap.add_argument("--xc", default="auto", choices=["auto", "GGA_PBE"],
+                    help="xc of the timed step: auto = LDA ('off') / LSDA ('on'), or GGA_PBE")
     ap.add_argument("--serve-structures", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-rate", type=float, default=400.0, help="offered Poisson rate, jobs/s")
@@ -369,6 +371,13 @@ def run_ours(args):
     wl = workload(args)
     ctx = L.Context(local)
     u, orbs, dm, vna, t_geom, t_tab = build_workload(ctx, wl)
+    # the same UCell with its sphere and overlap lists built on the GPU
+    t_geom_dev = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        L.UCell(u.Nspin, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"],
+                wl["origin"], Total_NumOrbs=wl["numorbs"], device=True, ctx=ctx)
+        t_geom_dev.append(time.perf_counter() - t0)
     # a dedicated (non-default) stream: the library launches on it and the
     # CUDA events below are recorded on it
     stream = torch.cuda.Stream()
@@ -378,7 +387,8 @@ def run_ours(args):
     # FP64 reference energy of this step (the drop-in), for the error of other forms
     spin = wl.get("spinpol", "off")
     nspin = len(dm)
-    job = L.GridStepJob(u, orbs, spin, "LDA" if spin == "off" else "LSDA", None, None, vna)
+    xc = args.xc if args.xc != "auto" else ("LDA" if spin == "off" else "LSDA")
+    job = L.GridStepJob(u, orbs, spin, xc, None, None, vna)
     job.set_dm(dm)
     ctx.set_precision("fp64")
     job.step()
@@ -484,12 +494,12 @@ def run_ours(args):
         "config": {"workload": wl["name"], "atoms": wl["natom"], "orbitals_per_atom": sorted(set(wl["numorbs"])),
                    "ngrid": list(wl["ngrid"]), "pairs": int(u.Nloop), "folded_pairs": int(u.n_unique),
                    "lens_points": int(u.sum_numolg), "precision": args.precision, "spinpol": spin,
-                   "xc": "LDA" if spin == "off" else "LSDA",
+                   "xc": xc,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (phi tables %.0f MB)"
                          % (sum(np.asarray(u.GridN_Atom, float) * np.asarray(wl["numorbs"])) * 8 / 1e6)},
         "stage_ms": dict(zip(names, [float(x) for x in stages])),
-        "setup_s": {"ucell_host": t_geom, "tabulation": t_tab},
+        "setup_s": {"ucell_host": t_geom, "ucell_device": min(t_geom_dev), "tabulation": t_tab},
         "roofline": roof,
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(nspin * u.Total_Hsize * 8),
                 "d2h_bytes_per_step": int(nspin * u.Total_Hsize * 8 + 40), "ms_per_step": e2e_s * 1e3},
@@ -595,8 +605,9 @@ def serving(args, wl_pool=None):
     jobs, dms, natoms = [], [], []
     t0 = time.perf_counter()
     for w in pool:
+        # sphere and overlap lists built on the GPU (the same lists as the host build)
         u = L.UCell(1, w["latvecs"], w["natom"], w["atom2spe"], w["gxyz"], w["cut"], w["ngrid"], w["origin"],
-                    Total_NumOrbs=w["numorbs"])
+                    Total_NumOrbs=w["numorbs"], device=True, ctx=ctx)
         orbs = L.Set_Orbitals_Grid(w["paos"], u, ctx)
         vna = smooth_vna(w["ngrid"], w["latvecs"], w["vna_seed"])
         jobs.append(L.GridStepJob(u, orbs, "off", "LDA", None, None, vna))
