@@ -1399,6 +1399,33 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
     ctx->launches++;
   }
   mark(1);
+  // The xc pass needs only rho: in an untimed step it runs on the context's
+  // second stream beside the FFT Poisson solve (without dVHart: vpot holds
+  // vxc), and vpot_eh_g adds dVHart + V_na and the E_H1 partials after both.
+  // "nc": the collinear pass on (Nup, Ndown), the rotation afterwards.
+  const int32_t sp_xc = job->spinpol == LCP_SPIN_NC ? LCP_SPIN_ON : job->spinpol;
+  auto xc_pass = [&](const lcp::GridCell& c, cudaStream_t xs) -> lcp_status {
+    if (job->xc == LCP_XC_GGA_PBE) {
+      API_CUDA(lcp::launch_gga_g(sp_xc, c, one, true, xs), "gga");
+      ctx->launches += 2;
+    } else {
+      API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, sp_xc, c, one, xs), "xc_vpot_energy");
+      ctx->launches++;
+    }
+    return LCP_OK;
+  };
+  const bool overlap = ev == nullptr;
+  if (overlap) {
+    if (!ctx->aux) API_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!ctx->ev_fork) API_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+    if (!ctx->ev_join) API_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming), "cudaEventCreate");
+    API_CUDA(cudaEventRecord(ctx->ev_fork, st), "fork");
+    API_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0), "fork");
+    lcp::GridCell gx = gc;
+    gx.dvh = nullptr;
+    if ((s = xc_pass(gx, ctx->aux))) return s;
+    API_CUDA(cudaEventRecord(ctx->ev_join, ctx->aux), "join");
+  }
   // 2. Poisson
   API_CUDA(lcp::launch_poisson_prep_g(job->spinpol, gc, one, st), "poisson_prep");
   FftPlans* plans = nullptr;  // the executing context's plans (any context may run the job)
@@ -1412,15 +1439,13 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
     return fail(LCP_EDEVICE, "cufftExecZ2D failed");
   ctx->launches += 2;
   mark(2);
-  // 3. xc + potential, with the FP64 energy tile partials in the same pass
-  // ("nc": the collinear pass on (Nup, Ndown), then the rotation into four channels)
-  const int32_t sp_xc = job->spinpol == LCP_SPIN_NC ? LCP_SPIN_ON : job->spinpol;
-  if (job->xc == LCP_XC_GGA_PBE) {
-    API_CUDA(lcp::launch_gga_g(sp_xc, gc, one, true, st), "gga");
-    ctx->launches += 2;
-  } else {
-    API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, sp_xc, gc, one, st), "xc_vpot_energy");
+  // 3. xc + potential, with the FP64 energy tile partials
+  if (overlap) {
+    API_CUDA(cudaStreamWaitEvent(st, ctx->ev_join, 0), "join");
+    API_CUDA(lcp::launch_vpot_eh_g(sp_xc, gc, one, st), "vpot_eh");
     ctx->launches++;
+  } else if ((s = xc_pass(gc, st))) {
+    return s;
   }
   if (job->spinpol == LCP_SPIN_NC) {
     // dVHart + V_na is common to both diagonal channels and drops out of tmp1

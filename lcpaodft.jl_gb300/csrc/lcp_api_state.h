@@ -91,8 +91,14 @@ struct lcp_ctx {
   // workspaces of the host-buffer entry points
   DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
   DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale;
+  // second stream of the step: the xc pass runs there beside the FFT Poisson solve
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ~lcp_ctx() {
     cudaSetDevice(device);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (aux) cudaStreamDestroy(aux);
     for (auto& kv : plans) {
       if (kv.second.fwd) cufftDestroy(kv.second.fwd);
       if (kv.second.inv) cufftDestroy(kv.second.inv);

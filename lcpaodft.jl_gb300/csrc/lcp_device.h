@@ -150,7 +150,11 @@ cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaS
 // The Poisson factors of a grid (ng0 * ng1 * (ng2/2+1) doubles), for GridCell::pfac.
 cudaError_t launch_poisson_table(const int32_t* ngrid, const double* recvecs, double* out, cudaStream_t st);
 // xc + potential + the energy-term tile partials in one pass (tiles of nn)
+// With dvh == nullptr in the cell, the xc pass writes vxc to vpot and leaves
+// the E_H1 partials zero; launch_vpot_eh_g then adds dVHart + V_na and the
+// E_H1 partials (spinpol "off" or "on").
 cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
+cudaError_t launch_vpot_eh_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
 // GGA-PBE pass of the grid step (cells with dcoef/dexc set): gradient + PBE
 // (+ energy tile partials where part is set), then, if potential, the
 // divergence term and, where dvh is set, vpot = dVHart + vxc + V_na (without

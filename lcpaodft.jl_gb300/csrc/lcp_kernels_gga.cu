@@ -13,8 +13,8 @@
 // consecutive points spans about 11 rows of a 96-point plane, and the rows of
 // the neighbouring planes it touches stay in L1/L2, so DRAM sees each field
 // about once per pass.  The pointwise functional dominates: it is FP64
-// arithmetic (about 40 divisions' worth of reciprocals, 4 logs, 1 exp and 6
-// cube roots per point), so the passes are bound by the FP64 pipe, not HBM.
+// arithmetic (a few divisions, cube roots and logs and an exp per point), so
+// the passes are bound by the FP64 pipe, not HBM.
 #include <cuda_runtime.h>
 
 #include "lcp_device.h"
@@ -27,201 +27,269 @@ namespace {
 constexpr double kDenMin = 1.0e-14;  // src/LCPAODFT.jl:71
 constexpr double kPi = 3.14159265358979323846;
 
-// One PW92 G(rs) term and its rs-derivative (src/XC/XC_PBE.jl:41-90).  With
-// t = 2 A b, the reference's c = 1 + 1/t and dcdrs/c = -dbdrs / (t + 1) share
-// one reciprocal r = 1 / (t (t + 1)).
-__device__ __forceinline__ void pw92_g(double rs, double srs, double isrs, double A, double a1, double b1,
-                                       double b2, double b3, double b4, double& G, double& dG) {
-  const double b = b1 * srs + rs * (b2 + b3 * srs + b4 * rs);
-  const double dbdrs = b1 * 0.5 * isrs + b2 + b3 * 1.5 * srs + b4 * 2 * rs;
-  const double t = 2 * A * b;
-  const double r = 1.0 / (t * (t + 1.0));
-  const double c = 1.0 + (t + 1.0) * r;  // 1 + 1/t
-  const double dcdrs_c = -dbdrs * 2 * A * r;  // dcdrs / c = -(c-1) dbdrs / (b c) = -2 A dbdrs / (t (t+1))
-  const double dum = log(c);
-  const double dum1 = 1 + a1 * rs;
-  G = -2 * A * dum1 * dum;
-  dG = -2 * A * (a1 * dum + dum1 * dcdrs_c);
-}
-
-// XC_PW92C (src/XC/XC_PBE.jl:1-126): Ec and Vc1/Vc2 of the densities d1, d2,
-// which it writes back as den_min/2 each where their sum is <= den_min.
-// SYM: d1 == d2 (zeta = 0), where the spin interpolation terms vanish exactly
-// and only G(0) is needed.
-template <bool SYM>
-__device__ __forceinline__ void pw92c(double& d1, double& d2, double& Ec, double& Vc1, double& Vc2, double& cz1,
-                                      double& cz2) {
-  double dtot = d1 + d2;
-  double rs;
-  if (dtot <= kDenMin) {
-    rs = 6203.504908994;
-    d1 = d2 = 0.5e-14;
-    dtot = kDenMin;
-  } else {
-    rs = 0.6203504908994 * rcbrt(dtot);
+// Reciprocals of N positive values with one division (Montgomery's
+// simultaneous inversion: prefix products, one reciprocal, back-substitution;
+// a few ulps each).  The callers keep the products inside the double range.
+template <int N>
+__device__ __forceinline__ void batch_recip(const double (&x)[N], double (&r)[N]) {
+  double p[N];
+  p[0] = x[0];
+#pragma unroll
+  for (int k = 1; k < N; ++k) p[k] = p[k - 1] * x[k];
+  double inv = 1.0 / p[N - 1];
+#pragma unroll
+  for (int k = N - 1; k > 0; --k) {
+    r[k] = inv * p[k - 1];
+    inv *= x[k];
   }
-  const double tmp0 = 1.0 / dtot;
-  const double srs = sqrt(rs), isrs = 1.0 / srs;
-  const double drsdd = -(1.0 / 3.0) * rs * tmp0;
-  double G0, dG0;
-  pw92_g(rs, srs, isrs, 0.0310910, 0.2137000, 7.5957000, 3.5876000, 1.6382000, 0.4929400, G0, dG0);
-  if (SYM) {
-    Ec = G0;
-    Vc1 = Vc2 = G0 + dtot * (dG0 * drsdd);
-    cz1 = cz2 = 1.0;
-    return;
-  }
-  double zeta = tmp0 * (d1 - d2);
-  zeta = zeta > 0.99 ? 0.99 : zeta;
-  zeta = zeta < -1.0 ? -0.99 : zeta;
-  const double dzdd1 = tmp0 * (1 - zeta);
-  const double dzdd2 = tmp0 * (-1 - zeta);
-  double G1, dG1, G2, dG2;
-  pw92_g(rs, srs, isrs, 0.0155450, 0.2054800, 14.1189000, 6.1977000, 3.3662000, 0.6251700, G1, dG1);
-  pw92_g(rs, srs, isrs, 0.0168870, 0.1112500, 10.3570000, 3.6231000, 0.8802600, 0.4967100, G2, dG2);
-  const double c = 1.92366105093154;
-  const double ifpp0 = 1.0 / 1.70992093416137;
-  cz1 = cbrt(1 + zeta);
-  cz2 = cbrt(1 - zeta);
-  const double z1sq = cz1 * cz1, z2sq = cz2 * cz2;
-  const double f = (z1sq * z1sq + z2sq * z2sq - 2) * c;
-  const double dfdz = (4.0 / 3.0) * (cz1 - cz2) * c;
-  const double z3 = zeta * zeta * zeta, z4 = z3 * zeta;
-  Ec = G0 - G2 * f * ifpp0 * (1 - z4) + (G1 - G0) * f * z4;
-  const double dEcdrs = dG0 - dG2 * f * ifpp0 * (1 - z4) + (dG1 - dG0) * f * z4;
-  const double dEcdz = -G2 * ifpp0 * (dfdz * (1 - z4) - f * 4 * z3) + (G1 - G0) * (dfdz * z4 + f * 4 * z3);
-  const double dum = dEcdrs * drsdd;
-  Vc1 = Ec + dtot * (dum + dEcdz * dzdd1);
-  Vc2 = Ec + dtot * (dum + dEcdz * dzdd2);
+  r[0] = inv;
 }
 
-// Spin-scaled PBE exchange of one spin channel (src/XC/XC_PBE.jl:356-448):
-// fx = DS * Ex_unif * F(s), dfx/dDS and the gradient factor k with
-// dfx/d(grad rho_s)_x = k * grad(rho_s)_x.  XC_EX with NSP = 1
-// (src/XC/XC_PBE.jl:132-184) gives Ex_unif = 0.75 VXP, VXP = -COE2 / RS.
-__device__ __forceinline__ void pbe_x_spin(double d, double gx, double gy, double gz, double& fx, double& dfx,
-                                           double& k) {
-  constexpr double kappa = 0.8040;
-  constexpr double mu = 0.06672455060314922 * kPi * kPi / 3;
-  const double DS = fmax(kDenMin, 2 * d);
-  const double GDMS = fmax(1e-14, 2 * sqrt(gx * gx + gy * gy + gz * gz));
-  const double cds = cbrt(DS);
-  const double KFS = 3.0936677262801355 * cds;  // cbrt(3 pi^2) cbrt(DS)
-  const double iDS = 1.0 / DS;
-  const double s = GDMS / (2 * KFS * DS);
-  const double f1 = 1 + mu * s * s / kappa;
-  const double if1 = 1.0 / f1;
-  const double f = 1 + kappa - kappa * if1;
-  // RS = COE1 DS^(-1/3): VXP = -COE2 / RS
-  const double VXP = -0.610887057710857 / (0.6203504908994 / cds);
-  const double EXP = 0.75 * VXP;
-  fx = DS * EXP * f;
-  const double DSDD = s * (-(1.0 / 3.0) * iDS - iDS);
-  const double DF1DD = 2 * (f1 - 1) * DSDD / s;
-  const double DFDD = kappa * DF1DD * if1 * if1;
-  dfx = VXP * f + DS * EXP * DFDD;
-  // DSDGD = (s / GDMS) 2 g / GDMS; DFDGD = kappa (2 mu s DSDGD / kappa) / f1^2
-  const double iG = 1.0 / GDMS;
-  k = DS * EXP * (2 * mu * s * (s * iG) * 2 * iG) * if1 * if1;
-}
+// PW92 parameters of G(0), G(1), G(2) (src/XC/XC_PBE.jl:7-13).
+__device__ __constant__ double kPwA[3] = {0.0310910, 0.0155450, 0.0168870};
+__device__ __constant__ double kPwA1[3] = {0.2137000, 0.2054800, 0.1112500};
+__device__ __constant__ double kPwB[3][4] = {{7.5957000, 3.5876000, 1.6382000, 0.4929400},
+                                             {14.1189000, 6.1977000, 3.3662000, 0.6251700},
+                                             {10.3570000, 3.6231000, 0.8802600, 0.4967100}};
 
-// XC_PBE! (src/XC/XC_PBE.jl:187-476) at one point: e = Exc[1] + Exc[2] (the
-// energy per particle), v[s] = DEXDD[s] + DECDD[s], and dg[3 s + a] =
-// DEXDGD + DECDGD, with g = (grad up, grad down).  SYM: the "off" case
-// (equal spin densities and gradients), where both spins share one exchange
-// evaluation and zeta = 0.
+// XC_PBE! (src/XC/XC_PBE.jl:187-476) with XC_PW92C (:1-126) and the
+// spin-scaled exchange through XC_EX (:132-184), at one point: e = Exc[1] +
+// Exc[2] (energy per particle), v[s] = DEXDD[s] + DECDD[s], dg[3 s + a] =
+// DEXDGD + DECDGD, g = (grad up, grad down).  SYM: the "off" case (equal spin
+// densities and gradients): zeta = 0, phi = 1, PW92's spin-interpolation terms
+// vanish exactly (only G(0) is needed), both spins share one exchange
+// evaluation, and DS = dt, GDMS = GDMT.
+//
+// The reference's expressions, rearranged to spend few FP64 divisions (the
+// GB300's FP64 pipe is the limit of this pass):
+//   - the reciprocals come in batches (batch_recip);
+//   - one cube root of dt serves rs, kF and ("off") the exchange's kF;
+//   - rsqrt gives sqrt(rs) and 1/sqrt(rs), and ks with 1/ks;
+//   - c = 1 + 1/t and dcdrs/c = -2 A dbdrs / (t (t + 1)) share 1/(t (t + 1));
+//   - f1/Ec = 1/(gamma phi^3) and DSDD/s = -(4/3)/DS: no 1/Ec or 1/s;
+//   - 1/f3, 1/(1 + A f3) and 1/(1 + f4) = (1 + A f3)/(1 + A f3 + f3 beta/gamma)
+//     share one division;
+//   - log1p(f4) for log(1 + f4); cbrt for XC_EX's truncated power
+//     D^(-0.333333333333333) (relative change <= |ln D| * 3.3e-16).
 template <bool SYM>
 __device__ __forceinline__ void xc_pbe_point(double d1, double d2, const double (&g)[6], double& e, double (&v)[2],
                                              double (&dg)[6]) {
   constexpr double beta = 0.06672455060314922;
   constexpr double gamma = 0.031090690869654901;  // (1 - ln 2) / pi^2
+  constexpr double igamma = 1.0 / gamma;
   constexpr double bg = beta / gamma;
+  constexpr double kappa = 0.8040;
+  constexpr double mu = beta * kPi * kPi / 3;
+  constexpr double c3pi2 = 3.0936677262801355;  // cbrt(3 pi^2)
+  constexpr double COE1 = 0.6203504908994, COE2 = 0.610887057710857;
+  constexpr int NS = SYM ? 1 : 2;
+  constexpr int NG = SYM ? 1 : 3;  // PW92 G terms
+
   d1 = fmax(0.5 * kDenMin, d1);
   d2 = fmax(0.5 * kDenMin, d2);
   const double dt = d1 + d2;
-  const double idt = 1.0 / dt;
-  const double GDT0 = g[0] + g[3], GDT1 = g[1] + g[4], GDT2 = g[2] + g[5];
-  const double GDMT = fmax(1e-14, sqrt(GDT0 * GDT0 + GDT1 * GDT1 + GDT2 * GDT2));
+  const double GDT[3] = {g[0] + g[3], g[1] + g[4], g[2] + g[5]};
+  const double GDMT = fmax(1e-14, sqrt(GDT[0] * GDT[0] + GDT[1] * GDT[1] + GDT[2] * GDT[2]));
+  double DS[2], GDMS[2], rcs[2], cds[2];
+  const double r3 = rcbrt(dt);
+  const double c3 = dt * r3 * r3;  // cbrt(dt)
+  if (SYM) {
+    // 2 d1 = dt >= den_min; |2 g| = 2 |g| exactly (GDT = 2 g)
+    DS[0] = dt;
+    GDMS[0] = GDMT;
+    rcs[0] = r3;
+    cds[0] = c3;
+  } else {
+    const double dd[2] = {d1, d2};
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      DS[s] = fmax(kDenMin, 2 * dd[s]);
+      const double* gs = g + 3 * s;
+      GDMS[s] = fmax(1e-14, 2 * sqrt(gs[0] * gs[0] + gs[1] * gs[1] + gs[2] * gs[2]));
+      rcs[s] = rcbrt(DS[s]);
+      cds[s] = DS[s] * rcs[s] * rcs[s];
+    }
+  }
 
-  double Ec, Vc1, Vc2, cz1, cz2;
-  pw92c<SYM>(d1, d2, Ec, Vc1, Vc2, cz1, cz2);
+  // XC_PW92C: its densities (reset to den_min/2 each where dt <= den_min), rs
+  const bool low = dt <= kDenMin;
+  const double pd1 = low ? 0.5e-14 : d1, pd2 = low ? 0.5e-14 : d2;
+  const double rs = low ? 6203.504908994 : COE1 * r3;
+  const double isrs = rsqrt(rs), srs = rs * isrs;
+  double Gb[NG], Gdb[NG], GT[NG];
+#pragma unroll
+  for (int k = 0; k < NG; ++k) {
+    Gb[k] = kPwB[k][0] * srs + rs * (kPwB[k][1] + kPwB[k][2] * srs + kPwB[k][3] * rs);
+    Gdb[k] = kPwB[k][0] * 0.5 * isrs + kPwB[k][1] + kPwB[k][2] * 1.5 * srs + kPwB[k][3] * 2 * rs;
+    GT[k] = 2 * kPwA[k] * Gb[k];
+  }
 
-  // correlation energy (:241-267)
-  const double kF = 3.0936677262801355 * cbrt(dt);  // cbrt(3 pi^2 dt)
-  const double ks = sqrt(4 * kF / kPi);
-  double zeta = 0.0, phi = 1.0, DPDZ = 0.0;
+  // first batch of reciprocals: dt, GDMT, the G terms' t (t + 1); "on" also DS, GDMS
+  constexpr int NA = SYM ? 2 + NG : 6 + NG;
+  double xa[NA], ra[NA];
+  xa[0] = dt;
+  xa[1] = GDMT;
+#pragma unroll
+  for (int k = 0; k < NG; ++k) xa[2 + k] = GT[k] * (GT[k] + 1.0);
   if (!SYM) {
-    zeta = (d1 - d2) * idt;
+    xa[2 + NG] = DS[0];
+    xa[3 + NG] = DS[1];
+    xa[4 + NG] = GDMS[0];
+    xa[5 + NG] = GDMS[1];
+  }
+  batch_recip<NA>(xa, ra);
+  const double idt = ra[0], iGT = ra[1];
+  double iDS[2], iG[2];
+  if (SYM) {
+    iDS[0] = idt;
+    iG[0] = iGT;
+  } else {
+    iDS[0] = ra[2 + NG];
+    iDS[1] = ra[3 + NG];
+    iG[0] = ra[4 + NG];
+    iG[1] = ra[5 + NG];
+  }
+  const double tmp0 = low ? 1.0 / kDenMin : idt;  // 1/dtot
+  const double dtot = low ? kDenMin : dt;
+  double G[NG], dG[NG];
+#pragma unroll
+  for (int k = 0; k < NG; ++k) {
+    const double r = ra[2 + k];
+    const double c = 1.0 + (GT[k] + 1.0) * r;        // 1 + 1/t
+    const double dcdrs_c = -Gdb[k] * 2 * kPwA[k] * r;  // dcdrs / c
+    const double dum = log(c);
+    const double dum1 = 1 + kPwA1[k] * rs;
+    G[k] = -2 * kPwA[k] * dum1 * dum;
+    dG[k] = -2 * kPwA[k] * (kPwA1[k] * dum + dum1 * dcdrs_c);
+  }
+  const double drsdd = -(1.0 / 3.0) * rs * tmp0;
+  double Ec, Vc[2], zeta = 0.0, cz1 = 1.0, cz2 = 1.0;
+  if (SYM) {
+    Ec = G[0];
+    Vc[0] = Vc[1] = G[0] + dtot * (dG[0] * drsdd);
+  } else {
+    zeta = tmp0 * (pd1 - pd2);
     zeta = zeta > 0.99 ? 0.99 : zeta;
     zeta = zeta < -1.0 ? -0.99 : zeta;
-    // pw92c's cube roots cbrt(1 +- zeta) are of this same clamped zeta (where
-    // it reset the densities, zeta is 0 there and here)
-    phi = 0.5 * (cz1 * cz1 + cz2 * cz2);
-    DPDZ = (1.0 / 3.0) * (1.0 / cz1 - 1.0 / cz2);
+    cz1 = cbrt(1 + zeta);
+    cz2 = cbrt(1 - zeta);
+    constexpr double c = 1.92366105093154;
+    constexpr double ifpp0 = 1.0 / 1.70992093416137;
+    const double z1sq = cz1 * cz1, z2sq = cz2 * cz2;
+    const double f = (z1sq * z1sq + z2sq * z2sq - 2) * c;
+    const double dfdz = (4.0 / 3.0) * (cz1 - cz2) * c;
+    const double z3 = zeta * zeta * zeta, z4 = z3 * zeta;
+    Ec = G[0] - G[2] * f * ifpp0 * (1 - z4) + (G[1] - G[0]) * f * z4;
+    const double dEcdrs = dG[0] - dG[2] * f * ifpp0 * (1 - z4) + (dG[1] - dG[0]) * f * z4;
+    const double dEcdz = -G[2] * ifpp0 * (dfdz * (1 - z4) - f * 4 * z3) + (G[1] - G[0]) * (dfdz * z4 + f * 4 * z3);
+    const double dum = dEcdrs * drsdd;
+    Vc[0] = Ec + dtot * (dum + dEcdz * (tmp0 * (1 - zeta)));
+    Vc[1] = Ec + dtot * (dum + dEcdz * (tmp0 * (-1 - zeta)));
   }
-  const double iphi = 1.0 / phi;
-  const double phi3 = phi * phi * phi;
-  const double t = GDMT / (2 * phi * ks * dt);
-  const double f1 = Ec / (gamma * phi3);
+
+  // exchange enhancement: s and f1 per spin (src/XC/XC_PBE.jl:359-367)
+  double sx[2], f1x[2];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    sx[s] = GDMS[s] * (0.5 / c3pi2) * rcs[s] * iDS[s];  // GDMS / (2 KFS DS)
+    f1x[s] = 1 + mu * sx[s] * sx[s] / kappa;
+  }
+  // second batch: 1/f1 per spin; "on" also 1/phi, 1/cbrt(1 +- zeta)
+  constexpr int NB = SYM ? 1 : 5;
+  double xb[NB], rb[NB];
+  xb[0] = f1x[0];
+  double phi = 1.0;
+  if (!SYM) {
+    phi = 0.5 * (cz1 * cz1 + cz2 * cz2);  // ((1+z)^(2/3) + (1-z)^(2/3)) / 2
+    xb[1] = f1x[1];
+    xb[2] = phi;
+    xb[3] = cz1;
+    xb[4] = cz2;
+  }
+  batch_recip<NB>(xb, rb);
+  double if1[2];
+  if1[0] = rb[0];
+  double iphi = 1.0, DPDZ = 0.0;
+  if (!SYM) {
+    if1[1] = rb[1];
+    iphi = rb[2];
+    DPDZ = (1.0 / 3.0) * (rb[3] - rb[4]);
+  }
+
+  // correlation gradient term H (src/XC/XC_PBE.jl:241-267)
+  const double kF = c3pi2 * c3;
+  const double xks = 4 * kF / kPi;
+  const double iks = rsqrt(xks), ks = xks * iks;
+  const double phi3 = phi * phi * phi, iphi3 = iphi * iphi * iphi;
+  const double K = 0.5 * iphi * iks * idt;  // t / GDMT
+  const double t = GDMT * K;
+  const double f1 = Ec * igamma * iphi3;
   const double f2 = exp(-f1);
-  const double A = bg / (f2 - 1);
+  const double E = f2 - 1;
+  const double iE = 1.0 / E;
+  const double A = bg * iE;
   const double t2 = t * t;
   const double f3 = t2 + A * t2 * t2;
-  const double iAf3 = 1.0 / (1 + A * f3);
-  const double f4 = bg * f3 * iAf3;
-  const double if4 = 1.0 / (1 + f4);
+  const double P = 1 + A * f3;  // 1 + A f3
+  const double Q = P + bg * f3;  // P (1 + f4)
+  double xc3[3] = {f3, P, Q}, rc3[3];
+  batch_recip<3>(xc3, rc3);
+  const double if3 = rc3[0], iP = rc3[1];
+  const double if4 = P * rc3[2];  // 1 / (1 + f4)
+  const double f4 = bg * f3 * iP;
   const double H = gamma * phi3 * log1p(f4);
   const double Fc = Ec + H;
 
   // correlation derivatives (:273-342)
-  const double iks = 1.0 / ks;
-  const double DKSDD = 0.5 * ks * (1.0 / 3.0) * idt;  // 0.5 ks DKFDD / kF, DKFDD = kF / (3 dt)
-  const double if3 = 1.0 / f3;
+  const double DKSDD = 0.5 * ks * (1.0 / 3.0) * idt;
   const double dt3 = 2 * t + 4 * A * t2 * t;
-  const double iEc = 1.0 / Ec;
-  const double if2m1 = 1.0 / (f2 - 1);
   double DFCDD[2];
 #pragma unroll
-  for (int is = 0; is < (SYM ? 1 : 2); ++is) {
-    const double Vc = is == 0 ? Vc1 : Vc2;
+  for (int is = 0; is < NS; ++is) {
     const double DZDD = is == 0 ? idt - zeta * idt : -idt - zeta * idt;
-    const double DECUDD = (Vc - Ec) * idt;
+    const double DECUDD = (Vc[is] - Ec) * idt;
     const double DPDD = DPDZ * DZDD;
     const double DTDD = (-t) * (DPDD * iphi + DKSDD * iks + idt);
-    const double DF1DD = f1 * (DECUDD * iEc - 3 * DPDD * iphi);
+    const double DF1DD = igamma * iphi3 * DECUDD - 3 * f1 * DPDD * iphi;
     const double DF2DD = -f2 * DF1DD;
-    const double DADD = -A * DF2DD * if2m1;
+    const double DADD = -A * DF2DD * iE;
     const double DF3DD = dt3 * DTDD + DADD * t2 * t2;
-    const double DF4DD = f4 * (DF3DD * if3 - (DADD * f3 + A * DF3DD) * iAf3);
+    const double DF4DD = f4 * (DF3DD * if3 - (DADD * f3 + A * DF3DD) * iP);
     const double DHDD = 3 * H * DPDD * iphi + gamma * phi3 * DF4DD * if4;
-    DFCDD[is] = Vc + H + dt * DHDD;
+    DFCDD[is] = Vc[is] + H + dt * DHDD;
   }
   if (SYM) DFCDD[1] = DFCDD[0];
-  // d Fc / d GDT_x = dt * gamma phi^3 f4 (1/f3 - A/(1 + A f3)) dt3 (t / GDMT^2) GDT_x / (1 + f4)
-  const double iGT = 1.0 / GDMT;
-  const double kc = dt * gamma * phi3 * f4 * (if3 - A * iAf3) * dt3 * (t * iGT) * iGT * if4;
+  // d Fc / d GDT_x = kc * GDT_x (the reference's f4 (1/f3 - A/(1 + A f3)), kept
+  // as written: for large t both terms nearly cancel)
+  const double kc = dt * gamma * phi3 * f4 * (if3 - A * iP) * dt3 * K * iGT * if4;
 
-  // exchange (:348-451)
-  double fx0, dfx0, kx0, fx1, dfx1, kx1;
-  pbe_x_spin(d1, g[0], g[1], g[2], fx0, dfx0, kx0);
-  if (SYM) {
-    fx1 = fx0;
-    dfx1 = dfx0;
-    kx1 = kx0;
-  } else {
-    pbe_x_spin(d2, g[3], g[4], g[5], fx1, dfx1, kx1);
+  // exchange (:348-451): fx = DS Ex_unif F(s), Ex_unif = 0.75 VXP, VXP = -COE2/COE1 cbrt(DS)
+  double fx[2], dfx[2], kx[2];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    const double f = 1 + kappa - kappa * if1[s];
+    const double VXP = -(COE2 / COE1) * cds[s];
+    const double EXP = 0.75 * VXP;
+    fx[s] = DS[s] * EXP * f;
+    const double DF1DD = 2 * (f1x[s] - 1) * (-(4.0 / 3.0) * iDS[s]);  // 2 (f1 - 1) DSDD / s
+    const double DFDD = kappa * DF1DD * if1[s] * if1[s];
+    dfx[s] = VXP * f + DS[s] * EXP * DFDD;
+    kx[s] = DS[s] * EXP * (2 * mu * sx[s] * (sx[s] * iG[s]) * 2 * iG[s]) * if1[s] * if1[s];
   }
-  const double Fx = 0.5 * (fx0 + fx1) * idt;
-  e = Fx + Fc;
-  v[0] = dfx0 + DFCDD[0];
-  v[1] = dfx1 + DFCDD[1];
-  // DEXDGD = DS Ex_unif DFDGD with GDS = 2 g: k * 2 g
-  dg[0] = kx0 * g[0] + kc * GDT0;
-  dg[1] = kx0 * g[1] + kc * GDT1;
-  dg[2] = kx0 * g[2] + kc * GDT2;
-  dg[3] = kx1 * g[3] + kc * GDT0;
-  dg[4] = kx1 * g[4] + kc * GDT1;
-  dg[5] = kx1 * g[5] + kc * GDT2;
+  if (SYM) {
+    fx[1] = fx[0];
+    dfx[1] = dfx[0];
+    kx[1] = kx[0];
+  }
+  e = 0.5 * (fx[0] + fx[1]) * idt + Fc;
+  v[0] = dfx[0] + DFCDD[0];
+  v[1] = dfx[1] + DFCDD[1];
+  dg[0] = kx[0] * g[0] + kc * GDT[0];
+  dg[1] = kx[0] * g[1] + kc * GDT[1];
+  dg[2] = kx[0] * g[2] + kc * GDT[2];
+  dg[3] = kx[1] * g[3] + kc * GDT[0];
+  dg[4] = kx[1] * g[4] + kc * GDT[1];
+  dg[5] = kx[1] * g[5] + kc * GDT[2];
 }
 
 struct GgaArgs {

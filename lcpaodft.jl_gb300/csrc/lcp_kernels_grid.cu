@@ -369,12 +369,39 @@ __global__ void __launch_bounds__(kRedThreads) xc_vpot_energy_g_kernel(const __g
       r1 = c.rho[1][x];
       lsda_ca(r0 + pc, r1 + pc, e, v[0], v[1]);
     }
-    const double dvh = c.dvh[x];
-    const double na = c.vna ? c.vna[x] : 0.0;
-    for (int s = 0; s < nv; ++s) c.vpot[s][x] = dvh + v[s] + na;
-    energy_terms(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, dvh, e, acc);
+    if (c.dvh) {
+      const double dvh = c.dvh[x];
+      const double na = c.vna ? c.vna[x] : 0.0;
+      for (int s = 0; s < nv; ++s) c.vpot[s][x] = dvh + v[s] + na;
+      energy_terms(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, dvh, e, acc);
+    } else {
+      // ahead of the Hartree potential: vxc only, the E_H1 term left to vpot_eh_g_kernel
+      for (int s = 0; s < nv; ++s) c.vpot[s][x] = v[s];
+      energy_terms(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, 0.0, e, acc);
+    }
   }
   block_reduce_store<3>(acc, c.part + t * 3);
+}
+
+// After an xc pass run without the Hartree potential (vpot holding vxc):
+// vpot = dVHart + vxc + V_na and the E_H1 tile partials, over the same tiles
+// and in the same order as the fused pass, so every sum keeps its bits.
+__global__ void __launch_bounds__(kRedThreads) vpot_eh_g_kernel(const __grid_constant__ GridArgs a) {
+  int64_t t;
+  const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
+  const int64_t x0 = t * kRedTile, x1 = min(c.nn, x0 + kRedTile);
+  double acc[1] = {0.0};
+  const int nv = a.spinpol == LCP_SPIN_OFF ? 1 : 2;
+  for (int64_t x = x0 + threadIdx.x; x < x1; x += kRedThreads) {
+    const double dvh = c.dvh[x];
+    const double na = c.vna ? c.vna[x] : 0.0;
+    for (int s = 0; s < nv; ++s) c.vpot[s][x] = dvh + c.vpot[s][x] + na;
+    const double r0 = c.rho[0][x];
+    const double ad = c.aden ? c.aden[x] : 0.0;
+    const double drho = a.spinpol == LCP_SPIN_OFF ? 2 * (r0 - ad) : r0 + c.rho[1][x] - 2 * ad;
+    acc[0] += drho * dvh;
+  }
+  block_reduce_store<1>(acc, c.part + t * 3);
 }
 
 // Sums of each cell's energy tile partials: sums[0..2] (one block per cell).
@@ -572,6 +599,13 @@ cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, con
   const unsigned n = tiled_blocks(b, red_tiles(c0.nn));
   if (n == 0) return cudaSuccess;
   xc_vpot_energy_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, xc, spinpol, 0));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vpot_eh_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st) {
+  const unsigned n = tiled_blocks(b, red_tiles(c0.nn));
+  if (n == 0) return cudaSuccess;
+  vpot_eh_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, 0, spinpol, 0));
   return cudaGetLastError();
 }
 
