@@ -548,6 +548,8 @@ __global__ void gather_offsets_kernel(const int64_t* __restrict__ pos, const int
 
 int grid_for(int64_t n, int threads) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 152 * 16)); }
 
+// Host -> device copy on the stream without waiting for it (unlike upload):
+// the callers keep `v` alive until they synchronise the stream.
 template <class T>
 cudaError_t to_device(DBuf& b, const std::vector<T>& v, cudaStream_t st) {
   cudaError_t e = b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T));
