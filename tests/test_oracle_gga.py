@@ -141,3 +141,16 @@ def test_diagonalize_nc_density_invariants():
     m = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)])
     np.testing.assert_allclose(m, np.stack([2 * d[2], -2 * d[3], d[0] - d[1]]), atol=1e-14)
     assert np.all(ph[:5] == 0.0) and np.all(th[5:8] == 0.5 * np.pi) and np.all(ph[5:8] == 0.0)
+
+
+def test_host_diff_coef_matches_oracle():
+    """The library's host Calc_Diff_Coef (C++, no GPU) against the oracle's."""
+    import lcpgrid as L
+    for lat, ng in ((SKEW, NG), (np.array([[5.1, 0, 5.1], [0, 5.1, 5.1], [5.1, 5.1, 0]]), (24, 24, 24)),
+                    (np.eye(3) * 7.0, (30, 32, 34))):
+        gl = o.glatvecs_of(lat, ng)
+        got = np.array(L.Calc_Diff_Coef(gl))
+        want = o.calc_diff_coef(gl)
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max())
+    with pytest.raises(L.LCPError):
+        L.Calc_Diff_Coef(np.zeros((3, 3)))  # singular fit: every neighbour at the centre
