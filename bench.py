@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section of the step bench line")
     ap.add_argument("--no-force", action="store_true", help="skip the grid force term section of the step bench line")
     ap.add_argument("--no-gga", action="store_true", help="skip the GGA-PBE section of the step bench line")
+    ap.add_argument("--no-nc", action="store_true", help="skip the non-collinear section of the step bench line")
     ap.add_argument("--xc", default="auto", choices=["auto", "GGA_PBE"],
                     help="xc of the timed step: auto = LDA ('off') / LSDA ('on'), or GGA_PBE")
     ap.add_argument("--serve-structures", type=int, default=24)
@@ -187,7 +188,11 @@ def force3_section(wl, u, dm, vna, reps=5):
     flops = force_work(u) * len(dm)
     fp64 = ctx.probe_fp64_tflops()
     ach = flops / (ms * 1e-3) / 1e12
-    return {"ms_per_call": ms, "calls": reps, "gradient_tabulation_s": t_tab,
+    try:
+        cpu = force3_cpu_baseline(wl, u, len(dm), reps=2)
+    except Exception as exc:  # the CPU side must not hide the GPU figures
+        cpu = {"value": None, "error": repr(exc)}
+    return {"ms_per_call": ms, "calls": reps, "gradient_tabulation_s": t_tab, "cpu_baseline": cpu,
             "max_abs_force": float(np.max(np.abs(F))),
             "roofline": {"bound": "fp64-alu", "achieved": ach, "peak": fp64, "unit": "TFLOP/s", "frac": ach / fp64,
                          "peak_source": "probe: FP64 FMA loop on this GPU",
@@ -248,6 +253,75 @@ def gga_section(wl, u, orbs, dm, vna, steps=10):
                                      % tuple(u.Ngrid)}
     out["roofline"] = {"bound": "fp64-alu", "note": "the PBE pass issues FP64 instructions at 87% of the FP64 "
                        "pipe's peak and the divergence pass at 76% (ncu); DRAM traffic is a few bytes per point"}
+    return out
+
+
+def force3_cpu_baseline(wl, ucell_gpu, nspin, reps=2):
+    """The oracle's Force3 (per-pair D phi_j and gradient dot products, as
+    _Calc_Force3_Blocked_Kernel!) on the pairs among the first 8 atoms, one
+    host core, extrapolated to the cell by the force work per pair."""
+    import numpy as np
+    from lcpgrid.workloads import psd_density_matrices_oracle, smooth_vna
+    from oracle import lcp_oracle as O
+    sample = [p for p in range(ucell_gpu.Nloop)
+              if ucell_gpu.MPI_atom[p] <= SAMPLE_ATOMS and ucell_gpu.MPI_natn[p] <= SAMPLE_ATOMS]
+    no = np.asarray(wl["numorbs"], dtype=np.float64)
+    a = ucell_gpu.MPI_atom - 1
+    b = ucell_gpu.MPI_natn - 1
+    wt = ucell_gpu.MPI_NumOLG.astype(np.float64) * (2 * no[a] * no[b] + 6 * no[a])
+    w_sample, w_total = float(wt[sample].sum()), float(wt.sum())
+    u = O.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+                total_numorbs=wl["numorbs"], pair_subset=sample)
+    pao = wl["paos"][0]
+    opao = O.PAO(pao.Spe_MaxL_Basis, pao.Spe_Num_Basis, pao.Spe_PAO_RV, pao.Spe_PAO_RWF)
+    first = set(range(SAMPLE_ATOMS))
+    orbs = O.set_orbitals_grid([opao], u, atoms=first)
+    dorbs = O.set_dorbitals_grid([opao], u, atoms=first)
+    dm = psd_density_matrices_oracle(u, wl["dm_seed"], trace=wl["trace"])[0]
+    vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.calc_force3("off", u, orbs, dorbs, [vna], [dm])
+    t = (time.perf_counter() - t0) / reps
+    ms = t * w_total / w_sample * nspin * 1e3
+    return {"value": ms, "unit": "ms per Force3 call", "cores": 1, "kind": "port",
+            "sample": "numpy oracle Force3 over the %d pairs among atoms 1-%d (%.2f%% of the force work) x %d, "
+                      "extrapolated by (2 NO_i NO_j + 6 NO_i) NumOLG" % (len(sample), SAMPLE_ATOMS,
+                                                                        100 * w_sample / w_total, reps)}
+
+
+def nc_section(wl, u, orbs, vna, steps=10):
+    """The same cell with the non-collinear channel set: four D/density/V/H
+    channels, diagonalize_nc_density!, LSDA rotated into four potentials;
+    split-BF16 step time (CUDA events), FP64 step time, energy error."""
+    import torch
+
+    import lcpgrid as L
+    from lcpgrid.workloads import psd_nc_density_matrices
+    dm = psd_nc_density_matrices(u, wl["dm_seed"], trace=wl["trace"])
+    out = {}
+    ctx = orbs.ctx
+    keep = ctx.precision
+    try:
+        for prec in ("bf16x3", "fp64"):
+            ctx.set_precision(prec)
+            job = L.GridStepJob(u, orbs, "nc", "LSDA", None, None, vna)
+            job.set_dm(dm)
+            for _ in range(2 if prec == "fp64" else 3):
+                job.step()
+            nrep = steps if prec == "bf16x3" else 1
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            torch.cuda.synchronize()
+            ev[0].record()
+            for _ in range(nrep):
+                job.step()
+            ev[1].record()
+            torch.cuda.synchronize()
+            out[prec] = {"ms_per_step": ev[0].elapsed_time(ev[1]) / nrep, "E_grid": float(job.energies()[4])}
+    finally:
+        ctx.set_precision(keep)
+    out["err_per_atom_uHa"] = abs(out["bf16x3"]["E_grid"] - out["fp64"]["E_grid"]) / wl["natom"] * 1e6
+    out["note"] = "four channels: one tensor-core density pass and one H pass per channel"
     return out
 
 
@@ -538,6 +612,11 @@ def run_ours(args):
             line["gga_pbe"] = gga_section(wl, u, orbs, dm, vna)
         except Exception as exc:  # the GGA section must not hide the step line
             line["gga_pbe"] = {"error": repr(exc)}
+    if rank == 0 and not args.no_nc and world == 1 and spin == "off":
+        try:
+            line["nc"] = nc_section(wl, u, orbs, vna)
+        except Exception as exc:  # the nc section must not hide the step line
+            line["nc"] = {"error": repr(exc)}
     if rank == 0 and not args.no_serving and world == 1:
         # the serving form on the same GPU: Poisson stream of mixed-size structures
         try:

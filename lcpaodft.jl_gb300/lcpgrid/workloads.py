@@ -115,6 +115,30 @@ def psd_density_matrices(ucell, seed, nspin=1, trace=256.0, nocc=None):
     return out
 
 
+def psd_nc_density_matrices(ucell, seed, trace=256.0, nocc=None):
+    """The four "nc" channels (Re11, Re22, Re12, Im12) of a seeded Hermitian
+    positive semi-definite 2x2-spinor density matrix M = C C^H (2 Norb x 2 Norb,
+    complex C), scaled to Tr(M) = trace, in the flat pair-block layout."""
+    rng = np.random.default_rng(seed)
+    no = np.asarray(ucell.Total_NumOrbs, dtype=np.int64)
+    off = np.concatenate([[0], np.cumsum(no)])
+    norb = int(off[-1])
+    nocc = nocc or max(1, norb // 4)
+    C = rng.normal(size=(2 * norb, nocc)) + 1j * rng.normal(size=(2 * norb, nocc))
+    M = C @ C.conj().T
+    M *= trace / np.trace(M).real
+    mats = [M[:norb, :norb].real, M[norb:, norb:].real, M[:norb, norb:].real, M[:norb, norb:].imag]
+    out = []
+    for m in mats:
+        dm = np.zeros(ucell.Total_Hsize)
+        for p, (a, b) in enumerate(zip(ucell.MPI_atom, ucell.MPI_natn)):
+            i, j = a - 1, b - 1
+            blk = m[off[i]:off[i + 1], off[j]:off[j + 1]]
+            dm[ucell.block_offset[p]:ucell.block_offset[p] + blk.size] = blk.reshape(-1)
+        out.append(dm)
+    return out
+
+
 def smooth_vna(ngrid, latvecs, seed, gmax=3.0, amplitude=0.5):
     """Real field from Fourier modes with |G| < gmax, random phases,
     scaled to max |V| = amplitude (Ha), C-order flat."""

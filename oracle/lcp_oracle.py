@@ -743,12 +743,17 @@ def set_orbitals_grid(paos, ucell, atoms=None):
     return res
 
 
-def set_dorbitals_grid(paos, ucell):
+def set_dorbitals_grid(paos, ucell, atoms=None):
     """Gradient tables [3][atom] -> [NumOrbs, GridN]
-    (src/Matrix/Set_dOrbitals_Grid.jl:23-362)."""
+    (src/Matrix/Set_dOrbitals_Grid.jl:23-362).  ``atoms`` restricts the
+    tabulation to those 0-based atoms (others None)."""
     rmin = 1.0e-13
     out = [[], [], []]
     for atom in range(ucell.Natom):
+        if atoms is not None and atom not in atoms:
+            for k in range(3):
+                out[k].append(None)
+            continue
         pao = paos[ucell.atom2spe[atom] - 1]
         rv = pao.Spe_PAO_RV
         x, y, z = _point_geometry(ucell, atom)
