@@ -571,8 +571,8 @@ def run_ours(args):
                 roof["note"] = ("achieved counts the FP64 algorithm's flops (folded pairs, no padding).  The "
                                 "split-BF16 form issues nine bf16 products per product (four MMAs with the B parts "
                                 "stacked along N) on 16-orbital blocks (13 used), so frac is bounded near 1/9 of "
-                                "that before padding; ncu shows the tensor pipe 40.6 %% active in the H kernel and "
-                                "DRAM at 27 %% (profiles/tc_kernels_si8_48cubed.md)")
+                                "that before padding; ncu shows the tensor pipe 40.6 % active in the H kernel and "
+                                "DRAM at 27 % (profiles/tc_kernels_si8_48cubed.md)")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     ms_step = total_ms / args.steps
