@@ -1089,6 +1089,14 @@ __device__ __forceinline__ void h_reduce_block(int64_t u, const int64_t* __restr
   float dh[8], dl[8], th[8], tl[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) dh[i] = dl[i] = th[i] = tl[i] = 0.0f;
+  const int fq = sb_fold[u], ch = sb_chunks[u];
+  const int ia = pr.atom[fq], ja = pr.jatom[fq];
+  const int noi = numorbs[ia], noj = numorbs[ja];
+  // rows of a partial past its atom's orbitals are padding: lane pair
+  // (2r, 2r+1) holds row r, which a direct partial indexes by the i chunk's
+  // orbitals and a transposed one by the j chunk's
+  const int row = lane >> 1;
+  const bool row_d = row < noi - (ch >> 8) * 16, row_t = row < noj - (ch & 255) * 16;
   const int64_t k0 = red_off[u], k1 = red_off[u + 1];
   for (int64_t kb = k0; kb < k1; kb += 256) {
     const int n = (int)min((int64_t)256, k1 - kb);
@@ -1102,6 +1110,7 @@ __device__ __forceinline__ void h_reduce_block(int64_t u, const int64_t* __restr
       for (int q = 0; q < 4; ++q) {
         const int jj = j + 8 * q;
         c[q] = jj < n ? s_code[jj] : -1;
+        if (c[q] >= 0 && !((c[q] & 1) ? row_t : row_d)) c[q] = -1;  // padding row: nothing to add
         if (c[q] >= 0) {
           const float4* src = reinterpret_cast<const float4*>(scratch + (c[q] >> 1) * 256) + lane * 2;
           v[q][0] = __ldg(src);
@@ -1134,14 +1143,11 @@ __device__ __forceinline__ void h_reduce_block(int64_t u, const int64_t* __restr
     lo += s_part[3][w][et];
   }
   const double acc = (double)hi + (double)lo;
-  const int q = sb_fold[u], ch = sb_chunks[u];
   const int ra = (ch >> 8) * 16 + a, rb = (ch & 255) * 16 + b;  // entry of the pair's block
-  const int i = pr.atom[q], jj = pr.jatom[q];
-  const int noi = numorbs[i], noj = numorbs[jj];
   if (ra < noi && rb < noj) {
     const double v = acc * dv;
-    H[pr.boff_p[q] + (int64_t)ra * noj + rb] = v;
-    if (!pr.self[q]) H[pr.boff_q[q] + (int64_t)rb * noi + ra] = v;
+    H[pr.boff_p[fq] + (int64_t)ra * noj + rb] = v;
+    if (!pr.self[fq]) H[pr.boff_q[fq] + (int64_t)rb * noi + ra] = v;
   }
 }
 
