@@ -116,3 +116,18 @@ def test_adenpcc_vs_oracle_on_device_ucell(ctx, spin):
     ar, pr, dr = O.set_adenpcc_grid(spin, init, angle, [pt], [vt], uo)
     for got, want in [(a, ar), (p, pr)] + list(zip(d, dr)):
         assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want))
+
+
+def test_adenpcc_two_species(ctx):
+    """Two species (Si and Fe tables) on one cell, spin "on": each atom reads
+    its own species' density and PCC tables."""
+    lat, pos, ng = si2_cell()
+    u = L.UCell(2, lat, 2, [1, 2], pos, [7.0, 6.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13], device=True, ctx=ctx)
+    uo = O.UCell(2, lat, 2, [1, 2], pos, [7.0, 6.0], ng, [0, 0, 0], total_numorbs=[13, 13])
+    sp = [_species("Si7.0", "Si_PBE19", 4.0), _species("Fe6.0H", "Fe_PBE19H", 16.0)]
+    tabs = [aden_tables("Si7.0", "Si_PBE19", 4.0), aden_tables("Fe6.0H", "Fe_PBE19H", 16.0)]
+    init = [[2.2, 1.8], [8.0, 6.0]]
+    a, p, d = L.Set_AdenPCC_Grid("on", init, None, [x[0] for x in sp], [x[1] for x in sp], u, ctx)
+    ar, pr, dr = O.set_adenpcc_grid("on", init, [[0, 0, 0, 0]] * 2, [t[0] for t in tabs], [t[1] for t in tabs], uo)
+    for got, want in [(a, ar), (p, pr)] + list(zip(d, dr)):
+        assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want))
