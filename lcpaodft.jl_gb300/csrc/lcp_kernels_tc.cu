@@ -98,13 +98,19 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 // a shared fixed-point grid: with a power-of-two scale S >= max|x|,
 // u = x / S in [-1, 1] is split as
 //
-//   u = hi + mid + lo + e,  hi = q1/2^7, mid = q2/2^15, lo = q3/2^23, |q| <= 128,
+//   u = hi + mid + lo + e,  hi = q1/2^8, mid = q2/2^17, lo = q3/2^26, |q| <= 256,
 //
-// so every part is an exact BF16 value and |e| <= 2^-24.  All nine part
-// products are formed (the mid*lo and lo*lo terms carry the small tails of
-// the orbitals, which a six-term product loses).  hi*hi' (integer multiples
-// of 2^-14) has its own accumulator, exact up to 1024 terms; the rest are
-// 2^-8 and smaller and go to one accumulator (density) or three more, one
+// so every part is an exact BF16 value (BF16 holds every integer up to 256
+// in magnitude: 8 significant bits, and 256 = 2^8) and |e| <= 2^-27.  The
+// quantisation error of the energies scales with the last part's quantum,
+// so nine bits per part (27 in all) instead of eight cut it by 8x at no
+// cost.  All nine part products are formed (the mid*lo and lo*lo terms carry
+// the small tails of the orbitals, which a six-term product loses).  hi*hi'
+// (integer multiples of 2^-16) has its own accumulator, exact while the sum
+// stays below 256 in magnitude (2^24 quanta: 512 terms of the largest size
+// for D, whose scale is twice its maximum, and 256 for the matrix elements);
+// the rest are 2^-9 and smaller and go to one accumulator (density) or
+// three more, one
 // per quantum (matrix elements).  What remains is the input quantisation e.
 // ==========================================================================
 
@@ -119,10 +125,10 @@ constexpr int kDsymElems = 768;                // D block: hi, mid, lo (256 each
 constexpr uint32_t kALbo = 2048, kASbo = 128;  // table block [h][g][8 pt][8 orb] as K-major A
 
 __device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
-  const double h = rint(u * 128.0) * (1.0 / 128.0);
+  const double h = rint(u * 256.0) * (1.0 / 256.0);
   const double r1 = u - h;
-  const double m = rint(r1 * 32768.0) * (1.0 / 32768.0);
-  const double l = rint((r1 - m) * 8388608.0) * (1.0 / 8388608.0);
+  const double m = rint(r1 * 131072.0) * (1.0 / 131072.0);
+  const double l = rint((r1 - m) * 67108864.0) * (1.0 / 67108864.0);
   hi = __float2bfloat16_rn((float)h);
   mid = __float2bfloat16_rn((float)m);
   lo = __float2bfloat16_rn((float)l);
@@ -132,21 +138,25 @@ __device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloa
 // (|e| <= 2^-23 |p|), in full-rate FP32 instructions only.  Rounding to an
 // integer uses the constant C = 1.5 * 2^23: for |x| <= 2^22, fma(y, 2^k, C)
 // lies in [2^23, 2^24) where the spacing is 1, so it rounds y * 2^k (exact)
-// to the nearest integer (ties to even) and subtracting C is exact.  Every
-// step but the last rounding is exact: p - hi and r1 - mid are multiples of
-// ulp(p) (resp. ulp(r1)) below 2^24 of them, so the parts are those of p + e
-// up to |lo residual| <= 2^-24.
+// to the nearest integer (ties to even) and subtracting C is exact.
+//   - r1 = p - hi is exact: hi is a multiple of 2^-8, itself a multiple of
+//     ulp(p), and |r1| <= 2^-9.
+//   - e joins r1 before mid is taken (one rounding, <= 2^-34), so that
+//     |r1 + e| * 2^17 <= 256 + 2^-6 and |mid| stays within 256 quanta.
+//   - r2 = (r1 + e) - mid is exact by the same argument, |r2| <= 2^-18, so
+//     |2^26 * r2| <= 256 and lo is exact too.
+// The parts are those of p + e up to |lo residual| <= 2^-27 + 2^-34.
 __device__ __forceinline__ void fx_split_f(float p, float e, __nv_bfloat16& hi, __nv_bfloat16& mid,
                                            __nv_bfloat16& lo) {
   constexpr float C = 12582912.0f;
-  const float hs = fmaf(p, 128.0f, C) - C;              // 2^7 * hi, an integer in [-128, 128]
-  const float r1 = fmaf(hs, -0.0078125f, p);            // p - hi, exact
-  const float ms = fmaf(r1, 32768.0f, C) - C;           // 2^15 * mid
-  const float r2 = fmaf(ms, -(1.0f / 32768.0f), r1) + e;
-  const float ls = fmaf(r2, 8388608.0f, C) - C;         // 2^23 * lo
-  hi = __float2bfloat16_rn(hs * 0.0078125f);
-  mid = __float2bfloat16_rn(ms * (1.0f / 32768.0f));
-  lo = __float2bfloat16_rn(ls * (1.0f / 8388608.0f));
+  const float hs = fmaf(p, 256.0f, C) - C;              // 2^8 * hi, an integer in [-256, 256]
+  const float r1 = fmaf(hs, -0.00390625f, p) + e;       // p - hi exact, then + e
+  const float ms = fmaf(r1, 131072.0f, C) - C;          // 2^17 * mid
+  const float r2 = fmaf(ms, -(1.0f / 131072.0f), r1);   // exact
+  const float ls = fmaf(r2, 67108864.0f, C) - C;        // 2^26 * lo
+  hi = __float2bfloat16_rn(hs * 0.00390625f);
+  mid = __float2bfloat16_rn(ms * (1.0f / 131072.0f));
+  lo = __float2bfloat16_rn(ls * (1.0f / 67108864.0f));
 }
 
 // Float-float accumulation (Knuth's TwoSum): hi + lo carries the running sum
@@ -733,11 +743,13 @@ constexpr int kHABytes = kHGroup * kImgBytes;   // one part of the A operand
 constexpr int kHBBytes = kHWin * kImgBytes;     // one part of a B stage
 constexpr size_t kHSmem = 3 * (size_t)kHABytes + (size_t)kHStages * 3 * kHBBytes;  // 192 KB
 // TMEM: two tile buffers of 256 columns; inside one, the four accumulators
-// (64 columns each), one per quantum of the products: hi*hi (2^-14),
-// hi*mid + mid*hi (2^-22), hi*lo + lo*hi + mid*mid (2^-30),
-// mid*lo + lo*mid + lo*lo (2^-38; lo*lo is the only term finer than its
-// quantum).  Over the 128 points of a brick the first three sums stay below
-// 2^24 of their quanta, so they are exact in FP32.  Four MMAs per K step
+// (64 columns each), one per quantum of the products: hi*hi (2^-16),
+// hi*mid + mid*hi (2^-25), hi*lo + lo*hi + mid*mid (2^-34),
+// mid*lo + lo*mid + lo*lo (2^-43; lo*lo is the only term finer than its
+// quantum).  Over the 128 points of a brick the first two sums stay within
+// 2^24 of their quanta (128 terms of at most 1, 256 of at most 2^-9), so
+// they are exact in FP32; the third could exceed it only if all of its 384
+// terms were near their bound with one sign.  Four MMAs per K step
 // fill them (B parts stacked along N), reading 34 KB of operands instead of
 // the 54 KB of nine separate products: the MMAs are bound by shared-memory
 // operand bandwidth (~128 B/clock), not by the tensor pipe.
@@ -917,7 +929,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
                            dal = tc::smem_desc(a0 + 2 * kHABytes + ko, 128, 2048);
             const uint64_t dbh = tc::smem_desc(b0 + ko, 128, 2048),  // [hi | mid | lo] from here
                            dbl = tc::smem_desc(b0 + 2 * kHBBytes + ko, 128, 2048);
-            // Accumulator k (quantum 2^-(14+8k)) at columns d0 + 64k: a product
+            // Accumulator k (quantum 2^-(16+9k)) at columns d0 + 64k: a product
             // of parts (i, j) lands in accumulator i + j when the MMA with
             // A part i starts at column d0 + 64 i.  lo*lo shares the last one.
             const uint32_t acc = ks > 0 ? 1u : 0u;
