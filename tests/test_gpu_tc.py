@@ -164,7 +164,7 @@ def test_job_energy_bf16x3_mx2(ctx):
     for prec in ("fp64", "bf16x3"):
         ctx.set_precision(prec)
         try:
-            job = L.GridStepJob(u, orbs, "on", "LDA", None, None, vna)
+            job = L.GridStepJob(u, orbs, "on", "LSDA", None, None, vna)
             job.set_dm(dm)
             job.step()
             E[prec] = job.energies()[4]
