@@ -722,12 +722,12 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
 // (brick, s-group of kHGroup images, t-window of kHWin images t >= the
 // group's first image); V weights the t side:
 //   warp 0     producer: per s-group the plain tables of its images into the
-//              A region (after a_free), per tile the raw t window into one of
-//              kHStages B stages -- one bulk copy per part, the images of a
-//              brick being consecutive blocks;
-//   warps 6-13 per tile the V-weighted fixed-point split of the B stage, in
-//              place (b_ready), with the brick's V / S_V prepared by
-//              vweight_kernel;
+//              A region (after a_free) -- one bulk copy per part, the images
+//              of a brick being consecutive blocks;
+//   warps 6-13 per tile the raw t window from the tables into registers,
+//              then (after b_empty) its V-weighted fixed-point split into one
+//              of kHStages B stages (b_ready), with the brick's V / S_V
+//              prepared by vweight_kernel;
 //   warp 1     MMA issuer: 8 K steps x 4 MMAs per tile into one of two TMEM
 //              tile buffers (4 accumulators x 64 columns each); after the
 //              group's last tile it commits a_free;
@@ -796,17 +796,16 @@ __global__ void __launch_bounds__(128) vweight_kernel(const __grid_constant__ Tc
 
 __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_kernel(const __grid_constant__ TcHamArgs args) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t bfull_bar[kHStages], bready_bar[kHStages], bempty_bar[kHStages], tfull_bar[2], tempty_bar[2];
+  __shared__ uint64_t bready_bar[kHStages], bempty_bar[kHStages], tfull_bar[2], tempty_bar[2];
   __shared__ uint64_t afull_bar, afree_bar, drain_bar;
   __shared__ uint32_t tslot;
   __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   uint8_t* sA = smem;                  // [part][s image][4096 B], plain tables
-  uint8_t* sB0 = smem + 3 * kHABytes;  // stages of [part][t image][4096 B], V-weighted in place
+  uint8_t* sB0 = smem + 3 * kHABytes;  // stages of [part][t image][4096 B], V-weighted
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (tid == 32) {
     for (int s = 0; s < kHStages; ++s) {
-      tc::mbar_init(&bfull_bar[s], 1);
       tc::mbar_init(&bready_bar[s], 32 * kHXformWarps);
       tc::mbar_init(&bempty_bar[s], 1);
     }
@@ -831,36 +830,15 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   };
 
   if (warp == 0) {
-    // ------------------------------------------------------------ producer
-    uint32_t it = 0, grp = 0;
-    // B tile `it` (images t0 .. t0+nt-1 of brick i0) into its stage
-    auto load_b = [&](const TcCell& cl, int64_t i0, int t0, int nt) -> bool {
-      const int stage = (int)(it % kHStages);
-      const uint32_t use = it / kHStages;
-      if (use > 0 && !tc::mbar_wait_abortable(&bempty_bar[stage], (use - 1) & 1, &abort_flag)) return false;
-      uint8_t* sB = sB0 + stage * 3 * kHBBytes;
-      if (lane == 0) {
-        tc::mbar_arrive_expect_tx(&bfull_bar[stage], nt * 3 * kImgBytes);
-        for (int part = 0; part < 3; ++part)
-          tc::bulk_g2s(sB + part * kHBBytes, cl.tab + ((int64_t)part * cl.nblocks + i0 + t0) * kPart,
-                       nt * kImgBytes, &bfull_bar[stage]);
-      }
-      __syncwarp();
-      ++it;
-      return true;
-    };
+    // ------------------------------------------------------------ producer: the A operand
+    uint32_t grp = 0;
     for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
       const int m = (int)(cl.img_off[hb + 1] - i0);
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup, ++grp) {
-        // the group's first B tile goes ahead of the A refill, which waits
-        // for the previous group's MMAs
-        if (!load_b(cl, i0, s0, min(kHWin, m - s0))) {
-          give_up();
-          break;
-        }
+        // the refill waits for the previous group's MMAs
         if (grp > 0 && !tc::mbar_wait_abortable(&afree_bar, (grp - 1) & 1, &abort_flag)) {
           give_up();
           break;
@@ -873,17 +851,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
                          na * kImgBytes, &afull_bar);
         }
         __syncwarp();
-        bool ok = true;
-        for (int t0 = s0 + kHWin; t0 < m && ok; t0 += kHWin) ok = load_b(cl, i0, t0, min(kHWin, m - t0));
-        if (!ok) {
-          give_up();
-          break;
-        }
       }
-    }
-    for (int s = 0; s < kHStages; ++s) {
-      const uint32_t uses = it / kHStages + ((uint32_t)s < it % kHStages ? 1u : 0u);
-      if (uses > 0 && !tc::mbar_wait(&bfull_bar[s], (uses - 1) & 1, 1u << 24)) give_up();
     }
     if (grp > 0 && !tc::mbar_wait(&afull_bar, (grp - 1) & 1, 1u << 24)) give_up();
   } else if (warp == 1) {
@@ -957,9 +925,16 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     }
     __syncwarp();
   } else if (warp >= 6) {
-    // ------------------------------------------------------------ V-weighting of the B tiles
-    const int tt = tid - 192;  // transform thread: always the same 8-orbital chunk q = tt of an image
-    static_assert(32 * kHXformWarps == 256, "one transform thread per chunk of an image");
+    // ------------------------------------------------------------ B tiles: load and V-weight
+    // Each thread owns chunk q = tt of every image of a tile: 8 orbitals of
+    // one point slot, all three parts.  It loads the tile's raw parts from
+    // the tables into registers (coalesced 16-byte loads, before waiting for
+    // the stage, so their latency overlaps the MMAs still reading it), then
+    // writes the V-weighted split into the stage.  Staging the raw tile in
+    // shared memory first made load, weighting and MMAs three chained phases
+    // over two stages; a third stage does not fit beside the A operand.
+    const int tt = tid - 192;
+    static_assert(32 * kHXformWarps == 256, "one B thread per chunk of an image");
     const int pt = ((tt >> 3) & 15) * 8 + (tt & 7);  // its point slot
     uint32_t it = 0;
     for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
@@ -970,41 +945,49 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
       if (m == 0) continue;
       const float2 w = cl.vw[hb * 128 + pt];
       const float vh = w.x, vl = w.y;
+      const uint4* tab4 = reinterpret_cast<const uint4*>(cl.tab) + tt;  // 16-byte chunk tt of block 0, part 0
+      const int64_t pstride = cl.nblocks * (kPart / 8);                 // one part, in 16-byte chunks
       for (int s0 = 0; s0 < m && !abort_flag; s0 += kHGroup) {
         for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
           const int nt = min(kHWin, m - t0);
           const int stage = (int)(it % kHStages);
-          if (!tc::mbar_wait_abortable(&bfull_bar[stage], (it / kHStages) & 1, &abort_flag)) {
+          const uint32_t use = it / kHStages;
+          uint4 raw[kHWin][3];
+          const uint4* src = tab4 + (i0 + t0) * (kPart / 8);
+#pragma unroll
+          for (int j = 0; j < kHWin; ++j) {
+            if (j < nt) {
+#pragma unroll
+              for (int part = 0; part < 3; ++part) raw[j][part] = __ldg(src + part * pstride + j * (kPart / 8));
+            }
+          }
+          if (use > 0 && !tc::mbar_wait_abortable(&bempty_bar[stage], (use - 1) & 1, &abort_flag)) {
             give_up();
             break;
           }
-          uint8_t* sB = sB0 + stage * 3 * kHBBytes;
-          // in place: V-weighted fixed-point split of the raw t images; chunk c
-          // = (image, q): 8 orbitals of point slot q's point (all three parts)
-          for (int c = tt; c < nt * 256; c += 32 * kHXformWarps) {
-            const int img = c >> 8, q = c & 255;  // q = (h*16 + g)*8 + r
-            uint4* ph = reinterpret_cast<uint4*>(sB + img * kImgBytes + q * 16);
-            uint4* pm = reinterpret_cast<uint4*>(sB + kHBBytes + img * kImgBytes + q * 16);
-            uint4* pl = reinterpret_cast<uint4*>(sB + 2 * kHBBytes + img * kImgBytes + q * 16);
-            const uint4 rh = *ph, rm = *pm, rl = *pl;
-            const __nv_bfloat16* xb_h = reinterpret_cast<const __nv_bfloat16*>(&rh);
-            const __nv_bfloat16* xb_m = reinterpret_cast<const __nv_bfloat16*>(&rm);
-            const __nv_bfloat16* xb_l = reinterpret_cast<const __nv_bfloat16*>(&rl);
-            uint4 oh, om, ol;
-            __nv_bfloat16* xh = reinterpret_cast<__nv_bfloat16*>(&oh);
-            __nv_bfloat16* xm = reinterpret_cast<__nv_bfloat16*>(&om);
-            __nv_bfloat16* xl = reinterpret_cast<__nv_bfloat16*>(&ol);
+          uint8_t* sB = sB0 + stage * 3 * kHBBytes + tt * 16;
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              const float u = (__bfloat162float(xb_h[e]) + __bfloat162float(xb_m[e])) + __bfloat162float(xb_l[e]);
-              // u * (vh + vl) = pr + er exactly up to u*vl's rounding (~2^-48)
-              const float pr = u * vh;
-              const float er = fmaf(u, vh, -pr) + u * vl;
-              fx_split_f(pr, er, xh[e], xm[e], xl[e]);
+          for (int j = 0; j < kHWin; ++j) {
+            if (j < nt) {
+              const __nv_bfloat16* xb_h = reinterpret_cast<const __nv_bfloat16*>(&raw[j][0]);
+              const __nv_bfloat16* xb_m = reinterpret_cast<const __nv_bfloat16*>(&raw[j][1]);
+              const __nv_bfloat16* xb_l = reinterpret_cast<const __nv_bfloat16*>(&raw[j][2]);
+              uint4 oh, om, ol;
+              __nv_bfloat16* xh = reinterpret_cast<__nv_bfloat16*>(&oh);
+              __nv_bfloat16* xm = reinterpret_cast<__nv_bfloat16*>(&om);
+              __nv_bfloat16* xl = reinterpret_cast<__nv_bfloat16*>(&ol);
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                const float u = (__bfloat162float(xb_h[e]) + __bfloat162float(xb_m[e])) + __bfloat162float(xb_l[e]);
+                // u * (vh + vl) = pr + er exactly up to u*vl's rounding (~2^-48)
+                const float pr = u * vh;
+                const float er = fmaf(u, vh, -pr) + u * vl;
+                fx_split_f(pr, er, xh[e], xm[e], xl[e]);
+              }
+              *reinterpret_cast<uint4*>(sB + j * kImgBytes) = oh;
+              *reinterpret_cast<uint4*>(sB + kHBBytes + j * kImgBytes) = om;
+              *reinterpret_cast<uint4*>(sB + 2 * kHBBytes + j * kImgBytes) = ol;
             }
-            *ph = oh;
-            *pm = om;
-            *pl = ol;
           }
           tc::fence_proxy_async_smem();
           tc::mbar_arrive(&bready_bar[stage]);
