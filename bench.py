@@ -41,15 +41,17 @@ UNIT = "grid steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32", "fp64"])
     ap.add_argument("--workload", default="si64", choices=["si64", "si8", "mx2"])
     ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 drop-in form")
+    ap.add_argument("--fp32-steps", type=int, default=3,
+                    help="timed steps of the FP32 form (CUDA-core FP32 pair contractions), for comparison")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--serving", action="store_true", help="run the serving form instead of the step bench")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section of the step bench line")
     ap.add_argument("--no-force", action="store_true", help="skip the grid force term section of the step bench line")
@@ -491,6 +493,23 @@ def run_ours(args):
         fe[1].record(stream)
         torch.cuda.synchronize()
         fp64_ms = fe[0].elapsed_time(fe[1]) / args.fp64_steps
+    # the FP32 form of the same step (density and H in FP32 on the CUDA
+    # cores, the rest FP64), the third precision of the comparison
+    fp32_form = None
+    if args.precision == "bf16x3" and args.fp32_steps > 0:
+        ctx.set_precision("fp32")
+        job.step()
+        e_fp32 = job.energies()
+        fe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        fe[0].record(stream)
+        for _ in range(args.fp32_steps):
+            job.step()
+        fe[1].record(stream)
+        torch.cuda.synchronize()
+        fp32_form = {"ms_per_step": fe[0].elapsed_time(fe[1]) / args.fp32_steps, "steps": args.fp32_steps,
+                     "err_per_atom_uHa": abs(e_fp32[4] - e_fp64[4]) / u.Natom * 1e6,
+                     "rel_err": abs(e_fp32[4] - e_fp64[4]) / abs(e_fp64[4])}
     ctx.set_precision(args.precision)
 
     for _ in range(max(3, args.warmup)):
@@ -603,6 +622,7 @@ def run_ours(args):
                    "terms_this_form": [float(x) for x in e_now], "terms_fp64": [float(x) for x in e_fp64]},
         "fp64_dropin": None if fp64_ms is None else {
             "ms_per_step": fp64_ms, "steps": args.fp64_steps, "speedup_of_this_form": fp64_ms / ms_step},
+        "fp32_form": fp32_form,
         "clocks": clk,
         "gpu_launches": int(launches),
         "gpu_launches_note": "library kernels per timed region; cuFFT adds 2 FFT launches per step",
