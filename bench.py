@@ -33,8 +33,8 @@ METRIC = "ms per SCF grid step & jobs/s (p50/p99) split-BF16 vs FP64, <=1uHa/ato
 # DRAM bytes per table block of one split-BF16 stage launch (ncu, 8-atom 48^3
 # cell: density_tc_kernel 149.7 + 3.3 MB; hamiltonian_tc_kernel 150.1 + 55.9 MB
 # and h_reduce_kernel 93.6 + 3.2 MB, over 12076 blocks)
-TRAFFIC_PER_BLOCK = {"density": (149.69e6 + 3.33e6) / 12076,
-                     "hamiltonian": (150.05e6 + 55.90e6 + 93.62e6 + 3.18e6) / 12076}
+TRAFFIC_PER_BLOCK = {"density": (149.71e6 + 3.85e6) / 12076,
+                     "hamiltonian": (150.05e6 + 56.28e6 + 93.62e6 + 3.18e6) / 12076}
 UNIT = "grid steps/s"
 
 
@@ -253,8 +253,8 @@ def gga_section(wl, u, orbs, dm, vna, steps=10):
     out["cpu_baseline"] = {"value": cpu_s * 1e3, "unit": "ms per GGA xc pass", "cores": 1, "kind": "port",
                            "sample": "the oracle's gradient + PBE + divergence pass on the same %dx%dx%d density"
                                      % tuple(u.Ngrid)}
-    out["roofline"] = {"bound": "fp64-alu", "note": "the PBE pass issues FP64 instructions at 87% of the FP64 "
-                       "pipe's peak and the divergence pass at 76% (ncu); DRAM traffic is a few bytes per point"}
+    out["roofline"] = {"bound": "fp64-alu", "note": "the PBE pass issues FP64 instructions at 85% of the FP64 "
+                       "pipe's peak and the divergence pass at 80% (ncu); DRAM traffic is a few bytes per point"}
     return out
 
 
@@ -590,8 +590,8 @@ def run_ours(args):
                 roof["note"] = ("achieved counts the FP64 algorithm's flops (folded pairs, no padding).  The "
                                 "split-BF16 form issues nine bf16 products per product (four MMAs with the B parts "
                                 "stacked along N) on 16-orbital blocks (13 used), so frac is bounded near 1/9 of "
-                                "that before padding; ncu shows the tensor pipe 40.6 % active in the H kernel and "
-                                "DRAM at 27 % (profiles/tc_kernels_si8_48cubed.md)")
+                                "that before padding; ncu shows the tensor pipe 42.9 % active in the H kernel and "
+                                "DRAM at 29 % (profiles/tc_kernels_si8_48cubed.md)")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     ms_step = total_ms / args.steps
