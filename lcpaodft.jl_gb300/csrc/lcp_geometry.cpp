@@ -759,13 +759,27 @@ std::string build_bricks(const UCell& u, Bricks& b, const int32_t* shape) {
       }
   }
   b.slot_base[b.nbricks] = gslot;
+  // The reduction visits the sub-blocks longest first (stable, so the order is
+  // fixed): their partial counts range from a few to thousands (self pairs),
+  // and a long one started last would run alone at the end of the launch.
+  // Each sub-block's own sum keeps its order, so H is the same bits.
+  std::vector<int64_t> order(nsb);
+  for (int64_t q = 0; q < nsb; ++q) order[q] = q;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t x, int64_t y) { return per_sb[x].size() > per_sb[y].size(); });
+  std::vector<int32_t> fold_o(nsb), chunks_o(nsb);
   b.red_off.assign(nsb + 1, 0);
   b.red_slot.clear();
   b.red_slot.reserve(gslot);
-  for (int64_t q = 0; q < nsb; ++q) {
+  for (int64_t k = 0; k < nsb; ++k) {
+    const int64_t q = order[k];
+    fold_o[k] = b.sb_fold[q];
+    chunks_o[k] = b.sb_chunks[q];
     b.red_slot.insert(b.red_slot.end(), per_sb[q].begin(), per_sb[q].end());
-    b.red_off[q + 1] = (int64_t)b.red_slot.size();
+    b.red_off[k + 1] = (int64_t)b.red_slot.size();
   }
+  b.sb_fold.swap(fold_o);
+  b.sb_chunks.swap(chunks_o);
   return "";
 }
 

@@ -100,7 +100,7 @@ struct Bricks {
   std::vector<int32_t> sub_chunks;   // [nsub] (row chunk << 8) | column chunk
   // 16 x 16 sub-blocks of the folded pairs' H blocks (kept orientation)
   std::vector<int64_t> sb_off;       // [n_unique+1]
-  std::vector<int32_t> sb_fold;      // [nsb] folded pair of each sub-block
+  std::vector<int32_t> sb_fold;      // [nsb] folded pair of each sub-block (reduction order: longest first)
   std::vector<int32_t> sb_chunks;    // [nsb] (row chunk << 8) | column chunk
   std::vector<int64_t> red_off;      // [nsb+1] CSR of slots per sub-block
   std::vector<int64_t> red_slot;     // global slot * 2 + (1 if the slot enters transposed)
