@@ -425,6 +425,16 @@ __device__ __forceinline__ const TcCell* tc_cell(const TcCell* c0, const TcBatch
 }
 
 
+// Brick of round j for this CTA of a persistent launch: the brick list is
+// sorted heaviest first and cut into rounds of gridDim.x consecutive bricks,
+// taken in alternating directions so that no CTA gets the heavier brick of
+// every round.  -1 past the end (the last round may be partial).  Every role
+// of a CTA walks the same sequence.
+__device__ __forceinline__ int64_t round_brick(int64_t j, int64_t ntotal) {
+  const int64_t g = gridDim.x, k = j * g + ((j & 1) ? g - 1 - (int64_t)blockIdx.x : (int64_t)blockIdx.x);
+  return k < ntotal ? k : -1;
+}
+
 // Density kernel roles (448 threads, one CTA per SM, persistent over bricks):
 //   warp 0     table producer: per K step (brick, window, image t) three 4 KB
 //              bulk copies of t's table block (operand A), completing as
@@ -488,7 +498,9 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
   if (warp == 0) {
     // ------------------------------------------------------------ table producer
     uint32_t it = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -522,7 +534,9 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
     // ------------------------------------------------------------ D gatherers
     const int gw = warp - 6;
     uint32_t it = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -584,7 +598,9 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     uint32_t it = 0, win = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -653,7 +669,9 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
     const uint32_t quarter = warp & 3;  // TMEM lanes [32 * quarter, 32 * quarter + 32)
     const int p = (int)quarter * 32 + lane;
     uint32_t it = 0, win = 0, mpar = 0;  // mpar: phase bit of mdone_bar per stage
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -832,7 +850,9 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   if (warp == 0) {
     // ------------------------------------------------------------ producer: the A operand
     uint32_t grp = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -857,7 +877,9 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     uint32_t it = 0, grp = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -937,7 +959,9 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     static_assert(32 * kHXformWarps == 256, "one B thread per chunk of an image");
     const int pt = ((tt >> 3) & 15) * 8 + (tt & 7);  // its point slot
     uint32_t it = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
@@ -999,7 +1023,9 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
     const uint32_t quarter = warp & 3;
     const int row = (int)quarter * 32 + lane;  // TMEM lane = M row = (s image, orbital)
     uint32_t it = 0;
-    for (int64_t k = blockIdx.x; k < ntotal && !abort_flag; k += gridDim.x) {
+    for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
+      const int64_t k = round_brick(j, ntotal);
+      if (k < 0) continue;
       int64_t hb;
       const TcCell& cl = *tc_cell(&args.cell0, args.batch, k, hb);
       const int64_t i0 = cl.img_off[hb];
