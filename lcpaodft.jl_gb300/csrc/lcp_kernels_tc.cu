@@ -1099,14 +1099,25 @@ __device__ __forceinline__ void ff_add8(float* hi, float* lo, float4 a, float4 b
   ff_add(hi[4], lo[4], b.x); ff_add(hi[5], lo[5], b.y); ff_add(hi[6], lo[6], b.z); ff_add(hi[7], lo[7], b.w);
 }
 
+constexpr int kRedRing = 8;        // partial blocks in flight per warp
+constexpr int kRedCodes = 1024;    // slot codes staged per pass
+// ring [warp][buffer][256 floats] (lane l owns floats 8l .. 8l+7 of each
+// buffer), then the staged slot codes; the ring is reused for the warps' sums
+constexpr size_t kRedRingBytes = (size_t)8 * kRedRing * 1024;
+constexpr size_t kRedSmem = kRedRingBytes + kRedCodes * sizeof(int64_t);  // 72 KB
+static_assert(kRedRingBytes >= 4 * 8 * 256 * sizeof(float), "the ring holds the warps' partial sums");
+
 __device__ __forceinline__ void h_reduce_block(int64_t u, const int64_t* __restrict__ red_off,
                                                const int64_t* __restrict__ red_slot,
                                                const int32_t* __restrict__ sb_fold,
                                                const int32_t* __restrict__ sb_chunks,
                                                const float* __restrict__ scratch, const DevPairs& pr,
                                                const int32_t* __restrict__ numorbs, double dv, double* H,
-                                               int64_t* s_code, float (*s_part)[8][256]) {
+                                               uint8_t* smem) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int64_t* s_code = reinterpret_cast<int64_t*>(smem + kRedRingBytes);
+  float (*s_part)[8][256] = reinterpret_cast<float (*)[8][256]>(smem);
+  float* my = reinterpret_cast<float*>(smem) + (warp * kRedRing) * 256 + lane * 8;
   float dh[8], dl[8], th[8], tl[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) dh[i] = dl[i] = th[i] = tl[i] = 0.0f;
@@ -1119,34 +1130,50 @@ __device__ __forceinline__ void h_reduce_block(int64_t u, const int64_t* __restr
   const int row = lane >> 1;
   const bool row_d = row < noi - (ch >> 8) * 16, row_t = row < noj - (ch & 255) * 16;
   const int64_t k0 = red_off[u], k1 = red_off[u + 1];
-  for (int64_t kb = k0; kb < k1; kb += 256) {
-    const int n = (int)min((int64_t)256, k1 - kb);
+  for (int64_t kb = k0; kb < k1; kb += kRedCodes) {
+    const int n = (int)min((int64_t)kRedCodes, k1 - kb);
+    __syncthreads();  // the previous pass's (or sub-block's) readers are done
+    for (int i = tid; i < n; i += blockDim.x) s_code[i] = red_slot[kb + i];
     __syncthreads();
-    if (tid < n) s_code[tid] = red_slot[kb + tid];
-    __syncthreads();
-    for (int j = warp; j < n; j += 32) {  // slots j, j+8, j+16, j+24 in flight together
-      float4 v[4][2];
-      int64_t c[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int jj = j + 8 * q;
-        c[q] = jj < n ? s_code[jj] : -1;
-        if (c[q] >= 0 && !((c[q] & 1) ? row_t : row_d)) c[q] = -1;  // padding row: nothing to add
-        if (c[q] >= 0) {
-          const float4* src = reinterpret_cast<const float4*>(scratch + (c[q] >> 1) * 256) + lane * 2;
-          v[q][0] = __ldg(src);
-          v[q][1] = __ldg(src + 1);
-        }
+    // warp w adds slots w, w + 8, w + 16, ... in that order.  Each lane
+    // copies its own 32 bytes of a partial into the warp's ring (cp.async,
+    // kRedRing partials ahead) and reads back only those, so its own
+    // wait_group is all the synchronisation it needs.
+    const int cnt = warp < n ? (n - warp + 7) / 8 : 0;
+    auto code_of = [&](int i) -> int64_t {
+      const int64_t c = s_code[warp + 8 * i];
+      return ((c & 1) ? row_t : row_d) ? c : -1;  // padding row: nothing to add
+    };
+    auto issue = [&](int i) {
+      const int64_t c = code_of(i);
+      if (c >= 0) {
+        const float* src = scratch + (c >> 1) * 256 + lane * 8;
+        float* dst = my + (i % kRedRing) * 256;
+        cp_async16(dst, src);
+        cp_async16(dst + 4, src + 4);
       }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (c[q] < 0) continue;
-        if (c[q] & 1) ff_add8(th, tl, v[q][0], v[q][1]);
-        else ff_add8(dh, dl, v[q][0], v[q][1]);
-      }
+    };
+#pragma unroll 1
+    for (int i = 0; i < kRedRing; ++i) {
+      if (i < cnt) issue(i);
+      cp_async_commit();
     }
+#pragma unroll 1
+    for (int i = 0; i < cnt; ++i) {
+      cp_async_wait<kRedRing - 1>();  // this lane's copies of slot i have landed
+      const int64_t c = code_of(i);
+      if (c >= 0) {
+        const float* b = my + (i % kRedRing) * 256;
+        const float4 x = *reinterpret_cast<const float4*>(b), y = *reinterpret_cast<const float4*>(b + 4);
+        if (c & 1) ff_add8(th, tl, x, y);
+        else ff_add8(dh, dl, x, y);
+      }
+      if (i + kRedRing < cnt) issue(i + kRedRing);
+      cp_async_commit();
+    }
+    cp_async_wait<0>();
   }
-  __syncthreads();  // the previous sub-block's readers of s_part are done
+  __syncthreads();  // every ring is drained and read: it now holds the warps' sums
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     s_part[0][warp][lane * 8 + i] = dh[i];
@@ -1178,17 +1205,15 @@ __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nsb, const int64_
                                                        const int32_t* __restrict__ sb_chunks,
                                                        const float* __restrict__ scratch, DevPairs pr,
                                                        const int32_t* __restrict__ numorbs, double dv, double* H) {
-  __shared__ int64_t s_code[256];
-  __shared__ float s_part[4][8][256];  // [direct hi, direct lo, transposed hi, transposed lo][warp][entry]
+  extern __shared__ __align__(16) uint8_t hsm[];
   for (int64_t u = blockIdx.x; u < nsb; u += gridDim.x)
-    h_reduce_block(u, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H, s_code, s_part);
+    h_reduce_block(u, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H, hsm);
 }
 
 // Batched: the sub-blocks of several cells, cell c's at start[c] .. start[c+1].
 __global__ void __launch_bounds__(256) h_reduce_batch_kernel(int32_t ncells, const RedCell* __restrict__ cells,
                                                              const int64_t* __restrict__ start) {
-  __shared__ int64_t s_code[256];
-  __shared__ float s_part[4][8][256];
+  extern __shared__ __align__(16) uint8_t hsm[];
   for (int64_t g = blockIdx.x; g < start[ncells]; g += gridDim.x) {
     int lo = 0, hi = ncells;
     while (hi - lo > 1) {
@@ -1198,7 +1223,7 @@ __global__ void __launch_bounds__(256) h_reduce_batch_kernel(int32_t ncells, con
     }
     const RedCell& c = cells[lo];
     h_reduce_block(g - start[lo], c.red_off, c.red_slot, c.sb_fold, c.sb_chunks, c.scratch, c.pr, c.numorbs, c.dv,
-                   c.H, s_code, s_part);
+                   c.H, hsm);
   }
 }
 
@@ -1270,7 +1295,8 @@ cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const in
                                   cudaStream_t st) {
   if (total == 0) return cudaSuccess;
   const int grid = (int)std::min<int64_t>(total, (int64_t)sm_count() * 8);
-  h_reduce_batch_kernel<<<grid, 256, 0, st>>>(ncells, cells, start);
+  LCP_CUDA_TRY(cudaFuncSetAttribute(h_reduce_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRedSmem));
+  h_reduce_batch_kernel<<<grid, 256, kRedSmem, st>>>(ncells, cells, start);
   return cudaGetLastError();
 }
 
@@ -1356,7 +1382,8 @@ cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* 
                             const int32_t* numorbs, double dv, double* H, cudaStream_t st) {
   if (nsb == 0) return cudaSuccess;
   const int grid = (int)std::min<int64_t>(nsb, (int64_t)sm_count() * 8);
-  h_reduce_kernel<<<grid, 256, 0, st>>>(nsb, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H);
+  LCP_CUDA_TRY(cudaFuncSetAttribute(h_reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRedSmem));
+  h_reduce_kernel<<<grid, 256, kRedSmem, st>>>(nsb, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H);
   return cudaGetLastError();
 }
 
