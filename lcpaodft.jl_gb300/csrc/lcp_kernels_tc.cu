@@ -198,6 +198,27 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Maximum of v over the block (blockDim.x a multiple of 32, at most 1024),
+// valid in thread 0.
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v) {
+  __shared__ unsigned long long s_max[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, v, o);
+    v = y > v ? y : v;
+  }
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) s_max[warp] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < nw ? s_max[threadIdx.x] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, v, o);
+      v = y > v ? y : v;
+    }
+  }
+  return v;
+}
+
 // max |x| over n doubles (non-negative doubles order like their bit patterns)
 __global__ void absmax_kernel(const double* __restrict__ x, int64_t n, unsigned long long* out) {
   // on the bits with the sign cleared (integer operations only)
@@ -206,11 +227,10 @@ __global__ void absmax_kernel(const double* __restrict__ x, int64_t n, unsigned 
     const unsigned long long b = (unsigned long long)__double_as_longlong(x[i]) & 0x7fffffffffffffffull;
     m = b > m ? b : m;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
-    m = y > m ? y : m;
-  }
-  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
+  // one atomic per block: thousands of warps' atomics on one address
+  // serialise in L2 and cost more than the loads
+  m = block_max_u64(m);
+  if (threadIdx.x == 0 && m > 0) atomicMax(out, m);
 }
 
 // scale[0] = power of two >= factor * max, scale[1] = its inverse
@@ -241,11 +261,8 @@ __global__ void absmax_batch_kernel(int32_t ncells, const DsymCell* __restrict__
     const unsigned long long b = (unsigned long long)__double_as_longlong(c.dm[i]) & 0x7fffffffffffffffull;
     m = b > m ? b : m;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
-    m = y > m ? y : m;
-  }
-  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(tmp + lo, m);
+  m = block_max_u64(m);
+  if (threadIdx.x == 0 && m > 0) atomicMax(tmp + lo, m);
 }
 
 __global__ void pow2_scale_batch_kernel(int32_t ncells, const unsigned long long* __restrict__ mx, double factor,
