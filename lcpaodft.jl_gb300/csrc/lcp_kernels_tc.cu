@@ -135,10 +135,12 @@ __device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloa
 }
 
 // Same split for a float p (|p| <= 1) carrying a small correction e
-// (|e| <= 2^-23 |p|), in full-rate FP32 instructions only.  Rounding to an
-// integer uses the constant C = 1.5 * 2^23: for |x| <= 2^22, fma(y, 2^k, C)
-// lies in [2^23, 2^24) where the spacing is 1, so it rounds y * 2^k (exact)
-// to the nearest integer (ties to even) and subtracting C is exact.
+// (|e| <= 2^-23 |p|), in full-rate FP32 additions only.  Adding and
+// subtracting C = 1.5 * 2^k rounds x (|x| <= 2^(k-1)) to the nearest multiple
+// of ulp(C) = 2^(k-23) (ties to even), exactly: x + C lies in [2^k, 2^(k+1))
+// where that is the spacing.  So C = 1.5 * 2^15, 1.5 * 2^6 and 1.5 * 2^-3
+// give the multiples of 2^-8, 2^-17 and 2^-26 directly (the __fadd_rn forms
+// keep the compiler from folding the pair away).
 //   - r1 = p - hi is exact: hi is a multiple of 2^-8, itself a multiple of
 //     ulp(p), and |r1| <= 2^-9.
 //   - e joins r1 before mid is taken (one rounding, <= 2^-34), so that
@@ -148,15 +150,15 @@ __device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloa
 // The parts are those of p + e up to |lo residual| <= 2^-27 + 2^-34.
 __device__ __forceinline__ void fx_split_f(float p, float e, __nv_bfloat16& hi, __nv_bfloat16& mid,
                                            __nv_bfloat16& lo) {
-  constexpr float C = 12582912.0f;
-  const float hs = fmaf(p, 256.0f, C) - C;              // 2^8 * hi, an integer in [-256, 256]
-  const float r1 = fmaf(hs, -0.00390625f, p) + e;       // p - hi exact, then + e
-  const float ms = fmaf(r1, 131072.0f, C) - C;          // 2^17 * mid
-  const float r2 = fmaf(ms, -(1.0f / 131072.0f), r1);   // exact
-  const float ls = fmaf(r2, 67108864.0f, C) - C;        // 2^26 * lo
-  hi = __float2bfloat16_rn(hs * 0.00390625f);
-  mid = __float2bfloat16_rn(ms * (1.0f / 131072.0f));
-  lo = __float2bfloat16_rn(ls * (1.0f / 67108864.0f));
+  constexpr float C8 = 49152.0f, C17 = 96.0f, C26 = 0.1875f;
+  const float h = __fadd_rn(__fadd_rn(p, C8), -C8);    // multiple of 2^-8, |h| <= 1
+  const float r1 = __fadd_rn(__fadd_rn(p, -h), e);      // p - hi exact, then + e
+  const float m = __fadd_rn(__fadd_rn(r1, C17), -C17);  // multiple of 2^-17
+  const float r2 = __fadd_rn(r1, -m);                   // exact
+  const float l = __fadd_rn(__fadd_rn(r2, C26), -C26);  // multiple of 2^-26
+  hi = __float2bfloat16_rn(h);
+  mid = __float2bfloat16_rn(m);
+  lo = __float2bfloat16_rn(l);
 }
 
 // Float-float accumulation (Knuth's TwoSum): hi + lo carries the running sum
