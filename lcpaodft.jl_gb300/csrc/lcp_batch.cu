@@ -49,6 +49,7 @@ struct Wave {
   int c0 = 0, c1 = 0;
   int64_t nbricks = 0, brick_off = 0;  // its brick list in hbrick_*
   int64_t nsb = 0;                     // H sub-blocks of its cells
+  int64_t order_off = 0;               // its reduction order in wred_order
 };
 
 }  // namespace
@@ -63,6 +64,7 @@ struct lcp_batch {
   DBuf tc_cells[2], brick_cell, brick_local;
   std::vector<Wave> waves;
   DBuf hbrick_cell, hbrick_local, wred_start;  // per-wave brick lists and reduction starts
+  DBuf wred_order;                             // per wave: its sub-blocks, longest first
   DBuf dsym_cells[2], dsym_start, abs_start;
   DBuf red_cells[2];
   DBuf grid_cells, pt_start, sp_start, h_start;
@@ -164,7 +166,8 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
       hb.brick_local = b->hbrick_local.as<int64_t>() + wv.brick_off;
       API_CUDA(lcp::launch_hamiltonian_tc_batch(none, hb, status, st), "batch hamiltonian");
       API_CUDA(lcp::launch_h_reduce_batch(wv.c1 - wv.c0, b->red_cells[c].as<lcp::RedCell>() + wv.c0,
-                                          wstart + wv.c0 + (int64_t)w, wv.nsb, st),
+                                          wstart + wv.c0 + (int64_t)w, b->wred_order.as<int64_t>() + wv.order_off,
+                                          wv.nsb, st),
                "batch h_reduce");
     }
   // 6. <D,H> and the energies of every cell
@@ -329,7 +332,7 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
       }
     };
     std::vector<int32_t> bc, hbc;
-    std::vector<int64_t> bl, hbl, wst;
+    std::vector<int64_t> bl, hbl, wst, word;
     sorted_bricks(0, nc, bc, bl);
     for (Wave& w : b->waves) {
       w.brick_off = (int64_t)hbc.size();
@@ -343,12 +346,27 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
       }
       wst.push_back(acc);
       w.nsb = acc;
+      // the wave's sub-blocks longest first (stable): the reduction of a long
+      // one started late would run alone at the end of the launch; each
+      // sub-block's own sum is unchanged
+      w.order_off = (int64_t)word.size();
+      std::vector<std::pair<int64_t, int64_t>> len;  // (-partials, wave index)
+      len.reserve(acc);
+      int64_t g = 0;
+      for (int k = w.c0; k < w.c1; ++k) {
+        const std::vector<int64_t>& ro = b->jobs[k]->orbs->bricks.red_off;
+        for (int64_t u = 0; u < nsbc[k]; ++u, ++g) len.emplace_back(-(ro[u + 1] - ro[u]), g);
+      }
+      std::stable_sort(len.begin(), len.end(),
+                       [](const auto& x, const auto& y) { return x.first < y.first; });
+      for (const auto& l : len) word.push_back(l.second);
     }
     API_CUDA(upload_pod(b->brick_cell, bc), "upload");
     API_CUDA(upload_pod(b->brick_local, bl), "upload");
     API_CUDA(upload_pod(b->hbrick_cell, hbc), "upload");
     API_CUDA(upload_pod(b->hbrick_local, hbl), "upload");
     API_CUDA(upload_pod(b->wred_start, wst), "upload");
+    API_CUDA(upload_pod(b->wred_order, word), "upload");
   }
 
   // per-cell tables

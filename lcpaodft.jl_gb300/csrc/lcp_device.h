@@ -251,8 +251,8 @@ struct RedCell {
   double dv;
   double* H;
 };
-cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, int64_t total,
-                                  cudaStream_t st);
+cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, const int64_t* order,
+                                  int64_t total, cudaStream_t st);
 cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,

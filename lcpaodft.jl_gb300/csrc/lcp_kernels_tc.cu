@@ -1231,9 +1231,11 @@ __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nsb, const int64_
 
 // Batched: the sub-blocks of several cells, cell c's at start[c] .. start[c+1].
 __global__ void __launch_bounds__(256) h_reduce_batch_kernel(int32_t ncells, const RedCell* __restrict__ cells,
-                                                             const int64_t* __restrict__ start) {
+                                                             const int64_t* __restrict__ start,
+                                                             const int64_t* __restrict__ order) {
   extern __shared__ __align__(16) uint8_t hsm[];
-  for (int64_t g = blockIdx.x; g < start[ncells]; g += gridDim.x) {
+  for (int64_t i = blockIdx.x; i < start[ncells]; i += gridDim.x) {
+    const int64_t g = order ? order[i] : i;  // visiting order (longest first), or as stored
     int lo = 0, hi = ncells;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -1310,12 +1312,12 @@ cudaError_t launch_absmax_scale_batch(int32_t ncells, const DsymCell* cells, con
   return cudaGetLastError();
 }
 
-cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, int64_t total,
-                                  cudaStream_t st) {
+cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, const int64_t* order,
+                                  int64_t total, cudaStream_t st) {
   if (total == 0) return cudaSuccess;
   const int grid = (int)std::min<int64_t>(total, (int64_t)sm_count() * 8);
   LCP_CUDA_TRY(cudaFuncSetAttribute(h_reduce_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRedSmem));
-  h_reduce_batch_kernel<<<grid, 256, kRedSmem, st>>>(ncells, cells, start);
+  h_reduce_batch_kernel<<<grid, 256, kRedSmem, st>>>(ncells, cells, start, order);
   return cudaGetLastError();
 }
 
