@@ -163,7 +163,9 @@ def smooth_vna(ngrid, latvecs, seed, gmax=3.0, amplitude=0.5):
 
 
 def si64_workload(seed=1234, ngrid=(96, 96, 96), nrep=2):
-    """The 64-atom precision-form workload; returns a dict of host inputs."""
+    """The 64-atom precision-form workload (nrep = 2; nrep = 1 is its 8-atom
+    cell); returns a dict of host inputs.  Tr D = 4 per atom (Si's valence
+    electrons): 256 for the 64-atom cell."""
     lat, pos = si_supercell(nrep)
     natom = pos.shape[0]
     pao = synthetic_species(seed)
@@ -172,7 +174,7 @@ def si64_workload(seed=1234, ngrid=(96, 96, 96), nrep=2):
         "latvecs": lat, "gxyz": pos, "natom": natom, "atom2spe": [1] * natom,
         "cut": [7.0] * natom, "ngrid": tuple(ngrid), "origin": [0.0, 0.0, 0.0],
         "numorbs": [pao.Spe_Total_NumOrbs] * natom, "paos": [pao],
-        "vna_seed": seed + 1, "dm_seed": seed + 2, "trace": 256.0,
+        "vna_seed": seed + 1, "dm_seed": seed + 2, "trace": 4.0 * natom,
     }
 
 
