@@ -177,7 +177,7 @@ def force3_section(wl, u, dm, vna, reps=5):
     import lcpgrid as L
     ctx = L.Context(0)
     t0 = time.perf_counter()
-    orbs = L.Set_dOrbitals_Grid(wl["paos"], u, ctx)
+    orbs = L.Set_dOrbitals_Grid(wl["paos"], u, ctx=ctx)
     ctx.synchronize()
     t_tab = time.perf_counter() - t0
     V = [np.asarray(vna, dtype=np.float64)] * len(dm)
@@ -430,7 +430,7 @@ def build_workload(ctx, wl):
                 Total_NumOrbs=wl["numorbs"])
     t_geom = time.perf_counter() - t0
     t0 = time.perf_counter()
-    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx)
+    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx=ctx)
     t_tab = time.perf_counter() - t0
     dm = psd_density_matrices(u, wl["dm_seed"], nspin=nspin, trace=wl["trace"])
     vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
@@ -591,7 +591,7 @@ def run_ours(args):
                                 "split-BF16 form issues nine bf16 products per product (four MMAs with the B parts "
                                 "stacked along N) on 16-orbital blocks (13 used), so frac is bounded near 1/9 of "
                                 "that before padding; ncu shows the tensor pipe 42.9 % active in the H kernel and "
-                                "DRAM at 29 % (profiles/tc_kernels_si8_48cubed.md)")
+                                "DRAM at 29 % on the 8-atom cell")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     ms_step = total_ms / args.steps
@@ -725,7 +725,7 @@ def serving(args, wl_pool=None):
         # sphere and overlap lists built on the GPU (the same lists as the host build)
         u = L.UCell(1, w["latvecs"], w["natom"], w["atom2spe"], w["gxyz"], w["cut"], w["ngrid"], w["origin"],
                     Total_NumOrbs=w["numorbs"], device=True, ctx=ctx)
-        orbs = L.Set_Orbitals_Grid(w["paos"], u, ctx)
+        orbs = L.Set_Orbitals_Grid(w["paos"], u, ctx=ctx)
         vna = smooth_vna(w["ngrid"], w["latvecs"], w["vna_seed"])
         jobs.append(L.GridStepJob(u, orbs, "off", "LDA", None, None, vna))
         dms.append(psd_density_matrices(u, w["dm_seed"], trace=w["trace"]))
@@ -839,7 +839,7 @@ def batching(args):
     if args.batch_autotune > 0:
         for ng, ks in classes.items():
             k = max(ks, key=lambda i: pool[i]["natom"])
-            orbs = L.Set_Orbitals_Grid(pool[k]["paos"], ucells[k], ctx)
+            orbs = L.Set_Orbitals_Grid(pool[k]["paos"], ucells[k], ctx=ctx)
             shape, ms = orbs.autotune_bricks(args.batch_autotune)
             tuned[ng] = shape
             tuned_orbs[k] = orbs
@@ -862,7 +862,7 @@ def batching(args):
         w, u = pool[k], ucells[k]
         orbs = tuned_orbs.get(k)
         if orbs is None:
-            orbs = L.Set_Orbitals_Grid(w["paos"], u, thread_ctx())
+            orbs = L.Set_Orbitals_Grid(w["paos"], u, ctx=thread_ctx())
             shape = tuned.get(tuple(w["ngrid"]))
             if shape is not None and shape in [c[0] for c in u.brick_shape_candidates(4)]:
                 orbs.set_brick_shape(shape)

@@ -414,15 +414,24 @@ lcp_status lcp_batch_info(const lcp_batch* batch, int64_t* out8);
  * held from the library's load on that device until exit; it fits cells of
  * up to 10921 neighbour pairs (Nloop) and larger ones are rejected with
  * LCP_EINVAL.  The orbitals' split-BF16 tables must already exist (any
- * allocating split-BF16 call on them builds them), else LCP_ESTATE.  The first
- * call on a device looks up the array's device address; make it before any
- * stream capture.  Every call on a device shares the array: calls that
- * overlap on the GPU (other host threads, other contexts of that device)
- * race and must be serialised by the caller.  Runs on the context's stream
- * and returns after it completes. */
+ * allocating split-BF16 call on them builds them), else LCP_ESTATE.
+ * The call is synchronous: it copies the error word to the host and waits for
+ * the context's stream before it returns, so it cannot be captured into a
+ * CUDA graph.  The first call on a context looks up the array's device
+ * address (cudaGetSymbolAddress); while another thread captures a stream in
+ * the global capture mode, that first call must not run.  Every call on a
+ * device shares the array and leaves its contents behind: calls that overlap
+ * on the GPU (other host threads, other contexts of that device) race and
+ * must be serialised by the caller.  Calls after cudaDeviceReset need a
+ * context created after the reset. */
 lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs* orbs,
                                         int32_t spinpol, const double* const* dm_dev,
                                         double* const* density_grid_dev);
+
+/* Device allocations (cudaMalloc calls) the library has made since it was
+ * loaded, over all contexts: a diagnostic for callers that must see none in
+ * a call (lcp_set_density_grid_noalloc).  No counterpart in the reference. */
+lcp_status lcp_device_alloc_count(int64_t* count);
 
 #ifdef __cplusplus
 }

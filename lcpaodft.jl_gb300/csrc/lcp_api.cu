@@ -1622,6 +1622,12 @@ lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops) {
   return LCP_OK;
 }
 
+lcp_status lcp_device_alloc_count(int64_t* count) {
+  if (!count) return fail(LCP_EINVAL, "NULL argument");
+  *count = g_device_allocs.load(std::memory_order_relaxed);
+  return LCP_OK;
+}
+
 lcp_status lcp_job_get_density(lcp_ctx* ctx, lcp_job* job, double* const* d) { return job_get(ctx, job, job ? job->rho : nullptr, job ? job->nn : 0, d); }
 lcp_status lcp_job_get_hks(lcp_ctx* ctx, lcp_job* job, double* const* h) { return job_get(ctx, job, job ? job->hks : nullptr, job ? job->hsize : 0, h); }
 lcp_status lcp_job_get_vpot(lcp_ctx* ctx, lcp_job* job, double* const* v) { return job_get(ctx, job, job ? job->vpot : nullptr, job ? job->nn : 0, v); }
@@ -1650,22 +1656,18 @@ constexpr int64_t kNoAllocMaxPairs = (int64_t)((kNoAllocBytes - kNoAllocHeader) 
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device (host code must not pass the symbol itself to a kernel).
-lcp_status noalloc_scratch(int device, unsigned char** out) {
-  if (device < 0 || device >= kNoAllocMaxDevices) return fail(LCP_EDEVICE, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[device]) {
+// Device address of g_noalloc_scratch on the context's device (host code
+// must not pass the symbol itself to a kernel).  Looked up by the context's
+// first call and kept in the context, so a context made after the device's
+// primary context was torn down and made again looks it up afresh.
+lcp_status noalloc_scratch(lcp_ctx* ctx, unsigned char** out) {
+  if (!ctx->noalloc_scratch) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    g_noalloc_addr[device] = p;
+    ctx->noalloc_scratch = p;
   }
-  *out = static_cast<unsigned char*>(g_noalloc_addr[device]);
+  *out = static_cast<unsigned char*>(ctx->noalloc_scratch);
   return LCP_OK;
 }
 
@@ -1699,7 +1701,7 @@ lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, co
                                 " D blocks (16 MiB); this cell has " + std::to_string(nsub) +
                                 " (16-orbital sub-blocks of its neighbour pairs)");
   unsigned char* base = nullptr;
-  if ((s = noalloc_scratch(ctx->device, &base))) return s;
+  if ((s = noalloc_scratch(ctx, &base))) return s;
   double* dscale = reinterpret_cast<double*>(base);
   unsigned long long* dmax = reinterpret_cast<unsigned long long*>(base + 16);
   int* status = reinterpret_cast<int*>(base + 24);

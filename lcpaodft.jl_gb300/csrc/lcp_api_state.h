@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <tuple>
@@ -30,6 +31,10 @@ static inline lcp_status cuda_fail(cudaError_t e, const char* where) {
     if (_e != cudaSuccess) return cuda_fail(_e, where); \
   } while (0)
 
+// Number of device allocations (cudaMalloc) made through DBuf since the
+// library was loaded, across all contexts; read by lcp_device_alloc_count.
+inline std::atomic<int64_t> g_device_allocs{0};
+
 // Owning device buffer.
 struct DBuf {
   void* p = nullptr;
@@ -46,6 +51,7 @@ struct DBuf {
     p = nullptr;
     bytes = 0;
     cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    g_device_allocs.fetch_add(1, std::memory_order_relaxed);
     if (e == cudaSuccess) bytes = n;
     return e;
   }
@@ -93,6 +99,9 @@ struct lcp_ctx {
   DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale;
   // second stream of the step: the xc pass runs there beside the FFT Poisson solve
   cudaStream_t aux = nullptr;
+  // device address of the no-allocation density's fixed scratch array, looked
+  // up by this context's first lcp_set_density_grid_noalloc call
+  void* noalloc_scratch = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ~lcp_ctx() {
     cudaSetDevice(device);

@@ -86,6 +86,7 @@ _SIGS = {
     "lcp_orbs_download": ([_vp, _vp, _i32, _i32, _pd, _i64], _i32),
     "lcp_set_density_grid": ([_vp, _vp, _vp, _i32, _ppd, _ppd], _i32),
     "lcp_set_density_grid_noalloc": ([_vp, _vp, _vp, _i32, _ppd, _ppd], _i32),
+    "lcp_device_alloc_count": ([ctypes.POINTER(_i64)], _i32),
     "lcp_solve_poisson": ([_vp, _pi32, _pd, _i32, _ppd, _pd, _pd], _i32),
     "lcp_solve_poisson_xyz": ([_vp, _pi32, _pd, _pd, _pd], _i32),
     "lcp_set_xc_grid": ([_vp, _i32, _i32, _i64, _pd, _ppd, _ppd], _i32),

@@ -15,7 +15,8 @@ from ._lib import LCPError, check, dptr, dptrs, iptr, lib
 __all__ = ["Context", "UCell", "DeviceOrbitalsGrid", "Rhor_Mixing", "XC_Func", "GridStepJob", "Batch", "Server",
            "Set_Orbitals_Grid", "Set_dOrbitals_Grid", "Set_AdenPCC_Grid", "Set_Density_Grid", "diagonalize_nc_density", "Solve_Poisson", "Solve_Poisson_xyz",
            "Calc_Diff_Coef", "Set_XC_Grid", "Set_Vpot_Grid", "Calc_MatrixElements_dVH_Vxc_off", "Calc_MatrixElements_dVH_Vxc_on",
-           "Calc_MatrixElements_dVH_Vxc_nc", "Force3_nospin", "Force3_spin", "Force3_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context"]
+           "Calc_MatrixElements_dVH_Vxc_nc", "Force3_nospin", "Force3_spin", "Force3_nc", "Calc_EH1", "Calc_EXC1", "Calc_Ngrid", "default_context",
+           "use_context"]
 
 
 def _f64(a):
@@ -82,9 +83,34 @@ _DEFAULT = {}
 
 
 def default_context(device=0):
+    """The module's context on `device`: the one installed by use_context, else
+    an FP64 context made on first use.  Functions whose reference signature has
+    no argument that could carry a context (diagonalize_nc_density, Calc_EH1,
+    the inner Solve_Poisson) run on it."""
     if device not in _DEFAULT:
         _DEFAULT[device] = Context(device)
     return _DEFAULT[device]
+
+
+def use_context(ctx):
+    """Installs `ctx` as the module's context on its device; returns the one it
+    replaces (or None).  This is the counterpart of the Julia binding's
+    module-level context, which lets the reference's call sites stay unchanged."""
+    old = _DEFAULT.get(ctx.device)
+    _DEFAULT[ctx.device] = ctx
+    return old
+
+
+def _ctx_of(*objs, ctx=None):
+    """The context a call runs on: an explicit keyword, else the first object
+    that carries one, else the module's default."""
+    if ctx is not None:
+        return ctx
+    for o in objs:
+        c = getattr(o, "ctx", None)
+        if c is not None:
+            return c
+    return default_context()
 
 
 class UCell:
@@ -96,10 +122,15 @@ class UCell:
 
     Lists are exposed with the reference's names: GridN_Atom, GridListAtom,
     CellListAtom (per atom), FNAN, natn, ncn, MPI_atom/MPI_natn/MPI_ncn,
-    MPI_NumOLG and MPI_GListTAtoms1/2 (per pair)."""
+    MPI_NumOLG and MPI_GListTAtoms1/2 (per pair).
+
+    ``ctx`` (keyword) is the context of the device build and of the calls that
+    take this UCell (Set_Orbitals_Grid, Set_AdenPCC_Grid); without it they use
+    the module's default context."""
 
     def __init__(self, Nspin, Latvecs, Natom, atom2spe, Gxyz, Atoms_Cut1, Ngrid, Grid_Origin, Total_NumOrbs=None,
                  device=False, ctx=None):
+        self.ctx = ctx
         self.Latvecs = _f64(Latvecs).reshape(3, 3)
         self.Natom = int(Natom)
         self.atom2spe = np.ascontiguousarray(atom2spe, dtype=np.int32)
@@ -117,7 +148,7 @@ class UCell:
         args = (self.Nspin, dptr(self.Latvecs), self.Natom, iptr(self.atom2spe), dptr(self.Gxyz),
                 dptr(self.Atoms_Cut1), iptr(ng), dptr(self.Grid_Origin), iptr(self.Total_NumOrbs), ctypes.byref(h))
         if device:
-            check(lib.lcp_ucell_create_device((ctx or default_context())._h, *args))
+            check(lib.lcp_ucell_create_device(_ctx_of(ctx=ctx)._h, *args))
         else:
             check(lib.lcp_ucell_create(*args))
         self._h = h
@@ -287,19 +318,20 @@ def _paos_struct(paos):
 
 
 def _tabulate(pao, ucell, ctx, grad):
-    ctx = ctx or default_context()
+    ctx = _ctx_of(ucell, ctx=ctx)
     arr, keep = _paos_struct(list(pao))
     h = ctypes.c_void_p()
     check(lib.lcp_set_orbitals_grid(ctx._h, ucell._h, len(keep) // 2, arr, 1 if grad else 0, ctypes.byref(h)))
     return DeviceOrbitalsGrid(ctx, ucell, h, grad)
 
 
-def Set_Orbitals_Grid(pao, ucell, ctx=None):
-    """src/Matrix/Set_Orbitals_Grid.jl:26-42."""
+def Set_Orbitals_Grid(pao, ucell, *, ctx=None):
+    """src/Matrix/Set_Orbitals_Grid.jl:26-42.  Runs on ``ctx`` (keyword), else
+    ucell's context, else the module's default."""
     return _tabulate(pao, ucell, ctx, False)
 
 
-def Set_dOrbitals_Grid(pao, ucell, ctx=None):
+def Set_dOrbitals_Grid(pao, ucell, *, ctx=None):
     """Values and gradient tables (src/Matrix/Set_dOrbitals_Grid.jl:1-20);
     ``.data(atom, k)`` for k = 1, 2, 3 gives d/dx, d/dy, d/dz."""
     return _tabulate(pao, ucell, ctx, True)
@@ -327,11 +359,11 @@ def Set_Density_Grid(SpinPol, ucell, Orbs_Grid, DM, Density_Grid):
     check(lib.lcp_set_density_grid(Orbs_Grid.ctx._h, ucell._h, Orbs_Grid._h, _lib.SPIN[s], pdm, pr))
 
 
-def diagonalize_nc_density(Density_Grid, ctx=None):
+def diagonalize_nc_density(Density_Grid, *, ctx=None):
     """``diagonalize_nc_density!`` (src/Matrix/Set_Density_Grid.jl:243-261):
     the four "nc" channels (Re11, Re22, Re12, Im12) become (Nup, Ndown,
-    theta, phi) in place."""
-    ctx = ctx or default_context()
+    theta, phi) in place.  Runs on the module's default context (or ``ctx``)."""
+    ctx = _ctx_of(ctx=ctx)
     for c in range(4):
         if Density_Grid[c].dtype != np.float64 or not Density_Grid[c].flags["C_CONTIGUOUS"]:
             raise TypeError("Density_Grid must hold C-contiguous float64 arrays")
@@ -350,13 +382,13 @@ def _radial(xv, rv, yv, keep):
     return _lib.lcp_radial(arrs[0].size, dptr(arrs[0]), dptr(arrs[1]), dptr(arrs[2]))
 
 
-def Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, ucell, ctx=None):
+def Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, ucell, *, ctx=None):
     """``Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, ucell)``
     (src/Matrix/Set_AdenPCC_Grid.jl:1-142) on the GPU: returns (ADensity_Grid,
     PCCDensity_Grid, Density_Grid).  ``pao[spe]`` carries Spe_PAO_XV,
     Spe_PAO_RV and Spe_Atomic_Den; ``pspot[spe]`` Spe_VPS_XV, Spe_VPS_RV and
-    Spe_Atomic_PCC (``PCC`` objects)."""
-    ctx = ctx or default_context()
+    Spe_Atomic_PCC (``PCC`` objects).  Runs on ucell's context (or ``ctx``)."""
+    ctx = _ctx_of(ucell, ctx=ctx)
     s = _spin(SpinPol)
     keep = []
     den = (_lib.lcp_radial * len(pao))(*[_radial(p.Spe_PAO_XV, p.Spe_PAO_RV, p.Spe_Atomic_Den, keep) for p in pao])
@@ -377,17 +409,20 @@ def Set_AdenPCC_Grid(SpinPol, Init_Atoms_Nspin, Init_Atoms_Angle, pao, pspot, uc
 
 class Rhor_Mixing:
     """The parts of ``DFT_Mixing`` the Poisson solve reads: Ngrid and Recvecs
-    (src/Mixing/DFT_Mixing.jl:47-95)."""
+    (src/Mixing/DFT_Mixing.jl:47-95), and the device context the solve runs on
+    (the module's default when None)."""
 
-    def __init__(self, Ngrid, Latvecs):
+    def __init__(self, Ngrid, Latvecs, ctx=None):
+        self.ctx = ctx
         self.Ngrid = tuple(int(x) for x in Ngrid)
         self.Latvecs = _f64(Latvecs).reshape(3, 3)
         self.Recvecs = 2 * np.pi * np.linalg.inv(self.Latvecs.T)
 
 
-def Solve_Poisson(SpinPol, dft_mixing, Density_Grid, ADensity_Grid, dVHart_Grid, ctx=None):
-    """``Solve_Poisson!`` (src/Poisson.jl:1-7): fills dVHart_Grid."""
-    ctx = ctx or default_context()
+def Solve_Poisson(SpinPol, dft_mixing, Density_Grid, ADensity_Grid, dVHart_Grid, *, ctx=None):
+    """``Solve_Poisson!`` (src/Poisson.jl:1-7): fills dVHart_Grid.  Runs on
+    dft_mixing's context (or ``ctx``)."""
+    ctx = _ctx_of(dft_mixing, ctx=ctx)
     s = _spin(SpinPol)
     nr = 1 if s == "off" else 2
     rho = [_f64(Density_Grid[c]) for c in range(nr)]
@@ -398,10 +433,11 @@ def Solve_Poisson(SpinPol, dft_mixing, Density_Grid, ADensity_Grid, dVHart_Grid,
     check(lib.lcp_solve_poisson(ctx._h, iptr(ng), dptr(rv), _lib.SPIN[s], pr, dptr(ad), dptr(dVHart_Grid)))
 
 
-def Solve_Poisson_xyz(Ngrid, Recvecs, Density_xyz, dVHart_Grid, ctx=None):
+def Solve_Poisson_xyz(Ngrid, Recvecs, Density_xyz, dVHart_Grid, *, ctx=None):
     """Inner ``Solve_Poisson!(Ngrid, Recvecs, Density_xyz, dVHart_Grid)`` for a
-    real Density_xyz (src/Poisson.jl:29-108)."""
-    ctx = ctx or default_context()
+    real Density_xyz (src/Poisson.jl:29-108), on the module's default context
+    (or ``ctx``)."""
+    ctx = _ctx_of(ctx=ctx)
     ng = np.array(Ngrid, dtype=np.int32)
     src = _f64(np.real(np.asarray(Density_xyz)).reshape(-1))
     check(lib.lcp_solve_poisson_xyz(ctx._h, iptr(ng), dptr(_f64(Recvecs)), dptr(src), dptr(dVHart_Grid)))
@@ -428,9 +464,12 @@ def Calc_Diff_Coef(gLatvecs):
 class XC_Func:
     """``XC_Func(xc_type, SpinPol, Nspin, Ngrid, gLatvecs)``
     (src/XC/XC_Func.jl:47-108).  GGA_PBE needs gLatvecs (rows Latvecs[i] /
-    Ngrid[i]) for its Diff_Coef and carries dDensity_Grid and dEXC_dGD."""
+    Ngrid[i]) for its Diff_Coef and carries dDensity_Grid and dEXC_dGD.
+    ``ctx`` is the device context of Set_XC_Grid / Set_Vpot_Grid on this
+    object (the module's default when None)."""
 
-    def __init__(self, xc_type, SpinPol, Nspin, Ngrid, gLatvecs=None):
+    def __init__(self, xc_type, SpinPol, Nspin, Ngrid, gLatvecs=None, ctx=None):
+        self.ctx = ctx
         xc = _xc_name(xc_type)
         sp = SpinPol.lower()
         if sp not in _lib.SPIN:
@@ -452,10 +491,11 @@ class XC_Func:
             self.dEXC_dGD = [[np.zeros(nn) for _ in range(3)] for _ in range(ns)]
 
 
-def Set_XC_Grid(xc_func, PCCDensity_Grid, Density_Grid, ctx=None):
+def Set_XC_Grid(xc_func, PCCDensity_Grid, Density_Grid, *, ctx=None):
     """``Set_XC_Grid!`` (src/XC/XC_Func.jl:111-160): fills xc_func.Vxc_Grid
-    (and, for GGA_PBE, xc_func.dDensity_Grid and xc_func.dEXC_dGD)."""
-    ctx = ctx or default_context()
+    (and, for GGA_PBE, xc_func.dDensity_Grid and xc_func.dEXC_dGD).  Runs on
+    xc_func's context (or ``ctx``)."""
+    ctx = _ctx_of(xc_func, ctx=ctx)
     n = _lib.NCHAN[xc_func.SpinPol]
     nn = int(np.prod(xc_func.Ngrid))
     rho = [_f64(Density_Grid[c]) for c in range(n)]
@@ -474,10 +514,11 @@ def Set_XC_Grid(xc_func, PCCDensity_Grid, Density_Grid, ctx=None):
     check(lib.lcp_set_xc_grid(ctx._h, _lib.XC[xc_func.xc_type], _lib.SPIN[xc_func.SpinPol], nn, dptr(pcc), pr, pv))
 
 
-def Set_Vpot_Grid(xc_func, dVHart_Grid, Vpot_Grid, Vna_Grid=None, ctx=None):
-    """``Set_Vpot_Grid!`` (src/Matrix/Set_Vpot_Grid.jl:1-19); Vna_Grid, when
-    given, is added to the spin-diagonal channels."""
-    ctx = ctx or default_context()
+def Set_Vpot_Grid(xc_func, dVHart_Grid, Vpot_Grid, *, Vna_Grid=None, ctx=None):
+    """``Set_Vpot_Grid!`` (src/Matrix/Set_Vpot_Grid.jl:1-19); Vna_Grid
+    (keyword), when given, is added to the spin-diagonal channels.  Runs on
+    xc_func's context (or ``ctx``)."""
+    ctx = _ctx_of(xc_func, ctx=ctx)
     n = _lib.NCHAN[xc_func.SpinPol]
     nn = int(np.prod(xc_func.Ngrid))
     px, k1 = dptrs([_f64(v) for v in xc_func.Vxc_Grid])
@@ -515,7 +556,7 @@ def _force3(spin, pao, Orbs_Grid, Vpot, DM, ucell):
     """The reference tabulates the gradient tables inside Force3; here they
     come with Orbs_Grid when it was made by Set_dOrbitals_Grid, else they are
     tabulated (on Orbs_Grid's context) for this call."""
-    orbs = Orbs_Grid if getattr(Orbs_Grid, "with_grad", False) else Set_dOrbitals_Grid(pao, ucell, Orbs_Grid.ctx)
+    orbs = Orbs_Grid if getattr(Orbs_Grid, "with_grad", False) else Set_dOrbitals_Grid(pao, ucell, ctx=Orbs_Grid.ctx)
     n = _lib.NCHAN[spin]
     vp, keep_v = dptrs([_f64(Vpot[c]) for c in range(n)])
     dp, keep_d = dptrs([_f64(DM[c]) for c in range(n)])
@@ -541,9 +582,9 @@ def Force3_nc(pao, Orbs_Grid, dVHart_Grid, Vxc_Grid, DM, ucell):
     return _force3("nc", pao, Orbs_Grid, V, DM, ucell)
 
 
-def Calc_EH1(SpinPol, GridVol, ADensity_Grid, Density_Grid, dVHart_Grid, ctx=None):
-    """src/Energy.jl:655-666."""
-    ctx = ctx or default_context()
+def Calc_EH1(SpinPol, GridVol, ADensity_Grid, Density_Grid, dVHart_Grid, *, ctx=None):
+    """src/Energy.jl:655-666, on the module's default context (or ``ctx``)."""
+    ctx = _ctx_of(ctx=ctx)
     s = _spin(SpinPol)
     nr = 1 if s == "off" else 2
     rho = [_f64(Density_Grid[c]) for c in range(nr)]
@@ -555,10 +596,11 @@ def Calc_EH1(SpinPol, GridVol, ADensity_Grid, Density_Grid, dVHart_Grid, ctx=Non
     return out.value
 
 
-def Calc_EXC1(SpinPol, xc_type, system_grid, ADensity_Grid, PCCDensity_Grid, Density_Grid, ctx=None):
+def Calc_EXC1(SpinPol, xc_type, system_grid, ADensity_Grid, PCCDensity_Grid, Density_Grid, *, ctx=None):
     """src/Energy.jl:669-700; ``system_grid`` supplies GridVol, and for
-    GGA_PBE also Ngrid and Latvecs (a UCell works)."""
-    ctx = ctx or default_context()
+    GGA_PBE also Ngrid and Latvecs (a UCell works).  Runs on system_grid's
+    context when it carries one (or ``ctx``), else the module's default."""
+    ctx = _ctx_of(system_grid, ctx=ctx)
     s = _spin(SpinPol)
     nr = 1 if s == "off" else 2
     rho = [_f64(Density_Grid[c]) for c in range(nr)]

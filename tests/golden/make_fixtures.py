@@ -17,10 +17,12 @@ This script is run once, in a checkout that has the reference project
 
 Usage::
 
-    python tests/golden/make_fixtures.py [REFERENCE_ROOT]
+    python tests/golden/make_fixtures.py REFERENCE_ROOT
+    LCP_REFERENCE_ROOT=... python tests/golden/make_fixtures.py
 
-REFERENCE_ROOT defaults to /root/reference.  The GPU tests never run this
-script: they read only the committed outputs.
+REFERENCE_ROOT is a checkout of LCPAODFT.jl (its test/ and DFT_DATA19/
+folders are read as text).  The GPU tests never run this script: they read
+only the committed outputs.
 """
 import json
 import os
@@ -252,7 +254,9 @@ def read_vps_file(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LCP_REFERENCE_ROOT")
+    if not ref:
+        sys.exit("usage: make_fixtures.py REFERENCE_ROOT (or set LCP_REFERENCE_ROOT)")
     gold = {
         "ucell_si_3x3x3": parse_ucell(ref),
         "orbs_si_3x3x3": parse_orbs(ref),

@@ -20,12 +20,12 @@ def _cells(ctx, spin="off", n_pool=6, seed=91, xc=None):
     for c in batch_pool(n_pool, seed=seed, nmax=10, amax_ang=7.0):
         u = L.UCell(2 if spin == "on" else 1, c["latvecs"], c["natom"], c["atom2spe"], c["gxyz"], c["cut"],
                     c["ngrid"], c["origin"], Total_NumOrbs=c["numorbs"])
-        cells.append((u, L.Set_Orbitals_Grid(c["paos"], u, ctx)))
+        cells.append((u, L.Set_Orbitals_Grid(c["paos"], u, ctx=ctx)))
     lat, pos, ng = si2_cell()
     for scale in (1.0, 1.01):
         u = L.UCell(2 if spin == "on" else 1, lat, 2, [1, 1], pos * scale, [7.0, 7.0], ng, [0, 0, 0],
                     Total_NumOrbs=[13, 13])
-        cells.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx)))
+        cells.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)))
     jobs = []
     nspin = 2 if spin == "on" else 1
     for k, (u, orbs) in enumerate(cells):

@@ -39,7 +39,7 @@ def test_force3_vs_oracle(ctx, spin):
     dm = psd_dm(u, 70 + n, nspin=n)
     rng = np.random.default_rng(80 + n)
     V = [rng.normal(size=u.NN) * 0.3 for _ in range(n)]
-    orbs = L.Set_dOrbitals_Grid(paos, u, ctx)
+    orbs = L.Set_dOrbitals_Grid(paos, u, ctx=ctx)
     oo = O.set_orbitals_grid(opaos, uo)
     do = O.set_dorbitals_grid(opaos, uo)
     if spin == "off":
@@ -70,7 +70,7 @@ def test_force3_mixed_basis_and_internal_tabulation(ctx):
     opaos = [O.PAO(p.Spe_MaxL_Basis, p.Spe_Num_Basis, p.Spe_PAO_RV, p.Spe_PAO_RWF) for p in specs]
     dm = psd_dm(u, 91)
     V = [np.random.default_rng(92).normal(size=u.NN)]
-    plain = L.Set_Orbitals_Grid(specs, u, ctx)
+    plain = L.Set_Orbitals_Grid(specs, u, ctx=ctx)
     F = L.Force3_nospin(specs, plain, V, dm, u)
     Fref = O.calc_force3("off", uo, O.set_orbitals_grid(opaos, uo), O.set_dorbitals_grid(opaos, uo), V, dm)
     _check(F, Fref)
@@ -79,7 +79,7 @@ def test_force3_mixed_basis_and_internal_tabulation(ctx):
 def test_force3_needs_gradient_tables(ctx):
     from lcpgrid import _lib
     u, uo, paos, _ = _si2(ctx)
-    plain = L.Set_Orbitals_Grid(paos, u, ctx)
+    plain = L.Set_Orbitals_Grid(paos, u, ctx=ctx)
     V = [np.zeros(u.NN)]
     dm = psd_dm(u, 3)
     vp, kv = _lib.dptrs(V)

@@ -67,7 +67,7 @@ def test_set_xc_grid_gga_vs_oracle(ctx, spin):
         rho = rho + [rng.uniform(0, np.pi, nn), rng.uniform(-np.pi, np.pi, nn)]
     gl = O.glatvecs_of(SKEW, NG)
     xf = L.XC_Func("GGA-PBE", spin, {"off": 1, "on": 2, "nc": 4}[spin], NG, gl)
-    L.Set_XC_Grid(xf, pcc, rho, ctx)
+    L.Set_XC_Grid(xf, pcc, rho, ctx=ctx)
     vref, dref, eref = O.set_xc_grid_gga(spin, NG, pcc, rho, O.calc_diff_coef(gl))
     for c in range(len(vref)):
         close(xf.Vxc_Grid[c], vref[c])
@@ -91,7 +91,7 @@ def test_reference_gga_fixtures(ctx, name, lat, spin):
     ng = (3, 3, 3)
     gl = O.glatvecs_of(lat, ng)
     xf = L.XC_Func("GGA-PBE", spin, len(rho), ng, gl)
-    L.Set_XC_Grid(xf, pcc, rho, ctx)
+    L.Set_XC_Grid(xf, pcc, rho, ctx=ctx)
     vref, dref, eref = O.set_xc_grid_gga(spin, ng, pcc, rho, O.calc_diff_coef(gl))
     for c in range(len(vref)):
         close(xf.Vxc_Grid[c], vref[c])
@@ -105,7 +105,7 @@ def test_calc_exc1_gga_vs_oracle(ctx, spin):
     ad = 0.5 * (rho[0] + rho[-1])
     gv = abs(np.linalg.det(SKEW)) / np.prod(NG)
     grid = type("G", (), {"GridVol": gv, "Ngrid": NG, "Latvecs": SKEW})()
-    got = L.Calc_EXC1(spin, "GGA_PBE", grid, ad, pcc, rho, ctx)
+    got = L.Calc_EXC1(spin, "GGA_PBE", grid, ad, pcc, rho, ctx=ctx)
     want = O.calc_exc1(spin, "GGA_PBE", gv, ad, pcc, rho, ngrid=NG, latvecs=SKEW)
     np.testing.assert_allclose(got[:ns], want[:ns], rtol=1e-11)
 
@@ -115,7 +115,7 @@ def si2(ctx):
     lat, pos, ng = si2_cell()
     u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
     uo = O.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], total_numorbs=[13, 13])
-    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx)
+    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)
     oo = O.set_orbitals_grid([oracle_pao()], uo)
     return u, uo, orbs, oo
 

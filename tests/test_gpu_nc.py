@@ -44,7 +44,12 @@ def test_diagonalize_nc_density_vs_oracle(ctx):
     d[2][70:80] = -0.02  # x < 0: phi = pi - asin
     ref = O.diagonalize_nc_density(d)
     got = [x.copy() for x in d]
-    L.diagonalize_nc_density(got, ctx)
+    old = L.use_context(ctx)  # the module's context: the reference's one-argument call
+    try:
+        L.diagonalize_nc_density(got)
+    finally:
+        if old is not None:
+            L.use_context(old)
     for c in range(4):
         np.testing.assert_allclose(got[c], ref[c], rtol=0, atol=1e-13)
     assert np.all(got[3][:50] == 0.0) and np.all(got[2][50:60] == 0.5 * np.pi)
@@ -55,7 +60,7 @@ def si2(ctx):
     lat, pos, ng = si2_cell()
     u = L.UCell(4, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
     uo = O.UCell(4, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], total_numorbs=[13, 13])
-    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx)
+    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)
     oo = O.set_orbitals_grid([oracle_pao()], uo)
     return u, uo, orbs, oo
 

@@ -24,7 +24,7 @@ def ctx():
 def fix(ctx):
     u = L.UCell(1, FIX_LAT, 2, [1, 1], FIX_POS, [7.0, 7.0], (3, 3, 3), [0, 0, 0], Total_NumOrbs=[13, 13])
     uo = O.UCell(1, FIX_LAT, 2, [1, 1], FIX_POS, [7.0, 7.0], (3, 3, 3), [0, 0, 0], total_numorbs=[13, 13])
-    orbs = L.Set_dOrbitals_Grid([product_pao()], u, ctx)
+    orbs = L.Set_dOrbitals_Grid([product_pao()], u, ctx=ctx)
     return u, uo, orbs
 
 
@@ -33,7 +33,7 @@ def si2(ctx):
     lat, pos, ng = si2_cell()
     u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
     uo = O.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], total_numorbs=[13, 13])
-    orbs = L.Set_dOrbitals_Grid([product_pao()], u, ctx)
+    orbs = L.Set_dOrbitals_Grid([product_pao()], u, ctx=ctx)
     oo = O.set_orbitals_grid([oracle_pao()], uo)
     return u, uo, orbs, oo
 
@@ -133,7 +133,7 @@ def test_poisson_golden_and_oracle(ctx):
     P = golden()["poisson_si_3x3x3"]
     rec = 2 * np.pi * np.linalg.inv(FIX_LAT.T)
     out = np.zeros(27)
-    L.Solve_Poisson_xyz((3, 3, 3), rec, np.array(P["density_xyz"]), out, ctx)
+    L.Solve_Poisson_xyz((3, 3, 3), rec, np.array(P["density_xyz"]), out, ctx=ctx)
     np.testing.assert_allclose(out, P["dVHart_Grid"], rtol=1.5e-8, atol=1e-15)
     rng = np.random.default_rng(0)
     for ng in ((24, 24, 24), (15, 14, 17), (9, 10, 11)):
@@ -141,17 +141,17 @@ def test_poisson_golden_and_oracle(ctx):
         rec = 2 * np.pi * np.linalg.inv(lat.T)
         src = rng.normal(size=int(np.prod(ng)))
         out = np.zeros(src.size)
-        L.Solve_Poisson_xyz(ng, rec, src, out, ctx)
+        L.Solve_Poisson_xyz(ng, rec, src, out, ctx=ctx)
         ref = O.solve_poisson_xyz(ng, rec, src)
         np.testing.assert_allclose(out, ref, rtol=0, atol=1e-12 * np.max(np.abs(ref)))
     # Solve_Poisson! with SpinPol: 2rho - 2rho_a and rho_up + rho_dn - 2rho_a
     ng = (12, 12, 12)
-    mix = L.Rhor_Mixing(ng, FIX_LAT)
+    mix = L.Rhor_Mixing(ng, FIX_LAT, ctx=ctx)  # the solve runs on the mixing object's context
     r = [rng.uniform(size=1728), rng.uniform(size=1728)]
     ad = rng.uniform(size=1728)
     for spin in ("off", "on"):
         out = np.zeros(1728)
-        L.Solve_Poisson(spin, mix, r, ad, out, ctx)
+        L.Solve_Poisson(spin, mix, r, ad, out)  # the reference's five arguments
         ref = O.solve_poisson_xyz(ng, mix.Recvecs, O.set_density_xyz(spin, ng, r, ad))
         np.testing.assert_allclose(out, ref, rtol=0, atol=1e-12 * np.max(np.abs(ref)))
 
@@ -161,14 +161,14 @@ def test_xc_golden(ctx, fix):
     g = golden()
     pt, vt = aden_tables("Si7.0", "Si_CA19", 4.0)
     a, p, d = O.set_adenpcc_grid("off", [[2., 2.], [2., 2.]], [[0, 0, 0, 0]] * 2, [pt], [vt], uo)
-    xf = L.XC_Func("LDA", "off", 1, (3, 3, 3))
-    L.Set_XC_Grid(xf, p, d, ctx)
+    xf = L.XC_Func("LDA", "off", 1, (3, 3, 3), ctx=ctx)
+    L.Set_XC_Grid(xf, p, d)  # the reference's three arguments
     np.testing.assert_allclose(xf.Vxc_Grid[0], g["xc_grid"]["XC_PBE Si LDA"][0], rtol=1.5e-8)
     ufe = O.UCell(2, FE_LAT, 1, [1], [[0, 0, 0]], [6.0], (3, 3, 3), [0, 0, 0])
     pt, vt = aden_tables("Fe6.0H", "Fe_CA19H", 16.0)
     a, p, d = O.set_adenpcc_grid("on", [[8., 6.]], [[0, 0, 0, 0]], [pt], [vt], ufe)
     xf = L.XC_Func("LSDA", "on", 2, (3, 3, 3))
-    L.Set_XC_Grid(xf, p, d, ctx)
+    L.Set_XC_Grid(xf, p, d, ctx=ctx)
     for s in range(2):
         np.testing.assert_allclose(xf.Vxc_Grid[s], g["xc_grid"]["XC_PBE BCC_Fe LSDA"][s], rtol=1.5e-8)
 
@@ -185,18 +185,18 @@ def test_xc_vpot_energies_vs_oracle(ctx):
     for spin, xc in (("off", "LDA"), ("on", "LSDA")):
         n = 1 if spin == "off" else 2
         xf = L.XC_Func(xc, spin, n, (16, 16, 16))
-        L.Set_XC_Grid(xf, pcc, rho, ctx)
+        L.Set_XC_Grid(xf, pcc, rho, ctx=ctx)
         ref = O.set_xc_grid(xc, spin, pcc, rho)
         for c in range(n):
             np.testing.assert_allclose(xf.Vxc_Grid[c], ref[c], rtol=1e-13, atol=1e-15)
         vp = [np.zeros(nn) for _ in range(n)]
-        L.Set_Vpot_Grid(xf, dvh, vp, vna, ctx)
+        L.Set_Vpot_Grid(xf, dvh, vp, Vna_Grid=vna, ctx=ctx)
         vref = O.set_vpot_grid(spin, dvh, ref, vna)
         for c in range(n):
             np.testing.assert_allclose(vp[c], vref[c], rtol=1e-13, atol=1e-14)
-        eh = L.Calc_EH1(spin, 0.01, ad, rho, dvh, ctx)
+        eh = L.Calc_EH1(spin, 0.01, ad, rho, dvh, ctx=ctx)
         assert eh == pytest.approx(O.calc_eh1(spin, 0.01, ad, rho, dvh), rel=1e-12)
-        ex = L.Calc_EXC1(spin, xc, type("G", (), {"GridVol": 0.01})(), ad, pcc, rho, ctx)
+        ex = L.Calc_EXC1(spin, xc, type("G", (), {"GridVol": 0.01})(), ad, pcc, rho, ctx=ctx)
         exr = O.calc_exc1(spin, xc, 0.01, ad, pcc, rho)
         np.testing.assert_allclose(ex[:n], exr[:n], rtol=1e-12)
 
@@ -207,7 +207,7 @@ def test_nc_xc_rotation(ctx):
     rho = [rng.uniform(0, 0.2, nn), rng.uniform(0, 0.2, nn), rng.uniform(0, 3, nn), rng.uniform(-3, 3, nn)]
     pcc = rng.uniform(0, 0.01, nn)
     xf = L.XC_Func("LSDA", "nc", 4, (8, 8, 8))
-    L.Set_XC_Grid(xf, pcc, rho, ctx)
+    L.Set_XC_Grid(xf, pcc, rho, ctx=ctx)
     ref = O.set_xc_grid("LSDA", "nc", pcc, rho)
     for c in range(4):
         np.testing.assert_allclose(xf.Vxc_Grid[c], ref[c], rtol=1e-12, atol=1e-15)
@@ -269,4 +269,4 @@ def test_errors(ctx, fix, si2):
     with pytest.raises(L.LCPError):
         L.XC_Func("LDA", "on", 2, (3, 3, 3))
     with pytest.raises(L.LCPError):
-        L.Set_Orbitals_Grid([product_pao("Si7.0", "s1p1")], u, ctx)  # basis does not match Total_NumOrbs
+        L.Set_Orbitals_Grid([product_pao("Si7.0", "s1p1")], u, ctx=ctx)  # basis does not match Total_NumOrbs

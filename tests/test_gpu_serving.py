@@ -18,14 +18,14 @@ def _structures(ctx):
     out = []
     lat, pos, ng = si2_cell()
     u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
-    out.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx)))
+    out.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)))
     wl = si64_workload(nrep=1, ngrid=(40, 40, 40))
     u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
                 Total_NumOrbs=wl["numorbs"])
-    out.append((u, L.Set_Orbitals_Grid(wl["paos"], u, ctx)))
+    out.append((u, L.Set_Orbitals_Grid(wl["paos"], u, ctx=ctx)))
     out.append(_mixed_cell(ctx))
     u = L.UCell(1, lat, 2, [1, 1], pos * 1.01, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
-    out.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx)))
+    out.append((u, L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)))
     jobs = []
     for k, (u, orbs) in enumerate(out):
         vna = smooth_vna(u.Ngrid, u.Latvecs, 40 + k)

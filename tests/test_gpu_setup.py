@@ -87,14 +87,14 @@ def test_adenpcc_golden(ctx):
     u = L.UCell(1, FIX_LAT, 2, [1, 1], FIX_POS, [7.0, 7.0], (3, 3, 3), [0, 0, 0], Total_NumOrbs=[13, 13])
     for name, vps in (("Set_AdenPCC_Grid Si LDA", "Si_CA19"), ("Set_AdenPCC_Grid Si GGA-PBE", "Si_PBE19")):
         pao, pcc = _species("Si7.0", vps, 4.0)
-        a, p, d = L.Set_AdenPCC_Grid("off", [[2., 2.], [2., 2.]], [[0, 0, 0, 0]] * 2, [pao], [pcc], u, ctx)
+        a, p, d = L.Set_AdenPCC_Grid("off", [[2., 2.], [2., 2.]], [[0, 0, 0, 0]] * 2, [pao], [pcc], u, ctx=ctx)
         ref = g[name]
         np.testing.assert_allclose(a, ref["ADensity_Grid"], rtol=1.5e-8)
         np.testing.assert_allclose(p, ref["PCCDensity_Grid"], rtol=1.5e-8)
         np.testing.assert_allclose(d[0], ref["Density_Grid"][0], rtol=1.5e-8)
     ufe = L.UCell(2, FE_LAT, 1, [1], [[0, 0, 0]], [6.0], (3, 3, 3), [0, 0, 0], Total_NumOrbs=[13])
     pao, pcc = _species("Fe6.0H", "Fe_PBE19H", 16.0)
-    a, p, d = L.Set_AdenPCC_Grid("on", [[8., 6.]], [[0, 0, 0, 0]], [pao], [pcc], ufe, ctx)
+    a, p, d = L.Set_AdenPCC_Grid("on", [[8., 6.]], [[0, 0, 0, 0]], [pao], [pcc], ufe, ctx=ctx)
     ref = g["Set_AdenPCC_Grid BCC_Fe GGA-PBE"]
     np.testing.assert_allclose(a, ref["ADensity_Grid"], rtol=1.5e-8)
     np.testing.assert_allclose(p, ref["PCCDensity_Grid"], rtol=1.5e-8)
@@ -112,7 +112,7 @@ def test_adenpcc_vs_oracle_on_device_ucell(ctx, spin):
     pt, vt = aden_tables("Si7.0", "Si_PBE19", 4.0)
     init = [[2.3, 1.7], [1.9, 2.1]]
     angle = [[0.7, 1.1, 0, 0], [2.0, -0.4, 0, 0]]
-    a, p, d = L.Set_AdenPCC_Grid(spin, init, angle, [pao], [pcc], u, ctx)
+    a, p, d = L.Set_AdenPCC_Grid(spin, init, angle, [pao], [pcc], u, ctx=ctx)
     ar, pr, dr = O.set_adenpcc_grid(spin, init, angle, [pt], [vt], uo)
     for got, want in [(a, ar), (p, pr)] + list(zip(d, dr)):
         assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want))
@@ -127,7 +127,7 @@ def test_adenpcc_two_species(ctx):
     sp = [_species("Si7.0", "Si_PBE19", 4.0), _species("Fe6.0H", "Fe_PBE19H", 16.0)]
     tabs = [aden_tables("Si7.0", "Si_PBE19", 4.0), aden_tables("Fe6.0H", "Fe_PBE19H", 16.0)]
     init = [[2.2, 1.8], [8.0, 6.0]]
-    a, p, d = L.Set_AdenPCC_Grid("on", init, None, [x[0] for x in sp], [x[1] for x in sp], u, ctx)
+    a, p, d = L.Set_AdenPCC_Grid("on", init, None, [x[0] for x in sp], [x[1] for x in sp], u, ctx=ctx)
     ar, pr, dr = O.set_adenpcc_grid("on", init, [[0, 0, 0, 0]] * 2, [t[0] for t in tabs], [t[1] for t in tabs], uo)
     for got, want in [(a, ar), (p, pr)] + list(zip(d, dr)):
         assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want))

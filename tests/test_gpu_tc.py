@@ -35,7 +35,7 @@ def _si2(ctx):
     from helpers import product_pao, si2_cell
     lat, pos, ng = si2_cell()
     u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
-    return u, L.Set_Orbitals_Grid([product_pao()], u, ctx)
+    return u, L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)
 
 
 def _si64(ctx):
@@ -43,7 +43,7 @@ def _si64(ctx):
     wl = si64_workload()
     u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
                 Total_NumOrbs=wl["numorbs"])
-    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx)
+    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx=ctx)
     dm = psd_density_matrices(u, wl["dm_seed"], trace=wl["trace"])
     vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
     return u, orbs, dm, vna
@@ -157,7 +157,7 @@ def test_job_energy_bf16x3_mx2(ctx):
     wl = mx2_monolayer()
     u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
                 Total_NumOrbs=wl["numorbs"])
-    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx)
+    orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx=ctx)
     dm = psd_density_matrices(u, wl["dm_seed"], nspin=2, trace=wl["trace"])
     vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
     E = {}
@@ -184,7 +184,7 @@ def _mixed_cell(ctx, nrep=1, ngrid=(44, 40, 48)):
     lat = np.diag([11.0, 10.0, 12.0])
     pos = np.array([[1.0, 2.0, 3.0], [5.5, 6.0, 8.5], [8.0, 1.5, 6.0]])
     u = L.UCell(1, lat, 3, [1, 2, 3], pos, [8.0, 7.0, 6.0], ngrid, [0, 0, 0], Total_NumOrbs=[18, 13, 4])
-    return u, L.Set_Orbitals_Grid(paos, u, ctx)
+    return u, L.Set_Orbitals_Grid(paos, u, ctx=ctx)
 
 
 def test_orbital_chunks_density_and_h(ctx):
@@ -280,5 +280,5 @@ def test_bricks_of_many_images(ctx):
     u = L.UCell(1, np.eye(3) * side, 16, [1] * 16, pos, [9.0] * 16, (48, 48, 48), [0, 0, 0],
                 Total_NumOrbs=[18] * 16)
     assert u.brick_info()["max_images"] > 64
-    orbs = L.Set_Orbitals_Grid([pao], u, ctx)
+    orbs = L.Set_Orbitals_Grid([pao], u, ctx=ctx)
     _check_vs_fp64(ctx, u, orbs, 63)

@@ -34,6 +34,12 @@ def _noalloc(ctx, u, orbs, spin, dm_dev, rho_dev):
     _lib.check(_lib.lib.lcp_set_density_grid_noalloc(ctx._h, u._h, orbs._h, _lib.SPIN[spin], pd, pr))
 
 
+def _alloc_count():
+    n = ctypes.c_int64()
+    _lib.check(_lib.lib.lcp_device_alloc_count(ctypes.byref(n)))
+    return n.value
+
+
 def _reference(ctx, u, orbs, spin, dm):
     out = [np.zeros(u.NN) for _ in dm]
     ctx.set_precision("bf16x3")
@@ -51,16 +57,22 @@ def test_density_noalloc_matches_allocating_entry():
     ctx = L.Context(0)
     lat, pos, ng = si2_cell()
     u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
-    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx)
-    for spin, n in (("off", 1), ("on", 2)):
-        dms = [psd_dm(u, seed, nspin=n) for seed in (101, 202)]
+    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)
+    from lcpgrid.workloads import psd_nc_density_matrices
+    for spin, n in (("off", 1), ("on", 2), ("nc", 4)):
+        if spin == "nc":
+            dms = [psd_nc_density_matrices(u, seed, trace=4.0) for seed in (101, 202)]
+        else:
+            dms = [psd_dm(u, seed, nspin=n) for seed in (101, 202)]
         refs = [_reference(ctx, u, orbs, spin, dm) for dm in dms]  # also builds the split-BF16 tables
         outs = []
         for dm in dms:  # two calls in a row on the shared scratch
             dm_dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in dm]
             rho_dev = [torch.full((u.NN,), float("nan"), dtype=torch.float64, device="cuda") for _ in range(n)]
             torch.cuda.synchronize()
+            before = _alloc_count()
             _noalloc(ctx, u, orbs, spin, dm_dev, rho_dev)
+            assert _alloc_count() == before  # the call made no device allocation of its own
             outs.append([r.cpu().numpy() for r in rho_dev])
         for ref, out in zip(refs, outs):
             for c in range(n):
@@ -77,7 +89,7 @@ def test_density_noalloc_rejections():
     # orbitals whose split-BF16 tables were never built
     lat, pos, ng = si2_cell()
     u = L.UCell(1, lat, 2, [1, 1], pos, [7.0, 7.0], ng, [0, 0, 0], Total_NumOrbs=[13, 13])
-    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx)
+    orbs = L.Set_Orbitals_Grid([product_pao()], u, ctx=ctx)
     dm_dev = [torch.zeros(u.Total_Hsize, dtype=torch.float64, device="cuda")]
     rho_dev = [torch.zeros(u.NN, dtype=torch.float64, device="cuda")]
     with pytest.raises(L.LCPError) as e:
@@ -88,7 +100,7 @@ def test_density_noalloc_rejections():
     nat = pos.shape[0]
     big = L.UCell(1, lat, nat, [1] * nat, pos, [7.0] * nat, (48, 48, 48), [0, 0, 0], Total_NumOrbs=[13] * nat)
     assert big.Nloop > 10921
-    borbs = L.Set_Orbitals_Grid([product_pao()], big, ctx)
+    borbs = L.Set_Orbitals_Grid([product_pao()], big, ctx=ctx)
     dm_dev = [torch.zeros(big.Total_Hsize, dtype=torch.float64, device="cuda")]
     rho_dev = [torch.zeros(big.NN, dtype=torch.float64, device="cuda")]
     with pytest.raises(L.LCPError) as e:
