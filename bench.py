@@ -45,11 +45,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp32", "fp64"])
-    ap.add_argument("--workload", default="si64", choices=["si64", "si8", "mx2"])
+    ap.add_argument("--workload", default="si64", choices=["si64", "si8", "mx2", "si2"],
+                    help="si64: 64-atom Si 96^3 (default); si8: its 8-atom cell at 48^3; mx2: the 432-atom "
+                         "LSDA cell; si2: the plain small case (Si2, real Si7.0 tables, 24^3)")
     ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 drop-in form")
     ap.add_argument("--fp32-steps", type=int, default=3,
                     help="timed steps of the FP32 form (CUDA-core FP32 pair contractions), for comparison")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU-baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="timed full steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--serving", action="store_true", help="run the serving form instead of the step bench")
@@ -57,6 +59,7 @@ def parse():
     ap.add_argument("--no-force", action="store_true", help="skip the grid force term section of the step bench line")
     ap.add_argument("--no-gga", action="store_true", help="skip the GGA-PBE section of the step bench line")
     ap.add_argument("--no-nc", action="store_true", help="skip the non-collinear section of the step bench line")
+    ap.add_argument("--no-si2", action="store_true", help="skip the plain Si2 section of the step bench line")
     ap.add_argument("--xc", default="auto", choices=["auto", "GGA_PBE"],
                     help="xc of the timed step: auto = LDA ('off') / LSDA ('on'), or GGA_PBE")
     ap.add_argument("--serve-structures", type=int, default=24)
@@ -263,8 +266,9 @@ def force3_cpu_baseline(wl, ucell_gpu, nspin, reps=2):
     _Calc_Force3_Blocked_Kernel!) on the pairs among the first 8 atoms, one
     host core, extrapolated to the cell by the force work per pair."""
     import numpy as np
-    from lcpgrid.workloads import psd_density_matrices_oracle, smooth_vna
     from oracle import lcp_oracle as O
+    W = _inputs()
+    psd_density_matrices_oracle, smooth_vna = W.psd_density_matrices_oracle, W.smooth_vna
     sample = [p for p in range(ucell_gpu.Nloop)
               if ucell_gpu.MPI_atom[p] <= SAMPLE_ATOMS and ucell_gpu.MPI_natn[p] <= SAMPLE_ATOMS]
     no = np.asarray(wl["numorbs"], dtype=np.float64)
@@ -329,94 +333,94 @@ def nc_section(wl, u, orbs, vna, steps=10):
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)
 
-SAMPLE_ATOMS = 8  # the CPU sample: pairs among the first conventional cell's 8 atoms
+SAMPLE_ATOMS = 8  # the Force3 CPU sample: pairs among the first conventional cell's 8 atoms
 
 
-def _cpu_inputs(wl, sample):
-    from lcpgrid.workloads import psd_density_matrices_oracle, smooth_vna
-    from oracle import lcp_oracle as O
-    u = O.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
-                total_numorbs=wl["numorbs"], pair_subset=sample)
-    pao = wl["paos"][0]
-    opao = O.PAO(pao.Spe_MaxL_Basis, pao.Spe_Num_Basis, pao.Spe_PAO_RV, pao.Spe_PAO_RWF)
-    orbs = O.set_orbitals_grid([opao], u, atoms=set(range(SAMPLE_ATOMS)))
-    dm = psd_density_matrices_oracle(u, wl["dm_seed"], trace=wl["trace"])[0]
-    vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
-    return u, orbs, dm, vna
+def _inputs():
+    """lcpgrid/workloads.py (with pao.py) loaded by path without importing the
+    lcpgrid package, whose __init__ loads liblcpgrid.so: the reference arm and
+    the CPU baseline build their inputs without the product library."""
+    import importlib.util
+    import types
+    name = "_lcp_inputs"
+    if name + ".workloads" in sys.modules:
+        return sys.modules[name + ".workloads"]
+    pkgdir = os.path.join(PKG, "lcpgrid")
+    pkg = types.ModuleType(name)
+    pkg.__path__ = [pkgdir]
+    sys.modules[name] = pkg
+    for mod in ("pao", "workloads"):
+        spec = importlib.util.spec_from_file_location(name + "." + mod, os.path.join(pkgdir, mod + ".py"))
+        m = importlib.util.module_from_spec(spec)
+        sys.modules[spec.name] = m
+        spec.loader.exec_module(m)
+    return sys.modules[name + ".workloads"]
 
 
-def _cpu_run(u, orbs, dm, vna, reps):
-    from oracle import lcp_oracle as O
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        O.set_density_grid("off", u, orbs, [dm])
-        O.calc_matrix_elements(u, orbs, [vna], 1)
-    return time.perf_counter() - t0
+SPECIES_TABLES = os.path.join(ROOT, "tests", "golden", "species_tables.npz")
 
 
-def _cpu_proc(wl, sample, reps, barrier, queue):
-    os.environ["OPENBLAS_NUM_THREADS"] = "1"
-    os.environ["OMP_NUM_THREADS"] = "1"
-    u, orbs, dm, vna = _cpu_inputs(wl, sample)
-    barrier.wait()
-    queue.put(_cpu_run(u, orbs, dm, vna, reps))
-
-
-def cpu_baseline(wl, ucell_gpu, budget_s, all_cores):
-    """Time the oracle (a restatement of the reference's per-pair, 512-point
-    blocked BLAS algorithm) on a bounded sample of the workload -- density + H
-    over the pairs among the first 8 atoms -- with one process per host core,
-    each single-threaded BLAS, as the reference's MPI pair split runs.  The full
-    step is extrapolated by the reference's own work weight NO_i*NO_j*NumOLG;
-    Poisson and xc are timed on the full grid.  Processes are spawned (this
-    runs after GPU work)."""
-    os.environ["OPENBLAS_NUM_THREADS"] = "1"
-    os.environ["OMP_NUM_THREADS"] = "1"
-    import multiprocessing as mp
-
+def cpu_spec(wl):
+    """Host inputs of the CPU grid step (oracle/cpu_step.py) for a workload."""
     import numpy as np
     from oracle import lcp_oracle as O
-
-    sample = [p for p in range(ucell_gpu.Nloop)
-              if ucell_gpu.MPI_atom[p] <= SAMPLE_ATOMS and ucell_gpu.MPI_natn[p] <= SAMPLE_ATOMS]
-    no = np.asarray(wl["numorbs"], dtype=np.float64)
-    olg = ucell_gpu.MPI_NumOLG.astype(np.float64)
-    wt = no[ucell_gpu.MPI_atom - 1] * no[ucell_gpu.MPI_natn - 1] * olg
-    w_sample = float(wt[sample].sum())
-    w_total = float(wt.sum())
-    u, orbs, dm, vna = _cpu_inputs(wl, sample)
-    t1 = _cpu_run(u, orbs, dm, vna, 1)
-    cores = (os.cpu_count() or 1) if all_cores else 1
-    reps = max(1, int(budget_s / max(t1, 1e-3)))
-    if cores > 1:
-        ctx = mp.get_context("spawn")
-        barrier = ctx.Barrier(cores)
-        queue = ctx.Queue()
-        procs = [ctx.Process(target=_cpu_proc, args=(wl, sample, reps, barrier, queue)) for _ in range(cores)]
-        for pr in procs:
-            pr.start()
-        times = [queue.get() for _ in procs]
-        for pr in procs:
-            pr.join()
-        wall = max(times)
+    W = _inputs()
+    spin = wl.get("spinpol", "off")
+    spec = {k: wl[k] for k in ("latvecs", "natom", "atom2spe", "gxyz", "cut", "ngrid", "origin", "numorbs")}
+    spec["paos"] = [(q.Spe_MaxL_Basis, q.Spe_Num_Basis, q.Spe_PAO_RV, q.Spe_PAO_RWF) for q in wl["paos"]]
+    spec["spinpol"] = spin
+    spec["xc"] = "LDA" if spin == "off" else "LSDA"
+    if "pcc" in wl:  # the plain case: the reference's own atomic and partial-core densities
+        u = O.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"],
+                    wl["origin"], total_numorbs=wl["numorbs"], pair_subset=[])
+        q, c = wl["paos"][0], wl["pcc"]
+        ad, pc, _ = O.set_adenpcc_grid("off", wl["init_nspin"], [[0, 0, 0, 0]] * wl["natom"],
+                                       [(q.Spe_PAO_XV, q.Spe_PAO_RV, q.Spe_Atomic_Den)],
+                                       [(c.Spe_VPS_XV, c.Spe_VPS_RV, c.Spe_Atomic_PCC)], u)
+        spec["aden"], spec["pcc"] = ad, pc
     else:
-        wall = _cpu_run(u, orbs, dm, vna, reps)
-    rate = cores * reps * w_sample / wall
-    t_pairs = w_total / rate
-    rho = np.abs(np.random.default_rng(0).normal(size=int(np.prod(wl["ngrid"])))) * 0.01
-    t0 = time.perf_counter()
-    O.solve_poisson_xyz(wl["ngrid"], 2 * np.pi * np.linalg.inv(np.asarray(wl["latvecs"]).T),
-                        O.set_density_xyz("off", wl["ngrid"], [rho], np.zeros_like(rho)))
-    O.set_xc_grid("LDA", "off", np.zeros_like(rho), [rho])
-    O.calc_exc1("off", "LDA", 1.0, np.zeros_like(rho), np.zeros_like(rho), [rho])
-    t_grid = time.perf_counter() - t0
-    step_s = t_pairs + t_grid
-    return {"value": 1.0 / step_s, "unit": UNIT, "cores": cores, "kind": "port",
-            "ms_per_step": step_s * 1e3,
-            "sample": "numpy oracle (per-pair 512-point blocks + BLAS, 1 BLAS thread/process): density+H over "
-                      "the %d pairs among atoms 1-%d (%.2f%% of the pair work) x %d reps on each of %d processes "
-                      "(%.1f s wall), extrapolated by NO_i*NO_j*NumOLG; Poisson+xc timed once on the full grid"
-                      % (len(sample), SAMPLE_ATOMS, 100 * w_sample / w_total, reps, cores, wall)}
+        spec["vna"] = W.smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
+    return spec
+
+
+def cpu_step_run(wl, steps, warmup=1, nproc=None):
+    """The reference's grid step restated on the host cores (oracle/cpu_step.py:
+    one process per core as one MPI rank each, the reference's pair split,
+    per-pair 512-point blocks with single-threaded BLAS, the rank grids summed,
+    Poisson, xc and energies on the full grid), timed over `steps` full steps
+    after `warmup`.  Returns (result dict, last step's output)."""
+    import numpy as np
+    from oracle.cpu_step import CpuGridStep
+    W = _inputs()
+    spec = cpu_spec(wl)
+    with CpuGridStep(spec, nproc=nproc) as cs:
+        nspin = cs.nspin
+        dm = W.psd_density_matrices_oracle(cs.u, wl["dm_seed"], nspin=nspin, trace=wl["trace"])
+        cs.set_dm(dm)
+        for _ in range(warmup):
+            out = cs.step()
+        per, stages = [], []
+        for _ in range(steps):
+            out = cs.step()
+            per.append(out["seconds"]["step"])
+            stages.append(out["seconds"])
+        ms = float(np.mean(per)) * 1e3
+        res = {"value": 1000.0 / ms, "unit": UNIT, "cores": cs.nproc, "kind": "port", "ms_per_step": ms,
+               "stage_ms": {k: float(np.mean([x[k] for x in stages])) * 1e3
+                            for k in ("density", "poisson", "xc_vpot", "hamiltonian", "energies")},
+               "setup_s": cs.setup_s, "E_grid": float(out["energies"][4]),
+               "sample": "full step, no extrapolation: %s, all %d pairs, %d timed steps after %d warm-up; "
+                         "oracle restatement with one process per host core as one MPI rank each, the "
+                         "reference's weighted contiguous pair split, 512-point blocks, 1 BLAS thread per "
+                         "process; no product library loaded" % (wl["name"], cs.u.Nloop, steps, warmup)}
+    return res, out
+
+
+def cpu_baseline(wl, steps=2):
+    """cpu_baseline of the GPU line: the full CPU step on all host cores.
+    Spawned processes (this runs after GPU work)."""
+    res, _ = cpu_step_run(wl, steps)
+    return res
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -431,19 +435,28 @@ def build_workload(ctx, wl):
     t_geom = time.perf_counter() - t0
     t0 = time.perf_counter()
     orbs = L.Set_Orbitals_Grid(wl["paos"], u, ctx=ctx)
+    ctx.synchronize()
     t_tab = time.perf_counter() - t0
     dm = psd_density_matrices(u, wl["dm_seed"], nspin=nspin, trace=wl["trace"])
-    vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
+    if "pcc" in wl:  # the plain case: atomic and partial-core densities, no V_na
+        ad, pc, _ = L.Set_AdenPCC_Grid("off", wl["init_nspin"], None, wl["paos"], [wl["pcc"]], u, ctx=ctx)
+        wl["_aden_pcc"] = (ad, pc)
+        vna = None
+    else:
+        vna = smooth_vna(wl["ngrid"], wl["latvecs"], wl["vna_seed"])
     return u, orbs, dm, vna, t_geom, t_tab
 
 
 def workload(args):
-    from lcpgrid.workloads import mx2_monolayer, si64_workload
+    import numpy as np
+    W = _inputs()
     if args.workload == "si8":
-        return si64_workload(nrep=1, ngrid=(48, 48, 48))
+        return W.si64_workload(nrep=1, ngrid=(48, 48, 48))
     if args.workload == "mx2":
-        return mx2_monolayer()
-    return si64_workload()
+        return W.mx2_monolayer()
+    if args.workload == "si2":
+        return W.si2_workload(np.load(SPECIES_TABLES))
+    return W.si64_workload()
 
 
 def run_ours(args):
@@ -477,12 +490,14 @@ def run_ours(args):
     spin = wl.get("spinpol", "off")
     nspin = len(dm)
     xc = args.xc if args.xc != "auto" else ("LDA" if spin == "off" else "LSDA")
-    job = L.GridStepJob(u, orbs, spin, xc, None, None, vna)
+    ad, pc = wl.get("_aden_pcc", (None, None))
+    job = L.GridStepJob(u, orbs, spin, xc, ad, pc, vna)
     job.set_dm(dm)
     ctx.set_precision("fp64")
     job.step()
     e_fp64 = job.energies()
     h_fp64 = [h.copy() for h in job.hks()]
+    rho_fp64 = [r.copy() for r in job.density()]
     fp64_ms = None
     if args.precision != "fp64" and args.fp64_steps > 0:
         fe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -543,6 +558,7 @@ def run_ours(args):
         total_ms = float(t.item())
     e_now = job.energies()
     h_now = job.hks()
+    rho_now = job.density()
 
     # e2e through the public API: pinned host D in, H and energies out, every step
     pin_dm = [torch.empty(u.Total_Hsize, dtype=torch.float64, pin_memory=True) for _ in range(nspin)]
@@ -618,7 +634,12 @@ def run_ours(args):
                    "err_per_atom_uHa": abs(float(e_now[4] - e_fp64[4])) / wl["natom"] * 1e6,
                    "rel_err": abs(float(e_now[4] - e_fp64[4])) / abs(float(e_fp64[4])),
                    "max_abs_dH": float(max(np.max(np.abs(a - b)) for a, b in zip(h_now, h_fp64))),
+                   "max_abs_dH_note": "each form with its own V; north_star's H bound of 1e-7 Ha is for the FP64 "
+                                      "drop-in, the precision form states its error",
+                   "max_abs_drho": float(max(np.max(np.abs(a - b)) for a, b in zip(rho_now, rho_fp64))),
+                   "max_abs_rho": float(max(np.max(np.abs(b)) for b in rho_fp64)),
                    "terms": ["E_H1", "E_xc1 up", "E_xc1 down", "sum <D,H>", "E_grid"],
+                   "terms_rel_err": [abs(float(a - b)) / max(abs(float(b)), 1e-300) for a, b in zip(e_now, e_fp64)],
                    "terms_this_form": [float(x) for x in e_now], "terms_fp64": [float(x) for x in e_fp64]},
         "fp64_dropin": None if fp64_ms is None else {
             "ms_per_step": fp64_ms, "steps": args.fp64_steps, "speedup_of_this_form": fp64_ms / ms_step},
@@ -627,28 +648,29 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "gpu_launches_note": "library kernels per timed region; cuFFT adds 2 FFT launches per step",
     }
-    if rank == 0 and not args.no_force and world == 1:
+    plain = args.workload == "si2"
+    if rank == 0 and not args.no_force and world == 1 and not plain:
         try:
             line["force3"] = force3_section(wl, u, dm, vna)
         except Exception as exc:  # the force section must not hide the step line
             line["force3"] = {"error": repr(exc)}
-    if rank == 0 and not args.no_gga and world == 1:
+    if rank == 0 and not args.no_gga and world == 1 and not plain:
         try:
             line["gga_pbe"] = gga_section(wl, u, orbs, dm, vna)
         except Exception as exc:  # the GGA section must not hide the step line
             line["gga_pbe"] = {"error": repr(exc)}
-    if rank == 0 and not args.no_nc and world == 1 and spin == "off":
+    if rank == 0 and not args.no_nc and world == 1 and spin == "off" and not plain:
         try:
             line["nc"] = nc_section(wl, u, orbs, vna)
         except Exception as exc:  # the nc section must not hide the step line
             line["nc"] = {"error": repr(exc)}
-    if rank == 0 and not args.no_serving and world == 1:
+    if rank == 0 and not args.no_serving and world == 1 and not plain:
         # the serving form on the same GPU: Poisson stream of mixed-size structures
         try:
             line["serving"] = serving(args)
         except Exception as exc:  # the serving run must not hide the step line
             line["serving"] = {"error": repr(exc)}
-    if rank == 0 and not args.no_batching and world == 1:
+    if rank == 0 and not args.no_batching and world == 1 and not plain:
         # the batching form on the same GPU: 256 mixed cells in one batched step
         try:
             del job
@@ -656,49 +678,145 @@ def run_ours(args):
             line["batching"] = batching(args)
         except Exception as exc:  # the batching run must not hide the step line
             line["batching"] = {"error": repr(exc)}
-    if rank == 0 and not args.no_cpu_baseline and len(wl["paos"]) > 1:
-        line["cpu_baseline"] = {"value": None, "note": "the CPU baseline is timed on the one-species 64-atom cell "
-                                                       "(the default workload)"}
+    if rank == 0 and world == 1 and args.workload == "si64" and not args.no_si2:
+        try:
+            line["plain_si2"] = si2_section(args)
+        except Exception as exc:  # the plain case must not hide the step line
+            line["plain_si2"] = {"error": repr(exc)}
+    if rank == 0 and not args.no_cpu_baseline and args.workload == "mx2":
+        line["cpu_baseline"] = {"value": None, "note": "the CPU baseline is timed on the 64-atom cell (the "
+                                                       "default workload) and the Si2 cell"}
     elif rank == 0 and not args.no_cpu_baseline:
         try:
-            line["cpu_baseline"] = cpu_baseline(wl, u, args.cpu_seconds, all_cores=True)
+            cb, cout = cpu_step_run(wl, args.cpu_steps)
+            # the full-size FP64 check: the GPU's FP64 step against the CPU restatement
+            cb["vs_gpu_fp64"] = {
+                "max_abs_drho": float(max(np.max(np.abs(a - b)) for a, b in zip(rho_fp64, cout["density"]))),
+                "max_abs_dH": float(max(np.max(np.abs(a - b)) for a, b in zip(h_fp64, cout["hks"]))),
+                "dE_per_atom_uHa": abs(float(e_fp64[4]) - cout["energies"][4]) / wl["natom"] * 1e6}
+            line["cpu_baseline"] = cb
         except Exception as exc:  # the baseline must not hide the GPU line
             line["cpu_baseline"] = {"value": None, "error": repr(exc)}
     if rank == 0:
-        print(json.dumps(line))
+        emit(line)
     if world > 1:
         dist.destroy_process_group()
 
 
+def si2_section(args, steps=50):
+    """The plain small case: the Si2 primitive cell with the real Si7.0-s2p2d1
+    tables, LDA with the reference's atomic and partial-core densities, 24^3.
+    The whole step on the GPU in FP64 and in split-BF16 (CUDA events on the
+    library's stream, device-resident) beside the full CPU step on the host
+    cores, with the GPU results against the CPU restatement."""
+    import numpy as np
+    import torch
+
+    import lcpgrid as L
+    wl = workload(argparse.Namespace(workload="si2"))
+    ctx = L.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    u, orbs, dm, vna, _, _ = build_workload(ctx, wl)
+    ad, pc = wl["_aden_pcc"]
+    job = L.GridStepJob(u, orbs, "off", "LDA", ad, pc, None)
+    job.set_dm(dm)
+    out, res = {}, {}
+    for prec in ("fp64", "bf16x3"):
+        ctx.set_precision(prec)
+        for _ in range(5):
+            job.step()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(steps):
+            job.step()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        res[prec] = (job.energies(), job.density()[0].copy(), job.hks()[0].copy())
+        out[prec] = {"ms_per_step": ev[0].elapsed_time(ev[1]) / steps}
+    cb, cout = cpu_step_run(wl, 3)
+    for prec, (e, rho, H) in res.items():
+        out[prec].update({"E_grid": float(e[4]),
+                          "dE_per_atom_uHa_vs_cpu": abs(float(e[4]) - cout["energies"][4]) / 2 * 1e6,
+                          "max_abs_drho_vs_cpu": float(np.max(np.abs(rho - cout["density"][0]))),
+                          "max_abs_dH_vs_cpu": float(np.max(np.abs(H - cout["hks"][0])))})
+    out["cpu"] = {"ms_per_step": cb["ms_per_step"], "cores": cb["cores"], "E_grid": cb["E_grid"]}
+    out["config"] = {"workload": wl["name"], "pairs": int(u.Nloop), "ngrid": list(wl["ngrid"])}
+    return out
+
+
+def emit(line):
+    """Prints the JSON line on stdout, with its bulky lists (the brick-shape
+    autotune log) moved to a second line on stderr, and a compact summary of
+    every form's numbers as the line's last key."""
+    bat = line.get("batching")
+    if isinstance(bat, dict) and "autotune" in bat:
+        print(json.dumps({"batching_autotune": bat.pop("autotune")}), file=sys.stderr)
+    line["summary"] = summary(line)
+    print(json.dumps(line))
+
+
+def summary(line):
+    """The headline numbers of every form, short keys (ms unless named)."""
+    def g(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return round(d, 5) if isinstance(d, float) else d
+    s = {"step": g(line, "ms_per_step"), "e2e": g(line, "e2e", "ms_per_step"),
+         "fp64": g(line, "fp64_dropin", "ms_per_step"), "fp32": g(line, "fp32_form", "ms_per_step"),
+         "err_uHa_atom": g(line, "energy", "err_per_atom_uHa"), "max_dH": g(line, "energy", "max_abs_dH"),
+         "max_drho": g(line, "energy", "max_abs_drho"), "roof_frac": g(line, "roofline", "frac"),
+         "cpu_full_step": g(line, "cpu_baseline", "ms_per_step"), "cpu_cores": g(line, "cpu_baseline", "cores"),
+         "cpu_vs_gpu_fp64_dE_uHa": g(line, "cpu_baseline", "vs_gpu_fp64", "dE_per_atom_uHa"),
+         "cpu_vs_gpu_fp64_drho": g(line, "cpu_baseline", "vs_gpu_fp64", "max_abs_drho"),
+         "cpu_vs_gpu_fp64_dH": g(line, "cpu_baseline", "vs_gpu_fp64", "max_abs_dH"),
+         "si2_fp64": g(line, "plain_si2", "fp64", "ms_per_step"), "si2_bf16": g(line, "plain_si2", "bf16x3", "ms_per_step"),
+         "si2_cpu": g(line, "plain_si2", "cpu", "ms_per_step"),
+         "si2_fp64_dE_uHa": g(line, "plain_si2", "fp64", "dE_per_atom_uHa_vs_cpu"),
+         "force3": g(line, "force3", "ms_per_call"), "gga": g(line, "gga_pbe", "bf16x3", "ms_per_step"),
+         "gga_err_uHa": g(line, "gga_pbe", "err_per_atom_uHa"), "nc": g(line, "nc", "bf16x3", "ms_per_step"),
+         "nc_fp64": g(line, "nc", "fp64", "ms_per_step"),
+         "batch_ms": g(line, "batching", "ms_per_step"), "batch_cells_s": g(line, "batching", "value"),
+         "batch_vs_1by1": g(line, "batching", "batch_speedup_vs_one_by_one"),
+         "batch_err_uHa": g(line, "batching", "fp64_per_cell_sample", "max_err_per_atom_uHa")}
+    sv = line.get("serving")
+    if isinstance(sv, dict):
+        s["serve_sat_bf16"] = g(sv, "saturated_bf16x3", "jobs_per_s")
+        s["serve_sat_fp64"] = g(sv, "saturated_fp64_dropin", "jobs_per_s")
+        s["serve_vs_fp64"] = g(sv, "jobs_per_s_vs_fp64")
+        s["serve_err_uHa"] = g(sv, "max_err_per_atom_uHa")
+        s["serve_sweep"] = [[g(r, "offered_rate"), g(r, "jobs_per_s"), g(r, "p50_ms"), g(r, "p99_ms")]
+                            for r in sv.get("sweep", [sv.get("stream")]) if isinstance(r, dict)]
+    return {k: v for k, v in s.items() if v is not None}
+
+
 def run_reference(args):
+    """The reference arm: the reference's grid step on the host cores (the
+    oracle restatement of its MPI-parallel algorithm, oracle/cpu_step.py), on
+    this arm's workload, metric and unit; W untimed and K timed full steps.
+    Nothing of the product library is loaded.  Under torchrun only rank 0
+    runs."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import lcpgrid as L
     wl = workload(args)
-    u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
-                Total_NumOrbs=wl["numorbs"])
-    vals = []
     t0 = time.perf_counter()
-    budget = max(4.0, 60.0 / max(1, args.steps + args.warmup))
-    for k in range(args.warmup + args.steps):
-        r = cpu_baseline(wl, u, budget, all_cores=True)
-        if k >= args.warmup:
-            vals.append(r)
+    cb, _ = cpu_step_run(wl, args.steps, warmup=args.warmup)
     wall = time.perf_counter() - t0
-    v = sum(x["value"] for x in vals) / len(vals)
-    ms = 1000.0 / v
-    cb = dict(vals[-1])
-    cb["value"] = v
+    v = cb["value"]
     print(json.dumps({
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded)", "impl": "reference",
+        "ms_per_step": cb["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
         "config": {"workload": wl["name"], "atoms": wl["natom"], "ngrid": list(wl["ngrid"]), "precision": "fp64"},
         "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
         "note": "Julia is not available on this machine; the reference's CPU path is timed through its numpy "
-                "restatement (oracle/), parallel over the host cores like the reference's MPI pair split"}))
+                "restatement (oracle/cpu_step.py): every pair of the cell, one process per host core as one MPI "
+                "rank each, measured full steps with no extrapolation; liblcpgrid.so is not loaded"}))
 
 
 # ------------------------------------------------------------------ serving form

@@ -66,6 +66,31 @@ def si2_primitive():
     return lat, frac @ lat
 
 
+def si2_workload(tables, seed=2024):
+    """The plain small case: the Si2 primitive cell with the real Si7.0-s2p2d1
+    radial tables and the Si_CA19 partial-core density, read from ``tables``
+    (a mapping with the arrays pao_Si7.0_{xv,rv,den,rwf} and
+    vps_Si_CA19_{xv,rv,pcc}, e.g. the species-table fixture of the tests),
+    LDA, grid Calc_Ngrid(150 Ry) = 24^3, Tr D = 4 per atom.  "pcc" holds the
+    PCC table object; the atomic densities come from Set_AdenPCC_Grid with two
+    electrons per spin per atom."""
+    lat, pos = si2_primitive()
+    xv, rv = np.asarray(tables["pao_Si7.0_xv"]), np.asarray(tables["pao_Si7.0_rv"])
+    rwf = np.asarray(tables["pao_Si7.0_rwf"])
+    from .pao import PCC, get_ialpha_index, normalize_atomic_den
+    maxl, nb = get_ialpha_index("s2p2d1")
+    pao = PAO(maxl, nb, rv, [[rwf[l, p] for p in range(nb[l])] for l in range(maxl + 1)], Spe_PAO_XV=xv,
+              Spe_Atomic_Den=normalize_atomic_den(4.0, xv, np.asarray(tables["pao_Si7.0_den"])),
+              Spe_Atom_Cut1=7.0, Atom_symbol="Si")
+    pcc = PCC(tables["vps_Si_CA19_xv"], tables["vps_Si_CA19_rv"], tables["vps_Si_CA19_pcc"])
+    return {
+        "name": "si2_fcc_24x24x24", "latvecs": lat, "gxyz": pos, "natom": 2, "atom2spe": [1, 1],
+        "cut": [7.0, 7.0], "ngrid": (24, 24, 24), "origin": [0.0, 0.0, 0.0], "numorbs": [13, 13],
+        "paos": [pao], "pcc": pcc, "init_nspin": [[2.0, 2.0], [2.0, 2.0]],
+        "vna_seed": seed + 1, "dm_seed": seed + 2, "trace": 8.0,
+    }
+
+
 def si_supercell(nrep=2, a_ang=5.43):
     """Cubic diamond Si supercell of nrep^3 conventional cells (8*nrep^3 atoms)."""
     a = a_ang * ANG_TO_BOHR
