@@ -764,7 +764,7 @@ def summary(line):
             if not isinstance(d, dict) or k not in d:
                 return None
             d = d[k]
-        return round(d, 5) if isinstance(d, float) else d
+        return float("%.5g" % d) if isinstance(d, float) else d
     s = {"step": g(line, "ms_per_step"), "e2e": g(line, "e2e", "ms_per_step"),
          "fp64": g(line, "fp64_dropin", "ms_per_step"), "fp32": g(line, "fp32_form", "ms_per_step"),
          "err_uHa_atom": g(line, "energy", "err_per_atom_uHa"), "max_dH": g(line, "energy", "max_abs_dH"),

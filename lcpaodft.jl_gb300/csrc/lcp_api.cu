@@ -1,7 +1,6 @@
 // C ABI of the lcpgrid library: argument checking, device memory, and the
 // orchestration of the kernels.  Declarations and conventions: lcpgrid.h.
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include <algorithm>
 #include <array>
@@ -27,32 +26,69 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error_cstr() { return g_last_error.c_str(); }
 }  // namespace lcp
 
+// Radices and roots of unity of a grid shape for the FFT Poisson solve.
+lcp_status make_fft_plan(const int32_t* ng, FftPlans* p) {
+  if (!lcp::fft_supported(ng))
+    return fail(LCP_ENOTSUP, "the FFT Poisson solve takes grid dimensions of 1 to " +
+                                 std::to_string(lcp::kFftMaxN) + " points");
+  std::vector<double> r64, a64;
+  std::vector<float> r32, a32;
+  size_t o64[3], o32[3];
+  for (int d = 0; d < 3; ++d) {
+    p->geom.n[d] = ng[d];
+    p->geom.nfac[d] = lcp::fft_factor(ng[d], p->geom.fac[d]);
+    lcp::fft_roots(ng[d], r64, r32);
+    o64[d] = a64.size();
+    o32[d] = a32.size();
+    a64.insert(a64.end(), r64.begin(), r64.end());
+    a32.insert(a32.end(), r32.begin(), r32.end());
+  }
+  const size_t b64 = a64.size() * sizeof(double);
+  API_CUDA(p->roots.ensure(b64 + a32.size() * sizeof(float)), "FFT roots alloc");
+  API_CUDA(cudaMemcpy(p->roots.p, a64.data(), b64, cudaMemcpyHostToDevice), "FFT roots upload");
+  API_CUDA(cudaMemcpy(static_cast<char*>(p->roots.p) + b64, a32.data(), a32.size() * sizeof(float),
+                      cudaMemcpyHostToDevice),
+           "FFT roots upload");
+  for (int d = 0; d < 3; ++d) {
+    p->geom.roots64[d] = p->roots.as<double>() + o64[d];
+    p->geom.roots32[d] = reinterpret_cast<float*>(static_cast<char*>(p->roots.p) + b64) + o32[d];
+  }
+  p->ok = true;
+  return LCP_OK;
+}
+
 lcp_status get_plans(lcp_ctx* ctx, const int32_t* ng, FftPlans** out) {
   auto key = std::make_tuple((int)ng[0], (int)ng[1], (int)ng[2]);
   auto it = ctx->plans.find(key);
   if (it == ctx->plans.end()) {
-    FftPlans p;
-    if (cufftPlan3d(&p.fwd, ng[0], ng[1], ng[2], CUFFT_D2Z) != CUFFT_SUCCESS ||
-        cufftPlan3d(&p.inv, ng[0], ng[1], ng[2], CUFFT_Z2D) != CUFFT_SUCCESS)
-      return fail(LCP_EDEVICE, "cuFFT plan creation failed");
-    p.ok = true;
-    it = ctx->plans.emplace(key, p).first;
+    it = ctx->plans.emplace(std::piecewise_construct, std::forward_as_tuple(key), std::forward_as_tuple()).first;
+    lcp_status s = make_fft_plan(ng, &it->second);
+    if (s) {
+      ctx->plans.erase(it);
+      return s;
+    }
   }
-  cufftSetStream(it->second.fwd, ctx->stream);
-  cufftSetStream(it->second.inv, ctx->stream);
   *out = &it->second;
   return LCP_OK;
 }
 
-// dvh = Poisson(real source already in `real`); spec is scratch.
+// dvh = Poisson(real source already in `real`), with the factors tabulated
+// into the context's workspace; spec is scratch.
 lcp_status poisson_device(lcp_ctx* ctx, FftPlans* pl, const int32_t* ng, const double* recvecs, double* real,
                           void* spec, double* dvh) {
-  if (cufftExecD2Z(pl->fwd, real, reinterpret_cast<cufftDoubleComplex*>(spec)) != CUFFT_SUCCESS)
-    return fail(LCP_EDEVICE, "cufftExecD2Z failed");
-  API_CUDA(lcp::launch_poisson_scale(ng, recvecs, spec, ctx->stream), "poisson_scale");
-  ctx->launches++;
-  if (cufftExecZ2D(pl->inv, reinterpret_cast<cufftDoubleComplex*>(spec), dvh) != CUFFT_SUCCESS)
-    return fail(LCP_EDEVICE, "cufftExecZ2D failed");
+  const int64_t nspec = (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1);
+  API_CUDA(ctx->w_pfac.ensure(nspec * sizeof(double)), "alloc");
+  API_CUDA(lcp::launch_poisson_table(ng, recvecs, ctx->w_pfac.as<double>(), ctx->stream), "poisson table");
+  lcp::GridCell c{};
+  for (int d = 0; d < 3; ++d) c.ng[d] = ng[d];
+  c.nn = (int64_t)ng[0] * ng[1] * ng[2];
+  c.real = real;
+  c.spec = spec;
+  c.pfac = ctx->w_pfac.as<double>();
+  c.dvh = dvh;
+  API_CUDA(lcp::launch_poisson_fft(pl->geom, ctx->precision == LCP_PREC_FP64, -1, c, nullptr, 1, ctx->stream),
+           "poisson fft");
+  ctx->launches += 6;
   return LCP_OK;
 }
 
@@ -1426,18 +1462,12 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
     if ((s = xc_pass(gx, ctx->aux))) return s;
     API_CUDA(cudaEventRecord(ctx->ev_join, ctx->aux), "join");
   }
-  // 2. Poisson
-  API_CUDA(lcp::launch_poisson_prep_g(job->spinpol, gc, one, st), "poisson_prep");
+  // 2. Poisson: the hand-written FFT solve, the source formed in its first pass
   FftPlans* plans = nullptr;  // the executing context's plans (any context may run the job)
   if ((s = get_plans(ctx, u.ngrid, &plans))) return s;
-  if (cufftExecD2Z(plans->fwd, job->real.as<double>(), reinterpret_cast<cufftDoubleComplex*>(job->spec.p)) !=
-      CUFFT_SUCCESS)
-    return fail(LCP_EDEVICE, "cufftExecD2Z failed");
-  API_CUDA(lcp::launch_poisson_scale_g(gc, one, st), "poisson_scale");
-  if (cufftExecZ2D(plans->inv, reinterpret_cast<cufftDoubleComplex*>(job->spec.p), job->dvh.as<double>()) !=
-      CUFFT_SUCCESS)
-    return fail(LCP_EDEVICE, "cufftExecZ2D failed");
-  ctx->launches += 2;
+  API_CUDA(lcp::launch_poisson_fft(plans->geom, ctx->precision == LCP_PREC_FP64, job->spinpol, gc, nullptr, 1, st),
+           "poisson fft");
+  ctx->launches += 5;
   mark(2);
   // 3. xc + potential, with the FP64 energy tile partials
   if (overlap) {

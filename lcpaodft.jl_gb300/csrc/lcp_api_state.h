@@ -4,7 +4,6 @@
 #pragma once
 
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include <atomic>
 #include <map>
@@ -82,8 +81,10 @@ struct lcp_ucell {
   lcp::UCell u;
 };
 
+// The hand-written FFT's plan of one grid shape: radices and roots of unity.
 struct FftPlans {
-  cufftHandle fwd = 0, inv = 0;
+  lcp::FftGeom geom{};
+  DBuf roots;
   bool ok = false;
 };
 
@@ -96,7 +97,7 @@ struct lcp_ctx {
   std::map<std::tuple<int, int, int>, FftPlans> plans;
   // workspaces of the host-buffer entry points
   DBuf w_in[4], w_out[4], w_aux[4], w_real, w_spec, w_part, w_scal, w_a, w_b;
-  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale;
+  DBuf w_dsym, w_status, w_hscratch, w_dscale, w_dtmp, w_vw, w_vscale, w_pfac;
   // second stream of the step: the xc pass runs there beside the FFT Poisson solve
   cudaStream_t aux = nullptr;
   // device address of the no-allocation density's fixed scratch array, looked
@@ -108,10 +109,6 @@ struct lcp_ctx {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (aux) cudaStreamDestroy(aux);
-    for (auto& kv : plans) {
-      if (kv.second.fwd) cufftDestroy(kv.second.fwd);
-      if (kv.second.inv) cufftDestroy(kv.second.inv);
-    }
     if (own) cudaStreamDestroy(own);
   }
 };
@@ -161,6 +158,7 @@ struct lcp_job {
 
 // helpers of lcp_api.cu used by the other orchestration files
 lcp_status get_plans(lcp_ctx* ctx, const int32_t* ng, FftPlans** out);
+lcp_status make_fft_plan(const int32_t* ng, FftPlans* p);
 lcp_status check_ctx(lcp_ctx* ctx);
 lcp_status check_pair(const lcp_ucell* ucell, const lcp_orbs* orbs);
 lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o);

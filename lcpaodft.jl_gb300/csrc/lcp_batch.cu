@@ -6,8 +6,9 @@
 //     blocks) of every cell.  The tensor-core kernels are persistent, with one
 //     CTA per SM walking a brick list that mixes the cells, heaviest bricks
 //     first;
-//   - Poisson runs batched cuFFT plans, one per grid shape, over contiguous
-//     per-shape buffers;
+//   - Poisson runs the hand-written FFT solve once per grid shape over all of
+//     that shape's cells (one block row per cell), in double-float with the
+//     FP64 scaling, over contiguous per-shape buffers;
 //   - the pointwise grid kernels and the FP64 reductions run over tiles of
 //     every cell.  Their partition per cell is the one of a single-cell step,
 //     so a cell's energy sums are the same bits as when its job steps alone.
@@ -21,7 +22,6 @@
 // Everything a step touches is allocated at creation; results land in the
 // jobs' own buffers (density, potential, H, energies).
 #include <cuda_runtime.h>
-#include <cufft.h>
 
 #include <algorithm>
 #include <map>
@@ -38,8 +38,9 @@ struct ShapeGroup {
   int32_t ng[3];
   std::vector<int> cells;  // batch cell indices, in order
   int64_t nn = 0, nspec = 0;
-  cufftHandle fwd = 0, inv = 0;
-  DBuf real, spec;  // count * nn doubles, count * nspec complex
+  FftPlans plan;      // radices and roots of unity of the shape
+  DBuf real, spec;    // count * nn doubles, count * nspec complex
+  DBuf fft_cells;     // the shape's cells (GridCell), in slot order
 };
 
 int64_t spec_len(const int32_t* ng) { return (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1); }
@@ -59,7 +60,6 @@ struct lcp_batch {
   int32_t spinpol = LCP_SPIN_OFF, xc = LCP_XC_LDA, nspin = 1, ncells = 0;
   std::vector<lcp_job*> jobs;
   std::vector<std::unique_ptr<ShapeGroup>> groups;
-  DBuf fft_work;
   // device tables (per spin channel where the pointers differ)
   DBuf tc_cells[2], brick_cell, brick_local;
   std::vector<Wave> waves;
@@ -78,10 +78,6 @@ struct lcp_batch {
     cudaSetDevice(device);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    for (auto& g : groups) {
-      if (g->fwd) cufftDestroy(g->fwd);
-      if (g->inv) cufftDestroy(g->inv);
-    }
   }
 };
 
@@ -134,17 +130,10 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
   }
   // 2. Poisson: sources, forward transforms per shape, 4 pi / G^2, inverse
   mark(1);
-  API_CUDA(lcp::launch_poisson_prep_g(b->spinpol, gnone, pts, st), "batch poisson prep");
   for (auto& g : b->groups)
-    if (cufftSetStream(g->fwd, st) != CUFFT_SUCCESS || cufftSetStream(g->inv, st) != CUFFT_SUCCESS)
-      return fail(LCP_EDEVICE, "cufftSetStream failed");
-  for (auto& g : b->groups)
-    if (cufftExecD2Z(g->fwd, g->real.as<double>(), g->spec.as<cufftDoubleComplex>()) != CUFFT_SUCCESS)
-      return fail(LCP_EDEVICE, "cufftExecD2Z (batched) failed");
-  API_CUDA(lcp::launch_poisson_scale_g(gnone, sps, st), "batch poisson scale");
-  for (auto& g : b->groups)
-    if (cufftExecZ2D(g->inv, g->spec.as<cufftDoubleComplex>(), g->real.as<double>()) != CUFFT_SUCCESS)
-      return fail(LCP_EDEVICE, "cufftExecZ2D (batched) failed");
+    API_CUDA(lcp::launch_poisson_fft(g->plan.geom, false, b->spinpol, gnone, g->fft_cells.as<lcp::GridCell>(),
+                                     (int)g->cells.size(), st),
+             "batch poisson");
   // 3./4. xc + potential + energy partials, then the per-cell sums
   mark(2);
   if (b->xc == LCP_XC_GGA_PBE)
@@ -232,30 +221,13 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
     cell_slot[k] = (int)g.cells.size();
     g.cells.push_back(k);
   }
-  // batched plans sharing one work area (the groups run one after another)
-  size_t work = 0;
+  // FFT plans and the per-shape source and spectrum buffers
   for (auto& gp : b->groups) {
     ShapeGroup& g = *gp;
-    long long n[3] = {g.ng[0], g.ng[1], g.ng[2]};
-    const long long cnt = (long long)g.cells.size();
-    size_t w1 = 0, w2 = 0;
-    if (cufftCreate(&g.fwd) != CUFFT_SUCCESS || cufftCreate(&g.inv) != CUFFT_SUCCESS)
-      return fail(LCP_EDEVICE, "cufftCreate failed");
-    cufftSetAutoAllocation(g.fwd, 0);
-    cufftSetAutoAllocation(g.inv, 0);
-    if (cufftMakePlanMany64(g.fwd, 3, n, nullptr, 1, g.nn, nullptr, 1, g.nspec, CUFFT_D2Z, cnt, &w1) !=
-            CUFFT_SUCCESS ||
-        cufftMakePlanMany64(g.inv, 3, n, nullptr, 1, g.nspec, nullptr, 1, g.nn, CUFFT_Z2D, cnt, &w2) !=
-            CUFFT_SUCCESS)
-      return fail(LCP_EDEVICE, "batched cuFFT plan creation failed");
-    work = std::max(work, std::max(w1, w2));
-    API_CUDA(g.real.ensure((size_t)cnt * g.nn * sizeof(double)), "batch grid alloc");
-    API_CUDA(g.spec.ensure((size_t)cnt * g.nspec * 2 * sizeof(double)), "batch spectrum alloc");
-  }
-  API_CUDA(b->fft_work.ensure(std::max<size_t>(work, 16)), "cuFFT work area");
-  for (auto& g : b->groups) {
-    cufftSetWorkArea(g->fwd, b->fft_work.p);
-    cufftSetWorkArea(g->inv, b->fft_work.p);
+    if ((s = make_fft_plan(g.ng, &g.plan))) return s;
+    const size_t cnt = g.cells.size();
+    API_CUDA(g.real.ensure(cnt * g.nn * sizeof(double)), "batch grid alloc");
+    API_CUDA(g.spec.ensure(cnt * g.nspec * 2 * sizeof(double)), "batch spectrum alloc");
   }
 
   // per-cell sizes and workspace offsets
@@ -381,6 +353,11 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
     gcs[k] = c;
   }
   API_CUDA(upload_pod(b->grid_cells, gcs), "upload");
+  for (auto& gp : b->groups) {
+    std::vector<lcp::GridCell> gc;
+    for (int k : gp->cells) gc.push_back(gcs[k]);
+    API_CUDA(upload_pod(gp->fft_cells, gc), "upload");
+  }
   for (int ch = 0; ch < ns; ++ch) {
     std::vector<lcp::TcCell> tcs(nc);
     std::vector<lcp::DsymCell> dcs(nc);
@@ -441,9 +418,10 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
   API_CUDA(upload_pod(b->sp_start, sp_off), "upload");
   API_CUDA(upload_pod(b->h_start, h_off), "upload");
   // our kernels per step: per channel absmax + pow2 + dsym + density, per
-  // channel and wave vweight + H + reduce; once prep, scale, xc, sums, dot,
-  // dot-finish (GGA-PBE: xc is two passes)
-  b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 6 + (b->xc == LCP_XC_GGA_PBE ? 1 : 0);
+  // channel and wave vweight + H + reduce; the five FFT passes per grid
+  // shape; once xc, sums, dot, dot-finish (GGA-PBE: xc is two passes)
+  b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 4 + 5 * (int64_t)b->groups.size() +
+                        (b->xc == LCP_XC_GGA_PBE ? 1 : 0);
   API_CUDA(cudaDeviceSynchronize(), "batch create");
   *out = b.release();
   return LCP_OK;
@@ -549,9 +527,9 @@ lcp_status lcp_batch_info(const lcp_batch* b, int64_t* out8) {
   out8[2] = b->nbricks;
   out8[3] = b->kernels_per_step;
   int64_t bytes = 0;
-  for (const DBuf* d : {&b->fft_work, &b->dsym, &b->vw, &b->vscale, &b->hscratch})
+  for (const DBuf* d : {&b->dsym, &b->vw, &b->vscale, &b->hscratch})
     bytes += (int64_t)d->bytes;
-  for (auto& g : b->groups) bytes += (int64_t)(g->real.bytes + g->spec.bytes);
+  for (auto& g : b->groups) bytes += (int64_t)(g->real.bytes + g->spec.bytes + g->plan.roots.bytes);
   out8[4] = bytes;
   out8[5] = b->exec ? 1 : 0;
   out8[6] = b->nsb;

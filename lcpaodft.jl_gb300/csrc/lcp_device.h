@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <algorithm>
+#include <vector>
 
 #include "lcpgrid.h"
 
@@ -145,6 +146,26 @@ struct GridBatch {
   const int64_t* start;
   int64_t nblocks;
 };
+// Hand-written FFT Poisson solve (lcp_fft.cu): per cell, dvh = the solve of
+// its source (2rho - 2rho_a "off", rho_up + rho_down - 2rho_a otherwise, or
+// with spinpol < 0 the cell's real array as is), through its half-spectrum
+// scratch spec and its factors pfac.  One cell by value (cells == nullptr) or
+// ncells cells of one grid shape from a device table.  fp64: FP64
+// transforms, else double-float transforms with the FP64 scaling.
+constexpr int kFftMaxN = 1024;       // longest supported grid dimension
+constexpr int kFftMaxFactors = 24;
+struct FftGeom {
+  int32_t n[3];
+  int32_t nfac[3];
+  int32_t fac[3][kFftMaxFactors];
+  const void* roots64[3];  // per axis: its n roots of unity, complex double
+  const void* roots32[3];  // the same as double-float: re.hi, re.lo, im.hi, im.lo
+};
+int fft_factor(int n, int* fac);
+bool fft_supported(const int32_t* ng);
+void fft_roots(int n, std::vector<double>& r64, std::vector<float>& r32);
+cudaError_t launch_poisson_fft(const FftGeom& g, bool fp64, int spinpol, const GridCell& c0, const GridCell* cells,
+                               int ncells, cudaStream_t st);
 cudaError_t launch_poisson_prep_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
 cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaStream_t st);
 // The Poisson factors of a grid (ng0 * ng1 * (ng2/2+1) doubles), for GridCell::pfac.

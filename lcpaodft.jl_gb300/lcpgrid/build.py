@@ -78,7 +78,7 @@ def build(verbose=False, force=False):
         objs.append(obj)
     cuda_lib = os.path.join(_cuda_root(nvcc), "lib64")
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-L", cuda_lib, "-lcufft", "-lcudart",
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-L", cuda_lib, "-lcudart",
            "-Xlinker", "-rpath=" + cuda_lib]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
