@@ -323,21 +323,27 @@ lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major,
 /* ---------------------------------------------------------------- serving */
 
 /* Serving engine for SCF grid-step requests on many device-resident
- * structures (the spec serving form; the reference has no serving
- * layer).  `nslots` execution slots, each a context of its own (stream and
- * workspaces) at `precision`, run requests concurrently; a worker thread
- * admits pending requests in arrival order as slots and their structures free
- * up.  Structures are admitted by device footprint against `budget_bytes`. */
+ * structures (the serving form; the reference has no serving layer).
+ * `nslots` execution slots, each a context of its own (stream and
+ * workspaces) at `precision` with a worker thread, take pending requests in
+ * arrival order as they and their structures free up; at LCP_PREC_BF16X3 a
+ * slot runs the requests it takes (up to lcp_server_set_max_batch) as one
+ * batched grid step, and the slots' steps overlap on the device.  Structures
+ * are admitted by device footprint against `budget_bytes`. */
 typedef struct lcp_server lcp_server;
 lcp_status lcp_server_create(int32_t device, int32_t nslots, int32_t precision, int64_t budget_bytes,
                              lcp_server** out);
 /* Waits for the requests in flight, then frees the server (not the jobs). */
 void lcp_server_destroy(lcp_server* srv);
-/* Admits a job (a structure with its orbital tables and step buffers, created
- * by the caller, who keeps ownership) if its footprint fits the free budget,
- * else LCP_ENOMEM.  nspin / hsize: channels and Total_Hsize of its D. */
+/* Adds a job (a structure with its orbital tables and step buffers, created
+ * by the caller, who keeps ownership): admitted now if its footprint (with
+ * the precision's tables) fits the free budget, else queued for admission
+ * with its requests until removals free the budget (lcp_server_state);
+ * LCP_ENOMEM only when it exceeds the whole budget.  nspin / hsize: channels
+ * and Total_Hsize of its D. */
 lcp_status lcp_server_add(lcp_server* srv, lcp_job* job, int32_t nspin, int64_t hsize, int32_t* id);
-/* Releases a structure's budget (LCP_ESTATE while it has requests queued). */
+/* Releases a structure's budget (LCP_ESTATE while it has requests queued)
+ * and admits queued structures that now fit, in order. */
 lcp_status lcp_server_remove(lcp_server* srv, int32_t id);
 /* Queues one grid step of structure `id` with density matrices dm[nspin]
  * (copied; the caller's buffers are free on return). */
@@ -348,6 +354,19 @@ lcp_status lcp_server_poll(lcp_server* srv, int32_t max, int32_t wait_ms, uint64
                            double* latency_ms, int32_t* n);
 /* out4 = submitted, completed, resident bytes, budget. */
 lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4);
+/* The serving form's own controls; no counterpart in the reference.
+ * lcp_server_state: 0 admitted, 1 waiting in the admission queue (the
+ * structure did not fit the free budget when added; removals admit queued
+ * structures in order), 2 being admitted. */
+lcp_status lcp_server_state(lcp_server* srv, int32_t id, int32_t* state);
+/* Requests per batched step: each slot takes up to max_batch pending requests
+ * of idle admitted structures with one SpinPol and xc and runs them as one
+ * batched grid step (split-BF16 servers only; default 16 at LCP_PREC_BF16X3,
+ * 1 otherwise: LCP_ENOTSUP for more than 1 at another precision). */
+lcp_status lcp_server_set_max_batch(lcp_server* srv, int32_t max_batch);
+/* out3 = batched steps run (more than one request), requests they carried,
+ * structures waiting for admission. */
+lcp_status lcp_server_batch_stats(lcp_server* srv, int64_t* out3);
 
 /* ---------------------------------------------------------------- brick tiling of the split-BF16 path */
 

@@ -1568,6 +1568,30 @@ lcp_status lcp_job_footprint(const lcp_job* job, int64_t* bytes) {
   return LCP_OK;
 }
 
+}  // extern "C"
+
+// Device bytes the job will hold once its tables for `precision` exist: its
+// footprint now plus, when not built yet, the split-BF16 brick tables (from
+// the host brick geometry) or the FP32 orbital copy.
+int64_t job_footprint_estimate(lcp_job* job, int32_t precision) {
+  int64_t fp = 0;
+  if (lcp_job_footprint(job, &fp) != LCP_OK) return -1;
+  const lcp_orbs* o = job->orbs;
+  if (precision == LCP_PREC_BF16X3 && !o->bricks_ready) {
+    lcp::Bricks b;
+    if (!lcp::build_bricks(o->ucell->u, b, o->brick_shape[0] > 0 ? o->brick_shape : nullptr).empty()) return -1;
+    fp += b.nblocks * 6144 * 2 + (int64_t)b.point_code.size() * 4 + (int64_t)b.tab_pair.size() * 8 +
+          (int64_t)(b.img_off.size() + b.slot_base.size() + b.red_off.size() + b.red_slot.size()) * 8 +
+          (int64_t)(b.img_block.size() + b.sub_pair.size() + b.sub_chunks.size() + b.sb_fold.size() +
+                    b.sb_chunks.size()) * 4;
+  } else if (precision == LCP_PREC_FP32 && !o->phi32.p) {
+    fp += o->table_elems * 4;
+  }
+  return fp;
+}
+
+extern "C" {
+
 lcp_status lcp_job_prepare(lcp_ctx* ctx, lcp_job* job) {
   lcp_status s = check_ctx(ctx);
   if (s) return s;

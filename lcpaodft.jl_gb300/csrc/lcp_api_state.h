@@ -168,3 +168,11 @@ lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const d
 lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const double* const* vpot,
                               double* const* hks, int64_t hsize);
 lcp::GridCell job_grid_cell(lcp_job* job);
+
+int64_t job_footprint_estimate(lcp_job* job, int32_t precision);
+
+// batches re-assembled over changing sets of jobs (lcp_batch.cu), for the serving engine
+lcp_batch* batch_new(int device);
+lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes);
+lcp_status batch_record(lcp_batch* b, cudaStream_t st);
+lcp_status batch_status(lcp_batch* b, cudaStream_t st);

@@ -38,9 +38,9 @@ struct ShapeGroup {
   int32_t ng[3];
   std::vector<int> cells;  // batch cell indices, in order
   int64_t nn = 0, nspec = 0;
-  FftPlans plan;      // radices and roots of unity of the shape
-  DBuf real, spec;    // count * nn doubles, count * nspec complex
-  DBuf fft_cells;     // the shape's cells (GridCell), in slot order
+  FftPlans* plan = nullptr;            // radices and roots of unity (the batch's plan cache)
+  int64_t real_off = 0, spec_off = 0;  // its count * nn source doubles and count * nspec complex, in grid_pool
+  int64_t cells_off = 0;               // its cells (GridCell) in fft_cells, in slot order
 };
 
 int64_t spec_len(const int32_t* ng) { return (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1); }
@@ -59,7 +59,9 @@ struct lcp_batch {
   int device = 0;
   int32_t spinpol = LCP_SPIN_OFF, xc = LCP_XC_LDA, nspin = 1, ncells = 0;
   std::vector<lcp_job*> jobs;
-  std::vector<std::unique_ptr<ShapeGroup>> groups;
+  std::vector<ShapeGroup> groups;
+  std::map<std::tuple<int, int, int>, std::unique_ptr<FftPlans>> plan_cache;
+  DBuf grid_pool, fft_cells;
   // device tables (per spin channel where the pointers differ)
   DBuf tc_cells[2], brick_cell, brick_local;
   std::vector<Wave> waves;
@@ -130,9 +132,9 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
   }
   // 2. Poisson: sources, forward transforms per shape, 4 pi / G^2, inverse
   mark(1);
-  for (auto& g : b->groups)
-    API_CUDA(lcp::launch_poisson_fft(g->plan.geom, false, b->spinpol, gnone, g->fft_cells.as<lcp::GridCell>(),
-                                     (int)g->cells.size(), st),
+  for (const ShapeGroup& g : b->groups)
+    API_CUDA(lcp::launch_poisson_fft(g.plan->geom, false, b->spinpol, gnone,
+                                     b->fft_cells.as<lcp::GridCell>() + g.cells_off, (int)g.cells.size(), st),
              "batch poisson");
   // 3./4. xc + potential + energy partials, then the per-cell sums
   mark(2);
@@ -168,19 +170,21 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
 
 }  // namespace
 
-extern "C" {
-
-lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes,
-                            lcp_batch** out) {
-  lcp_status s = check_ctx(ctx);
-  if (s) return s;
-  if (!jobs || !out || njobs <= 0 || scratch_bytes < 0)
-    return fail(LCP_EINVAL, "lcp_batch_create: NULL argument, no jobs or a negative budget");
-  *out = nullptr;
-  if (ctx->precision != LCP_PREC_BF16X3)
-    return fail(LCP_ENOTSUP, "the batched step runs the split-BF16 contractions (precision bf16x3)");
-  std::unique_ptr<lcp_batch> b(new lcp_batch());
-  b->device = ctx->device;
+// Fills batch b (new or used before) for these jobs: validation, shape groups,
+// brick lists, waves and every device table.  Device buffers only grow, and
+// FFT plans are kept per grid shape, so re-assembling a batch over another
+// set of jobs of at most the same sizes allocates nothing.  The tables are
+// uploaded with synchronous copies; the jobs' split-BF16 tables are built on
+// ctx's stream when missing.
+lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes) {
+  lcp_status s = LCP_OK;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->jobs.clear();
+  b->groups.clear();
+  b->waves.clear();
   b->ncells = njobs;
   for (int k = 0; k < njobs; ++k) {
     lcp_job* j = jobs[k];
@@ -210,24 +214,37 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
     auto it = gidx.find(key);
     if (it == gidx.end()) {
       it = gidx.emplace(key, (int)b->groups.size()).first;
-      std::unique_ptr<ShapeGroup> g(new ShapeGroup());
-      for (int d = 0; d < 3; ++d) g->ng[d] = ng[d];
-      g->nn = (int64_t)ng[0] * ng[1] * ng[2];
-      g->nspec = spec_len(ng);
-      b->groups.push_back(std::move(g));
+      ShapeGroup g;
+      for (int d = 0; d < 3; ++d) g.ng[d] = ng[d];
+      g.nn = (int64_t)ng[0] * ng[1] * ng[2];
+      g.nspec = spec_len(ng);
+      auto pc = b->plan_cache.find(key);
+      if (pc == b->plan_cache.end()) {
+        std::unique_ptr<FftPlans> p(new FftPlans());
+        if ((s = make_fft_plan(ng, p.get()))) return s;
+        pc = b->plan_cache.emplace(key, std::move(p)).first;
+      }
+      g.plan = pc->second.get();
+      b->groups.push_back(g);
     }
-    ShapeGroup& g = *b->groups[it->second];
+    ShapeGroup& g = b->groups[it->second];
     cell_group[k] = it->second;
     cell_slot[k] = (int)g.cells.size();
     g.cells.push_back(k);
   }
-  // FFT plans and the per-shape source and spectrum buffers
-  for (auto& gp : b->groups) {
-    ShapeGroup& g = *gp;
-    if ((s = make_fft_plan(g.ng, &g.plan))) return s;
-    const size_t cnt = g.cells.size();
-    API_CUDA(g.real.ensure(cnt * g.nn * sizeof(double)), "batch grid alloc");
-    API_CUDA(g.spec.ensure(cnt * g.nspec * 2 * sizeof(double)), "batch spectrum alloc");
+  // the per-shape source and spectrum buffers, carved from one pool
+  {
+    int64_t off = 0, coff = 0;
+    for (ShapeGroup& g : b->groups) {
+      const int64_t cnt = (int64_t)g.cells.size();
+      g.real_off = off;
+      off += cnt * g.nn;
+      g.spec_off = off;
+      off += cnt * g.nspec * 2;
+      g.cells_off = coff;
+      coff += cnt;
+    }
+    API_CUDA(b->grid_pool.ensure((size_t)std::max<int64_t>(off, 1) * sizeof(double)), "batch grid alloc");
   }
 
   // per-cell sizes and workspace offsets
@@ -281,7 +298,7 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
     API_CUDA(b->hscratch.ensure((size_t)std::max<int64_t>(most, 1) * 256 * sizeof(float)), "batch H scratch");
   }
   API_CUDA(b->status.ensure(sizeof(int)), "alloc");
-  API_CUDA(cudaMemset(b->status.p, 0, sizeof(int)), "memset");
+  API_CUDA(cudaMemsetAsync(b->status.p, 0, sizeof(int), ctx->stream), "memset");
 
   // brick list: every cell's bricks, heaviest first (the persistent CTAs take
   // bricks k, k + grid, ... so a descending order balances them); the order
@@ -345,18 +362,19 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
   std::vector<lcp::GridCell> gcs(nc);
   for (int k = 0; k < nc; ++k) {
     lcp_job* j = b->jobs[k];
-    ShapeGroup& g = *b->groups[cell_group[k]];
+    const ShapeGroup& g = b->groups[cell_group[k]];
     lcp::GridCell c = job_grid_cell(j);
-    c.real = g.real.as<double>() + (int64_t)cell_slot[k] * g.nn;
-    c.spec = g.spec.as<double>() + (int64_t)cell_slot[k] * g.nspec * 2;
+    c.real = b->grid_pool.as<double>() + g.real_off + (int64_t)cell_slot[k] * g.nn;
+    c.spec = b->grid_pool.as<double>() + g.spec_off + (int64_t)cell_slot[k] * g.nspec * 2;
     c.dvh = c.real;  // the inverse transform writes back over the source
     gcs[k] = c;
   }
   API_CUDA(upload_pod(b->grid_cells, gcs), "upload");
-  for (auto& gp : b->groups) {
-    std::vector<lcp::GridCell> gc;
-    for (int k : gp->cells) gc.push_back(gcs[k]);
-    API_CUDA(upload_pod(gp->fft_cells, gc), "upload");
+  {
+    std::vector<lcp::GridCell> fc;
+    for (const ShapeGroup& g : b->groups)
+      for (int k : g.cells) fc.push_back(gcs[k]);
+    API_CUDA(upload_pod(b->fft_cells, fc), "upload");
   }
   for (int ch = 0; ch < ns; ++ch) {
     std::vector<lcp::TcCell> tcs(nc);
@@ -422,6 +440,45 @@ lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, i
   // shape; once xc, sums, dot, dot-finish (GGA-PBE: xc is two passes)
   b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 4 + 5 * (int64_t)b->groups.size() +
                         (b->xc == LCP_XC_GGA_PBE ? 1 : 0);
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "batch tables");
+  return LCP_OK;
+}
+
+lcp_batch* batch_new(int device) {
+  lcp_batch* b = new lcp_batch();
+  b->device = device;
+  return b;
+}
+
+// Records one eager step of an assembled batch on `st` (no graph).
+lcp_status batch_record(lcp_batch* b, cudaStream_t st) { return record_step(b, st); }
+
+// The device status word of the batch's tensor-core kernels (for a caller
+// that synchronises the stream itself); clears it.
+lcp_status batch_status(lcp_batch* b, cudaStream_t st) {
+  int v = 0;
+  API_CUDA(cudaMemcpyAsync(&v, b->status.p, sizeof(int), cudaMemcpyDeviceToHost, st), "status");
+  API_CUDA(cudaStreamSynchronize(st), "status");
+  if (v) {
+    cudaMemsetAsync(b->status.p, 0, sizeof(int), st);
+    return fail(v, "a device wait timed out (batched tensor-core step)");
+  }
+  return LCP_OK;
+}
+
+extern "C" {
+
+lcp_status lcp_batch_create(lcp_ctx* ctx, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes,
+                            lcp_batch** out) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!jobs || !out || njobs <= 0 || scratch_bytes < 0)
+    return fail(LCP_EINVAL, "lcp_batch_create: NULL argument, no jobs or a negative budget");
+  *out = nullptr;
+  if (ctx->precision != LCP_PREC_BF16X3)
+    return fail(LCP_ENOTSUP, "the batched step runs the split-BF16 contractions (precision bf16x3)");
+  std::unique_ptr<lcp_batch> b(batch_new(ctx->device));
+  if ((s = batch_assemble(ctx, b.get(), njobs, jobs, scratch_bytes))) return s;
   API_CUDA(cudaDeviceSynchronize(), "batch create");
   *out = b.release();
   return LCP_OK;
@@ -529,7 +586,8 @@ lcp_status lcp_batch_info(const lcp_batch* b, int64_t* out8) {
   int64_t bytes = 0;
   for (const DBuf* d : {&b->dsym, &b->vw, &b->vscale, &b->hscratch})
     bytes += (int64_t)d->bytes;
-  for (auto& g : b->groups) bytes += (int64_t)(g->real.bytes + g->spec.bytes + g->plan.roots.bytes);
+  bytes += (int64_t)b->grid_pool.bytes;
+  for (const auto& kv : b->plan_cache) bytes += (int64_t)kv.second->roots.bytes;
   out8[4] = bytes;
   out8[5] = b->exec ? 1 : 0;
   out8[6] = b->nsb;

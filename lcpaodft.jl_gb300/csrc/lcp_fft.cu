@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "lcp_device.h"
@@ -218,7 +219,7 @@ __device__ __forceinline__ const GridCell& fft_cell(const FftArgs& a) { return a
 
 template <class T>
 __device__ __forceinline__ const Cx<T>* roots_of(const FftGeom& g, int axis) {
-  return reinterpret_cast<const Cx<T>*>(sizeof(T) == 8 ? g.roots64[axis] : g.roots32[axis]);
+  return reinterpret_cast<const Cx<T>*>(std::is_same<T, double>::value ? g.roots64[axis] : g.roots32[axis]);
 }
 
 // Copies the pencil length's roots into shared memory.
@@ -408,7 +409,7 @@ cudaError_t launch_fft_t(const FftGeom& g, const FftArgs& args, int ncells, cuda
 // sevens and any larger primes.
 int fft_factor(int n, int* fac) {
   int k = 0;
-  while (n % 4 == 0 && n > 4 && k < kFftMaxFactors) {
+  while (n % 4 == 0 && k < kFftMaxFactors) {
     fac[k++] = 4;
     n /= 4;
   }

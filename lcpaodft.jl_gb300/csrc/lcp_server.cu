@@ -1,14 +1,24 @@
 // Serving engine: SCF grid-step requests for many structures, each with its
 // orbital tables and step buffers resident on the device (an lcp_job).
 //
-// Structures are admitted by HBM footprint against a budget.  Requests carry
-// a new density matrix.  Each of `nslots` execution slots -- a context of its
-// own (stream and workspaces) with a worker thread -- takes the oldest pending
-// request whose structure is idle, so requests on different slots run
-// concurrently on the device, kernel launches are issued from several host
-// threads, and new requests start while others are still in flight.  Latency
-// is measured from submission to the moment the slot's worker sees the result
-// (its completion event).
+// Admission: a structure's device footprint (with the tables its precision
+// needs) is charged against a byte budget.  A structure that does not fit
+// the free budget waits in an admission queue, with its requests, until
+// removals free enough of the budget (first come, first admitted); only a
+// structure larger than the whole budget is refused.
+//
+// Continuous batching: each of `nslots` execution slots -- a context of its
+// own (stream and workspaces) with a worker thread -- repeatedly takes the
+// pending requests of idle admitted structures, oldest first, up to
+// `max_batch` of them with one SpinPol and xc, and runs them as ONE batched
+// grid step (lcp_batch re-assembled over those jobs: one persistent
+// tensor-core launch per contraction over the bricks of every request's
+// cell, one FFT solve per grid shape, tiled grid kernels over all cells).
+// Requests that arrive while a batch is on the GPU join the next batch of a
+// free slot, and the slots' batches overlap on the device.  A batch of one
+// (or a server at FP64 / FP32, or "nc" structures) runs the single-job step.
+// Latency is measured from submission to the moment the worker sees the
+// result on the host.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -22,7 +32,7 @@
 #include <thread>
 #include <vector>
 
-#include "lcp_internal.h"
+#include "lcp_api_state.h"
 
 namespace {
 
@@ -42,27 +52,29 @@ struct Request {
   lcp_status status = LCP_OK;
 };
 
+enum { kAdmitted = 0, kWaiting = 1, kAdmitting = 2 };
+
 struct Structure {
   lcp_job* job = nullptr;
   int nspin = 1;
   int64_t hsize = 0;
-  int64_t footprint = 0;
+  int64_t footprint = 0;  // charged against the budget (an estimate while not admitted)
+  int state = kAdmitted;
   bool busy = false;
   int64_t queued = 0;          // requests submitted and not yet completed
   std::vector<double*> free_dm;  // pinned staging buffers
 };
 
-lcp_status fail(lcp_status code, const std::string& msg) {
-  lcp::set_error(msg);
-  return code;
-}
-
 }  // namespace
 
 struct lcp_server {
   int device = 0;
+  int32_t precision = LCP_PREC_BF16X3;
+  int32_t max_batch = 1;  // requests per batched step
   int64_t budget = 0, resident = 0;
   std::vector<lcp_ctx*> slots;
+  std::vector<lcp_batch*> runners;  // per slot, re-assembled for every batch
+  std::deque<int32_t> waiting;      // structures in the admission queue, in order
   lcp_ctx* admin = nullptr;  // prepares structures' tables at admission (caller's thread)
   std::vector<cudaStream_t> streams;
   std::map<int32_t, Structure> structs;
@@ -76,7 +88,7 @@ struct lcp_server {
   std::condition_variable cv_work, cv_done;
   bool stop = false;
   std::vector<std::thread> workers;
-  int64_t submitted = 0, completed = 0;
+  int64_t submitted = 0, completed = 0, batches = 0, batched_requests = 0;
   lcp_status sticky = LCP_OK;
   std::string sticky_msg;
 
@@ -91,54 +103,149 @@ struct lcp_server {
     r->status = s;
   }
 
-  // One worker per slot: take the oldest pending request whose structure is
-  // idle, run it on this slot, wait for it, publish the result.
+  // Whether request r can join `batch` (same SpinPol and xc; the batched
+  // step takes split-BF16 "off"/"on" jobs).
+  bool joins(const std::vector<Request*>& batch, const Request* r) const {
+    if (batch.empty()) return true;
+    if (max_batch < 2 || precision != LCP_PREC_BF16X3) return false;
+    const lcp_job* a = batch.front()->job;
+    const lcp_job* b = r->job;
+    return a->spinpol != LCP_SPIN_NC && b->spinpol == a->spinpol && b->xc == a->xc;
+  }
+
+  void finish(Request* r) {  // under mu
+    Structure& st = structs[r->id];
+    st.busy = false;
+    st.queued--;
+    st.free_dm.push_back(r->dm);
+    r->dm = nullptr;
+    if (r->status != LCP_OK && sticky == LCP_OK) {
+      sticky = r->status;
+      sticky_msg = lcp_last_error() ? lcp_last_error() : "request failed";
+    }
+    done.push_back(r);
+    completed++;
+  }
+
+  // The requests of one batched step on this slot: D in, the step, the
+  // energies out, one wait.
+  lcp_status run_batch(int slot, std::vector<Request*>& batch) {
+    lcp_ctx* ctx = slots[slot];
+    cudaStream_t st = streams[slot];
+    if (!runners[slot]) runners[slot] = batch_new(device);
+    std::vector<lcp_job*> jobs;
+    for (Request* r : batch) jobs.push_back(r->job);
+    lcp_status s = batch_assemble(ctx, runners[slot], (int32_t)jobs.size(), jobs.data(), 0);
+    for (size_t k = 0; k < batch.size() && s == LCP_OK; ++k) {
+      Request* r = batch[k];
+      for (int c = 0; c < r->nspin && s == LCP_OK; ++c)
+        if (cudaMemcpyAsync(r->job->dm[c].p, r->dm + (size_t)c * r->hsize, r->hsize * sizeof(double),
+                            cudaMemcpyHostToDevice, st) != cudaSuccess)
+          s = LCP_EDEVICE;
+    }
+    if (s == LCP_OK) s = batch_record(runners[slot], st);
+    for (size_t k = 0; k < batch.size() && s == LCP_OK; ++k)
+      s = lcp_job_energies_async(ctx, batch[k]->job, batch[k]->energies);
+    if (s == LCP_OK) s = batch_status(runners[slot], st);  // waits for the stream
+    return s;
+  }
+
+  // One worker per slot: take the pending requests of idle admitted
+  // structures (oldest first, up to max_batch that batch together), run
+  // them on this slot, wait, publish the results.
   void run(int slot) {
     cudaSetDevice(device);
     while (true) {
-      Request* r = nullptr;
+      std::vector<Request*> batch;
       {
         std::unique_lock<std::mutex> lk(mu);
         while (true) {
-          for (auto it = pending.begin(); it != pending.end(); ++it) {
+          for (auto it = pending.begin(); it != pending.end() && (int)batch.size() < std::max(1, max_batch);) {
             Structure& st = structs[(*it)->id];
-            if (!st.busy) {
+            if (!st.busy && st.state == kAdmitted && joins(batch, *it)) {
               st.busy = true;
-              r = *it;
-              pending.erase(it);
-              break;
+              batch.push_back(*it);
+              it = pending.erase(it);
+            } else {
+              ++it;
             }
           }
-          if (r || (stop && pending.empty())) break;
+          if (!batch.empty() || stop) break;
           cv_work.wait_for(lk, std::chrono::milliseconds(5));
         }
+        if (batch.size() > 1) {
+          batches++;
+          batched_requests += (int64_t)batch.size();
+        }
       }
-      if (!r) break;
-      r->slot = slot;
-      launch(r);
-      if (r->status == LCP_OK) {
-        const cudaError_t e = cudaEventSynchronize(r->done);
-        if (e != cudaSuccess) r->status = LCP_EDEVICE;
+      if (batch.empty()) break;  // stopping, nothing runnable
+      if (batch.size() == 1) {
+        Request* r = batch.front();
+        r->slot = slot;
+        launch(r);
+        if (r->status == LCP_OK) {
+          const cudaError_t e = cudaEventSynchronize(r->done);
+          if (e != cudaSuccess) r->status = LCP_EDEVICE;
+        }
+        if (r->status == LCP_OK) r->status = lcp_ctx_check_status(slots[slot]);
+      } else {
+        const lcp_status s = run_batch(slot, batch);
+        for (Request* r : batch) {
+          r->slot = slot;
+          r->status = s;
+        }
       }
-      if (r->status == LCP_OK) r->status = lcp_ctx_check_status(slots[slot]);
-      r->t_done = Clock::now();
+      const Clock::time_point now = Clock::now();
       {
         std::lock_guard<std::mutex> lk(mu);
-        Structure& st = structs[r->id];
-        st.busy = false;
-        st.queued--;
-        st.free_dm.push_back(r->dm);
-        r->dm = nullptr;
-        if (r->status != LCP_OK && sticky == LCP_OK) {
-          sticky = r->status;
-          sticky_msg = lcp_last_error() ? lcp_last_error() : "request failed";
+        for (Request* r : batch) {
+          r->t_done = now;
+          finish(r);
         }
-        done.push_back(r);
-        completed++;
       }
       cv_done.notify_all();
-      cv_work.notify_all();  // this structure may have more requests waiting
+      cv_work.notify_all();  // these structures may have more requests waiting
     }
+  }
+
+  // Admits queued structures, in order, while they fit the free budget: their
+  // precision's tables are built on the admission context (caller's thread).
+  lcp_status admit_waiting() {
+    std::vector<int32_t> ids;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      while (!waiting.empty()) {
+        Structure& st = structs[waiting.front()];
+        if (resident + st.footprint > budget) break;
+        resident += st.footprint;
+        st.state = kAdmitting;
+        ids.push_back(waiting.front());
+        waiting.pop_front();
+      }
+    }
+    lcp_status first = LCP_OK;
+    for (int32_t id : ids) {
+      lcp_job* job = nullptr;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        job = structs[id].job;
+      }
+      lcp_status s = lcp_job_prepare(admin, job);
+      int64_t fp = 0;
+      if (s == LCP_OK) s = lcp_job_footprint(job, &fp);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        Structure& st = structs[id];
+        if (s == LCP_OK) {
+          resident += fp - st.footprint;
+          st.footprint = fp;
+        }
+        st.state = kAdmitted;  // a failure shows up in the structure's requests
+      }
+      if (s != LCP_OK && first == LCP_OK) first = s;
+    }
+    if (!ids.empty()) cv_work.notify_all();
+    return first;
   }
 };
 
@@ -153,12 +260,15 @@ lcp_status lcp_server_create(int32_t device, int32_t nslots, int32_t precision, 
   std::unique_ptr<lcp_server> s(new lcp_server());
   s->device = device;
   s->budget = budget_bytes;
+  s->precision = precision;
+  s->max_batch = precision == LCP_PREC_BF16X3 ? 16 : 1;
   if (cudaSetDevice(device) != cudaSuccess) return fail(LCP_EDEVICE, "cudaSetDevice failed");
   for (int k = 0; k < nslots; ++k) {
     lcp_ctx* c = nullptr;
     lcp_status st = lcp_ctx_create(device, &c);
     if (st) return st;
     s->slots.push_back(c);
+    s->runners.push_back(nullptr);
     cudaStream_t stream;
     if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
       return fail(LCP_EDEVICE, "cudaStreamCreate failed");
@@ -196,6 +306,12 @@ void lcp_server_destroy(lcp_server* srv) {
     delete r;
   }
   for (auto e : srv->free_events) cudaEventDestroy(e);
+  for (auto* r : srv->pending) {  // requests of structures that never ran (the admission queue)
+    if (r->done) cudaEventDestroy(r->done);
+    if (r->dm) cudaFreeHost(r->dm);
+    delete r;
+  }
+  for (auto* b : srv->runners) lcp_batch_destroy(b);
   for (auto& kv : srv->structs)
     for (double* p : kv.second.free_dm) cudaFreeHost(p);
   if (srv->energy_arena) cudaFreeHost(srv->energy_arena);
@@ -208,35 +324,84 @@ void lcp_server_destroy(lcp_server* srv) {
 lcp_status lcp_server_add(lcp_server* srv, lcp_job* job, int32_t nspin, int64_t hsize, int32_t* id) {
   if (!srv || !job || !id) return fail(LCP_EINVAL, "NULL argument");
   if (nspin < 1 || nspin > 4 || hsize < 0) return fail(LCP_EINVAL, "bad nspin / hsize");
-  // the precision's tables are built now, so that the footprint is complete
+  const int64_t est = job_footprint_estimate(job, srv->precision);
+  if (est < 0) return fail(LCP_EINVAL, "the structure's footprint cannot be estimated (bricks)");
+  if (est > srv->budget)
+    return fail(LCP_ENOMEM, "admission: the structure needs " + std::to_string(est) +
+                                " device bytes, more than the whole budget of " + std::to_string(srv->budget));
+  bool now = false;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    Structure st;
+    st.job = job;
+    st.nspin = nspin;
+    st.hsize = hsize;
+    st.footprint = est;
+    now = srv->waiting.empty() && srv->resident + est <= srv->budget;
+    st.state = now ? kAdmitting : kWaiting;
+    *id = srv->next_id++;
+    if (now) srv->resident += est;
+    else srv->waiting.push_back(*id);
+    srv->structs.emplace(*id, std::move(st));
+  }
+  if (!now) return LCP_OK;  // admitted when removals free the budget
+  // the precision's tables are built now, and the footprint measured
   lcp_status s = lcp_job_prepare(srv->admin, job);
-  if (s) return s;
   int64_t fp = 0;
-  if ((s = lcp_job_footprint(job, &fp))) return s;
+  if (s == LCP_OK) s = lcp_job_footprint(job, &fp);
   std::lock_guard<std::mutex> lk(srv->mu);
-  if (srv->resident + fp > srv->budget)
-    return fail(LCP_ENOMEM, "admission: the structure needs " + std::to_string(fp) + " device bytes; " +
-                                std::to_string(srv->budget - srv->resident) + " of the budget are free");
-  Structure st;
-  st.job = job;
-  st.nspin = nspin;
-  st.hsize = hsize;
+  Structure& st = srv->structs[*id];
+  if (s != LCP_OK) {
+    srv->resident -= st.footprint;
+    srv->structs.erase(*id);
+    return s;
+  }
+  srv->resident += fp - st.footprint;
   st.footprint = fp;
-  *id = srv->next_id++;
-  srv->structs.emplace(*id, std::move(st));
-  srv->resident += fp;
+  st.state = kAdmitted;
   return LCP_OK;
 }
 
 lcp_status lcp_server_remove(lcp_server* srv, int32_t id) {
   if (!srv) return fail(LCP_EINVAL, "NULL server");
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->structs.find(id);
+    if (it == srv->structs.end()) return fail(LCP_EINVAL, "unknown structure id");
+    if (it->second.queued > 0) return fail(LCP_ESTATE, "the structure has requests in flight");
+    if (it->second.state == kAdmitting) return fail(LCP_ESTATE, "the structure is being admitted");
+    for (double* p : it->second.free_dm) cudaFreeHost(p);
+    if (it->second.state == kWaiting) {
+      for (auto w = srv->waiting.begin(); w != srv->waiting.end(); ++w)
+        if (*w == id) {
+          srv->waiting.erase(w);
+          break;
+        }
+    } else {
+      srv->resident -= it->second.footprint;
+    }
+    srv->structs.erase(it);
+  }
+  return srv->admit_waiting();
+}
+
+// 0: admitted, 1: waiting in the admission queue, 2: being admitted.
+lcp_status lcp_server_state(lcp_server* srv, int32_t id, int32_t* state) {
+  if (!srv || !state) return fail(LCP_EINVAL, "NULL argument");
   std::lock_guard<std::mutex> lk(srv->mu);
   auto it = srv->structs.find(id);
   if (it == srv->structs.end()) return fail(LCP_EINVAL, "unknown structure id");
-  if (it->second.queued > 0) return fail(LCP_ESTATE, "the structure has requests in flight");
-  for (double* p : it->second.free_dm) cudaFreeHost(p);
-  srv->resident -= it->second.footprint;
-  srv->structs.erase(it);
+  *state = it->second.state;
+  return LCP_OK;
+}
+
+lcp_status lcp_server_set_max_batch(lcp_server* srv, int32_t max_batch) {
+  if (!srv) return fail(LCP_EINVAL, "NULL server");
+  if (max_batch < 1 || max_batch > 4096) return fail(LCP_EINVAL, "max_batch must be in 1..4096");
+  if (max_batch > 1 && srv->precision != LCP_PREC_BF16X3)
+    return fail(LCP_ENOTSUP, "batched serving steps run the split-BF16 contractions (precision bf16x3)");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->max_batch = max_batch;
   return LCP_OK;
 }
 
@@ -322,6 +487,15 @@ lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4) {
   out4[1] = srv->completed;
   out4[2] = srv->resident;
   out4[3] = srv->budget;
+  return LCP_OK;
+}
+
+lcp_status lcp_server_batch_stats(lcp_server* srv, int64_t* out3) {
+  if (!srv || !out3) return fail(LCP_EINVAL, "NULL argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  out3[0] = srv->batches;
+  out3[1] = srv->batched_requests;
+  out3[2] = (int64_t)srv->waiting.size();
   return LCP_OK;
 }
 

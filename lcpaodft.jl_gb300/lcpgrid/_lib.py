@@ -115,6 +115,9 @@ _SIGS = {
     "lcp_server_submit": ([_vp, _i32, _ppd, ctypes.c_uint64], _i32),
     "lcp_server_poll": ([_vp, _i32, _i32, ctypes.POINTER(ctypes.c_uint64), _pd, _pd, ctypes.POINTER(_i32)], _i32),
     "lcp_server_stats": ([_vp, ctypes.POINTER(_i64)], _i32),
+    "lcp_server_state": ([_vp, _i32, ctypes.POINTER(_i32)], _i32),
+    "lcp_server_set_max_batch": ([_vp, _i32], _i32),
+    "lcp_server_batch_stats": ([_vp, ctypes.POINTER(_i64)], _i32),
     "lcp_calc_force3": ([_vp, _vp, _vp, _i32, _ppd, _ppd, _pd], _i32),
     "lcp_brick_shape_candidates": ([_vp, _i32, ctypes.POINTER(_i32), _pd, ctypes.POINTER(_i32)], _i32),
     "lcp_orbs_set_brick_shape": ([_vp, _vp, ctypes.POINTER(_i32)], _i32),

@@ -769,19 +769,45 @@ class Batch:
 
 class Server:
     """Serving engine for SCF grid-step requests on device-resident structures
-    (lcp_server_*): `nslots` concurrent execution slots at one precision,
-    structures admitted by device footprint against `budget_bytes`."""
+    (lcp_server_*): `nslots` execution slots at one precision, each stepping
+    the pending requests it takes as one batched step (split-BF16: up to
+    `max_batch` requests per step, 16 by default; FP64/FP32: one), structures
+    admitted by device footprint against `budget_bytes`, with an admission
+    queue for those that do not fit yet."""
 
-    def __init__(self, device=0, nslots=4, precision="bf16x3", budget_bytes=160e9):
+    ADMITTED, WAITING, ADMITTING = 0, 1, 2
+
+    def __init__(self, device=0, nslots=4, precision="bf16x3", budget_bytes=160e9, max_batch=None):
         h = ctypes.c_void_p()
         check(lib.lcp_server_create(int(device), int(nslots), _lib.PREC[precision], int(budget_bytes),
                                     ctypes.byref(h)))
         self._h = h
         self._jobs = {}
+        if max_batch is not None:
+            self.set_max_batch(max_batch)
+
+    def set_max_batch(self, n):
+        """Requests per batched step (1: every request steps alone)."""
+        check(lib.lcp_server_set_max_batch(self._h, int(n)))
+
+    def state(self, sid):
+        """Server.ADMITTED, WAITING (admission queue) or ADMITTING."""
+        out = ctypes.c_int32()
+        check(lib.lcp_server_state(self._h, int(sid), ctypes.byref(out)))
+        return out.value
+
+    def batch_stats(self):
+        """(batched steps run, requests they carried, structures waiting for admission)."""
+        out = (ctypes.c_int64 * 3)()
+        check(lib.lcp_server_batch_stats(self._h, out))
+        return tuple(int(x) for x in out)
 
     def add(self, job):
-        """Admits a GridStepJob (kept alive by the server object); returns its id.
-        Raises LCPError (LCP_ENOMEM) when its footprint exceeds the free budget."""
+        """Adds a GridStepJob (kept alive by the server object); returns its id.
+        It is admitted now when its footprint fits the free budget, else it
+        waits in the admission queue (its requests wait with it) until
+        removals free the budget.  Raises LCPError (LCP_ENOMEM) only when the
+        footprint exceeds the whole budget."""
         i = ctypes.c_int32()
         check(lib.lcp_server_add(self._h, job._h, job.nspin, job.ucell.Total_Hsize, ctypes.byref(i)))
         self._jobs[i.value] = job

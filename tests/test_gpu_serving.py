@@ -1,6 +1,7 @@
-"""Serving engine (lcp_server_*): concurrent grid-step requests on several
-device-resident structures.  Each result must be the same alone and in a
-mixed stream, and structures are admitted by device footprint."""
+"""Serving engine (lcp_server_*): grid-step requests on several
+device-resident structures, batched per slot and concurrent across slots.
+Each result must be the same alone and in a mixed, batched stream, and
+structures are admitted by device footprint, queued while they do not fit."""
 import numpy as np
 import pytest
 
@@ -73,6 +74,38 @@ def test_server_results_alone_and_mixed():
     srv.close()
 
 
+def test_server_batches_requests():
+    """With one slot and requests already queued, the slot steps them as
+    batches of several structures; every result equals the request alone."""
+    ctx = L.Context(0)
+    jobs = _structures(ctx)
+    srv = L.Server(0, nslots=1, precision="bf16x3", budget_bytes=64e9, max_batch=1)
+    ids = [srv.add(job) for job, _ in jobs]
+    alone = {}
+    for sid, (job, dm) in zip(ids, jobs):
+        srv.submit(sid, dm, tag=sid)
+        got = []
+        while not got:
+            got = srv.poll(wait_ms=2000)
+        alone[sid] = got[0][1]
+    assert srv.batch_stats()[0] == 0
+    srv.set_max_batch(8)
+    order = [int(x) for x in np.repeat(ids, 4)]
+    for n, sid in enumerate(order):
+        srv.submit(sid, jobs[ids.index(sid)][1], tag=100 + n)
+    results = []
+    while len(results) < len(order):
+        results += srv.poll(wait_ms=2000)
+    nb, nreq, nwait = srv.batch_stats()
+    assert nb >= 1 and nreq >= 2 * nb and nwait == 0
+    for tag, e, lat in results:
+        np.testing.assert_allclose(e, alone[order[tag - 100]], rtol=1e-12, atol=0)
+    srv.close()
+    with pytest.raises(L.LCPError) as ex:
+        L.Server(0, nslots=1, precision="fp64", budget_bytes=1e9, max_batch=4)
+    assert ex.value.status == 5  # LCP_ENOTSUP: batched steps are split-BF16
+
+
 def test_server_admission_by_footprint():
     ctx = L.Context(0)
     jobs = _structures(ctx)
@@ -83,14 +116,23 @@ def test_server_admission_by_footprint():
     probe.close()
     fp = [job.footprint() for job, _ in jobs]
     assert min(fp) > 0
+    with pytest.raises(L.LCPError) as e:  # larger than the whole budget: refused
+        L.Server(0, nslots=1, precision="bf16x3", budget_bytes=fp[1] // 2).add(jobs[1][0])
+    assert e.value.status == 2  # LCP_ENOMEM
     srv = L.Server(0, nslots=2, precision="bf16x3", budget_bytes=fp[1] + fp[0] // 2)
     a = srv.add(jobs[0][0])
-    with pytest.raises(L.LCPError) as e:
-        srv.add(jobs[1][0])
-    assert e.value.status == 2  # LCP_ENOMEM
-    srv.remove(a)
-    b = srv.add(jobs[1][0])
-    srv.submit(b, jobs[1][1], tag=7)
+    b = srv.add(jobs[1][0])  # does not fit beside a: queued
+    assert srv.state(a) == L.Server.ADMITTED and srv.state(b) == L.Server.WAITING
+    assert srv.batch_stats()[2] == 1
+    srv.submit(b, jobs[1][1], tag=7)  # waits with its structure
+    srv.submit(a, jobs[0][1], tag=6)
+    got = []
+    while not got:
+        got = srv.poll(wait_ms=2000)
+    assert [g[0] for g in got] == [6]
+    assert srv.poll(wait_ms=300) == []  # b's request cannot run before b is admitted
+    srv.remove(a)  # frees the budget: b is admitted and its request runs
+    assert srv.state(b) == L.Server.ADMITTED
     got = []
     while not got:
         got = srv.poll(wait_ms=2000)
