@@ -447,6 +447,25 @@ lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, co
                                         int32_t spinpol, const double* const* dm_dev,
                                         double* const* density_grid_dev);
 
+/* For tests of the failure path only; no counterpart in the reference.
+ * poll_limit (0: the default of 2^24 polls) bounds every wait of the
+ * split-BF16 density kernel on this context; stall = 1 makes one of its
+ * epilogue warps withhold its stage releases, so the producers' waits run out
+ * and the kernel unwinds: it records LCP_ETIMEDOUT in the context's error
+ * word, stops every role, waits (bounded) for its copies and MMAs in flight,
+ * frees its tensor memory and returns, and the call returns LCP_ETIMEDOUT.
+ * Off (0, 0) by default; set it back to (0, 0) to run normally. */
+lcp_status lcp_ctx_set_fault_test(lcp_ctx* ctx, uint32_t poll_limit, int32_t stall);
+
+/* The check build (liblcpgrid_check.so, compiled with LCP_BOUNDS_CHECK) tests
+ * every index the pair and tensor-core kernels gather with (lens entries,
+ * sphere-list grid indices, DM/H block offsets, split-D pair indices, table
+ * blocks, partial-block slots, grid writes) and records the first violation
+ * instead of making the access: word = (site << 56) | (index + 1), 0 when
+ * none; read and cleared here after the context's stream completes.
+ * LCP_ENOTSUP in the normal build.  No counterpart in the reference. */
+lcp_status lcp_bounds_check_status(lcp_ctx* ctx, int64_t* word);
+
 /* Device allocations (cudaMalloc calls) the library has made since it was
  * loaded, over all contexts: a diagnostic for callers that must see none in
  * a call (lcp_set_density_grid_noalloc).  No counterpart in the reference. */

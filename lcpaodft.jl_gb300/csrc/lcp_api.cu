@@ -215,7 +215,7 @@ lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, co
              "dsym");
     API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale,
                                     ctx->w_dsym.as<__nv_bfloat16>(), ctx->w_dscale.as<double>(), (int)nsub, rho[c],
-                                    ctx->w_status.as<int>(), ctx->stream),
+                                    ctx->w_status.as<int>(), ctx->stream, ctx->fault_poll, ctx->fault_stall),
              "density_tc");
     ctx->launches += 4;
   }
@@ -693,6 +693,7 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
   pr.lens_off = o->p_lensoff.as<int64_t>();
   pr.g1 = o->p_g1.as<int32_t>();
   pr.g2 = o->p_g2.as<int32_t>();
+  pr.hsize = u.total_hsize;
   pr.nitems = (int64_t)ip.size();
   pr.item_pair = o->it_pair.as<int64_t>();
   pr.item_start = o->it_start.as<int64_t>();
@@ -1673,6 +1674,29 @@ lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops) {
   cudaEventDestroy(b);
   ctx->launches += 2;
   *tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (ms * 1e-3) / 1e12;
+  return LCP_OK;
+}
+
+lcp_status lcp_ctx_set_fault_test(lcp_ctx* ctx, uint32_t poll_limit, int32_t stall) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (stall < 0 || stall > 1) return fail(LCP_EINVAL, "stall is 0 or 1");
+  ctx->fault_poll = poll_limit;
+  ctx->fault_stall = stall;
+  return LCP_OK;
+}
+
+lcp_status lcp_bounds_check_status(lcp_ctx* ctx, int64_t* word) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!word) return fail(LCP_EINVAL, "NULL argument");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "bounds check");
+  unsigned long long a = 0, b = 0;
+  cudaError_t e = lcp::bounds_take_pairs(&a);
+  if (e == cudaErrorNotSupported) return fail(LCP_ENOTSUP, "this library was built without bounds checks");
+  API_CUDA(e, "bounds word");
+  API_CUDA(lcp::bounds_take_tc(&b), "bounds word");
+  *word = (int64_t)(a ? a : b);
   return LCP_OK;
 }
 

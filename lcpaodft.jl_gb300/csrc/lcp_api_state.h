@@ -103,6 +103,10 @@ struct lcp_ctx {
   // device address of the no-allocation density's fixed scratch array, looked
   // up by this context's first lcp_set_density_grid_noalloc call
   void* noalloc_scratch = nullptr;
+  // failure-path tests only (lcp_ctx_set_fault_test): the split-BF16 density
+  // kernel's poll limit (0: its default) and its stall switch
+  uint32_t fault_poll = 0;
+  int32_t fault_stall = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ~lcp_ctx() {
     cudaSetDevice(device);

@@ -59,6 +59,7 @@ struct DevPairs {
   const int64_t* lens_off;   // nu+1
   const int32_t* g1;         // index into atom's sphere list
   const int32_t* g2;         // index into jatom's sphere list
+  int64_t hsize;             // Total_Hsize (DM/H blocks), for the check build
   // chunked work items over the lens lists
   int64_t nitems;
   const int64_t* item_pair;  // folded pair of each item
@@ -72,6 +73,12 @@ cudaError_t launch_tabulate(const DevGeom& g, const DevSpecies* dspe, const doub
                             double* phi, double* dphi_x, double* dphi_y, double* dphi_z,
                             cudaStream_t st);
 cudaError_t launch_convert_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
+
+// The check build's first bounds violation of the pair kernels and of the
+// tensor-core kernels (0: none), read and cleared; cudaErrorNotSupported in
+// the normal build.
+cudaError_t bounds_take_pairs(unsigned long long* word);
+cudaError_t bounds_take_tc(unsigned long long* word);
 
 // exact-lens pair contractions
 cudaError_t launch_density_pairs(int prec, const DevGeom& g, const DevPairs& pr, int nspin,
@@ -274,7 +281,11 @@ struct RedCell {
 };
 cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const int64_t* start, const int64_t* order,
                                   int64_t total, cudaStream_t st);
-cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
+// poll: polls of every bounded wait before it gives up (0: 2^24); stall: for
+// failure-path tests only, 1 makes one epilogue warp withhold its stage
+// releases so that the kernel times out and unwinds.
+cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st,
+                                    uint32_t poll = 0, int32_t stall = 0);
 cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,
                                 cudaStream_t st);
@@ -286,7 +297,7 @@ cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* su
                         const double* dm, const double* scale, __nv_bfloat16* out, cudaStream_t st);
 cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
                               const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
-                              int* status, cudaStream_t st);
+                              int* status, cudaStream_t st, uint32_t poll = 0, int32_t stall = 0);
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int K, int a_mn, int b_mn,
                                int order, int* status, cudaStream_t st);
 // vw: nbricks * 128 float2 and vscale: nbricks floats of workspace (the

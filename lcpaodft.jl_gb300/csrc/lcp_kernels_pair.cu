@@ -15,6 +15,7 @@
 // items.  FP64 results reach the grids/blocks through FP64 atomics.
 #include <cuda_runtime.h>
 
+#include "lcp_bounds.cuh"
 #include "lcp_device.h"
 
 namespace lcp {
@@ -49,6 +50,9 @@ __global__ void __launch_bounds__(kPairThreads) density_pairs_kernel(DevGeom g, 
     const int noi = g.numorbs[i], noj = g.numorbs[j];
     const int64_t bp = pr.boff_p[q], bq = pr.boff_q[q];
     const bool self = pr.self[q] != 0;
+    // check build: the pair's D blocks lie inside DM (else they read as zero)
+    const bool okp = bounds_ok(bp + (int64_t)noi * noj - 1, pr.hsize, 1);
+    const bool okq = self || bounds_ok(bq + (int64_t)noi * noj - 1, pr.hsize, 2);
     __syncthreads();
     // the whole NOMAX x NOMAX tile is written (zeros outside NOi x NOj): the
     // contraction below reads every column, multiplying the padding by zero
@@ -57,8 +61,8 @@ __global__ void __launch_bounds__(kPairThreads) density_pairs_kernel(DevGeom g, 
       for (int s = 0; s < nspin; ++s) {
         double v = 0.0;
         if (a < noi && b < noj) {
-          v = dm.c[s][bp + (int64_t)a * noj + b];
-          if (!self) v += dm.c[s][bq + (int64_t)b * noi + a];
+          if (okp) v = dm.c[s][bp + (int64_t)a * noj + b];
+          if (!self && okq) v += dm.c[s][bq + (int64_t)b * noi + a];
         }
         Ds[s][a * NOMAX + b] = (T)v;
       }
@@ -69,9 +73,13 @@ __global__ void __launch_bounds__(kPairThreads) density_pairs_kernel(DevGeom g, 
     const T* phi_i = phi + g.phi_off[i];
     const T* phi_j = phi + g.phi_off[j];
     const int32_t* gl_i = g.glist + g.sph_off[i];
+    const int64_t gn_i = g.sph_off[i + 1] - g.sph_off[i], gn_j = g.sph_off[j + 1] - g.sph_off[j];
+    const int64_t nn = (int64_t)g.ngrid[0] * g.ngrid[1] * g.ngrid[2];
     for (int pt = threadIdx.x; pt < count; pt += blockDim.x) {
       const int64_t k = start + pt;
       const int g1 = pr.g1[k], g2 = pr.g2[k];
+      // check build: lens entries inside both spheres, the point inside the grid
+      if (!bounds_ok(g1, gn_i, 3) || !bounds_ok(g2, gn_j, 4) || !bounds_ok(gl_i[g1], nn, 5)) continue;
       T pi[NOMAX], pj[NOMAX];
 #pragma unroll
       for (int a = 0; a < NOMAX; ++a) pi[a] = a < noi ? ldg(phi_i + (int64_t)g1 * noi + a) : T(0);
@@ -129,12 +137,16 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
         if (pt < nt) {
           const int64_t k = start + t0 + pt;
           const int g1 = pr.g1[k], g2 = pr.g2[k];
-          if (a < noi) {
+          // check build: an entry outside its sphere or grid contributes nothing
+          const bool ok = bounds_ok(g1, g.sph_off[i + 1] - g.sph_off[i], 3) &&
+                          bounds_ok(g2, g.sph_off[j + 1] - g.sph_off[j], 4) &&
+                          bounds_ok(gl_i[g1], (int64_t)g.ngrid[0] * g.ngrid[1] * g.ngrid[2], 5);
+          if (ok && a < noi) {
             wi = ldg(phi_i + (int64_t)g1 * noi + a);
             const int gidx = gl_i[g1];
             for (int c = 0; c < nch; ++c) v[c] = ldg(vpot.c[c] + gidx);
           }
-          if (a < noj) wj = ldg(phi_j + (int64_t)g2 * noj + a);
+          if (ok && a < noj) wj = ldg(phi_j + (int64_t)g2 * noj + a);
         }
         for (int c = 0; c < nch; ++c) W[((size_t)c * kTile + pt) * NOMAX + a] = wi * (T)v[c];
         P[pt * NOMAX + a] = wj;
@@ -162,6 +174,9 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
     }
     const bool self = pr.self[q] != 0;
     const int64_t bp = pr.boff_p[q], bq = pr.boff_q[q];
+    // check build: the pair's H blocks lie inside H (else nothing is written)
+    const bool okp = bounds_ok(bp + (int64_t)noi * noj - 1, pr.hsize, 6);
+    const bool okq = self || bounds_ok(bq + (int64_t)noi * noj - 1, pr.hsize, 7);
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) {
       const int e = threadIdx.x + s * kPairThreads;
@@ -172,8 +187,8 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
           for (int c = 0; c < 4; ++c) {
             if (c < nch) {
               const double val = (double)acc[c][s] * g.gridvol;
-              atomicAdd(hks.c[c] + bp + (int64_t)a * noj + b, val);
-              if (!self) atomicAdd(hks.c[c] + bq + (int64_t)b * noi + a, val);
+              if (okp) atomicAdd(hks.c[c] + bp + (int64_t)a * noj + b, val);
+              if (!self && okq) atomicAdd(hks.c[c] + bq + (int64_t)b * noi + a, val);
             }
           }
         }
@@ -399,6 +414,15 @@ cudaError_t launch_hamiltonian_pairs(int prec, const DevGeom& g, const DevPairs&
   }
   if (max_no <= 16) return run_hamiltonian<double, 16>(g, pr, nch, phi64, vpot, hks, st);
   return run_hamiltonian<double, 32>(g, pr, nch, phi64, vpot, hks, st);
+}
+
+cudaError_t bounds_take_pairs(unsigned long long* word) {
+#ifdef LCP_BOUNDS_CHECK
+  return bounds_take(word);
+#else
+  *word = 0;
+  return cudaErrorNotSupported;
+#endif
 }
 
 }  // namespace lcp

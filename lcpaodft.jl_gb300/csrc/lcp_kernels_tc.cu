@@ -7,6 +7,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "lcp_bounds.cuh"
 #include "lcp_device.h"
 #include "lcp_tc.cuh"
 
@@ -431,6 +432,8 @@ struct TcDensArgs {
   TcCell cell0;          // the cell of a single-cell launch
   TcBatch batch;         // or the cells of a batch
   int* status;
+  uint32_t poll;         // polls of every bounded wait before it gives up
+  int32_t stall;         // failure-path tests only: 1 = epilogue warp 2 never releases its stages
 };
 
 // Cell and cell-local brick index of brick k of a launch.
@@ -529,15 +532,18 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
           const int t = m - 1 - k;
           const int stage = (int)(it % kDStages);
           const uint32_t use = it / kDStages;
-          if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[stage], (use - 1) & 1, &abort_flag)) {
+          if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[stage], (use - 1) & 1, &abort_flag, args.poll)) {
             give_up();
             break;
           }
           if (lane == 0) {
             uint8_t* sA = smem + stage * kDStageBytes;
             tc::mbar_arrive_expect_tx(&full_bar[stage], kDStageA);
+            // check build: a block outside the tables is replaced by block 0 (the
+            // copy keeps the stage's transaction count) and recorded
+            const int64_t blk = bounds_ok(i0 + t, cl.nblocks, 9) ? i0 + t : 0;
             for (int part = 0; part < 3; ++part)
-              tc::bulk_g2s(sA + part * 4096, cl.tab + ((int64_t)part * cl.nblocks + i0 + t) * kPart, 4096,
+              tc::bulk_g2s(sA + part * 4096, cl.tab + ((int64_t)part * cl.nblocks + blk) * kPart, 4096,
                            &full_bar[stage]);
           }
           __syncwarp();
@@ -547,7 +553,7 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
     // wait for the copies still in flight before the CTA's shared memory goes away
     for (int s = 0; s < kDStages; ++s) {
       const uint32_t uses = it / kDStages + ((uint32_t)s < it % kDStages ? 1u : 0u);
-      if (uses > 0 && !tc::mbar_wait(&full_bar[s], (uses - 1) & 1, 1u << 24)) give_up();
+      if (uses > 0 && !tc::mbar_wait(&full_bar[s], (uses - 1) & 1, args.poll)) give_up();
     }
   } else if (warp >= 6) {
     // ------------------------------------------------------------ D gatherers
@@ -571,7 +577,7 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
           const int nimg = min(t, c1 - 1) - c0 + 1;
           const int stage = (int)(it % kDStages);
           const uint32_t use = it / kDStages;
-          if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[stage], (use - 1) & 1, &abort_flag)) {
+          if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[stage], (use - 1) & 1, &abort_flag, args.poll)) {
             give_up();
             break;
           }
@@ -590,7 +596,8 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
             const int c = gw * 32 + lane + r * kDGatherWarps * 32;
             if (c < nimg * 96) {
               const int si = c / 96, w = c - si * 96, part = w >> 5, kh = (w >> 4) & 1, q = w & 15;
-              const int64_t pp = pr[r] < 0 ? cl.zero_pair : pr[r];
+              int64_t pp = pr[r] < 0 ? cl.zero_pair : pr[r];
+              if (!bounds_ok(pp, cl.zero_pair + 1, 8)) pp = cl.zero_pair;  // check build
               cp_async16(sB + part * (2 * kDBLbo) + kh * kDBLbo + si * 256 + q * 16,
                          dsym + pp * (kDsymElems * 2) + part * 512 + kh * 256 + q * 16);
             }
@@ -627,7 +634,7 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
       for (int c0 = 0; c0 < m && !abort_flag; c0 += kDWin, ++win) {
         const int c1 = min(c0 + kDWin, m);
         const uint32_t buf = win & 1, wuse = win >> 1;
-        if (wuse > 0 && !tc::mbar_wait_warp(&tempty_bar[buf], (wuse - 1) & 1, &abort_flag)) {
+        if (wuse > 0 && !tc::mbar_wait_warp(&tempty_bar[buf], (wuse - 1) & 1, &abort_flag, args.poll)) {
           give_up();
           break;
         }
@@ -637,7 +644,7 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
           const int t = m - 1 - k;
           const int nimg = min(t, c1 - 1) - c0 + 1;
           const int stage = (int)(it % kDStages);
-          if (!tc::mbar_wait_warp(&full_bar[stage], (it / kDStages) & 1, &abort_flag)) {
+          if (!tc::mbar_wait_warp(&full_bar[stage], (it / kDStages) & 1, &abort_flag, args.poll)) {
             give_up();
             break;
           }
@@ -680,13 +687,16 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
     // every MMA issued by the elected thread has finished before TMEM is released
     if (tc::elect_one()) {
       tc::mma_commit(&drain_bar);
-      if (!tc::mbar_wait(&drain_bar, 0, 1u << 24)) give_up();
+      if (!tc::mbar_wait(&drain_bar, 0, args.poll)) give_up();
     }
     __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
     const uint32_t quarter = warp & 3;  // TMEM lanes [32 * quarter, 32 * quarter + 32)
     const int p = (int)quarter * 32 + lane;
+    // failure-path tests: this warp withholds its releases, so the producers'
+    // bounded waits for those stages run out and every role unwinds
+    const bool withhold = args.stall == 1 && warp == 2;
     uint32_t it = 0, win = 0, mpar = 0;  // mpar: phase bit of mdone_bar per stage
     for (int64_t j = 0; j * gridDim.x < ntotal && !abort_flag; ++j) {
       const int64_t k = round_brick(j, ntotal);
@@ -702,7 +712,7 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
         it += (uint32_t)(m - c1);  // steps t >= c1 touch no final column
         for (int t = c1 - 1; t >= c0; --t, ++it) {
           const int stage = (int)(it % kDStages);
-          if (!tc::mbar_wait_abortable(&mdone_bar[stage], (mpar >> stage) & 1u, &abort_flag)) {
+          if (!tc::mbar_wait_abortable(&mdone_bar[stage], (mpar >> stage) & 1u, &abort_flag, args.poll)) {
             give_up();
             break;
           }
@@ -719,15 +729,16 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
           ff_add(acc_hi, acc_lo, d);
           tc::fence_before_sync();
           __syncwarp();
-          if (lane == 0) tc::mbar_arrive(&empty_bar[stage]);
+          if (lane == 0 && !withhold) tc::mbar_arrive(&empty_bar[stage]);
         }
         if (abort_flag) break;
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&tempty_bar[buf]);
+        if (lane == 0 && !withhold) tc::mbar_arrive(&tempty_bar[buf]);
       }
       if (abort_flag) break;
       const int64_t gi = p < cl.npts ? brick_point_index(hb, p, cl.bdim, cl.nb, cl.ngrid) : -1;
-      if (gi >= 0) cl.rho[gi] = ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * cl.dscale[0]);
+      if (gi >= 0 && bounds_ok(gi, (int64_t)cl.ngrid[0] * cl.ngrid[1] * cl.ngrid[2], 10))
+        cl.rho[gi] = ((double)acc_hi + (double)acc_lo) * (cl.phi_scale * cl.phi_scale * cl.dscale[0]);
     }
   }
   tc::fence_before_sync();
@@ -885,8 +896,10 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
         const int na = min(kHGroup, m - s0);
         if (lane == 0) {
           tc::mbar_arrive_expect_tx(&afull_bar, na * 3 * kImgBytes);
+          // check build: a group outside the tables is replaced by blocks 0.. (same bytes)
+          const int64_t blk = bounds_ok(i0 + s0 + na - 1, cl.nblocks, 11) ? i0 + s0 : 0;
           for (int part = 0; part < 3; ++part)
-            tc::bulk_g2s(sA + part * kHABytes, cl.tab + ((int64_t)part * cl.nblocks + i0 + s0) * kPart,
+            tc::bulk_g2s(sA + part * kHABytes, cl.tab + ((int64_t)part * cl.nblocks + blk) * kPart,
                          na * kImgBytes, &afull_bar);
         }
         __syncwarp();
@@ -1077,7 +1090,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
               tc::tmem_wait_ld();
 #pragma unroll
               for (int k = 0; k < 4; ++k) tc::tmem_regs_ready(y[k]);
-              if (slot[j] >= 0) {
+              if (slot[j] >= 0 && bounds_ok(sbase + slot[j], cl.slot_base[cl.nbricks], 12)) {
                 float o[16];
 #pragma unroll
                 for (int c = 0; c < 16; ++c)
@@ -1343,11 +1356,14 @@ static int tc_grid(const TcCell& cell0, const TcBatch& batch) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(n, sm_count()));
 }
 
-cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st) {
+cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st,
+                                    uint32_t poll, int32_t stall) {
   TcDensArgs a{};
   a.cell0 = cell0;
   a.batch = batch;
   a.status = status;
+  a.poll = poll ? poll : (1u << 24);
+  a.stall = stall;
   // 512 TMEM columns per CTA: the shared-memory ring (> half an SM) keeps one CTA per SM
   static_assert(kDSmem > 120 * 1024, "one CTA per SM");
   LCP_CUDA_TRY(cudaFuncSetAttribute(density_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDSmem));
@@ -1357,14 +1373,14 @@ cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, i
 
 cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
                               const __nv_bfloat16* dsym, const double* dscale, int zero_pair, double* rho,
-                              int* status, cudaStream_t st) {
+                              int* status, cudaStream_t st, uint32_t poll, int32_t stall) {
   TcCell c = tc_cell_of(bg, tab);
   c.phi_scale = phi_scale;
   c.dsym = dsym;
   c.zero_pair = zero_pair;
   c.dscale = dscale;
   c.rho = rho;
-  return launch_density_tc_batch(c, TcBatch{}, status, st);
+  return launch_density_tc_batch(c, TcBatch{}, status, st, poll, stall);
 }
 
 cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st) {
@@ -1406,6 +1422,15 @@ cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* 
   LCP_CUDA_TRY(cudaFuncSetAttribute(h_reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRedSmem));
   h_reduce_kernel<<<grid, 256, kRedSmem, st>>>(nsb, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H);
   return cudaGetLastError();
+}
+
+cudaError_t bounds_take_tc(unsigned long long* word) {
+#ifdef LCP_BOUNDS_CHECK
+  return bounds_take(word);
+#else
+  *word = 0;
+  return cudaErrorNotSupported;
+#endif
 }
 
 }  // namespace lcp

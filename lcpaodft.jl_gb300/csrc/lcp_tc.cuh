@@ -141,8 +141,9 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint64_t* mbar, uint32_t par
 
 // The abortable wait with one outcome for the whole warp (for warps that
 // then issue through elect.sync, which needs the converged warp).
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* mbar, uint32_t parity, const volatile int* abort) {
-  return __all_sync(0xffffffffu, mbar_wait_abortable(mbar, parity, abort)) != 0;
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* mbar, uint32_t parity, const volatile int* abort,
+                                               uint32_t max_iters = (1u << 24)) {
+  return __all_sync(0xffffffffu, mbar_wait_abortable(mbar, parity, abort, max_iters)) != 0;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {

@@ -10,7 +10,10 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "liblcpgrid.so")
+# LCPGRID_BOUNDS_CHECK=1 selects the check build (device bounds checks on every
+# gathered index, read with lcp_bounds_check_status)
+LIB_PATH = os.path.join(_HERE, "liblcpgrid_check.so" if os.environ.get("LCPGRID_BOUNDS_CHECK") == "1"
+                        else "liblcpgrid.so")
 
 LCP_OK, LCP_EINVAL, LCP_ENOMEM, LCP_EDEVICE, LCP_ETIMEDOUT, LCP_ENOTSUP, LCP_ESTATE = range(7)
 SPIN = {"off": 0, "on": 1, "nc": 2}
@@ -87,6 +90,8 @@ _SIGS = {
     "lcp_set_density_grid": ([_vp, _vp, _vp, _i32, _ppd, _ppd], _i32),
     "lcp_set_density_grid_noalloc": ([_vp, _vp, _vp, _i32, _ppd, _ppd], _i32),
     "lcp_device_alloc_count": ([ctypes.POINTER(_i64)], _i32),
+    "lcp_ctx_set_fault_test": ([_vp, ctypes.c_uint32, _i32], _i32),
+    "lcp_bounds_check_status": ([_vp, ctypes.POINTER(_i64)], _i32),
     "lcp_solve_poisson": ([_vp, _pi32, _pd, _i32, _ppd, _pd, _pd], _i32),
     "lcp_solve_poisson_xyz": ([_vp, _pi32, _pd, _pd, _pd], _i32),
     "lcp_set_xc_grid": ([_vp, _i32, _i32, _i64, _pd, _ppd, _ppd], _i32),

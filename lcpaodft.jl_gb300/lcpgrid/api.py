@@ -63,6 +63,13 @@ class Context:
                                   b.ctypes.data, d.ctypes.data))
         return d
 
+    def set_fault_test(self, poll_limit=0, stall=0):
+        """Failure-path tests only: poll limit of the split-BF16 density
+        kernel's bounded waits (0: default) and its stall switch (1: one
+        epilogue warp withholds its stage releases, so the kernel times out
+        and unwinds; the call raises LCPError LCP_ETIMEDOUT)."""
+        check(lib.lcp_ctx_set_fault_test(self._h, int(poll_limit), int(stall)))
+
     @property
     def launch_count(self):
         return int(lib.lcp_ctx_launch_count(self._h))
