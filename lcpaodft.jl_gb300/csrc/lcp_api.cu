@@ -563,6 +563,7 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
   // species tables
   std::vector<DevSpecies> sp(nspecies);
   std::vector<double> radial;
+  std::vector<int32_t> buckets;
   for (int k = 0; k < nspecies; ++k) {
     const lcp_pao& p = paos[k];
     if (p.max_l < 0 || p.max_l > 3) return fail(LCP_ENOTSUP, "not support PAO l > 3");
@@ -585,6 +586,7 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
     radial.insert(radial.end(), p.rv, p.rv + p.num_mesh);
     d.rwf_off = (int64_t)radial.size();
     radial.insert(radial.end(), p.rwf, p.rwf + (size_t)d.nrad * p.num_mesh);
+    lcp::append_spline_tables(p.rv, p.rwf, p.num_mesh, p.num_basis, p.max_l, d, radial, buckets);
     sp[k] = d;
   }
   std::vector<int32_t> spe0(u.natom);
@@ -616,6 +618,7 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
   API_CUDA(upload(o->numorbs, u.numorbs, st), "upload");
   API_CUDA(upload(o->species, sp, st), "upload");
   API_CUDA(upload(o->radial, radial, st), "upload");
+  API_CUDA(upload(o->buckets, buckets, st), "upload");
   DevGeom& g = o->geom;
   g.natom = u.natom;
   for (int d = 0; d < 3; ++d) {
@@ -705,18 +708,22 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
     for (int k = 0; k < 3; ++k) API_CUDA(o->dphi[k].ensure(o->table_elems * sizeof(double)), "dphi alloc");
   std::vector<int32_t> batom;
   std::vector<int64_t> bstart;
+  const int tab_chunk = o->grad ? 64 : lcp::kTabBlock;  // points per block of the gradient / value kernel
   for (int a = 0; a < u.natom; ++a)
-    for (int64_t k = u.sphere_off[a]; k < u.sphere_off[a + 1]; k += 64) {
+    for (int64_t k = u.sphere_off[a]; k < u.sphere_off[a + 1]; k += tab_chunk) {
       batom.push_back(a);
       bstart.push_back(k);
     }
+  int max_no_spe = 1;
+  for (const DevSpecies& d : sp) max_no_spe = std::max(max_no_spe, (int)d.no);
   DBuf d_batom, d_bstart;
   API_CUDA(upload(d_batom, batom, st), "upload");
   API_CUDA(upload(d_bstart, bstart, st), "upload");
-  API_CUDA(lcp::launch_tabulate(g, o->species.as<DevSpecies>(), o->radial.as<double>(), (int64_t)batom.size(),
-                                d_batom.as<int32_t>(), d_bstart.as<int64_t>(), o->phi.as<double>(),
-                                o->grad ? o->dphi[0].as<double>() : nullptr, o->grad ? o->dphi[1].as<double>() : nullptr,
-                                o->grad ? o->dphi[2].as<double>() : nullptr, st),
+  API_CUDA(lcp::launch_tabulate(g, o->species.as<DevSpecies>(), o->radial.as<double>(), o->buckets.as<int32_t>(),
+                                (int64_t)batom.size(), d_batom.as<int32_t>(), d_bstart.as<int64_t>(),
+                                o->phi.as<double>(), o->grad ? o->dphi[0].as<double>() : nullptr,
+                                o->grad ? o->dphi[1].as<double>() : nullptr,
+                                o->grad ? o->dphi[2].as<double>() : nullptr, max_no_spe, st),
            "tabulate kernel");
   ctx->launches++;
   API_CUDA(cudaStreamSynchronize(st), "tabulate");

@@ -126,7 +126,7 @@ struct lcp_orbs {
   lcp::DevPairs pairs{};
   // device arrays
   DBuf atv, gxyz, spe, sph_off, glist, clist, phi_off, numorbs;
-  DBuf species, radial;
+  DBuf species, radial, buckets;
   DBuf phi, dphi[3], phi32;
   DBuf p_atom, p_jatom, p_boffp, p_boffq, p_self, p_lensoff, p_g1, p_g2, it_pair, it_start, it_count;
   DBuf f_off, f_code;  // per atom, its work-item halves (item * 2 + orientation) for the force term

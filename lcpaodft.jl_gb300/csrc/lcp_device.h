@@ -20,6 +20,17 @@ namespace lcp {
 
 constexpr int kMaxL = 3;
 
+// Raises kernel's dynamic shared-memory limit on the current device to at
+// least `bytes` (never lowers it).  The limit is one attribute of the kernel
+// shared by every host thread that launches it, so a launcher whose size
+// varies between calls must not set it to its own size: another thread's
+// larger launch in between would fail.
+cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
+template <class F>
+cudaError_t raise_smem(F* kernel, size_t bytes) {
+  return raise_smem_limit(reinterpret_cast<const void*>(kernel), bytes);
+}
+
 // Radial tables of one species in device memory.
 struct DevSpecies {
   int32_t max_l;
@@ -29,7 +40,18 @@ struct DevSpecies {
   int32_t no;        // orbitals = sum_l nb[l]*(2l+1)
   int64_t rv_off;    // offset of RV in the packed radial array
   int64_t rwf_off;   // offset of RWF[(l,p)][mesh] in the packed radial array
+  // value tables' spline, precomputed per mesh interval (append_spline_tables):
+  int64_t iv_off;    // per interval m: RV[m-1], 1/(RV[m]-RV[m-1]), then per radial c0..c3
+  int64_t ex_off;    // per radial: a, b, c, d of the extrapolation below RV[0]
+  int64_t bk_off;    // bucket table (int32 array): first mesh index of each log2(R) bucket
+  float bk_lo, bk_inv;  // bucket of R: (log2(R) - bk_lo) * bk_inv
 };
+constexpr int kSplineBuckets = 4096;
+// Appends the per-interval cubic coefficients of the value tables'
+// radial spline, the extrapolation coefficients and the interval buckets of
+// one species (rv, rwf as lcp_pao) to `radial` / `buckets`; fills d's offsets.
+void append_spline_tables(const double* rv, const double* rwf, int nmesh, const int* num_basis, int max_l,
+                          DevSpecies& d, std::vector<double>& radial, std::vector<int32_t>& buckets);
 
 // Geometry the kernels read (device pointers).
 struct DevGeom {
@@ -68,9 +90,13 @@ struct DevPairs {
 };
 
 // tabulation
-cudaError_t launch_tabulate(const DevGeom& g, const DevSpecies* dspe, const double* radial,
+// nblocks blocks of kTabBlock sphere points (block_atom / block_start); phi
+// alone: the value kernel; with dphi_*: values and gradient tables.  max_no:
+// the largest orbital count of the species (shared-memory staging).
+constexpr int kTabBlock = 128;
+cudaError_t launch_tabulate(const DevGeom& g, const DevSpecies* dspe, const double* radial, const int32_t* buckets,
                             int64_t nblocks, const int32_t* block_atom, const int64_t* block_start,
-                            double* phi, double* dphi_x, double* dphi_y, double* dphi_z,
+                            double* phi, double* dphi_x, double* dphi_y, double* dphi_z, int max_no,
                             cudaStream_t st);
 cudaError_t launch_convert_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
 

@@ -28,7 +28,10 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "lcp_device.h"
@@ -382,8 +385,8 @@ cudaError_t launch_fft_t(const FftGeom& g, const FftArgs& args, int ncells, cuda
   const int64_t pairs = ((int64_t)n1 * n2 + 1) / 2;
   const dim3 rgrid((unsigned)((pairs + kRowWarps - 1) / kRowWarps), (unsigned)ncells);
   const size_t rsm = (size_t)n3 * 16 * (1 + 2 * kRowWarps);
-  LCP_CUDA_TRY(cudaFuncSetAttribute(fft_rows_fwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
-  LCP_CUDA_TRY(cudaFuncSetAttribute(fft_rows_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
+  LCP_CUDA_TRY(raise_smem(fft_rows_fwd_kernel<T>, rsm));
+  LCP_CUDA_TRY(raise_smem(fft_rows_inv_kernel<T>, rsm));
   fft_rows_fwd_kernel<T><<<rgrid, 32 * kRowWarps, rsm, st>>>(args);
   LCP_CUDA_TRY(cudaGetLastError());
   auto cols = [&](auto kern, int axis, bool with_pf) -> cudaError_t {
@@ -392,7 +395,7 @@ cudaError_t launch_fft_t(const FftGeom& g, const FftArgs& args, int ncells, cuda
     const int ntile = (h + W - 1) / W;
     const int outer = axis == 1 ? n1 : n2;
     const size_t sm = (size_t)n * 16 * (1 + 2 * W) + (with_pf ? (size_t)W * n * 8 : 0);
-    LCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    LCP_CUDA_TRY(raise_smem(kern, sm));
     kern<<<dim3((unsigned)(outer * ntile), (unsigned)ncells), 32 * W, sm, st>>>(args, axis, W);
     return cudaGetLastError();
   };
@@ -404,6 +407,19 @@ cudaError_t launch_fft_t(const FftGeom& g, const FftArgs& args, int ncells, cuda
 }
 
 }  // namespace
+
+cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> set;
+  int dev = 0;
+  LCP_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = set[std::make_pair(kernel, dev)];
+  if (bytes <= cur) return cudaSuccess;
+  LCP_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+  return cudaSuccess;
+}
 
 // Radices of a pencil length: fours first, then a two, then threes, fives,
 // sevens and any larger primes.

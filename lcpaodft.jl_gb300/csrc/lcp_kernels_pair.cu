@@ -351,8 +351,7 @@ cudaError_t run_force3(const DevGeom& g, const DevPairs& pr, int nch, const doub
     w.w[c] = coef[c];
   }
   const size_t smem = (size_t)2 * nch * NOMAX * NOMAX * sizeof(double);
-  LCP_CUDA_TRY(cudaFuncSetAttribute(force3_pairs_kernel<NOMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
+  LCP_CUDA_TRY(raise_smem(force3_pairs_kernel<NOMAX>, smem));
   force3_pairs_kernel<NOMAX><<<persistent_blocks(pr.nitems, 4), kPairThreads, smem, st>>>(
       g, pr, nch, phi, dphi[0], dphi[1], dphi[2], v, d, w, part);
   return cudaGetLastError();
