@@ -612,6 +612,30 @@ def run_ours(args):
                                 "DRAM at 29 % on the 8-atom cell")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
+    # tabulation and Poisson against the HBM roofline (algorithmic bytes:
+    # tables written + sphere indices read; FP64 tables read + three BF16
+    # parts written; 80 bytes per grid point per solve)
+    tab_ms, split_ms = orbs.timings()
+    gridn = np.asarray(u.GridN_Atom, dtype=np.float64)
+    elems = float(np.sum(gridn * np.asarray(wl["numorbs"], dtype=np.float64)))
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tab_bytes = elems * 8 + float(gridn.sum()) * 8
+    split_bytes = elems * (8 + 6)
+    pois_bytes = 80.0 * u.NN
+    gbs = lambda b, ms: b / (ms * 1e-3) / 1e9 if ms else None
+    tabulation = {"kernel_ms": tab_ms, "bytes": tab_bytes, "gbs": gbs(tab_bytes, tab_ms),
+                  "split_tables_ms": split_ms, "split_bytes": split_bytes, "split_gbs": gbs(split_bytes, split_ms),
+                  "peak_gbs": hbm, "peak_source": psrc + " hbm_gbs",
+                  "note": "FP64 tables written + sphere indices read (bytes); split-BF16 build: FP64 tables read and "
+                          "three BF16 parts written.  The FP64 tabulation is FP64-pipe bound (spline and Y_lm per "
+                          "point), not HBM bound"}
+    tabulation["frac"] = tabulation["gbs"] / hbm if tabulation["gbs"] else None
+    tabulation["split_frac"] = tabulation["split_gbs"] / hbm if tabulation["split_gbs"] else None
+    poisson = {"ms": float(stages[1]), "bytes": pois_bytes, "gbs": gbs(pois_bytes, float(stages[1])),
+               "peak_gbs": hbm, "transform": "fp64" if args.precision == "fp64" else "double-float (FP32 pipe), FP64 "
+               "scaling", "note": "80 bytes per grid point per solve; the 96^3 arrays stay in L2"}
+    poisson["frac"] = poisson["gbs"] / hbm if poisson["gbs"] else None
+
     ms_step = total_ms / args.steps
     line = {
         "metric": METRIC, "value": world * 1000.0 / ms_step, "unit": UNIT, "n_gpus": world,
@@ -630,6 +654,8 @@ def run_ours(args):
         "stage_ms": dict(zip(names, [float(x) for x in stages])),
         "setup_s": {"ucell_host": t_geom, "ucell_device": min(t_geom_dev), "tabulation": t_tab},
         "roofline": roof,
+        "tabulation": tabulation,
+        "poisson": poisson,
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(nspin * u.Total_Hsize * 8),
                 "d2h_bytes_per_step": int(nspin * u.Total_Hsize * 8 + 40), "ms_per_step": e2e_s * 1e3},
         "energy": {"E_grid": float(e_now[4]), "E_grid_fp64": float(e_fp64[4]),
@@ -771,6 +797,9 @@ def summary(line):
          "fp64": g(line, "fp64_dropin", "ms_per_step"), "fp32": g(line, "fp32_form", "ms_per_step"),
          "err_uHa_atom": g(line, "energy", "err_per_atom_uHa"), "max_dH": g(line, "energy", "max_abs_dH"),
          "max_drho": g(line, "energy", "max_abs_drho"), "roof_frac": g(line, "roofline", "frac"),
+         "tab_ms": g(line, "tabulation", "kernel_ms"), "tab_frac": g(line, "tabulation", "frac"),
+         "split_tab_ms": g(line, "tabulation", "split_tables_ms"), "split_tab_frac": g(line, "tabulation", "split_frac"),
+         "poisson_ms": g(line, "poisson", "ms"), "poisson_frac": g(line, "poisson", "frac"),
          "cpu_full_step": g(line, "cpu_baseline", "ms_per_step"), "cpu_cores": g(line, "cpu_baseline", "cores"),
          "cpu_vs_gpu_fp64_dE_uHa": g(line, "cpu_baseline", "vs_gpu_fp64", "dE_per_atom_uHa"),
          "cpu_vs_gpu_fp64_drho": g(line, "cpu_baseline", "vs_gpu_fp64", "max_abs_drho"),

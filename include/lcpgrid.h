@@ -447,6 +447,11 @@ lcp_status lcp_set_density_grid_noalloc(lcp_ctx* ctx, const lcp_ucell* ucell, co
                                         int32_t spinpol, const double* const* dm_dev,
                                         double* const* density_grid_dev);
 
+/* Device times (ms, CUDA events) of the orbitals' last tabulation kernel and
+ * of their split-BF16 table build (0 until built).  No counterpart in the
+ * reference (its TimerOutputs timers time the whole functions). */
+lcp_status lcp_orbs_timings(const lcp_orbs* orbs, double* out2);
+
 /* For tests of the failure path only; no counterpart in the reference.
  * poll_limit (0: the default of 2^24 polls) bounds every wait of the
  * split-BF16 density kernel on this context; stall = 1 makes one of its

@@ -149,13 +149,33 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   API_CUDA(o->b_tab.ensure((size_t)std::max<int64_t>(b.nblocks, 1) * 6144 * 2), "brick table alloc");
   API_CUDA(o->b_scale.ensure(2 * sizeof(double)), "alloc");
   API_CUDA(o->b_tmp.ensure(sizeof(unsigned long long)), "alloc");
+  cudaEvent_t te[2];
+  API_CUDA(cudaEventCreate(&te[0]), "event");
+  API_CUDA(cudaEventCreate(&te[1]), "event");
+  API_CUDA(cudaEventRecord(te[0], st), "event");
   API_CUDA(lcp::launch_absmax_scale(o->phi.as<double>(), o->table_elems, 1.0, o->b_tmp.as<unsigned long long>(),
                                     o->b_scale.as<double>(), st),
            "table scale");
-  API_CUDA(lcp::launch_brick_table(o->phi.as<double>(), o->geom.phi_off, o->geom.numorbs, o->geom.sph_off, u.natom,
-                                   o->b_code.as<int32_t>(), (int64_t)b.point_code.size(), o->b_scale.as<double>(),
-                                   o->b_tab.as<__nv_bfloat16>(), b.nblocks, st),
+  // the first block of every atom image: images take ceil(NO / 16) consecutive blocks
+  std::vector<int32_t> first;
+  for (int64_t blk = 0; blk < b.nblocks;) {
+    first.push_back((int32_t)blk);
+    blk += (u.numorbs[b.block_atom[blk]] + 15) / 16;
+  }
+  DBuf d_first, d_batom, d_slots;
+  API_CUDA(upload(d_first, first, st), "upload");
+  API_CUDA(upload(d_batom, b.block_atom, st), "upload");
+  API_CUDA(d_slots.ensure((size_t)std::max<int64_t>(b.nblocks, 1) * 128 * sizeof(int32_t)), "table slots alloc");
+  API_CUDA(lcp::launch_brick_table(o->phi.as<double>(), o->geom.phi_off, o->geom.numorbs, o->geom.sph_off,
+                                   o->b_code.as<int32_t>(), (int64_t)b.point_code.size(), d_batom.as<int32_t>(),
+                                   d_first.as<int32_t>(), (int64_t)first.size(), d_slots.as<int32_t>(),
+                                   o->b_scale.as<double>(), o->b_tab.as<__nv_bfloat16>(), b.nblocks, st),
            "brick table");
+  API_CUDA(cudaEventRecord(te[1], st), "event");
+  API_CUDA(cudaStreamSynchronize(st), "brick table");  // before the scratch above is freed
+  cudaEventElapsedTime(&o->split_ms, te[0], te[1]);
+  cudaEventDestroy(te[0]);
+  cudaEventDestroy(te[1]);
   ctx->launches += 3;
   API_CUDA(cudaMemcpyAsync(&o->phi_scale, o->b_scale.p, sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   lcp::TcBrickGeom& g = o->bgeom;
@@ -719,6 +739,10 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
   DBuf d_batom, d_bstart;
   API_CUDA(upload(d_batom, batom, st), "upload");
   API_CUDA(upload(d_bstart, bstart, st), "upload");
+  cudaEvent_t te[2];
+  API_CUDA(cudaEventCreate(&te[0]), "event");
+  API_CUDA(cudaEventCreate(&te[1]), "event");
+  API_CUDA(cudaEventRecord(te[0], st), "event");
   API_CUDA(lcp::launch_tabulate(g, o->species.as<DevSpecies>(), o->radial.as<double>(), o->buckets.as<int32_t>(),
                                 (int64_t)batom.size(), d_batom.as<int32_t>(), d_bstart.as<int64_t>(),
                                 o->phi.as<double>(), o->grad ? o->dphi[0].as<double>() : nullptr,
@@ -726,7 +750,11 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
                                 o->grad ? o->dphi[2].as<double>() : nullptr, max_no_spe, st),
            "tabulate kernel");
   ctx->launches++;
+  API_CUDA(cudaEventRecord(te[1], st), "event");
   API_CUDA(cudaStreamSynchronize(st), "tabulate");
+  cudaEventElapsedTime(&o->tab_ms, te[0], te[1]);
+  cudaEventDestroy(te[0]);
+  cudaEventDestroy(te[1]);
   *out = o.release();
   return LCP_OK;
 }
@@ -1704,6 +1732,13 @@ lcp_status lcp_bounds_check_status(lcp_ctx* ctx, int64_t* word) {
   API_CUDA(e, "bounds word");
   API_CUDA(lcp::bounds_take_tc(&b), "bounds word");
   *word = (int64_t)(a ? a : b);
+  return LCP_OK;
+}
+
+lcp_status lcp_orbs_timings(const lcp_orbs* orbs, double* out2) {
+  if (!orbs || !out2) return fail(LCP_EINVAL, "NULL argument");
+  out2[0] = orbs->tab_ms;
+  out2[1] = orbs->split_ms;
   return LCP_OK;
 }
 

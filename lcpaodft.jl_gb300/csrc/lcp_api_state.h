@@ -142,6 +142,8 @@ struct lcp_orbs {
   DBuf o_atom, o_jatom, o_boff, o_partner;  // ordered pair list
   DBuf b_scale, b_tmp;                       // fixed-point scale of the tables: [S_phi, 1/S_phi]
   double phi_scale = 1.0;
+  // device times of the last tabulation and split-table build (ms)
+  float tab_ms = 0.f, split_ms = 0.f;
 };
 
 struct lcp_job {

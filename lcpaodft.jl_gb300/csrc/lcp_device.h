@@ -315,9 +315,15 @@ cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, i
 cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
 cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,
                                 cudaStream_t st);
+// The split-BF16 tables from the FP64 tables: first_block[nimg] lists the
+// first block of every atom image (its 16-orbital chunks follow it), which
+// together cover all nblocks blocks; slot_point is scratch of nblocks * 128
+// ints.
 cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const int32_t* numorbs,
-                               const int64_t* sph_off, int natom, const int32_t* point_code, int64_t npoints,
-                               const double* scale, __nv_bfloat16* tab, int64_t nblocks, cudaStream_t st);
+                               const int64_t* sph_off, const int32_t* point_code, int64_t npoints,
+                               const int32_t* block_atom, const int32_t* first_block, int64_t nimg,
+                               int32_t* slot_point, const double* scale, __nv_bfloat16* tab, int64_t nblocks,
+                               cudaStream_t st);
 cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* sub_chunks, const int32_t* pair_atom,
                         const int32_t* pair_jatom, const int64_t* boff, const int32_t* partner, const int32_t* numorbs,
                         const double* dm, const double* scale, __nv_bfloat16* out, cudaStream_t st);

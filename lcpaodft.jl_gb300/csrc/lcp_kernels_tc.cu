@@ -278,34 +278,53 @@ __global__ void pow2_scale_batch_kernel(int32_t ncells, const unsigned long long
   }
 }
 
-__global__ void brick_table_kernel(const double* __restrict__ phi, const int64_t* __restrict__ phi_off,
-                                   const int32_t* __restrict__ numorbs, const int64_t* __restrict__ sph_off,
-                                   int natom, const int32_t* __restrict__ point_code, int64_t npoints,
-                                   const double* __restrict__ scale, __nv_bfloat16* __restrict__ tab,
-                                   int64_t nblocks) {
+// Sphere point of every (first block, slot) of the table: code = block * 128
+// + slot of each sphere point k (one thread per point).
+__global__ void brick_slot_kernel(const int32_t* __restrict__ point_code, int64_t npoints, int32_t* __restrict__ slot_point) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npoints; k += (int64_t)gridDim.x * blockDim.x)
+    slot_point[point_code[k]] = (int32_t)k;
+}
+
+// The split-BF16 tables, one atom image per block of 256 threads: for each
+// of its 16-orbital chunks, thread (h, g, r) -- orbital half h, point group
+// g, point r of the group -- reads eight orbitals of its point's FP64 row and
+// writes the three parts as one 16-byte store each, so every part of a table
+// block is written as 4 KB of consecutive stores.  Empty slots and orbitals
+// past the atom's are zeros.  phi / S_phi is split in FP32 from its value and
+// remainder (fx_split_f), one FP64 multiply and subtract per entry.
+__global__ void __launch_bounds__(256) brick_table_kernel(const double* __restrict__ phi,
+                                                          const int64_t* __restrict__ phi_off,
+                                                          const int32_t* __restrict__ numorbs,
+                                                          const int64_t* __restrict__ sph_off,
+                                                          const int32_t* __restrict__ block_atom,
+                                                          const int32_t* __restrict__ first_block, int64_t nimg,
+                                                          const int32_t* __restrict__ slot_point,
+                                                          const double* __restrict__ scale,
+                                                          __nv_bfloat16* __restrict__ tab, int64_t nblocks) {
   const double inv = scale[1];
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npoints; k += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = natom;  // atom with sph_off[atom] <= k < sph_off[atom+1]
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (sph_off[mid] <= k) lo = mid;
-      else hi = mid;
-    }
-    const int atom = lo;
+  const int t = threadIdx.x, r = t & 7, g = (t >> 3) & 15, h = t >> 7;
+  const int slot = g * 8 + r;
+  for (int64_t im = blockIdx.x; im < nimg; im += gridDim.x) {
+    const int64_t b0 = first_block[im];
+    const int atom = block_atom[b0];
     const int no = numorbs[atom];
-    const double* src = phi + phi_off[atom] + (k - sph_off[atom]) * no;
-    const int code = point_code[k];
-    const int64_t blk = code >> 7;
-    const int slot = code & 127, g = slot >> 3, r = slot & 7;
-    __nv_bfloat16* base = tab + blk * kPart;  // part p of block blk at (p * nblocks + blk) * kPart
-    for (int a = 0; a < no; ++a) {  // orbital a: chunk a / 16 (block + a / 16), slot a % 16
-      __nv_bfloat16 h, m, l;
-      fx_split(src[a] * inv, h, m, l);
-      const int ac = a & 15;
-      const int off = (a >> 4) * kPart + ((ac >> 3) * 16 + g) * 64 + r * 8 + (ac & 7);
-      base[off] = h;
-      base[nblocks * kPart + off] = m;
-      base[2 * nblocks * kPart + off] = l;
+    const int k = slot_point[b0 * 128 + slot];
+    const double* src = k >= 0 ? phi + phi_off[atom] + (k - sph_off[atom]) * (int64_t)no : nullptr;
+    for (int c = 0; c * 16 < no; ++c) {
+      uint4 part[3];
+      __nv_bfloat16* ph = reinterpret_cast<__nv_bfloat16*>(&part[0]);
+      __nv_bfloat16* pm = reinterpret_cast<__nv_bfloat16*>(&part[1]);
+      __nv_bfloat16* pl = reinterpret_cast<__nv_bfloat16*>(&part[2]);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int o = c * 16 + h * 8 + e;
+        const double x = (src && o < no) ? src[o] * inv : 0.0;
+        const float xf = (float)x;
+        fx_split_f(xf, (float)(x - (double)xf), ph[e], pm[e], pl[e]);
+      }
+      const int64_t off = (b0 + c) * kPart + (int64_t)((h * 16 + g) * 64 + r * 8);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4*>(tab + q * nblocks * kPart + off) = part[q];
     }
   }
 }
@@ -1283,13 +1302,20 @@ cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsig
 }
 
 cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const int32_t* numorbs,
-                               const int64_t* sph_off, int natom, const int32_t* point_code, int64_t npoints,
-                               const double* scale, __nv_bfloat16* tab, int64_t nblocks, cudaStream_t st) {
-  LCP_CUDA_TRY(cudaMemsetAsync(tab, 0, (size_t)nblocks * kBlockElems * sizeof(__nv_bfloat16), st));
-  if (npoints == 0) return cudaSuccess;
-  int blocks = (int)std::min<int64_t>((npoints + 255) / 256, (int64_t)sm_count() * 16);
-  brick_table_kernel<<<blocks, 256, 0, st>>>(phi, phi_off, numorbs, sph_off, natom, point_code, npoints, scale, tab,
-                                              nblocks);
+                               const int64_t* sph_off, const int32_t* point_code, int64_t npoints,
+                               const int32_t* block_atom, const int32_t* first_block, int64_t nimg,
+                               int32_t* slot_point, const double* scale, __nv_bfloat16* tab, int64_t nblocks,
+                               cudaStream_t st) {
+  if (nimg == 0) return cudaSuccess;
+  LCP_CUDA_TRY(cudaMemsetAsync(slot_point, 0xff, (size_t)nblocks * 128 * sizeof(int32_t), st));
+  if (npoints > 0) {
+    const int blocks = (int)std::min<int64_t>((npoints + 255) / 256, (int64_t)sm_count() * 16);
+    brick_slot_kernel<<<blocks, 256, 0, st>>>(point_code, npoints, slot_point);
+    LCP_CUDA_TRY(cudaGetLastError());
+  }
+  const int blocks = (int)std::min<int64_t>(nimg, (int64_t)sm_count() * 8);
+  brick_table_kernel<<<blocks, 256, 0, st>>>(phi, phi_off, numorbs, sph_off, block_atom, first_block, nimg, slot_point,
+                                              scale, tab, nblocks);
   return cudaGetLastError();
 }
 

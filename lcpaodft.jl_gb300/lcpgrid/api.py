@@ -295,6 +295,12 @@ class DeviceOrbitalsGrid:
         check(lib.lcp_orbs_autotune_bricks(self.ctx._h, self._h, int(ncand), iptr(sh), ctypes.byref(ms)))
         return tuple(int(x) for x in sh), float(ms.value)
 
+    def timings(self):
+        """(tabulation kernel ms, split-BF16 table build ms), device times."""
+        out = np.zeros(2)
+        check(lib.lcp_orbs_timings(self._h, dptr(out)))
+        return float(out[0]), float(out[1])
+
     def release_fp64(self):
         """Keep only the split-BF16 tables (frees the FP64 tables)."""
         check(lib.lcp_orbs_release_fp64(self.ctx._h, self._h))
