@@ -817,6 +817,7 @@ def summary(line):
     if isinstance(sv, dict):
         s["serve_sat_bf16"] = g(sv, "saturated_bf16x3", "jobs_per_s")
         s["serve_sat_fp64"] = g(sv, "saturated_fp64_dropin", "jobs_per_s")
+        s["serve_sat_unbatched"] = g(sv, "saturated_bf16x3_unbatched", "jobs_per_s")
         s["serve_vs_fp64"] = g(sv, "jobs_per_s_vs_fp64")
         s["serve_err_uHa"] = g(sv, "max_err_per_atom_uHa")
         s["serve_sweep"] = [[g(r, "offered_rate"), g(r, "jobs_per_s"), g(r, "p50_ms"), g(r, "p99_ms")]
@@ -884,9 +885,10 @@ def serving(args, wl_pool=None):
         natoms.append(w["natom"])
     t_setup = time.perf_counter() - t0
 
-    def run_server(precision, nslots, rate, seconds, max_requests):
+    def run_server(precision, nslots, rate, seconds, max_requests, max_batch=None):
+        srv_max_batch = (args.serve_max_batch if max_batch is None else max_batch) if precision == "bf16x3" else 1
         srv = L.Server(0, nslots=nslots, precision=precision, budget_bytes=args.serve_budget_gb * 1e9,
-                       max_batch=args.serve_max_batch if precision == "bf16x3" else 1)
+                       max_batch=srv_max_batch)
         ids = [srv.add(j) for j in jobs]
         # warm-up: every structure once (split-BF16 tables, FFT plans, workspaces)
         for sid in ids:
@@ -922,13 +924,15 @@ def serving(args, wl_pool=None):
             for _tag, _e, lat in srv.poll(wait_ms=5000):
                 lat_ms.append(lat)
         t_end = time.perf_counter()
-        nb, nbr, _ = srv.batch_stats()
+        nb, nbr, _, t_asm, t_bat = srv.batch_stats()
         srv.close()
         lat = np.array(lat_ms)
         return {"jobs_per_s": n_req / (t_end - t_start), "requests": n_req,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                 "offered_rate": rate, "slots": nslots, "precision": precision,
-                "batched_steps": nb, "mean_batch": (nbr / nb) if nb else 1.0}, energies
+                "batched_steps": nb, "mean_batch": (nbr / nb) if nb else 1.0,
+                "batch_assemble_ms": (t_asm / nb) if nb else None, "batch_wall_ms": (t_bat / nb) if nb else None,
+                "max_batch": srv_max_batch}, energies
 
     sweep, e_tc = [], None
     for rate in [float(x) for x in args.serve_rates.split(",") if x]:
@@ -936,11 +940,14 @@ def serving(args, wl_pool=None):
         sweep.append(res)
         e_tc = e_tc or e
     sat_tc, e_sat = run_server("bf16x3", args.serve_slots, 0, 0, args.serve_saturate)
+    # the same saturated stream with every request stepping alone (no batching)
+    sat_alone, _ = run_server("bf16x3", args.serve_slots, 0, 0, args.serve_saturate, max_batch=1)
     e_tc = e_tc or e_sat
     sat_64, e_64 = run_server("fp64", 1, 0, 0, args.serve_fp64_requests)
     err = max(abs(e_tc[k][4] - e_64[k][4]) / natoms[k] * 1e6 for k in range(len(jobs)))
     return {
-        "sweep": sweep, "saturated_bf16x3": sat_tc, "saturated_fp64_dropin": sat_64,
+        "sweep": sweep, "saturated_bf16x3": sat_tc, "saturated_bf16x3_unbatched": sat_alone,
+        "saturated_fp64_dropin": sat_64,
         "jobs_per_s_vs_fp64": sat_tc["jobs_per_s"] / sat_64["jobs_per_s"],
         "max_err_per_atom_uHa": err,
         "structures": {"count": len(jobs), "atoms": natoms, "setup_s": t_setup,

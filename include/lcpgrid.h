@@ -364,9 +364,10 @@ lcp_status lcp_server_state(lcp_server* srv, int32_t id, int32_t* state);
  * batched grid step (split-BF16 servers only; default 16 at LCP_PREC_BF16X3,
  * 1 otherwise: LCP_ENOTSUP for more than 1 at another precision). */
 lcp_status lcp_server_set_max_batch(lcp_server* srv, int32_t max_batch);
-/* out3 = batched steps run (more than one request), requests they carried,
- * structures waiting for admission. */
-lcp_status lcp_server_batch_stats(lcp_server* srv, int64_t* out3);
+/* out5 = batched steps run (more than one request), requests they carried,
+ * structures waiting for admission, host microseconds spent assembling those
+ * batches and their total wall microseconds (assembly to completion). */
+lcp_status lcp_server_batch_stats(lcp_server* srv, int64_t* out5);
 
 /* ---------------------------------------------------------------- brick tiling of the split-BF16 path */
 

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <numeric>
@@ -45,6 +46,29 @@ struct ShapeGroup {
 
 int64_t spec_len(const int32_t* ng) { return (int64_t)ng[0] * ng[1] * (ng[2] / 2 + 1); }
 
+// A table of a batch: a place in the batch's table buffer.
+struct TabRef {
+  void* p = nullptr;
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// The host side of an assembly's tables: each vector at a 256-byte aligned
+// offset of one byte image, bound to its TabRef once the device buffer exists.
+struct Stage {
+  std::vector<char> bytes;
+  std::vector<std::pair<TabRef*, size_t>> refs;
+  template <class T>
+  void add(TabRef& r, const std::vector<T>& v) {
+    const size_t off = (bytes.size() + 255) & ~size_t(255);
+    bytes.resize(off + std::max<size_t>(v.size(), 1) * sizeof(T));
+    if (!v.empty()) std::memcpy(bytes.data() + off, v.data(), v.size() * sizeof(T));
+    refs.emplace_back(&r, off);
+  }
+};
+
 // Cells [c0, c1) of the matrix-element pass that share the scratch area.
 struct Wave {
   int c0 = 0, c1 = 0;
@@ -61,15 +85,21 @@ struct lcp_batch {
   std::vector<lcp_job*> jobs;
   std::vector<ShapeGroup> groups;
   std::map<std::tuple<int, int, int>, std::unique_ptr<FftPlans>> plan_cache;
-  DBuf grid_pool, fft_cells;
+  DBuf grid_pool;
+  TabRef fft_cells;
   // device tables (per spin channel where the pointers differ)
-  DBuf tc_cells[2], brick_cell, brick_local;
+  TabRef tc_cells[2], brick_cell, brick_local;
   std::vector<Wave> waves;
-  DBuf hbrick_cell, hbrick_local, wred_start;  // per-wave brick lists and reduction starts
-  DBuf wred_order;                             // per wave: its sub-blocks, longest first
-  DBuf dsym_cells[2], dsym_start, abs_start;
-  DBuf red_cells[2];
-  DBuf grid_cells, pt_start, sp_start, h_start;
+  TabRef hbrick_cell, hbrick_local, wred_start;  // per-wave brick lists and reduction starts
+  TabRef wred_order;                             // per wave: its sub-blocks, longest first
+  TabRef dsym_cells[2], dsym_start, abs_start;
+  TabRef red_cells[2];
+  TabRef grid_cells, pt_start, sp_start, h_start;
+  // every table above lives in `tables`, uploaded from one pinned staging
+  // buffer by one asynchronous copy per assembly
+  DBuf tables;
+  char* stage_host = nullptr;
+  size_t stage_cap = 0;
   // workspaces
   DBuf dsym, dscale, dtmp, vw, vscale, hscratch, status;
   int64_t nbricks = 0, dsym_blocks = 0, abs_total = 0, nsb = 0, pt_tiles = 0, sp_tiles = 0, h_tiles = 0;
@@ -80,17 +110,12 @@ struct lcp_batch {
     cudaSetDevice(device);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    if (stage_host) cudaFreeHost(stage_host);
   }
 };
 
 namespace {
 
-template <class T>
-cudaError_t upload_pod(DBuf& b, const std::vector<T>& v) {
-  cudaError_t e = b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T));
-  if (e != cudaSuccess || v.empty()) return e;
-  return cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-}
 
 std::vector<int64_t> prefix(const std::vector<int64_t>& counts) {
   std::vector<int64_t> s(counts.size() + 1, 0);
@@ -173,9 +198,11 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
 // Fills batch b (new or used before) for these jobs: validation, shape groups,
 // brick lists, waves and every device table.  Device buffers only grow, and
 // FFT plans are kept per grid shape, so re-assembling a batch over another
-// set of jobs of at most the same sizes allocates nothing.  The tables are
-// uploaded with synchronous copies; the jobs' split-BF16 tables are built on
-// ctx's stream when missing.
+// set of jobs of at most the same sizes allocates nothing.  The tables go up
+// as one asynchronous copy on ctx's stream from pinned staging, which the
+// caller must not let the next assembly of the same batch overwrite before
+// the stream has passed it (a step on that stream, then a wait).  The jobs'
+// split-BF16 tables are built on ctx's stream when missing.
 lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* const* jobs, int64_t scratch_bytes) {
   lcp_status s = LCP_OK;
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -186,6 +213,7 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
   b->groups.clear();
   b->waves.clear();
   b->ncells = njobs;
+  Stage stage;
   for (int k = 0; k < njobs; ++k) {
     lcp_job* j = jobs[k];
     if (!j) return fail(LCP_EINVAL, "lcp_batch_create: NULL job");
@@ -350,12 +378,12 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
                        [](const auto& x, const auto& y) { return x.first < y.first; });
       for (const auto& l : len) word.push_back(l.second);
     }
-    API_CUDA(upload_pod(b->brick_cell, bc), "upload");
-    API_CUDA(upload_pod(b->brick_local, bl), "upload");
-    API_CUDA(upload_pod(b->hbrick_cell, hbc), "upload");
-    API_CUDA(upload_pod(b->hbrick_local, hbl), "upload");
-    API_CUDA(upload_pod(b->wred_start, wst), "upload");
-    API_CUDA(upload_pod(b->wred_order, word), "upload");
+    stage.add(b->brick_cell, bc);
+    stage.add(b->brick_local, bl);
+    stage.add(b->hbrick_cell, hbc);
+    stage.add(b->hbrick_local, hbl);
+    stage.add(b->wred_start, wst);
+    stage.add(b->wred_order, word);
   }
 
   // per-cell tables
@@ -369,12 +397,12 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
     c.dvh = c.real;  // the inverse transform writes back over the source
     gcs[k] = c;
   }
-  API_CUDA(upload_pod(b->grid_cells, gcs), "upload");
+  stage.add(b->grid_cells, gcs);
   {
     std::vector<lcp::GridCell> fc;
     for (const ShapeGroup& g : b->groups)
       for (int k : g.cells) fc.push_back(gcs[k]);
-    API_CUDA(upload_pod(b->fft_cells, fc), "upload");
+    stage.add(b->fft_cells, fc);
   }
   for (int ch = 0; ch < ns; ++ch) {
     std::vector<lcp::TcCell> tcs(nc);
@@ -426,21 +454,35 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
       r.H = j->hks[ch].as<double>();
       rcs[k] = r;
     }
-    API_CUDA(upload_pod(b->tc_cells[ch], tcs), "upload");
-    API_CUDA(upload_pod(b->dsym_cells[ch], dcs), "upload");
-    API_CUDA(upload_pod(b->red_cells[ch], rcs), "upload");
+    stage.add(b->tc_cells[ch], tcs);
+    stage.add(b->dsym_cells[ch], dcs);
+    stage.add(b->red_cells[ch], rcs);
   }
-  API_CUDA(upload_pod(b->dsym_start, dsym_off), "upload");
-  API_CUDA(upload_pod(b->abs_start, ab_off), "upload");
-  API_CUDA(upload_pod(b->pt_start, pt_off), "upload");
-  API_CUDA(upload_pod(b->sp_start, sp_off), "upload");
-  API_CUDA(upload_pod(b->h_start, h_off), "upload");
+  stage.add(b->dsym_start, dsym_off);
+  stage.add(b->abs_start, ab_off);
+  stage.add(b->pt_start, pt_off);
+  stage.add(b->sp_start, sp_off);
+  stage.add(b->h_start, h_off);
   // our kernels per step: per channel absmax + pow2 + dsym + density, per
   // channel and wave vweight + H + reduce; the five FFT passes per grid
   // shape; once xc, sums, dot, dot-finish (GGA-PBE: xc is two passes)
   b->kernels_per_step = 4 * ns + 3 * ns * (int64_t)b->waves.size() + 4 + 5 * (int64_t)b->groups.size() +
                         (b->xc == LCP_XC_GGA_PBE ? 1 : 0);
-  API_CUDA(cudaStreamSynchronize(ctx->stream), "batch tables");
+  // one copy of every table: pinned staging (grown when needed), one device buffer
+  const size_t nbytes = std::max<size_t>(stage.bytes.size(), 1);
+  API_CUDA(b->tables.ensure(nbytes), "batch tables alloc");
+  if (nbytes > b->stage_cap) {
+    if (b->stage_host) cudaFreeHost(b->stage_host);
+    b->stage_host = nullptr;
+    b->stage_cap = 0;
+    API_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&b->stage_host), nbytes, cudaHostAllocDefault),
+             "batch staging alloc");
+    b->stage_cap = nbytes;
+  }
+  std::memcpy(b->stage_host, stage.bytes.data(), stage.bytes.size());
+  API_CUDA(cudaMemcpyAsync(b->tables.p, b->stage_host, stage.bytes.size(), cudaMemcpyHostToDevice, ctx->stream),
+           "batch tables upload");
+  for (auto& r : stage.refs) r.first->p = static_cast<char*>(b->tables.p) + r.second;
   return LCP_OK;
 }
 

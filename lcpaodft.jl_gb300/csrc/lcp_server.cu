@@ -89,6 +89,7 @@ struct lcp_server {
   bool stop = false;
   std::vector<std::thread> workers;
   int64_t submitted = 0, completed = 0, batches = 0, batched_requests = 0;
+  double assemble_ms = 0.0, batch_ms = 0.0;  // host time of the batched steps' assembly, and their wall time
   lcp_status sticky = LCP_OK;
   std::string sticky_msg;
 
@@ -135,7 +136,9 @@ struct lcp_server {
     if (!runners[slot]) runners[slot] = batch_new(device);
     std::vector<lcp_job*> jobs;
     for (Request* r : batch) jobs.push_back(r->job);
+    const Clock::time_point t0 = Clock::now();
     lcp_status s = batch_assemble(ctx, runners[slot], (int32_t)jobs.size(), jobs.data(), 0);
+    const Clock::time_point t1 = Clock::now();
     for (size_t k = 0; k < batch.size() && s == LCP_OK; ++k) {
       Request* r = batch[k];
       for (int c = 0; c < r->nspin && s == LCP_OK; ++c)
@@ -147,6 +150,12 @@ struct lcp_server {
     for (size_t k = 0; k < batch.size() && s == LCP_OK; ++k)
       s = lcp_job_energies_async(ctx, batch[k]->job, batch[k]->energies);
     if (s == LCP_OK) s = batch_status(runners[slot], st);  // waits for the stream
+    const Clock::time_point t2 = Clock::now();
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      assemble_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+      batch_ms += std::chrono::duration<double, std::milli>(t2 - t0).count();
+    }
     return s;
   }
 
@@ -490,12 +499,14 @@ lcp_status lcp_server_stats(lcp_server* srv, int64_t* out4) {
   return LCP_OK;
 }
 
-lcp_status lcp_server_batch_stats(lcp_server* srv, int64_t* out3) {
-  if (!srv || !out3) return fail(LCP_EINVAL, "NULL argument");
+lcp_status lcp_server_batch_stats(lcp_server* srv, int64_t* out5) {
+  if (!srv || !out5) return fail(LCP_EINVAL, "NULL argument");
   std::lock_guard<std::mutex> lk(srv->mu);
-  out3[0] = srv->batches;
-  out3[1] = srv->batched_requests;
-  out3[2] = (int64_t)srv->waiting.size();
+  out5[0] = srv->batches;
+  out5[1] = srv->batched_requests;
+  out5[2] = (int64_t)srv->waiting.size();
+  out5[3] = (int64_t)(srv->assemble_ms * 1000.0);
+  out5[4] = (int64_t)(srv->batch_ms * 1000.0);
   return LCP_OK;
 }
 

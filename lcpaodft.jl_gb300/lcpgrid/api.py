@@ -810,10 +810,11 @@ class Server:
         return out.value
 
     def batch_stats(self):
-        """(batched steps run, requests they carried, structures waiting for admission)."""
-        out = (ctypes.c_int64 * 3)()
+        """(batched steps run, requests they carried, structures waiting for
+        admission, ms assembling those batches, their wall ms)."""
+        out = (ctypes.c_int64 * 5)()
         check(lib.lcp_server_batch_stats(self._h, out))
-        return tuple(int(x) for x in out)
+        return tuple(int(x) for x in out[:3]) + (out[3] / 1000.0, out[4] / 1000.0)
 
     def add(self, job):
         """Adds a GridStepJob (kept alive by the server object); returns its id.

@@ -96,8 +96,8 @@ def test_server_batches_requests():
     results = []
     while len(results) < len(order):
         results += srv.poll(wait_ms=2000)
-    nb, nreq, nwait = srv.batch_stats()
-    assert nb >= 1 and nreq >= 2 * nb and nwait == 0
+    nb, nreq, nwait, t_asm, t_batch = srv.batch_stats()
+    assert nb >= 1 and nreq >= 2 * nb and nwait == 0 and 0 < t_asm <= t_batch
     for tag, e, lat in results:
         np.testing.assert_allclose(e, alone[order[tag - 100]], rtol=1e-12, atol=0)
     srv.close()
