@@ -818,6 +818,7 @@ def summary(line):
         s["serve_sat_bf16"] = g(sv, "saturated_bf16x3", "jobs_per_s")
         s["serve_sat_fp64"] = g(sv, "saturated_fp64_dropin", "jobs_per_s")
         s["serve_sat_unbatched"] = g(sv, "saturated_bf16x3_unbatched", "jobs_per_s")
+        s["serve_back_to_back"] = g(sv, "pool_step_ms", "jobs_per_s_back_to_back")
         s["serve_vs_fp64"] = g(sv, "jobs_per_s_vs_fp64")
         s["serve_err_uHa"] = g(sv, "max_err_per_atom_uHa")
         s["serve_sweep"] = [[g(r, "offered_rate"), g(r, "jobs_per_s"), g(r, "p50_ms"), g(r, "p99_ms")]
@@ -885,6 +886,26 @@ def serving(args, wl_pool=None):
         natoms.append(w["natom"])
     t_setup = time.perf_counter() - t0
 
+    # every structure stepped alone (split-BF16, CUDA events): the pool's mean
+    # device time per request, i.e. the jobs/s of a GPU that runs one request
+    # after another with no host gaps
+    tctx = L.Context(0, precision="bf16x3")
+    tstream = torch.cuda.Stream()
+    tctx.set_stream(tstream.cuda_stream)
+    alone_ms = []
+    for j, d in zip(jobs, dms):
+        j.set_dm(d)
+        j.step(tctx)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record(tstream)
+        for _ in range(5):
+            j.step(tctx)
+        ev[1].record(tstream)
+        torch.cuda.synchronize()
+        alone_ms.append(ev[0].elapsed_time(ev[1]) / 5)
+    tctx.close()
+
     def run_server(precision, nslots, rate, seconds, max_requests, max_batch=None):
         srv_max_batch = (args.serve_max_batch if max_batch is None else max_batch) if precision == "bf16x3" else 1
         srv = L.Server(0, nslots=nslots, precision=precision, budget_bytes=args.serve_budget_gb * 1e9,
@@ -950,6 +971,10 @@ def serving(args, wl_pool=None):
         "saturated_fp64_dropin": sat_64,
         "jobs_per_s_vs_fp64": sat_tc["jobs_per_s"] / sat_64["jobs_per_s"],
         "max_err_per_atom_uHa": err,
+        "pool_step_ms": {"per_structure": alone_ms, "mean": float(np.mean(alone_ms)),
+                         "jobs_per_s_back_to_back": 1000.0 / float(np.mean(alone_ms)),
+                         "note": "each structure's split-BF16 step alone on the device (CUDA events); requests pick "
+                                 "structures uniformly, so 1000 / mean is the jobs/s of back-to-back single steps"},
         "structures": {"count": len(jobs), "atoms": natoms, "setup_s": t_setup,
                        "resident_bytes": int(sum(j.footprint() for j in jobs))},
     }

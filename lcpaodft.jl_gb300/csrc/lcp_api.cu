@@ -149,13 +149,6 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   API_CUDA(o->b_tab.ensure((size_t)std::max<int64_t>(b.nblocks, 1) * 6144 * 2), "brick table alloc");
   API_CUDA(o->b_scale.ensure(2 * sizeof(double)), "alloc");
   API_CUDA(o->b_tmp.ensure(sizeof(unsigned long long)), "alloc");
-  cudaEvent_t te[2];
-  API_CUDA(cudaEventCreate(&te[0]), "event");
-  API_CUDA(cudaEventCreate(&te[1]), "event");
-  API_CUDA(cudaEventRecord(te[0], st), "event");
-  API_CUDA(lcp::launch_absmax_scale(o->phi.as<double>(), o->table_elems, 1.0, o->b_tmp.as<unsigned long long>(),
-                                    o->b_scale.as<double>(), st),
-           "table scale");
   // the first block of every atom image: images take ceil(NO / 16) consecutive blocks
   std::vector<int32_t> first;
   for (int64_t blk = 0; blk < b.nblocks;) {
@@ -166,6 +159,14 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   API_CUDA(upload(d_first, first, st), "upload");
   API_CUDA(upload(d_batom, b.block_atom, st), "upload");
   API_CUDA(d_slots.ensure((size_t)std::max<int64_t>(b.nblocks, 1) * 128 * sizeof(int32_t)), "table slots alloc");
+  // device time of the build (scale, slot map, tables), without the host work above
+  cudaEvent_t te[2];
+  API_CUDA(cudaEventCreate(&te[0]), "event");
+  API_CUDA(cudaEventCreate(&te[1]), "event");
+  API_CUDA(cudaEventRecord(te[0], st), "event");
+  API_CUDA(lcp::launch_absmax_scale(o->phi.as<double>(), o->table_elems, 1.0, o->b_tmp.as<unsigned long long>(),
+                                    o->b_scale.as<double>(), st),
+           "table scale");
   API_CUDA(lcp::launch_brick_table(o->phi.as<double>(), o->geom.phi_off, o->geom.numorbs, o->geom.sph_off,
                                    o->b_code.as<int32_t>(), (int64_t)b.point_code.size(), d_batom.as<int32_t>(),
                                    d_first.as<int32_t>(), (int64_t)first.size(), d_slots.as<int32_t>(),
@@ -176,7 +177,7 @@ lcp_status ensure_bricks(lcp_ctx* ctx, lcp_orbs* o) {
   cudaEventElapsedTime(&o->split_ms, te[0], te[1]);
   cudaEventDestroy(te[0]);
   cudaEventDestroy(te[1]);
-  ctx->launches += 3;
+  ctx->launches += 4;
   API_CUDA(cudaMemcpyAsync(&o->phi_scale, o->b_scale.p, sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   lcp::TcBrickGeom& g = o->bgeom;
   g.nbricks = b.nbricks;

@@ -332,20 +332,36 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
   // bricks k, k + grid, ... so a descending order balances them); the order
   // changes no result -- each brick writes its own points and partial blocks
   {
+    // heaviest first = most images first (the cost m^2 + 8m grows with m):
+    // a stable counting sort by m, so ties keep (cell, brick) order -- the
+    // order of a stable comparison sort, in linear time
     auto sorted_bricks = [&](int c0, int c1, std::vector<int32_t>& bc, std::vector<int64_t>& bl) {
-      std::vector<std::tuple<int64_t, int32_t, int64_t>> order;  // (-cost, cell, brick)
+      int64_t maxm = 0, n = 0;
+      for (int k = c0; k < c1; ++k) {
+        const lcp::Bricks& br = b->jobs[k]->orbs->bricks;
+        for (int64_t hb = 0; hb < br.nbricks; ++hb) maxm = std::max(maxm, br.img_off[hb + 1] - br.img_off[hb]);
+        n += br.nbricks;
+      }
+      std::vector<int64_t> pos(maxm + 1, 0);
+      for (int k = c0; k < c1; ++k) {
+        const lcp::Bricks& br = b->jobs[k]->orbs->bricks;
+        for (int64_t hb = 0; hb < br.nbricks; ++hb) ++pos[br.img_off[hb + 1] - br.img_off[hb]];
+      }
+      int64_t acc = (int64_t)bc.size();
+      for (int64_t m = maxm; m >= 0; --m) {
+        const int64_t c = pos[m];
+        pos[m] = acc;
+        acc += c;
+      }
+      bc.resize(bc.size() + n);
+      bl.resize(bl.size() + n);
       for (int k = c0; k < c1; ++k) {
         const lcp::Bricks& br = b->jobs[k]->orbs->bricks;
         for (int64_t hb = 0; hb < br.nbricks; ++hb) {
-          const int64_t m = br.img_off[hb + 1] - br.img_off[hb];
-          order.emplace_back(-(m * m + 8 * m), (int32_t)k, hb);
+          const int64_t i = pos[br.img_off[hb + 1] - br.img_off[hb]]++;
+          bc[i] = (int32_t)k;
+          bl[i] = hb;
         }
-      }
-      std::stable_sort(order.begin(), order.end(),
-                       [](const auto& x, const auto& y) { return std::get<0>(x) < std::get<0>(y); });
-      for (auto& o : order) {
-        bc.push_back(std::get<1>(o));
-        bl.push_back(std::get<2>(o));
       }
     };
     std::vector<int32_t> bc, hbc;
@@ -353,7 +369,12 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
     sorted_bricks(0, nc, bc, bl);
     for (Wave& w : b->waves) {
       w.brick_off = (int64_t)hbc.size();
-      sorted_bricks(w.c0, w.c1, hbc, hbl);
+      if (w.c0 == 0 && w.c1 == nc) {  // one wave: the same list
+        hbc.insert(hbc.end(), bc.begin(), bc.end());
+        hbl.insert(hbl.end(), bl.begin(), bl.end());
+      } else {
+        sorted_bricks(w.c0, w.c1, hbc, hbl);
+      }
       w.nbricks = (int64_t)hbc.size() - w.brick_off;
       // reduction starts of the wave's cells, rebased: wst[c0 + w .. c1 + w]
       int64_t acc = 0;
@@ -367,16 +388,29 @@ lcp_status batch_assemble(lcp_ctx* ctx, lcp_batch* b, int32_t njobs, lcp_job* co
       // one started late would run alone at the end of the launch; each
       // sub-block's own sum is unchanged
       w.order_off = (int64_t)word.size();
-      std::vector<std::pair<int64_t, int64_t>> len;  // (-partials, wave index)
-      len.reserve(acc);
+      // (a stable counting sort by the number of partials)
+      int64_t maxl = 0;
+      for (int k = w.c0; k < w.c1; ++k) {
+        const std::vector<int64_t>& ro = b->jobs[k]->orbs->bricks.red_off;
+        for (int64_t u = 0; u < nsbc[k]; ++u) maxl = std::max(maxl, ro[u + 1] - ro[u]);
+      }
+      std::vector<int64_t> pos(maxl + 1, 0);
+      for (int k = w.c0; k < w.c1; ++k) {
+        const std::vector<int64_t>& ro = b->jobs[k]->orbs->bricks.red_off;
+        for (int64_t u = 0; u < nsbc[k]; ++u) ++pos[ro[u + 1] - ro[u]];
+      }
+      int64_t at = (int64_t)word.size();
+      for (int64_t l = maxl; l >= 0; --l) {
+        const int64_t c = pos[l];
+        pos[l] = at;
+        at += c;
+      }
+      word.resize(word.size() + acc);
       int64_t g = 0;
       for (int k = w.c0; k < w.c1; ++k) {
         const std::vector<int64_t>& ro = b->jobs[k]->orbs->bricks.red_off;
-        for (int64_t u = 0; u < nsbc[k]; ++u, ++g) len.emplace_back(-(ro[u + 1] - ro[u]), g);
+        for (int64_t u = 0; u < nsbc[k]; ++u, ++g) word[pos[ro[u + 1] - ro[u]]++] = g;
       }
-      std::stable_sort(len.begin(), len.end(),
-                       [](const auto& x, const auto& y) { return x.first < y.first; });
-      for (const auto& l : len) word.push_back(l.second);
     }
     stage.add(b->brick_cell, bc);
     stage.add(b->brick_local, bl);

@@ -457,7 +457,6 @@ void fft_roots(int n, std::vector<double>& r64, std::vector<float>& r32) {
   r32.resize((size_t)4 * n);
   const long double two_pi = 6.283185307179586476925286766559005768L;
   for (int m = 0; m < n; ++m) {
-    // reduce the angle to the first octant's neighbourhood for accuracy
     const long double t = two_pi * (long double)m / (long double)n;
     const long double c = cosl(t), s = -sinl(t);
     const long double v[2] = {c, s};
