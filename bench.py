@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--serve-saturate", type=int, default=1500, help="requests of the saturated run")
     ap.add_argument("--serve-fp64-requests", type=int, default=60)
     ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--case", choices=["poisson", "tables"],
+                    help="one small kernel case for profiler captures: the 96^3 FFT Poisson solve (double-float, "
+                         "then FP64), or the 8-atom 48^3 cell's tabulation and split-BF16 table build")
     ap.add_argument("--batching", action="store_true", help="run the batching form instead of the step bench")
     ap.add_argument("--no-batching", action="store_true", help="skip the batching section of the step bench line")
     ap.add_argument("--batch-cells", type=int, default=256)
@@ -1185,9 +1188,45 @@ def batching(args):
     }
 
 
+def run_case(args):
+    """Small cases of single kernels, sized for profiler captures; prints their
+    device times (CUDA events on the library's stream)."""
+    import numpy as np
+    import torch
+
+    import lcpgrid as L
+    out = {"case": args.case}
+    ctx = L.Context(0, precision="bf16x3")
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    if args.case == "poisson":
+        ng = (96, 96, 96)
+        lat = np.eye(3) * 20.52
+        rec = 2 * np.pi * np.linalg.inv(lat.T)
+        src = np.random.default_rng(0).normal(size=int(np.prod(ng)))
+        res = np.zeros(src.size)
+        for prec in ("bf16x3", "fp64"):
+            ctx.set_precision(prec)
+            t0 = time.perf_counter()
+            L.Solve_Poisson_xyz(ng, rec, src, res, ctx=ctx)  # host in and out, as the reference calls it
+            out[prec + "_call_ms"] = (time.perf_counter() - t0) * 1e3
+    else:
+        wl = _inputs().si64_workload(nrep=1, ngrid=(48, 48, 48))
+        u = L.UCell(1, wl["latvecs"], wl["natom"], wl["atom2spe"], wl["gxyz"], wl["cut"], wl["ngrid"], wl["origin"],
+                    Total_NumOrbs=wl["numorbs"], ctx=ctx)
+        orbs = L.Set_Orbitals_Grid(wl["paos"], u)
+        job = L.GridStepJob(u, orbs, "off", "LDA")
+        job.prepare()
+        out["tabulation_ms"], out["split_tables_ms"] = orbs.timings()
+    ctx.synchronize()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.batching:
         print(json.dumps(batching(args)))

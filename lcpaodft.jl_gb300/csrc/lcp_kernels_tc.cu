@@ -162,6 +162,40 @@ __device__ __forceinline__ void fx_split_f(float p, float e, __nv_bfloat16& hi, 
   lo = __float2bfloat16_rn(l);
 }
 
+// The same three parts of x = v / 2^k (|x| <= 1) for an FP64 v, in integer
+// arithmetic on v's bits, without the FP64 pipe: x is rounded once to the
+// nearest multiple of 2^-26 (ties to even), q = x * 2^26 (|q| <= 2^26), and
+// |q| is cut into signed 9-bit digits rounded to nearest, q = q1 2^18 + q2 2^9
+// + q3 with |q1|, |q2|, |q3| <= 256.  The parts q1 2^-8, q2 2^-17, q3 2^-26
+// are exact in BF16 and carry x to within 2^-27.
+__device__ __forceinline__ void fx_split_bits(double v, int k, __nv_bfloat16& hi, __nv_bfloat16& mid,
+                                              __nv_bfloat16& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  long long a = 0;  // |q|
+  if (e != 0) {     // zeros and subnormals (below 2^-1022) give q = 0
+    const unsigned long long m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = 1049 + k - e;  // x * 2^26 = m * 2^-sh
+    if (sh <= 0) {
+      a = 1ll << 26;  // |x| > 1 does not occur for the tables (S_phi >= max |phi|): saturate
+    } else if (sh < 64) {
+      const unsigned long long half = 1ull << (sh - 1);
+      const unsigned long long rem = m & ((half << 1) - 1);
+      unsigned long long q = m >> sh;
+      if (rem > half || (rem == half && (q & 1))) ++q;  // round to nearest, ties to even
+      a = (long long)q;
+    }
+  }
+  const long long q1 = (a + (1ll << 17)) >> 18;          // nearest multiple of 2^18 (ties up)
+  const long long r = a - (q1 << 18);                     // [-2^17, 2^17)
+  const long long q2 = (r + 256) >> 9;                    // floor((r + 256) / 512)
+  const long long q3 = r - (q2 << 9);                     // [-256, 256)
+  const float sgn = (b >> 63) ? -1.0f : 1.0f;
+  hi = __float2bfloat16_rn(sgn * (float)q1 * 0.00390625f);            // 2^-8
+  mid = __float2bfloat16_rn(sgn * (float)q2 * 7.62939453125e-06f);     // 2^-17
+  lo = __float2bfloat16_rn(sgn * (float)q3 * 1.4901161193847656e-08f); // 2^-26
+}
+
 // Float-float accumulation (Knuth's TwoSum): hi + lo carries the running sum
 // with ~2^-48 relative error, at a handful of FP32 operations per term.
 __device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
@@ -290,8 +324,8 @@ __global__ void brick_slot_kernel(const int32_t* __restrict__ point_code, int64_
 // g, point r of the group -- reads eight orbitals of its point's FP64 row and
 // writes the three parts as one 16-byte store each, so every part of a table
 // block is written as 4 KB of consecutive stores.  Empty slots and orbitals
-// past the atom's are zeros.  phi / S_phi is split in FP32 from its value and
-// remainder (fx_split_f), one FP64 multiply and subtract per entry.
+// past the atom's are zeros.  phi / S_phi is split from phi's FP64 bits in
+// integer arithmetic (fx_split_bits): no FP64 instruction per entry.
 __global__ void __launch_bounds__(256) brick_table_kernel(const double* __restrict__ phi,
                                                           const int64_t* __restrict__ phi_off,
                                                           const int32_t* __restrict__ numorbs,
@@ -301,7 +335,6 @@ __global__ void __launch_bounds__(256) brick_table_kernel(const double* __restri
                                                           const int32_t* __restrict__ slot_point,
                                                           const double* __restrict__ scale,
                                                           __nv_bfloat16* __restrict__ tab, int64_t nblocks) {
-  const double inv = scale[1];
   const int t = threadIdx.x, r = t & 7, g = (t >> 3) & 15, h = t >> 7;
   const int slot = g * 8 + r;
   for (int64_t im = blockIdx.x; im < nimg; im += gridDim.x) {
@@ -310,6 +343,8 @@ __global__ void __launch_bounds__(256) brick_table_kernel(const double* __restri
     const int no = numorbs[atom];
     const int k = slot_point[b0 * 128 + slot];
     const double* src = k >= 0 ? phi + phi_off[atom] + (k - sph_off[atom]) * (int64_t)no : nullptr;
+    // the scale is a power of two: phi / S_phi is phi with its exponent lowered by ks
+    const int ks = (int)(((unsigned long long)__double_as_longlong(scale[0]) >> 52) & 0x7ff) - 1023;
     for (int c = 0; c * 16 < no; ++c) {
       uint4 part[3];
       __nv_bfloat16* ph = reinterpret_cast<__nv_bfloat16*>(&part[0]);
@@ -318,9 +353,7 @@ __global__ void __launch_bounds__(256) brick_table_kernel(const double* __restri
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
         const int o = c * 16 + h * 8 + e;
-        const double x = (src && o < no) ? src[o] * inv : 0.0;
-        const float xf = (float)x;
-        fx_split_f(xf, (float)(x - (double)xf), ph[e], pm[e], pl[e]);
+        fx_split_bits((src && o < no) ? src[o] : 0.0, ks, ph[e], pm[e], pl[e]);
       }
       const int64_t off = (b0 + c) * kPart + (int64_t)((h * 16 + g) * 64 + r * 8);
 #pragma unroll

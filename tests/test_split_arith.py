@@ -6,6 +6,10 @@ numpy float32 (IEEE round-to-nearest-even, as the GPU's FP32 adds):
   256 quanta, hence exact in BF16, and the parts carry p + e to within
   2^-27 + 2^-34;
 - the FP64 table split (fx_split) gives the same parts;
+- the integer split of an FP64 value's bits (fx_split_bits, the split-BF16
+  table build): parts of at most 256 quanta, exact in BF16, carrying
+  v / 2^k to within 2^-27, and equal to the exact rounding of v / 2^k to
+  2^-26 split into nearest digits;
 - the brick dealing of the persistent kernels (round_brick) visits every
   brick exactly once for any brick count and grid size.
 """
@@ -75,6 +79,55 @@ def test_fp64_split_matches_and_is_exact():
     hf, mf, lf = split_f(uf, (u - uf.astype(np.float64)).astype(np.float32))
     same = (hf == h) & (mf == m) & (lf == lo)
     assert same.mean() > 0.999  # ties of the last part may round apart
+
+
+def split_bits(v, k):
+    """fx_split_bits restated on the IEEE bits of float64 v (numpy int64)."""
+    v = np.asarray(v, dtype=np.float64)
+    b = v.view(np.uint64)
+    e = ((b >> np.uint64(52)) & np.uint64(0x7ff)).astype(np.int64)
+    m = ((b & np.uint64((1 << 52) - 1)) | np.uint64(1 << 52)).astype(object)
+    sh = 1049 + k - e
+    a = np.zeros(v.shape, dtype=object)
+    for i in range(v.size):
+        if e.flat[i] == 0:
+            continue
+        s_ = int(sh.flat[i])
+        if s_ <= 0:
+            a.flat[i] = 1 << 26
+        elif s_ < 64:
+            mm = int(m.flat[i])
+            half = 1 << (s_ - 1)
+            rem = mm & ((half << 1) - 1)
+            q = mm >> s_
+            if rem > half or (rem == half and (q & 1)):
+                q += 1
+            a.flat[i] = q
+    a = a.astype(np.int64)
+    q1 = (a + (1 << 17)) >> 18
+    r = a - (q1 << 18)
+    q2 = (r + 256) >> 9
+    q3 = r - (q2 << 9)
+    sgn = np.where((b >> np.uint64(63)) != 0, -1.0, 1.0)
+    return sgn * q1 * 2.0 ** -8, sgn * q2 * 2.0 ** -17, sgn * q3 * 2.0 ** -26, sgn * a
+
+
+def test_integer_bits_split():
+    rng = np.random.default_rng(8)
+    n = 20000
+    for k in (-3, 0, 2, 7):
+        v = rng.uniform(-1, 1, n) * 2.0 ** -rng.integers(0, 45, n) * 2.0 ** k
+        v[:5] = [2.0 ** k, -(2.0 ** k), 0.0, 2.0 ** (k - 27), 3 * 2.0 ** (k - 28)]
+        h, m, lo, q = split_bits(v, k)
+        x = v / 2.0 ** k
+        for part, qu in ((h, 2.0 ** -8), (m, 2.0 ** -17), (lo, 2.0 ** -26)):
+            kk = part / qu
+            assert np.all(kk == np.rint(kk)) and np.all(np.abs(kk) <= 256)
+            assert _is_bf16_exact(part.astype(np.float32))
+            assert np.all(part.astype(np.float32).astype(np.float64) == part)
+        assert np.max(np.abs(h + m + lo - x)) <= 2.0 ** -27
+        # q is x * 2^26 rounded to nearest, ties to even (exact in float64 here)
+        assert np.array_equal(np.abs(q).astype(np.float64), np.abs(np.rint(x * 2.0 ** 26)))
 
 
 def round_brick(j, b, g, ntotal):
