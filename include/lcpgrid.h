@@ -390,11 +390,11 @@ lcp_status lcp_orbs_release_fp64(lcp_ctx* ctx, lcp_orbs* orbs);
 /* ---------------------------------------------------------------- batching */
 
 /* Batched grid step over the device-resident jobs of many cells (the
- * spec batching form; the reference steps one cell at a time).  Each
+ * batching form; the reference steps one cell at a time).  Each
  * stage runs once for all cells: one persistent tensor-core launch over the
- * bricks of every cell for the density and for the matrix elements, batched
- * cuFFT plans per grid shape, tiled grid kernels and FP64 reductions over all
- * cells.  The step is captured once as a CUDA graph and replayed.  Results
+ * bricks of every cell for the density and for the matrix elements, one
+ * FFT Poisson solve per grid shape, tiled grid kernels and FP64 reductions
+ * over all cells.  The step is captured once as a CUDA graph and replayed.  Results
  * land in the jobs' own buffers (read them with lcp_job_get_* /
  * lcp_job_energies); each cell's density, H and energy sums are computed as
  * in a single-cell split-BF16 step.  The jobs (same SpinPol and xc, split-BF16

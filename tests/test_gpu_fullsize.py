@@ -10,7 +10,7 @@
   that density, the potential on the full grid, and the H blocks of the
   sampled pairs, which the GPU's FP64 and split-BF16 steps must match.
 
-Tolerances (the benchmark spec): rho <= 1e-8 e/bohr^3, H <= 1e-7 Ha, total grid energy
+Tolerances of the drop-in: rho <= 1e-8 e/bohr^3, H <= 1e-7 Ha, total grid energy
 <= 1 uHa/atom for FP64.  Split-BF16: rho and H within 1e-6 of their maximum,
 energy within 1 uHa/atom (reference: src/Matrix/Set_Density_Grid.jl:60-169,
 src/Hamiltonian.jl:235-324).
