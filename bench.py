@@ -636,7 +636,9 @@ def run_ours(args):
     tabulation["split_frac"] = tabulation["split_gbs"] / hbm if tabulation["split_gbs"] else None
     poisson = {"ms": float(stages[1]), "bytes": pois_bytes, "gbs": gbs(pois_bytes, float(stages[1])),
                "peak_gbs": hbm, "transform": "fp64" if args.precision == "fp64" else "double-float (FP32 pipe), FP64 "
-               "scaling", "note": "80 bytes per grid point per solve; the 96^3 arrays stay in L2"}
+               "scaling", "note": "80 bytes per grid point per solve (five passes over the half spectrum, source and "
+               "output); the spectrum (%.0f MB) %s" % (u.NN * 8 / 1e6, "stays in L2" if u.NN * 8 < 64e6 else
+                                                        "exceeds L2")}
     poisson["frac"] = poisson["gbs"] / hbm if poisson["gbs"] else None
 
     ms_step = total_ms / args.steps

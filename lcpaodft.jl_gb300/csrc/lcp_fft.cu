@@ -42,8 +42,9 @@ namespace {
 
 // ------------------------------------------------------------ double-float arithmetic
 //
-// A value is hi + lo with |lo| <= ulp(hi)/2: Dekker's exact product (here
-// with an FMA) and Knuth's two-sum, renormalised after every operation.
+// A value is hi + lo with |lo| about ulp(hi)/2 or less: Dekker's exact
+// product (with an FMA) and Knuth's two-sum.  Sums that only feed other sums
+// skip the renormalisation (add_lazy); every other result is renormalised.
 
 struct Dfl {
   float hi, lo;
@@ -54,13 +55,17 @@ __device__ __forceinline__ Dfl quick_two_sum(float s, float e) {
   return {r, e - (r - s)};
 }
 
-__device__ __forceinline__ Dfl operator+(Dfl a, Dfl b) {
+// hi parts summed with their exact rounding error, low parts added, not renormalised
+__device__ __forceinline__ Dfl add_lazy(Dfl a, Dfl b) {
   const float s = a.hi + b.hi;
   const float bb = s - a.hi;
-  const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
-  return quick_two_sum(s, e);
+  return {s, ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo)};
 }
 __device__ __forceinline__ Dfl operator-(Dfl a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ Dfl operator+(Dfl a, Dfl b) {
+  const Dfl t = add_lazy(a, b);
+  return quick_two_sum(t.hi, t.lo);
+}
 __device__ __forceinline__ Dfl operator-(Dfl a, Dfl b) { return a + (-b); }
 __device__ __forceinline__ Dfl operator*(Dfl a, Dfl b) {
   const float p = a.hi * b.hi;
@@ -68,6 +73,55 @@ __device__ __forceinline__ Dfl operator*(Dfl a, Dfl b) {
   e = fmaf(a.hi, b.lo, e);
   e = fmaf(a.lo, b.hi, e);
   return quick_two_sum(p, e);
+}
+// a b + c d with one renormalisation: both high products exact (FMA), their
+// sum by two-sum, the cross terms accumulated in FP32.
+__device__ __forceinline__ Dfl dot2(Dfl a, Dfl b, Dfl c, Dfl d) {
+  const float p1 = a.hi * b.hi, p2 = c.hi * d.hi;
+  float t = fmaf(a.hi, b.hi, -p1) + fmaf(c.hi, d.hi, -p2);
+  const float s = p1 + p2;
+  const float bb = s - p1;
+  const float e = (p1 - (s - bb)) + (p2 - bb);
+  t = fmaf(a.hi, b.lo, t);
+  t = fmaf(a.lo, b.hi, t);
+  t = fmaf(c.hi, d.lo, t);
+  t = fmaf(c.lo, d.hi, t);
+  return quick_two_sum(s, e + t);
+}
+
+__device__ __forceinline__ double add_lazy(double a, double b) { return a + b; }
+__device__ __forceinline__ double dot2(double a, double b, double c, double d) { return fma(a, b, c * d); }
+
+// FP64 <-> double-float on the integer and FP32 pipes (this GPU's FP64 pipe,
+// conversions included, runs at 2 operations per clock per SM).
+// dfl_of: hi is x cut to 24 significant bits, lo the other 29 bits rounded
+// to nearest FP32 (|lo| < ulp(hi), about 48 bits in all).  |x| below 2^-60
+// keeps hi alone, and below 2^-126 gives 0: the solve's values lie far above.
+__device__ __forceinline__ Dfl dfl_of(double x) {
+  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+  const int e = (int)((hw >> 20) & 0x7ff);
+  const unsigned sign = hw & 0x80000000u;
+  if (e < 897) return {0.f, 0.f};
+  if (e > 1150) return {__uint_as_float(sign | 0x7f800000u), 0.f};  // |x| >= 2^128: infinite
+  const float hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  if (e < 963) return {hi, 0.f};
+  // lo = r 2^(e - 1075), r the low 29 bits: r = r1 64 + r0 exactly in two
+  // FP32 (the 2^23 magic add), one rounding in the FMA, then two exact scalings
+  const unsigned r = lw & 0x1fffffffu;
+  const float r1 = __uint_as_float(0x4B000000u | (r >> 6)) - 8388608.0f;
+  const float r0 = __uint_as_float(0x4B000000u | (r & 63u)) - 8388608.0f;
+  const float sc = __uint_as_float((unsigned)(e - 1023 + 127) << 23);  // 2^(e - 1023), normal for e >= 897
+  const float lo = fmaf(r1, 64.0f, r0) * 2.220446049250313e-16f * sc;  // * 2^-52 * 2^(e - 1023)
+  return {hi, sign ? -lo : lo};
+}
+// an FP32 as FP64 from its bits (subnormal FP32 give +-0; inf and NaN stay so)
+__device__ __forceinline__ double dbl_of_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  const unsigned sign = u & 0x80000000u;
+  if (ex == 0) return __hiloint2double((int)sign, 0);
+  const unsigned e64 = ex == 0xffu ? 0x7ffu : ex + 896u;
+  return __hiloint2double((int)(sign | (e64 << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
 }
 
 template <class T>
@@ -77,16 +131,15 @@ struct Num<double> {
   __device__ static double from(double x) { return x; }
   __device__ static double to(double x) { return x; }
   __device__ static double half(double x) { return 0.5 * x; }
+  __device__ static double twice(double x) { return x + x; }
   __device__ static double zero() { return 0.0; }
 };
 template <>
 struct Num<Dfl> {
-  __device__ static Dfl from(double x) {
-    const float h = (float)x;
-    return {h, (float)(x - (double)h)};
-  }
-  __device__ static double to(Dfl x) { return (double)x.hi + (double)x.lo; }
+  __device__ static Dfl from(double x) { return dfl_of(x); }
+  __device__ static double to(Dfl x) { return dbl_of_bits(x.hi) + dbl_of_bits(x.lo); }  // one FP64 add
   __device__ static Dfl half(Dfl x) { return {0.5f * x.hi, 0.5f * x.lo}; }
+  __device__ static Dfl twice(Dfl x) { return {x.hi + x.hi, x.lo + x.lo}; }
   __device__ static Dfl zero() { return {0.f, 0.f}; }
 };
 
@@ -99,8 +152,12 @@ __device__ __forceinline__ Cx<T> operator+(Cx<T> a, Cx<T> b) { return {a.x + b.x
 template <class T>
 __device__ __forceinline__ Cx<T> operator-(Cx<T> a, Cx<T> b) { return {a.x - b.x, a.y - b.y}; }
 template <class T>
-__device__ __forceinline__ Cx<T> operator*(Cx<T> a, Cx<T> b) {
-  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+__device__ __forceinline__ Cx<T> cadd_l(Cx<T> a, Cx<T> b) { return {add_lazy(a.x, b.x), add_lazy(a.y, b.y)}; }
+template <class T>
+__device__ __forceinline__ Cx<T> csub_l(Cx<T> a, Cx<T> b) { return {add_lazy(a.x, -b.x), add_lazy(a.y, -b.y)}; }
+template <class T>
+__device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
+  return {dot2(a.x, b.x, -a.y, b.y), dot2(a.x, b.y, a.y, b.x)};
 }
 template <class T>
 __device__ __forceinline__ Cx<T> conj(Cx<T> a) { return {a.x, -a.y}; }
@@ -116,8 +173,6 @@ static_assert(sizeof(Cx<double>) == 16 && sizeof(Cx<Dfl>) == 16, "16-byte spectr
 
 // ------------------------------------------------------------ one pencil in shared memory
 
-constexpr int kRegRadix = 8;  // radices up to this size keep their points in registers
-
 // Roots of unity of the pencil length n: w[m] = exp(-2 pi i m / n); the
 // inverse transform uses their conjugates.
 template <class T, bool INV>
@@ -126,8 +181,108 @@ __device__ __forceinline__ Cx<T> root(const Cx<T>* w, int m) {
   return INV ? conj(r) : r;
 }
 
+// One butterfly of a Stockham stage: inputs a[j + r nb] (r < R), each times
+// its twiddle omega_n^(r k tstep) when tw (ns > 1), outputs b[o + s ns].
+template <class T, bool INV>
+__device__ __forceinline__ void bfly2(const Cx<T>* a, Cx<T>* b, int j, int nb, int o, int ns, bool tw, int m,
+                                      const Cx<T>* w) {
+  const Cx<T> v0 = a[j];
+  Cx<T> v1 = a[j + nb];
+  if (tw) v1 = cmul(v1, root<T, INV>(w, m));
+  b[o] = v0 + v1;
+  b[o + ns] = v0 - v1;
+}
+
+template <class T, bool INV>
+__device__ __forceinline__ void bfly4(const Cx<T>* a, Cx<T>* b, int j, int nb, int o, int ns, bool tw, int m,
+                                      const Cx<T>* w) {
+  const Cx<T> v0 = a[j];
+  Cx<T> v1 = a[j + nb], v2 = a[j + 2 * nb], v3 = a[j + 3 * nb];
+  if (tw) {
+    v1 = cmul(v1, root<T, INV>(w, m));
+    v2 = cmul(v2, root<T, INV>(w, 2 * m));
+    v3 = cmul(v3, root<T, INV>(w, 3 * m));
+  }
+  const Cx<T> t0 = cadd_l(v0, v2), t1 = csub_l(v0, v2), t2 = cadd_l(v1, v3), t3 = csub_l(v1, v3);
+  const Cx<T> r3 = INV ? mul_pi(t3) : mul_mi(t3);  // omega_4 * t3
+  b[o] = t0 + t2;
+  b[o + ns] = t1 + r3;
+  b[o + 2 * ns] = t0 - t2;
+  b[o + 3 * ns] = t1 - r3;
+}
+
+template <class T, bool INV>
+__device__ __forceinline__ void bfly3(const Cx<T>* a, Cx<T>* b, int j, int nb, int o, int ns, bool tw, int m,
+                                      const Cx<T>* w, int n) {
+  const Cx<T> v0 = a[j];
+  Cx<T> v1 = a[j + nb], v2 = a[j + 2 * nb];
+  if (tw) {
+    v1 = cmul(v1, root<T, INV>(w, m));
+    v2 = cmul(v2, root<T, INV>(w, 2 * m));
+  }
+  // omega_3 = -1/2 -+ i sqrt(3)/2: Im(w[n/3]) = -sqrt(3)/2
+  const T s = w[n / 3].y;
+  const Cx<T> t = cadd_l(v1, v2), d = csub_l(v1, v2);
+  const Cx<T> mm = csub_l(v0, Cx<T>{Num<T>::half(t.x), Num<T>::half(t.y)});
+  const Cx<T> q = scale(INV ? mul_mi(d) : mul_pi(d), s);  // -+ i sqrt(3)/2 * d
+  b[o] = v0 + t;
+  b[o + ns] = mm + q;
+  b[o + 2 * ns] = mm - q;
+}
+
+// radix 5: with t1 = v1 + v4, t2 = v2 + v3, t3 = v1 - v4, t4 = v2 - v3,
+// y0 = v0 + t1 + t2, y1,4 = a1 -+ i b1, y2,3 = a2 -+ i b2 (forward; the
+// inverse swaps the signs), a1 = v0 + c1 t1 + c2 t2, a2 = v0 + c2 t1 + c1 t2,
+// b1 = s1 t3 + s2 t4, b2 = s2 t3 - s1 t4, with omega_5^k = c_k - i s_k.
+template <class T, bool INV>
+__device__ __forceinline__ void bfly5(const Cx<T>* a, Cx<T>* b, int j, int nb, int o, int ns, bool tw, int m,
+                                      const Cx<T>* w, int n) {
+  const Cx<T> v0 = a[j];
+  Cx<T> v1 = a[j + nb], v2 = a[j + 2 * nb], v3 = a[j + 3 * nb], v4 = a[j + 4 * nb];
+  if (tw) {
+    v1 = cmul(v1, root<T, INV>(w, m));
+    v2 = cmul(v2, root<T, INV>(w, 2 * m));
+    v3 = cmul(v3, root<T, INV>(w, 3 * m));
+    v4 = cmul(v4, root<T, INV>(w, 4 * m));
+  }
+  const Cx<T> w1 = w[n / 5], w2 = w[2 * (n / 5)];
+  const T c1 = w1.x, c2 = w2.x, s1 = -w1.y, s2 = -w2.y;
+  const Cx<T> t1 = cadd_l(v1, v4), t2 = cadd_l(v2, v3), t3 = csub_l(v1, v4), t4 = csub_l(v2, v3);
+  const Cx<T> a1 = cadd_l(v0, Cx<T>{dot2(c1, t1.x, c2, t2.x), dot2(c1, t1.y, c2, t2.y)});
+  const Cx<T> a2 = cadd_l(v0, Cx<T>{dot2(c2, t1.x, c1, t2.x), dot2(c2, t1.y, c1, t2.y)});
+  const Cx<T> b1 = {dot2(s1, t3.x, s2, t4.x), dot2(s1, t3.y, s2, t4.y)};
+  const Cx<T> b2 = {dot2(s2, t3.x, -s1, t4.x), dot2(s2, t3.y, -s1, t4.y)};
+  const Cx<T> ib1 = INV ? mul_pi(b1) : mul_mi(b1), ib2 = INV ? mul_pi(b2) : mul_mi(b2);
+  b[o] = v0 + cadd_l(t1, t2);
+  b[o + ns] = a1 + ib1;
+  b[o + 4 * ns] = a1 - ib1;
+  b[o + 2 * ns] = a2 + ib2;
+  b[o + 3 * ns] = a2 - ib2;
+}
+
+// any other radix: the twiddles applied in place (the lane owns these
+// inputs), then the direct DFT with the inputs read from shared memory.
+template <class T, bool INV>
+__device__ void bfly_dft(Cx<T>* a, Cx<T>* b, int j, int nb, int o, int ns, bool tw, int m, const Cx<T>* w, int n,
+                         int R) {
+  if (tw)
+    for (int r = 1; r < R; ++r) a[j + r * nb] = cmul(a[j + r * nb], root<T, INV>(w, r * m));
+  const int wstep = n / R;  // omega_R = w[n / R]
+  for (int s = 0; s < R; ++s) {
+    Cx<T> acc = a[j];
+    int rs = 0;
+    for (int r = 1; r < R; ++r) {
+      rs += s;
+      if (rs >= R) rs -= R;  // (r s) mod R
+      acc = acc + cmul(a[j + r * nb], root<T, INV>(w, rs * wstep));
+    }
+    b[o + s * ns] = acc;
+  }
+}
+
 // Stockham autosort FFT of length n on a (natural order), b scratch; returns
-// the buffer holding the result.  One warp per pencil (lane = 0..31).
+// the buffer holding the result.  One warp per pencil (lane = 0..31); both
+// buffers may be overwritten.
 template <class T, bool INV>
 __device__ Cx<T>* fft_warp(Cx<T>* a, Cx<T>* b, int n, const int* fac, int nfac, const Cx<T>* w, int lane) {
   int ns = 1;
@@ -135,70 +290,21 @@ __device__ Cx<T>* fft_warp(Cx<T>* a, Cx<T>* b, int n, const int* fac, int nfac, 
     const int R = fac[st];
     const int nb = n / R;
     const int tstep = n / (ns * R);  // root index step of this stage's twiddles
+    const bool tw = ns > 1;
     for (int j = lane; j < nb; j += 32) {
       const int k = j % ns;
       const int o = (j - k) * R + k;  // (j / ns) * ns * R + k
-      if (R == 2) {
-        Cx<T> v0 = a[j], v1 = a[j + nb];
-        if (k) v1 = v1 * root<T, INV>(w, k * tstep);
-        b[o] = v0 + v1;
-        b[o + ns] = v0 - v1;
-      } else if (R == 4) {
-        Cx<T> v0 = a[j], v1 = a[j + nb], v2 = a[j + 2 * nb], v3 = a[j + 3 * nb];
-        if (k) {
-          v1 = v1 * root<T, INV>(w, k * tstep);
-          v2 = v2 * root<T, INV>(w, 2 * k * tstep);
-          v3 = v3 * root<T, INV>(w, 3 * k * tstep);
-        }
-        const Cx<T> t0 = v0 + v2, t1 = v0 - v2, t2 = v1 + v3, t3 = v1 - v3;
-        const Cx<T> r3 = INV ? mul_pi(t3) : mul_mi(t3);  // omega_4 * t3
-        b[o] = t0 + t2;
-        b[o + ns] = t1 + r3;
-        b[o + 2 * ns] = t0 - t2;
-        b[o + 3 * ns] = t1 - r3;
-      } else if (R == 3) {
-        Cx<T> v0 = a[j], v1 = a[j + nb], v2 = a[j + 2 * nb];
-        if (k) {
-          v1 = v1 * root<T, INV>(w, k * tstep);
-          v2 = v2 * root<T, INV>(w, 2 * k * tstep);
-        }
-        // omega_3 = -1/2 -+ i sqrt(3)/2: Im(w[n/3]) = -sqrt(3)/2
-        const T s = w[n / 3].y;
-        const Cx<T> t = v1 + v2, d = v1 - v2;
-        const Cx<T> m = {v0.x - Num<T>::half(t.x), v0.y - Num<T>::half(t.y)};
-        const Cx<T> q = scale(INV ? mul_mi(d) : mul_pi(d), s);  // -+ i sqrt(3)/2 * d
-        b[o] = v0 + t;
-        b[o + ns] = m + q;
-        b[o + 2 * ns] = m - q;
-      } else if (R <= kRegRadix) {
-        Cx<T> v[kRegRadix];
-#pragma unroll
-        for (int r = 0; r < kRegRadix; ++r)
-          if (r < R) {
-            v[r] = a[j + r * nb];
-            if (k && r) v[r] = v[r] * root<T, INV>(w, r * k * tstep);
-          }
-        const int wstep = n / R;  // omega_R = w[n / R]
-#pragma unroll
-        for (int s = 0; s < kRegRadix; ++s)
-          if (s < R) {
-            Cx<T> acc = v[0];
-            for (int r = 1; r < R; ++r) acc = acc + v[r] * root<T, INV>(w, ((r * s) % R) * wstep);
-            b[o + s * ns] = acc;
-          }
-      } else {
-        // a larger prime radix: its direct DFT, points read from shared memory
-        const int wstep = n / R;
-        for (int s = 0; s < R; ++s) {
-          Cx<T> acc = a[j];
-          for (int r = 1; r < R; ++r) {
-            Cx<T> x = a[j + r * nb];
-            if (k) x = x * root<T, INV>(w, r * k * tstep);
-            acc = acc + x * root<T, INV>(w, ((r * s) % R) * wstep);
-          }
-          b[o + s * ns] = acc;
-        }
-      }
+      const int m = k * tstep;
+      if (R == 4)
+        bfly4<T, INV>(a, b, j, nb, o, ns, tw, m, w);
+      else if (R == 2)
+        bfly2<T, INV>(a, b, j, nb, o, ns, tw, m, w);
+      else if (R == 3)
+        bfly3<T, INV>(a, b, j, nb, o, ns, tw, m, w, n);
+      else if (R == 5)
+        bfly5<T, INV>(a, b, j, nb, o, ns, tw, m, w, n);
+      else
+        bfly_dft<T, INV>(a, b, j, nb, o, ns, tw, m, w, n, R);
     }
     __syncwarp();
     Cx<T>* t = a;
@@ -216,6 +322,9 @@ struct FftArgs {
   GridCell c0;            // the cell when cells == nullptr
   const GridCell* cells;  // else blockIdx.y selects the cell
   int spinpol;            // source: LCP_SPIN_OFF / ON (rho_up + rho_down); -1: the cell's real array as is
+  int W;                  // passes 2-4: pencils (warps) per block
+  int colstride;          // their shared-memory stride in elements (odd: no bank conflicts)
+  int pfstride;           // the factors' stride in doubles (pass 3)
 };
 
 __device__ __forceinline__ const GridCell& fft_cell(const FftArgs& a) { return a.cells ? a.cells[blockIdx.y] : a.c0; }
@@ -231,9 +340,27 @@ __device__ __forceinline__ void load_roots(Cx<T>* dst, const Cx<T>* src, int n) 
   for (int m = threadIdx.x; m < n; m += blockDim.x) dst[m] = src[m];
 }
 
+// The source at grid point x: 2 rho - 2 rho_a ("off"), rho_up + rho_down -
+// 2 rho_a ("on"), or the cell's real array.  FP64 for the FP64 form; for
+// double-float, each term converted and summed in double-float.
+template <class T>
+__device__ __forceinline__ T source_at(const GridCell& c, int spinpol, int64_t x) {
+  if (spinpol < 0) return Num<T>::from(c.real[x]);
+  if (std::is_same<T, double>::value) {
+    const double aa = c.aden ? c.aden[x] : 0.0;
+    return Num<T>::from(spinpol == LCP_SPIN_OFF ? 2 * c.rho[0][x] - 2 * aa : c.rho[0][x] + c.rho[1][x] - 2 * aa);
+  }
+  T v = spinpol == LCP_SPIN_OFF ? Num<T>::twice(Num<T>::from(c.rho[0][x]))
+                                : Num<T>::from(c.rho[0][x]) + Num<T>::from(c.rho[1][x]);
+  if (c.aden) v = v - Num<T>::twice(Num<T>::from(c.aden[x]));
+  return v;
+}
+
+constexpr int kRowWarps = 4;
+
 // Pass 1: the source rows (two per warp) to their half spectra.
 template <class T>
-__global__ void fft_rows_fwd_kernel(const __grid_constant__ FftArgs a) {
+__global__ void __launch_bounds__(32 * kRowWarps, 8) fft_rows_fwd_kernel(const __grid_constant__ FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GridCell& c = fft_cell(a);
   const int n = a.g.n[2], h = n / 2 + 1;
@@ -247,22 +374,10 @@ __global__ void fft_rows_fwd_kernel(const __grid_constant__ FftArgs a) {
   const int64_t ra = 2 * pair, rb = ra + 1;
   if (ra >= nrows) return;
   const bool has_b = rb < nrows;
-  const double* r0 = c.rho[0];
-  const double* r1 = c.rho[1];
-  const double* ad = c.aden;
   for (int k = lane; k < n; k += 32) {
-    double v[2] = {0.0, 0.0};
-    for (int q = 0; q < 2; ++q) {
-      if (q == 1 && !has_b) break;
-      const int64_t x = (ra + q) * n + k;
-      if (a.spinpol < 0) {
-        v[q] = c.real[x];
-      } else {
-        const double aa = ad ? ad[x] : 0.0;
-        v[q] = a.spinpol == LCP_SPIN_OFF ? 2 * r0[x] - 2 * aa : r0[x] + r1[x] - 2 * aa;
-      }
-    }
-    buf[k] = {Num<T>::from(v[0]), Num<T>::from(v[1])};
+    const T va = source_at<T>(c, a.spinpol, ra * n + k);
+    const T vb = has_b ? source_at<T>(c, a.spinpol, rb * n + k) : Num<T>::zero();
+    buf[k] = {va, vb};
   }
   __syncwarp();
   const Cx<T>* z = fft_warp<T, false>(buf, buf + n, n, a.g.fac[2], a.g.nfac[2], w, lane);
@@ -277,7 +392,7 @@ __global__ void fft_rows_fwd_kernel(const __grid_constant__ FftArgs a) {
 
 // Pass 5: the half spectra of two rows to the real output rows.
 template <class T>
-__global__ void fft_rows_inv_kernel(const __grid_constant__ FftArgs a) {
+__global__ void __launch_bounds__(32 * kRowWarps, 8) fft_rows_inv_kernel(const __grid_constant__ FftArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GridCell& c = fft_cell(a);
   const int n = a.g.n[2], h = n / 2 + 1;
@@ -317,43 +432,48 @@ __global__ void fft_rows_inv_kernel(const __grid_constant__ FftArgs a) {
   }
 }
 
-// Passes 2-4: pencils along axis 1 (j) or 0 (i) of the half spectrum, W
-// consecutive k' columns per block (one warp each).  MODE 0 forward, 1
-// inverse, 2 forward, times the FP64 factors, inverse.
+// Passes 2-4: pencils along axis 1 (j) or 0 (i) of the half spectrum.  The
+// pencils are numbered c = outer * h + k' (outer = i for axis 1, j for axis
+// 0), and a block takes W consecutive ones, one warp each, so every block is
+// full.  Thread t of the block stages column t mod W (consecutive addresses
+// for consecutive threads) into a shared-memory stride that is odd in 16-byte
+// elements, so these stores hit distinct banks.  MODE 0 forward, 1 inverse, 2
+// forward, times the FP64 factors, inverse.
 template <class T, int MODE>
-__global__ void fft_cols_kernel(const __grid_constant__ FftArgs a, int axis, int W) {
+__global__ void __launch_bounds__(256, 4) fft_cols_kernel(const __grid_constant__ FftArgs a, int axis) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GridCell& c = fft_cell(a);
-  const int n1 = a.g.n[0], n2 = a.g.n[1], h = a.g.n[2] / 2 + 1;
+  const int n2 = a.g.n[1], h = a.g.n[2] / 2 + 1;
   const int n = a.g.n[axis];
+  const int W = a.W, S = a.colstride;
+  const int64_t ncols = (int64_t)(axis == 1 ? a.g.n[0] : n2) * h;
   const int64_t estride = axis == 1 ? h : (int64_t)n2 * h;
-  const int ntile = (h + W - 1) / W;
-  const int outer = blockIdx.x / ntile;  // i for axis 1, j for axis 0
-  const int k0 = (blockIdx.x % ntile) * W;
-  const int64_t base = axis == 1 ? (int64_t)outer * n2 * h + k0 : (int64_t)outer * h + k0;
-  const int cols = min(W, h - k0);
   Cx<T>* w = reinterpret_cast<Cx<T>*>(smem);
-  Cx<T>* bufs = w + n;  // [W][2][n]
-  double* pf = reinterpret_cast<double*>(bufs + (size_t)W * 2 * n);  // MODE 2: [W][n]
+  Cx<T>* bufs = w + n;  // [W][S], S >= 2n
+  double* pf = reinterpret_cast<double*>(bufs + (size_t)W * S);  // MODE 2: [W][pfstride]
   load_roots(w, roots_of<T>(a.g, axis), n);
   Cx<T>* spec = reinterpret_cast<Cx<T>*>(c.spec);
-  const int total = n * cols;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int e = idx / cols, col = idx - e * cols;
-    const int64_t x = base + e * estride + col;
-    bufs[(size_t)col * 2 * n + e] = spec[x];
-    if (MODE == 2) pf[(size_t)col * n + e] = c.pfac[x];
-  }
+  const int col = threadIdx.x % W;
+  const int64_t cid = (int64_t)blockIdx.x * W + col;
+  const bool live = cid < ncols;
+  const int64_t base = axis == 1 ? (cid / h) * n2 * h + cid % h : cid;
+  const int rows = blockDim.x / W;  // elements staged per thread step
+  if (live)
+    for (int e = threadIdx.x / W; e < n; e += rows) {
+      const int64_t x = base + e * estride;
+      bufs[(size_t)col * S + e] = spec[x];
+      if (MODE == 2) pf[(size_t)col * a.pfstride + e] = c.pfac[x];
+    }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int* fac = a.g.fac[axis];
   const int nfac = a.g.nfac[axis];
-  if (warp < cols) {
-    Cx<T>* p = bufs + (size_t)warp * 2 * n;
+  if ((int64_t)blockIdx.x * W + warp < ncols) {
+    Cx<T>* p = bufs + (size_t)warp * S;
     Cx<T>* q = p + n;
     Cx<T>* r = fft_warp<T, MODE == 1>(p, q, n, fac, nfac, w, lane);
     if (MODE == 2) {
-      const double* f = pf + (size_t)warp * n;
+      const double* f = pf + (size_t)warp * a.pfstride;
       for (int e = lane; e < n; e += 32) {
         const Cx<T> v = r[e];
         r[e] = {Num<T>::from(Num<T>::to(v.x) * f[e]), Num<T>::from(Num<T>::to(v.y) * f[e])};
@@ -366,37 +486,63 @@ __global__ void fft_cols_kernel(const __grid_constant__ FftArgs a, int axis, int
   // every warp's result sits in the same half of its buffer pair
   const int passes = MODE == 2 ? 2 * nfac : nfac;
   const size_t res = (passes & 1) ? (size_t)n : 0;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int e = idx / cols, col = idx - e * cols;
-    spec[base + e * estride + col] = bufs[(size_t)col * 2 * n + res + e];
-  }
+  if (live)
+    for (int e = threadIdx.x / W; e < n; e += rows) spec[base + e * estride] = bufs[(size_t)col * S + res + e];
 }
 
-constexpr int kRowWarps = 4;
+// Shared-memory budget of a pass 2-4 block: four blocks per SM.
+constexpr size_t kColsSmem = 54 * 1024;
 
-int cols_width(int n) {
-  const int w = (int)(96 * 1024 / (2 * (size_t)n * 16));
-  return std::max(1, std::min(8, w));
+// The factors' stride: 2 mod 16 doubles, so the 16 lanes of one 8-byte
+// shared-memory wavefront (eight columns, two elements) hit distinct banks.
+int pf_stride(int n) { return n + (18 - n % 16) % 16; }
+
+int cols_width(int n, bool with_pf) {
+  const size_t roots = (size_t)n * 16;
+  const size_t per = (size_t)(2 * n + 1) * 16 + (with_pf ? (size_t)pf_stride(n) * 8 : 0);
+  const size_t w = roots < kColsSmem ? (kColsSmem - roots) / per : 0;
+  return (int)std::max<size_t>(1, std::min<size_t>(8, w));
+}
+
+// The preferred shared-memory carveout, set once per kernel and device.
+cudaError_t prefer_shared(const void* kernel) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, bool> done;
+  int dev = 0;
+  LCP_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  bool& d = done[std::make_pair(kernel, dev)];
+  if (d) return cudaSuccess;
+  LCP_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    (int)cudaSharedmemCarveoutMaxShared));
+  d = true;
+  return cudaSuccess;
 }
 
 template <class T>
-cudaError_t launch_fft_t(const FftGeom& g, const FftArgs& args, int ncells, cudaStream_t st) {
+cudaError_t launch_fft_t(const FftGeom& g, FftArgs args, int ncells, cudaStream_t st) {
   const int n1 = g.n[0], n2 = g.n[1], n3 = g.n[2], h = n3 / 2 + 1;
   const int64_t pairs = ((int64_t)n1 * n2 + 1) / 2;
   const dim3 rgrid((unsigned)((pairs + kRowWarps - 1) / kRowWarps), (unsigned)ncells);
   const size_t rsm = (size_t)n3 * 16 * (1 + 2 * kRowWarps);
   LCP_CUDA_TRY(raise_smem(fft_rows_fwd_kernel<T>, rsm));
   LCP_CUDA_TRY(raise_smem(fft_rows_inv_kernel<T>, rsm));
+  LCP_CUDA_TRY(prefer_shared(reinterpret_cast<const void*>(fft_rows_fwd_kernel<T>)));
+  LCP_CUDA_TRY(prefer_shared(reinterpret_cast<const void*>(fft_rows_inv_kernel<T>)));
   fft_rows_fwd_kernel<T><<<rgrid, 32 * kRowWarps, rsm, st>>>(args);
   LCP_CUDA_TRY(cudaGetLastError());
   auto cols = [&](auto kern, int axis, bool with_pf) -> cudaError_t {
     const int n = g.n[axis];
-    const int W = cols_width(n);
-    const int ntile = (h + W - 1) / W;
-    const int outer = axis == 1 ? n1 : n2;
-    const size_t sm = (size_t)n * 16 * (1 + 2 * W) + (with_pf ? (size_t)W * n * 8 : 0);
+    const int W = cols_width(n, with_pf);
+    args.W = W;
+    args.colstride = 2 * n + 1;
+    args.pfstride = pf_stride(n);
+    const int64_t ncols = (int64_t)(axis == 1 ? n1 : n2) * h;
+    const size_t sm = (size_t)n * 16 + (size_t)W * args.colstride * 16 +
+                      (with_pf ? (size_t)W * args.pfstride * 8 : 0);
     LCP_CUDA_TRY(raise_smem(kern, sm));
-    kern<<<dim3((unsigned)(outer * ntile), (unsigned)ncells), 32 * W, sm, st>>>(args, axis, W);
+    LCP_CUDA_TRY(prefer_shared(reinterpret_cast<const void*>(kern)));
+    kern<<<dim3((unsigned)((ncols + W - 1) / W), (unsigned)ncells), 32 * W, sm, st>>>(args, axis);
     return cudaGetLastError();
   };
   LCP_CUDA_TRY(cols(fft_cols_kernel<T, 0>, 1, false));

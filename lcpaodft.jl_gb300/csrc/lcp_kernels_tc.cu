@@ -162,6 +162,17 @@ __device__ __forceinline__ void fx_split_f(float p, float e, __nv_bfloat16& hi, 
   lo = __float2bfloat16_rn(l);
 }
 
+// +-q * p as a BF16, for |q| <= 256 and p a power of two, with the sign of
+// q flipped when sv is 1: |q| becomes an FP32 by the 2^23 magic add and the
+// product is exact with at most eight significant bits, so its BF16 is the
+// FP32's upper half (no conversion instruction).
+__device__ __forceinline__ __nv_bfloat16 bf16_of_digit(int q, float p, unsigned sv) {
+  const unsigned aq = (unsigned)(q < 0 ? -q : q);
+  const float f = (__uint_as_float(0x4B000000u | aq) - 8388608.0f) * p;
+  const unsigned sign = (sv ^ (unsigned)(q < 0)) << 15;
+  return __ushort_as_bfloat16((unsigned short)((__float_as_uint(f) >> 16) | sign));
+}
+
 // The same three parts of x = v / 2^k (|x| <= 1) for an FP64 v, in integer
 // arithmetic on v's bits, without the FP64 pipe: x is rounded once to the
 // nearest multiple of 2^-26 (ties to even), q = x * 2^26 (|q| <= 2^26), and
@@ -186,14 +197,14 @@ __device__ __forceinline__ void fx_split_bits(double v, int k, __nv_bfloat16& hi
       a = (long long)q;
     }
   }
-  const long long q1 = (a + (1ll << 17)) >> 18;          // nearest multiple of 2^18 (ties up)
-  const long long r = a - (q1 << 18);                     // [-2^17, 2^17)
-  const long long q2 = (r + 256) >> 9;                    // floor((r + 256) / 512)
-  const long long q3 = r - (q2 << 9);                     // [-256, 256)
-  const float sgn = (b >> 63) ? -1.0f : 1.0f;
-  hi = __float2bfloat16_rn(sgn * (float)q1 * 0.00390625f);            // 2^-8
-  mid = __float2bfloat16_rn(sgn * (float)q2 * 7.62939453125e-06f);     // 2^-17
-  lo = __float2bfloat16_rn(sgn * (float)q3 * 1.4901161193847656e-08f); // 2^-26
+  const int q1 = (int)((a + (1ll << 17)) >> 18);  // nearest multiple of 2^18 (ties up)
+  const int r = (int)(a - ((long long)q1 << 18));   // [-2^17, 2^17)
+  const int q2 = (r + 256) >> 9;                    // floor((r + 256) / 512)
+  const int q3 = r - (q2 << 9);                     // [-256, 256)
+  const unsigned sv = (unsigned)(b >> 63);
+  hi = bf16_of_digit(q1, 0.00390625f, sv);          // 2^-8
+  mid = bf16_of_digit(q2, 7.62939453125e-06f, sv);  // 2^-17
+  lo = bf16_of_digit(q3, 1.4901161193847656e-08f, sv);  // 2^-26
 }
 
 // Float-float accumulation (Knuth's TwoSum): hi + lo carries the running sum
