@@ -319,6 +319,15 @@ lcp_status lcp_probe_fp64_tflops(lcp_ctx* ctx, double* tflops);
  * (order 0) or MN-groups outer (order 1); row-major host inputs, FP32 result. */
 lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major, int32_t order, int32_t n,
                            int32_t k, const float* a, const float* b, float* d);
+/* The xc functional per point, as the grid step's xc pass evaluates it: LDA
+ * (xc = LCP_XC_LDA, density 2 (up + pcc)) or LSDA (up + pcc, dn + pcc), in
+ * FP64 (double_float = 0: the FP64 drop-in) or in double-float (1: the
+ * precision forms).  out[3 i] = exc, out[3 i + 1] = vxc up, out[3 i + 2] =
+ * vxc down (0 for LDA); host arrays of n points; dn ignored for LDA, pcc may
+ * be NULL.  Replaces nothing of the reference: it checks one arithmetic
+ * against the other (src/XC/LDA_CA.jl:4-41, src/XC/LSDA_CA.jl:1-138). */
+lcp_status lcp_xc_selftest(lcp_ctx* ctx, int32_t xc, int32_t double_float, int64_t n, const double* up,
+                           const double* dn, const double* pcc, double* out);
 
 /* ---------------------------------------------------------------- serving */
 

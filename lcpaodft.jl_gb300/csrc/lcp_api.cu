@@ -1482,7 +1482,8 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
       API_CUDA(lcp::launch_gga_g(sp_xc, c, one, true, xs), "gga");
       ctx->launches += 2;
     } else {
-      API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, sp_xc, c, one, xs), "xc_vpot_energy");
+      API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, sp_xc, c, one, ctx->precision != LCP_PREC_FP64, xs),
+               "xc_vpot_energy");
       ctx->launches++;
     }
     return LCP_OK;
@@ -1684,6 +1685,36 @@ lcp_status lcp_tc_selftest(lcp_ctx* ctx, int32_t a_mn_major, int32_t b_mn_major,
   API_CUDA(cudaMemcpyAsync(d, dd.p, (size_t)128 * n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
   API_CUDA(cudaStreamSynchronize(ctx->stream), "tc selftest");
   if (st) return fail(st, "tensor-core self-test: MMA completion wait timed out");
+  return LCP_OK;
+}
+
+lcp_status lcp_xc_selftest(lcp_ctx* ctx, int32_t xc, int32_t double_float, int64_t n, const double* up,
+                           const double* dn, const double* pcc, double* out) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!up || !out || (xc != LCP_XC_LDA && !dn)) return fail(LCP_EINVAL, "NULL argument");
+  if (xc != LCP_XC_LDA && xc != LCP_XC_LSDA) return fail(LCP_EINVAL, "xc: LDA or LSDA");
+  if (n < 0) return fail(LCP_EINVAL, "n < 0");
+  if (n == 0) return LCP_OK;
+  DBuf dup, ddn, dpc, dout;
+  const size_t b = (size_t)n * sizeof(double);
+  API_CUDA(dup.ensure(b), "alloc");
+  API_CUDA(dout.ensure(3 * b), "alloc");
+  API_CUDA(cudaMemcpyAsync(dup.p, up, b, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  if (xc != LCP_XC_LDA) {
+    API_CUDA(ddn.ensure(b), "alloc");
+    API_CUDA(cudaMemcpyAsync(ddn.p, dn, b, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  }
+  if (pcc) {
+    API_CUDA(dpc.ensure(b), "alloc");
+    API_CUDA(cudaMemcpyAsync(dpc.p, pcc, b, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+  }
+  API_CUDA(lcp::launch_xc_selftest(xc, double_float != 0, n, dup.as<double>(), ddn.as<double>(),
+                                   pcc ? dpc.as<double>() : nullptr, dout.as<double>(), ctx->stream),
+           "xc selftest");
+  ctx->launches++;
+  API_CUDA(cudaMemcpyAsync(out, dout.p, 3 * b, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+  API_CUDA(cudaStreamSynchronize(ctx->stream), "xc selftest");
   return LCP_OK;
 }
 

@@ -166,7 +166,7 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
   if (b->xc == LCP_XC_GGA_PBE)
     API_CUDA(lcp::launch_gga_g(b->spinpol, gnone, pts, true, st), "batch gga");
   else
-    API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, st), "batch xc");
+    API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, true, st), "batch xc");
   mark(3);
   API_CUDA(lcp::launch_grid_sums_g(gnone, per, st), "batch sums");
   mark(4);

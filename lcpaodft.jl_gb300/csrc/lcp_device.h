@@ -207,7 +207,11 @@ cudaError_t launch_poisson_table(const int32_t* ngrid, const double* recvecs, do
 // With dvh == nullptr in the cell, the xc pass writes vxc to vpot and leaves
 // the E_H1 partials zero; launch_vpot_eh_g then adds dVHart + V_na and the
 // E_H1 partials (spinpol "off" or "on").
-cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
+// dfl: the functional in double-float (the precision forms), else FP64.
+cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, bool dfl,
+                                    cudaStream_t st);
+cudaError_t launch_xc_selftest(int xc, bool dfl, int64_t nn, const double* up, const double* dn, const double* pcc,
+                               double* out, cudaStream_t st);
 cudaError_t launch_vpot_eh_g(int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st);
 // GGA-PBE pass of the grid step (cells with dcoef/dexc set): gradient + PBE
 // (+ energy tile partials where part is set), then, if potential, the

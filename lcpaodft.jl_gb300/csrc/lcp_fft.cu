@@ -35,94 +35,19 @@
 #include <vector>
 
 #include "lcp_device.h"
+#include "lcp_dfloat.cuh"
 
 namespace lcp {
 
 namespace {
 
-// ------------------------------------------------------------ double-float arithmetic
+// ------------------------------------------------------------ arithmetic
 //
-// A value is hi + lo with |lo| about ulp(hi)/2 or less: Dekker's exact
-// product (with an FMA) and Knuth's two-sum.  Sums that only feed other sums
-// skip the renormalisation (add_lazy); every other result is renormalised.
-
-struct Dfl {
-  float hi, lo;
-};
-
-__device__ __forceinline__ Dfl quick_two_sum(float s, float e) {
-  const float r = s + e;
-  return {r, e - (r - s)};
-}
-
-// hi parts summed with their exact rounding error, low parts added, not renormalised
-__device__ __forceinline__ Dfl add_lazy(Dfl a, Dfl b) {
-  const float s = a.hi + b.hi;
-  const float bb = s - a.hi;
-  return {s, ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo)};
-}
-__device__ __forceinline__ Dfl operator-(Dfl a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ Dfl operator+(Dfl a, Dfl b) {
-  const Dfl t = add_lazy(a, b);
-  return quick_two_sum(t.hi, t.lo);
-}
-__device__ __forceinline__ Dfl operator-(Dfl a, Dfl b) { return a + (-b); }
-__device__ __forceinline__ Dfl operator*(Dfl a, Dfl b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return quick_two_sum(p, e);
-}
-// a b + c d with one renormalisation: both high products exact (FMA), their
-// sum by two-sum, the cross terms accumulated in FP32.
-__device__ __forceinline__ Dfl dot2(Dfl a, Dfl b, Dfl c, Dfl d) {
-  const float p1 = a.hi * b.hi, p2 = c.hi * d.hi;
-  float t = fmaf(a.hi, b.hi, -p1) + fmaf(c.hi, d.hi, -p2);
-  const float s = p1 + p2;
-  const float bb = s - p1;
-  const float e = (p1 - (s - bb)) + (p2 - bb);
-  t = fmaf(a.hi, b.lo, t);
-  t = fmaf(a.lo, b.hi, t);
-  t = fmaf(c.hi, d.lo, t);
-  t = fmaf(c.lo, d.hi, t);
-  return quick_two_sum(s, e + t);
-}
+// Double-float (lcp_dfloat.cuh) for the precision forms, FP64 for the
+// drop-in; the same butterflies serve both through these overloads.
 
 __device__ __forceinline__ double add_lazy(double a, double b) { return a + b; }
 __device__ __forceinline__ double dot2(double a, double b, double c, double d) { return fma(a, b, c * d); }
-
-// FP64 <-> double-float on the integer and FP32 pipes (this GPU's FP64 pipe,
-// conversions included, runs at 2 operations per clock per SM).
-// dfl_of: hi is x cut to 24 significant bits, lo the other 29 bits rounded
-// to nearest FP32 (|lo| < ulp(hi), about 48 bits in all).  |x| below 2^-60
-// keeps hi alone, and below 2^-126 gives 0: the solve's values lie far above.
-__device__ __forceinline__ Dfl dfl_of(double x) {
-  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
-  const int e = (int)((hw >> 20) & 0x7ff);
-  const unsigned sign = hw & 0x80000000u;
-  if (e < 897) return {0.f, 0.f};
-  if (e > 1150) return {__uint_as_float(sign | 0x7f800000u), 0.f};  // |x| >= 2^128: infinite
-  const float hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
-  if (e < 963) return {hi, 0.f};
-  // lo = r 2^(e - 1075), r the low 29 bits: r = r1 64 + r0 exactly in two
-  // FP32 (the 2^23 magic add), one rounding in the FMA, then two exact scalings
-  const unsigned r = lw & 0x1fffffffu;
-  const float r1 = __uint_as_float(0x4B000000u | (r >> 6)) - 8388608.0f;
-  const float r0 = __uint_as_float(0x4B000000u | (r & 63u)) - 8388608.0f;
-  const float sc = __uint_as_float((unsigned)(e - 1023 + 127) << 23);  // 2^(e - 1023), normal for e >= 897
-  const float lo = fmaf(r1, 64.0f, r0) * 2.220446049250313e-16f * sc;  // * 2^-52 * 2^(e - 1023)
-  return {hi, sign ? -lo : lo};
-}
-// an FP32 as FP64 from its bits (subnormal FP32 give +-0; inf and NaN stay so)
-__device__ __forceinline__ double dbl_of_bits(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned ex = (u >> 23) & 0xffu;
-  const unsigned sign = u & 0x80000000u;
-  if (ex == 0) return __hiloint2double((int)sign, 0);
-  const unsigned e64 = ex == 0xffu ? 0x7ffu : ex + 896u;
-  return __hiloint2double((int)(sign | (e64 << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
-}
 
 template <class T>
 struct Num;
@@ -137,7 +62,7 @@ struct Num<double> {
 template <>
 struct Num<Dfl> {
   __device__ static Dfl from(double x) { return dfl_of(x); }
-  __device__ static double to(Dfl x) { return dbl_of_bits(x.hi) + dbl_of_bits(x.lo); }  // one FP64 add
+  __device__ static double to(Dfl x) { return dbl_of(x); }  // one FP64 add
   __device__ static Dfl half(Dfl x) { return {0.5f * x.hi, 0.5f * x.lo}; }
   __device__ static Dfl twice(Dfl x) { return {x.hi + x.hi, x.lo + x.lo}; }
   __device__ static Dfl zero() { return {0.f, 0.f}; }
@@ -161,6 +86,11 @@ __device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
 }
 template <class T>
 __device__ __forceinline__ Cx<T> conj(Cx<T> a) { return {a.x, -a.y}; }
+// renormalised (double-float): the passes store normalised elements
+__device__ __forceinline__ Cx<double> norm(Cx<double> a) { return a; }
+__device__ __forceinline__ Cx<Dfl> norm(Cx<Dfl> a) {
+  return {quick_two_sum(a.x.hi, a.x.lo), quick_two_sum(a.y.hi, a.y.lo)};
+}
 // -i * a and +i * a
 template <class T>
 __device__ __forceinline__ Cx<T> mul_mi(Cx<T> a) { return {a.y, -a.x}; }
@@ -182,15 +112,18 @@ __device__ __forceinline__ Cx<T> root(const Cx<T>* w, int m) {
 }
 
 // One butterfly of a Stockham stage: inputs a[j + r nb] (r < R), each times
-// its twiddle omega_n^(r k tstep) when tw (ns > 1), outputs b[o + s ns].
+// its twiddle omega_n^(r k tstep) when tw (ns > 1), outputs b[o + s ns].  In
+// double-float the outputs are left unnormalised (a stage's sums feed the
+// next stage's sums and FMA-based products, which take them as they are);
+// the passes renormalise what they store.
 template <class T, bool INV>
 __device__ __forceinline__ void bfly2(const Cx<T>* a, Cx<T>* b, int j, int nb, int o, int ns, bool tw, int m,
                                       const Cx<T>* w) {
   const Cx<T> v0 = a[j];
   Cx<T> v1 = a[j + nb];
   if (tw) v1 = cmul(v1, root<T, INV>(w, m));
-  b[o] = v0 + v1;
-  b[o + ns] = v0 - v1;
+  b[o] = cadd_l(v0, v1);
+  b[o + ns] = csub_l(v0, v1);
 }
 
 template <class T, bool INV>
@@ -205,10 +138,10 @@ __device__ __forceinline__ void bfly4(const Cx<T>* a, Cx<T>* b, int j, int nb, i
   }
   const Cx<T> t0 = cadd_l(v0, v2), t1 = csub_l(v0, v2), t2 = cadd_l(v1, v3), t3 = csub_l(v1, v3);
   const Cx<T> r3 = INV ? mul_pi(t3) : mul_mi(t3);  // omega_4 * t3
-  b[o] = t0 + t2;
-  b[o + ns] = t1 + r3;
-  b[o + 2 * ns] = t0 - t2;
-  b[o + 3 * ns] = t1 - r3;
+  b[o] = cadd_l(t0, t2);
+  b[o + ns] = cadd_l(t1, r3);
+  b[o + 2 * ns] = csub_l(t0, t2);
+  b[o + 3 * ns] = csub_l(t1, r3);
 }
 
 template <class T, bool INV>
@@ -225,9 +158,9 @@ __device__ __forceinline__ void bfly3(const Cx<T>* a, Cx<T>* b, int j, int nb, i
   const Cx<T> t = cadd_l(v1, v2), d = csub_l(v1, v2);
   const Cx<T> mm = csub_l(v0, Cx<T>{Num<T>::half(t.x), Num<T>::half(t.y)});
   const Cx<T> q = scale(INV ? mul_mi(d) : mul_pi(d), s);  // -+ i sqrt(3)/2 * d
-  b[o] = v0 + t;
-  b[o + ns] = mm + q;
-  b[o + 2 * ns] = mm - q;
+  b[o] = cadd_l(v0, t);
+  b[o + ns] = cadd_l(mm, q);
+  b[o + 2 * ns] = csub_l(mm, q);
 }
 
 // radix 5: with t1 = v1 + v4, t2 = v2 + v3, t3 = v1 - v4, t4 = v2 - v3,
@@ -253,11 +186,11 @@ __device__ __forceinline__ void bfly5(const Cx<T>* a, Cx<T>* b, int j, int nb, i
   const Cx<T> b1 = {dot2(s1, t3.x, s2, t4.x), dot2(s1, t3.y, s2, t4.y)};
   const Cx<T> b2 = {dot2(s2, t3.x, -s1, t4.x), dot2(s2, t3.y, -s1, t4.y)};
   const Cx<T> ib1 = INV ? mul_pi(b1) : mul_mi(b1), ib2 = INV ? mul_pi(b2) : mul_mi(b2);
-  b[o] = v0 + cadd_l(t1, t2);
-  b[o + ns] = a1 + ib1;
-  b[o + 4 * ns] = a1 - ib1;
-  b[o + 2 * ns] = a2 + ib2;
-  b[o + 3 * ns] = a2 - ib2;
+  b[o] = cadd_l(v0, cadd_l(t1, t2));
+  b[o + ns] = cadd_l(a1, ib1);
+  b[o + 4 * ns] = csub_l(a1, ib1);
+  b[o + 2 * ns] = cadd_l(a2, ib2);
+  b[o + 3 * ns] = csub_l(a2, ib2);
 }
 
 // any other radix: the twiddles applied in place (the lane owns these
@@ -487,7 +420,7 @@ __global__ void __launch_bounds__(256, 4) fft_cols_kernel(const __grid_constant_
   const int passes = MODE == 2 ? 2 * nfac : nfac;
   const size_t res = (passes & 1) ? (size_t)n : 0;
   if (live)
-    for (int e = threadIdx.x / W; e < n; e += rows) spec[base + e * estride] = bufs[(size_t)col * S + res + e];
+    for (int e = threadIdx.x / W; e < n; e += rows) spec[base + e * estride] = norm(bufs[(size_t)col * S + res + e]);
 }
 
 // Shared-memory budget of a pass 2-4 block: four blocks per SM.

@@ -126,6 +126,68 @@ __device__ __forceinline__ void lsda_ca(double up, double dn, double& exc, doubl
   vd = v + t0 * (-1 - zeta) * dfz;
 }
 
+// LSDA_CA in double-float for the precision forms (as lda_ca_df): the same
+// expressions, zeta from a refined reciprocal, (1 +- zeta)^(1/3) as
+// x rcbrt(x)^2, the rs < 1 logarithm in FP64, the results rounded to FP64
+// once.
+__device__ __forceinline__ void lsda_ca_df(double up, double dn, double& exc, double& vu, double& vd) {
+  const double tden = up + dn;
+  const double min_den = 1e-15;
+  if (tden <= min_den) {
+    exc = vu = vd = 0.0;
+    return;
+  }
+  const Dfl T = dfl_of(tden);
+  Dfl zeta = dfl_of(up - dn) * dfl_rcp(T);
+  if (!(zeta < 1.0f) && !(zeta.hi == 1.0f && zeta.lo == 0.0f)) zeta = dflc(1 - min_den);
+  if (zeta < -1.0f) zeta = dflc(-1 + min_den);
+  const Dfl rs = dfl_rcbrt(T) * dflc(0.6203504908994);
+  const Dfl irs = dfl_rcp(rs);
+  const Dfl tmp0 = irs * dflc(0.458165293632163);
+  const Dfl ExP = -tmp0, dExP = tmp0 * irs;
+  const Dfl ExF = ExP * dflc(1.25992104989487), dExF = dExP * dflc(1.25992104989487);
+  Dfl EcP, dEcP, EcF, dEcF;
+  if (!(rs < 1.0f)) {
+    const Dfl it = dfl_rsqrt(rs), t = rs * it;
+    Dfl idum = dfl_rcp(dflc(1.0) + dot2(dflc(1.0529), t, dflc(0.3334), rs));
+    Dfl t1 = idum * dflc(0.1423);
+    EcP = -t1;
+    dEcP = (t1 * idum) * dot2(dflc(0.52645), it, dflc(1.0), dflc(0.3334));
+    idum = dfl_rcp(dflc(1.0) + dot2(dflc(1.3981), t, dflc(0.2611), rs));
+    t1 = idum * dflc(0.0843);
+    EcF = -t1;
+    dEcF = (t1 * idum) * dot2(dflc(0.69905), it, dflc(1.0), dflc(0.2611));
+  } else {
+    const Dfl lr = dfl_of(log(dbl_of(rs)));
+    EcP = dflc(-0.0480) + dot2(dflc(0.0311), lr, rs, dot2(dflc(0.0020), lr, dflc(1.0), dflc(-0.0116)));
+    dEcP = dot2(dflc(0.0311), irs, dflc(0.0020), lr) + dflc(-0.0096);
+    EcF = dflc(-0.0269) + dot2(dflc(0.01555), lr, rs, dot2(dflc(0.0007), lr, dflc(1.0), dflc(-0.0048)));
+    dEcF = dot2(dflc(0.01555), irs, dflc(0.0007), lr) + dflc(-0.0041);
+  }
+  const Dfl p1 = dflc(1.0) + zeta, m1 = dflc(1.0) - zeta;
+  const Dfl y0 = dfl_rcbrt(p1), y1 = dfl_rcbrt(m1);
+  const Dfl z0 = p1 * (y0 * y0), z1 = m1 * (y1 * y1);  // (1 +- zeta)^(1/3)
+  const Dfl z02 = z0 * z0, z04 = z02 * z02, z12 = z1 * z1, z14 = z12 * z12;
+  const Dfl t0 = (ExF + EcF) - (ExP + EcP);
+  // switch 0 uses (1 +- zeta)^(4/3) directly
+  const Dfl fz0 = (dot2(p1, z0, m1, z1) - dflc(2.0)) * dflc(1.92366105093154);
+  exc = dbl_of((ExP + EcP) + t0 * fz0);
+  const Dfl fz = ((z04 + z14) - dflc(2.0)) * dflc(1.92366105093154);
+  const Dfl dfz = (z0 - z1) * dflc(2.56488140124205);
+  const Dfl e1 = (ExP + EcP) + t0 * fz;
+  const Dfl de = (dExP + dEcP) + ((dExF + dEcF) - (dExP + dEcP)) * fz;
+  const Dfl v = e1 - rs * de * dflc(1.0 / 3.0);
+  const Dfl tz = t0 * dfz;
+  vu = dbl_of(v + tz * m1);
+  vd = dbl_of(v - tz * p1);
+}
+
+template <bool DF>
+__device__ __forceinline__ void lsda_eval(double up, double dn, double& exc, double& vu, double& vd) {
+  if (DF) lsda_ca_df(up, dn, exc, vu, vd);
+  else lsda_ca(up, dn, exc, vu, vd);
+}
+
 struct XcArgs {
   int xc, spinpol;
   int64_t nn;
@@ -352,6 +414,8 @@ __global__ void __launch_bounds__(kRedThreads) poisson_scale_g_kernel(const __gr
 // xc_vpot_kernel) and the energy-term partial sums (as
 // energy_partials_kernel, over the same tiles in the same order, so the sums
 // are the same bits), evaluating the xc functional once per point.
+// DF: the functional in double-float (the precision forms), FP64 otherwise.
+template <bool DF>
 __global__ void __launch_bounds__(kRedThreads) xc_vpot_energy_g_kernel(const __grid_constant__ GridArgs a) {
   int64_t t;
   const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
@@ -364,20 +428,20 @@ __global__ void __launch_bounds__(kRedThreads) xc_vpot_energy_g_kernel(const __g
     double v[2] = {0, 0};
     double e, r1 = 0.0;
     if (a.xc == LCP_XC_LDA) {
-      lda_ca(2 * (r0 + pc), e, v[0]);
+      lda_eval<DF>(2 * (r0 + pc), e, v[0]);
     } else {
       r1 = c.rho[1][x];
-      lsda_ca(r0 + pc, r1 + pc, e, v[0], v[1]);
+      lsda_eval<DF>(r0 + pc, r1 + pc, e, v[0], v[1]);
     }
     if (c.dvh) {
       const double dvh = c.dvh[x];
       const double na = c.vna ? c.vna[x] : 0.0;
       for (int s = 0; s < nv; ++s) c.vpot[s][x] = dvh + v[s] + na;
-      energy_terms(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, dvh, e, acc);
+      energy_terms<DF>(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, dvh, e, acc);
     } else {
       // ahead of the Hartree potential: vxc only, the E_H1 term left to vpot_eh_g_kernel
       for (int s = 0; s < nv; ++s) c.vpot[s][x] = v[s];
-      energy_terms(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, 0.0, e, acc);
+      energy_terms<DF>(a.xc, a.spinpol, r0, r1, c.aden ? c.aden[x] : 0.0, pc, 0.0, e, acc);
     }
   }
   block_reduce_store<3>(acc, c.part + t * 3);
@@ -595,10 +659,39 @@ cudaError_t launch_poisson_scale_g(const GridCell& c0, const GridBatch& b, cudaS
   return cudaGetLastError();
 }
 
-cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, cudaStream_t st) {
+cudaError_t launch_xc_vpot_energy_g(int xc, int spinpol, const GridCell& c0, const GridBatch& b, bool dfl,
+                                    cudaStream_t st) {
   const unsigned n = tiled_blocks(b, red_tiles(c0.nn));
   if (n == 0) return cudaSuccess;
-  xc_vpot_energy_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, b, xc, spinpol, 0));
+  if (dfl)
+    xc_vpot_energy_g_kernel<true><<<n, kRedThreads, 0, st>>>(grid_args(c0, b, xc, spinpol, 0));
+  else
+    xc_vpot_energy_g_kernel<false><<<n, kRedThreads, 0, st>>>(grid_args(c0, b, xc, spinpol, 0));
+  return cudaGetLastError();
+}
+
+// Per point: the LDA (xc LCP_XC_LDA, density 2 (up + pcc)) or LSDA functional
+// in FP64 or double-float: out[3 x] = exc, out[3 x + 1..2] = vxc (up, down).
+template <bool DF>
+__global__ void xc_selftest_kernel(int xc, int64_t nn, const double* up, const double* dn, const double* pcc,
+                                   double* out) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nn; x += (int64_t)gridDim.x * blockDim.x) {
+    const double pc = pcc ? pcc[x] : 0.0;
+    double e, v0, v1 = 0.0;
+    if (xc == LCP_XC_LDA) lda_eval<DF>(2 * (up[x] + pc), e, v0);
+    else lsda_eval<DF>(up[x] + pc, dn[x] + pc, e, v0, v1);
+    out[3 * x] = e;
+    out[3 * x + 1] = v0;
+    out[3 * x + 2] = v1;
+  }
+}
+
+cudaError_t launch_xc_selftest(int xc, bool dfl, int64_t nn, const double* up, const double* dn, const double* pcc,
+                               double* out, cudaStream_t st) {
+  if (nn <= 0) return cudaSuccess;
+  const unsigned g = grid_blocks(nn, 256);
+  if (dfl) xc_selftest_kernel<true><<<g, 256, 0, st>>>(xc, nn, up, dn, pcc, out);
+  else xc_selftest_kernel<false><<<g, 256, 0, st>>>(xc, nn, up, dn, pcc, out);
   return cudaGetLastError();
 }
 

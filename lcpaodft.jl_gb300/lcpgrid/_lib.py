@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_HERE, "liblcpgrid_check.so" if os.environ.get("LCPGRID_
                         else "liblcpgrid.so")
 
 LCP_OK, LCP_EINVAL, LCP_ENOMEM, LCP_EDEVICE, LCP_ETIMEDOUT, LCP_ENOTSUP, LCP_ESTATE = range(7)
+LCP_XC_LDA, LCP_XC_LSDA, LCP_XC_GGA_PBE = range(3)
 SPIN = {"off": 0, "on": 1, "nc": 2}
 NCHAN = {"off": 1, "on": 2, "nc": 4}
 XC = {"LDA": 0, "LSDA": 1, "GGA_PBE": 2}
@@ -143,6 +144,7 @@ _SIGS = {
     "lcp_probe_fp64_tflops": ([_vp, _pd], _i32),
     "lcp_tc_selftest": ([_vp, _i32, _i32, _i32, _i32, _i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                         _i32),
+    "lcp_xc_selftest": ([_vp, _i32, _i32, _i64, _pd, _pd, _pd, _pd], _i32),
 }
 
 for _name, (_args, _res) in _SIGS.items():
