@@ -472,6 +472,15 @@ lcp_status lcp_orbs_timings(const lcp_orbs* orbs, double* out2);
  * Off (0, 0) by default; set it back to (0, 0) to run normally. */
 lcp_status lcp_ctx_set_fault_test(lcp_ctx* ctx, uint32_t poll_limit, int32_t stall);
 
+/* The arithmetic of this context's drop-in GGA-PBE entry points
+ * (lcp_set_xc_grid_gga, lcp_calc_exc1_gga): 0 = FP64, the reference's (the
+ * default); 1 = double-float on the FP32 pipe with FP64 sums, as the
+ * precision forms' grid step evaluates GGA-PBE (about 2^-44 relative to
+ * FP64).  The grid step follows its precision form
+ * whatever this says.  Replaces nothing of the reference (an option of this
+ * library, src/XC/XC_PBE.jl:187-476, src/XC/GGA_PBE.jl:53-462). */
+lcp_status lcp_ctx_set_xc_arithmetic(lcp_ctx* ctx, int32_t double_float);
+
 /* The check build (liblcpgrid_check.so, compiled with LCP_BOUNDS_CHECK) tests
  * every index the pair and tensor-core kernels gather with (lens entries,
  * sphere-list grid indices, DM/H block offsets, split-D pair indices, table

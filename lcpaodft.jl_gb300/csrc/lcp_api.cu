@@ -1182,7 +1182,7 @@ lcp_status lcp_set_xc_grid_gga(lcp_ctx* ctx, int32_t spinpol, const int32_t* ngr
     if (!vxc_grid[k]) return fail(LCP_EINVAL, "NULL channel");
   lcp::GridCell c;
   if ((s = gga_cell_host(ctx, spinpol, ngrid, diff_coef, pcc, density_grid, ddensity_grid != nullptr, c))) return s;
-  API_CUDA(lcp::launch_gga_g(spinpol, c, lcp::GridBatch{}, true, ctx->stream), "gga");
+  API_CUDA(lcp::launch_gga_g(spinpol, c, lcp::GridBatch{}, true, ctx->xc_dfl != 0, ctx->stream), "gga");
   ctx->launches += 2;
   if (spinpol == LCP_SPIN_NC) {
     for (int k = 2; k < 4; ++k) API_CUDA(ctx->w_out[k].ensure(nn * sizeof(double)), "alloc");
@@ -1339,7 +1339,7 @@ lcp_status lcp_calc_exc1_grid(lcp_ctx* ctx, int32_t xc, int32_t spinpol, const i
   API_CUDA(ctx->w_scal.ensure(16 * sizeof(double)), "alloc");
   c.part = ctx->w_part.as<double>();
   c.sums = ctx->w_scal.as<double>();
-  API_CUDA(lcp::launch_gga_g(sp, c, lcp::GridBatch{}, false, ctx->stream), "gga energy");
+  API_CUDA(lcp::launch_gga_g(sp, c, lcp::GridBatch{}, false, ctx->xc_dfl != 0, ctx->stream), "gga energy");
   API_CUDA(lcp::launch_grid_sums_g(c, lcp::GridBatch{}, ctx->stream), "gga energy sums");
   ctx->launches += 2;
   double out[3];
@@ -1479,7 +1479,7 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   const int32_t sp_xc = job->spinpol == LCP_SPIN_NC ? LCP_SPIN_ON : job->spinpol;
   auto xc_pass = [&](const lcp::GridCell& c, cudaStream_t xs) -> lcp_status {
     if (job->xc == LCP_XC_GGA_PBE) {
-      API_CUDA(lcp::launch_gga_g(sp_xc, c, one, true, xs), "gga");
+      API_CUDA(lcp::launch_gga_g(sp_xc, c, one, true, ctx->precision != LCP_PREC_FP64, xs), "gga");
       ctx->launches += 2;
     } else {
       API_CUDA(lcp::launch_xc_vpot_energy_g(job->xc, sp_xc, c, one, ctx->precision != LCP_PREC_FP64, xs),
@@ -1750,6 +1750,14 @@ lcp_status lcp_ctx_set_fault_test(lcp_ctx* ctx, uint32_t poll_limit, int32_t sta
   if (stall < 0 || stall > 1) return fail(LCP_EINVAL, "stall is 0 or 1");
   ctx->fault_poll = poll_limit;
   ctx->fault_stall = stall;
+  return LCP_OK;
+}
+
+lcp_status lcp_ctx_set_xc_arithmetic(lcp_ctx* ctx, int32_t double_float) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (double_float < 0 || double_float > 1) return fail(LCP_EINVAL, "double_float is 0 or 1");
+  ctx->xc_dfl = double_float;
   return LCP_OK;
 }
 

@@ -106,6 +106,7 @@ struct lcp_ctx {
   // failure-path tests only (lcp_ctx_set_fault_test): the split-BF16 density
   // kernel's poll limit (0: its default) and its stall switch
   uint32_t fault_poll = 0;
+  int32_t xc_dfl = 0;  // drop-in GGA-PBE entry points in double-float (lcp_ctx_set_xc_arithmetic)
   int32_t fault_stall = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ~lcp_ctx() {

@@ -164,7 +164,7 @@ lcp_status record_step(lcp_batch* b, cudaStream_t st, cudaEvent_t* ev = nullptr)
   // 3./4. xc + potential + energy partials, then the per-cell sums
   mark(2);
   if (b->xc == LCP_XC_GGA_PBE)
-    API_CUDA(lcp::launch_gga_g(b->spinpol, gnone, pts, true, st), "batch gga");
+    API_CUDA(lcp::launch_gga_g(b->spinpol, gnone, pts, true, true, st), "batch gga");
   else
     API_CUDA(lcp::launch_xc_vpot_energy_g(b->xc, b->spinpol, gnone, pts, true, st), "batch xc");
   mark(3);

@@ -217,7 +217,8 @@ cudaError_t launch_vpot_eh_g(int spinpol, const GridCell& c0, const GridBatch& b
 // (+ energy tile partials where part is set), then, if potential, the
 // divergence term and, where dvh is set, vpot = dVHart + vxc + V_na (without
 // dvh, vpot receives vxc).  spinpol "off" or "on".
-cudaError_t launch_gga_g(int spinpol, const GridCell& c0, const GridBatch& b, bool potential, cudaStream_t st);
+cudaError_t launch_gga_g(int spinpol, const GridCell& c0, const GridBatch& b, bool potential, bool dfl,
+                         cudaStream_t st);
 // "nc": diagonalize_nc_density! in place, (Re11, Re22, Re12, Im12) -> (Nup,
 // Ndown, theta, phi), and the rotation of collinear potentials (vu, vd) into
 // the four channels by the local angles; out[0..1] may be vu/vd.  sign3 is the

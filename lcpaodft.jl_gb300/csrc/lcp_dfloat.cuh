@@ -91,6 +91,54 @@ __device__ __forceinline__ Dfl dfl_rcbrt(Dfl x) {
   return quick_two_sum(y0, y0 * (r * (1.0f / 3.0f)));
 }
 
+// cube root of x >= 0 as x rcbrt(x)^2, and 0 for 0
+__device__ __forceinline__ Dfl dfl_cbrt(Dfl x) {
+  if (x.hi == 0.0f) return {0.0f, 0.0f};
+  const Dfl y = dfl_rcbrt(x);
+  return x * (y * y);
+}
+
+// expm1(x): x = k ln2 + r with k = round(x / ln2) and r in double-float
+// (|r| <= 0.35), expm1(r / 16) by its Taylor series (the terms from y^4 on in
+// FP32, where they stay below 1e-8 of y), four doublings expm1(2y) =
+// expm1(y) (expm1(y) + 2), which keep the relative error, then
+// 2^k (expm1(r) + 1) - 1.  Relative error about (1 + |x|) 2^-47, the
+// conditioning of x's own double-float rounding.  |x| > 80 goes to FP64.
+__device__ __forceinline__ Dfl dfl_expm1(Dfl x) {
+  if (fabsf(x.hi) > 80.0f) {
+    const double v = expm1((double)x.hi + (double)x.lo);
+    const float h = (float)v;
+    return {h, (float)(v - (double)h)};
+  }
+  const Dfl ln2 = dflc(0.6931471805599453);
+  const float k = rintf(x.hi * 1.4426950408889634f);
+  const float p = k * ln2.hi;
+  const Dfl r = x - quick_two_sum(p, fmaf(k, ln2.lo, fmaf(k, ln2.hi, -p)));
+  const Dfl y = {r.hi * 0.0625f, r.lo * 0.0625f};
+  const float yh = y.hi;
+  const float T = fmaf(yh, fmaf(yh, fmaf(yh, fmaf(yh, fmaf(yh, 1.0f / 362880.0f, 1.0f / 40320.0f), 1.0f / 5040.0f),
+                                        1.0f / 720.0f), 1.0f / 120.0f), 1.0f / 24.0f);
+  const Dfl q = dflc(1.0 / 6.0) + y * T;
+  const Dfl r2 = dflc(0.5) + y * q;
+  Dfl e = y + (y * y) * r2;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) e = e * (e + dflc(2.0));
+  if (k == 0.0f) return e;
+  const float sc = __uint_as_float((unsigned)(127 + (int)k) << 23);  // 2^k, |k| <= 116
+  const Dfl s1 = e + dflc(1.0);
+  return Dfl{s1.hi * sc, s1.lo * sc} - dflc(1.0);
+}
+// log(u) from an FP32 estimate y0 by one Newton step on exp(y) = u in
+// double-float: y = y0 + ((u - 1) + u expm1(-y0)), with u and u - 1 both
+// given accurately (so log1p keeps its precision near 0 and log near 1).
+__device__ __forceinline__ Dfl log_newton(float y0, Dfl u, Dfl um1) {
+  return Dfl{y0, 0.0f} + (um1 + u * dfl_expm1(Dfl{-y0, 0.0f}));
+}
+// log1p(x) for x > -1 and log(x) for x > 0; relative error about 2^-45 for
+// the arguments of this library (|log| < 10)
+__device__ __forceinline__ Dfl dfl_log1p(Dfl x) { return log_newton(log1pf(x.hi), x + dflc(1.0), x); }
+__device__ __forceinline__ Dfl dfl_log(Dfl x) { return log_newton(logf(x.hi), x, x - dflc(1.0)); }
+
 // FP64 <-> double-float on the integer and FP32 pipes.
 // dfl_of: hi is x cut to 24 significant bits, lo the other 29 bits rounded
 // to nearest FP32 (|lo| < ulp(hi), about 48 bits in all).  |x| below 2^-60

@@ -43,11 +43,11 @@ __device__ __forceinline__ void lda_ca(double den, double& exc, double& vxc) {
 }
 
 // The same functional in double-float for the precision forms: rs from the
-// Newton-refined reciprocal cube root, the reciprocals and the square root
-// refined the same way, the logarithm of the rs < 1 branch (the densest
-// points) in FP64, the results rounded to FP64 once.  It agrees with the FP64
-// evaluation to about 2^-45 relative and issues a handful of FP64
-// instructions instead of about a hundred.
+// Newton-refined reciprocal cube root, the reciprocals, the square root and
+// the logarithm of the rs < 1 branch refined the same way (lcp_dfloat.cuh),
+// the results rounded to FP64 once.  It agrees with the FP64 evaluation to
+// about 2^-45 relative and issues a few FP64 instructions (conversions back,
+// the density test) instead of about a hundred.
 __device__ __forceinline__ void lda_ca_df(double den, double& exc, double& vxc) {
   if (den <= 1e-15) {
     exc = 0.0;
@@ -67,7 +67,7 @@ __device__ __forceinline__ void lda_ca_df(double den, double& exc, double& vxc) 
     Ec = -t1;
     dEc = (t1 * idum) * dot2(dflc(0.52645), it, dflc(1.0), dflc(0.3334));
   } else {
-    const Dfl lr = dfl_of(log(dbl_of(rs)));
+    const Dfl lr = dfl_log(rs);
     Ec = dflc(-0.0480) + dot2(dflc(0.0311), lr, rs, dot2(dflc(0.0020), lr, dflc(1.0), dflc(-0.0116)));
     dEc = dot2(dflc(0.0311), irs, dflc(0.0020), lr) + dflc(-0.0096);
   }

@@ -127,9 +127,10 @@ __device__ __forceinline__ void lsda_ca(double up, double dn, double& exc, doubl
 }
 
 // LSDA_CA in double-float for the precision forms (as lda_ca_df): the same
-// expressions, zeta from a refined reciprocal, (1 +- zeta)^(1/3) as
-// x rcbrt(x)^2, the rs < 1 logarithm in FP64, the results rounded to FP64
-// once.
+// expressions, zeta from a refined reciprocal (exactly +-1 when a spin is
+// empty), 1 +- zeta as 2 up / tden and 2 dn / tden, (1 +- zeta)^(1/3) as
+// x rcbrt(x)^2, the rs < 1 logarithm in double-float, the results rounded to
+// FP64 once.
 __device__ __forceinline__ void lsda_ca_df(double up, double dn, double& exc, double& vu, double& vd) {
   const double tden = up + dn;
   const double min_den = 1e-15;
@@ -137,10 +138,19 @@ __device__ __forceinline__ void lsda_ca_df(double up, double dn, double& exc, do
     exc = vu = vd = 0.0;
     return;
   }
-  const Dfl T = dfl_of(tden);
-  Dfl zeta = dfl_of(up - dn) * dfl_rcp(T);
-  if (!(zeta < 1.0f) && !(zeta.hi == 1.0f && zeta.lo == 0.0f)) zeta = dflc(1 - min_den);
-  if (zeta < -1.0f) zeta = dflc(-1 + min_den);
+  const Dfl T = dfl_of(tden), iT = dfl_rcp(T);
+  const Dfl U2 = dfl_of(up) * 2.0f, D2 = dfl_of(dn) * 2.0f;
+  // one spin empty: zeta is exactly +-1, as the FP64 division gives it
+  Dfl zeta = dn == 0.0 ? dflc(1.0) : (up == 0.0 ? dflc(-1.0) : dfl_of(up - dn) * iT);
+  bool clamped = false;
+  if (!(zeta < 1.0f) && !(zeta.hi == 1.0f && zeta.lo == 0.0f)) {
+    zeta = dflc(1 - min_den);
+    clamped = true;
+  }
+  if (zeta < -1.0f) {
+    zeta = dflc(-1 + min_den);
+    clamped = true;
+  }
   const Dfl rs = dfl_rcbrt(T) * dflc(0.6203504908994);
   const Dfl irs = dfl_rcp(rs);
   const Dfl tmp0 = irs * dflc(0.458165293632163);
@@ -158,15 +168,16 @@ __device__ __forceinline__ void lsda_ca_df(double up, double dn, double& exc, do
     EcF = -t1;
     dEcF = (t1 * idum) * dot2(dflc(0.69905), it, dflc(1.0), dflc(0.2611));
   } else {
-    const Dfl lr = dfl_of(log(dbl_of(rs)));
+    const Dfl lr = dfl_log(rs);
     EcP = dflc(-0.0480) + dot2(dflc(0.0311), lr, rs, dot2(dflc(0.0020), lr, dflc(1.0), dflc(-0.0116)));
     dEcP = dot2(dflc(0.0311), irs, dflc(0.0020), lr) + dflc(-0.0096);
     EcF = dflc(-0.0269) + dot2(dflc(0.01555), lr, rs, dot2(dflc(0.0007), lr, dflc(1.0), dflc(-0.0048)));
     dEcF = dot2(dflc(0.01555), irs, dflc(0.0007), lr) + dflc(-0.0041);
   }
-  const Dfl p1 = dflc(1.0) + zeta, m1 = dflc(1.0) - zeta;
-  const Dfl y0 = dfl_rcbrt(p1), y1 = dfl_rcbrt(m1);
-  const Dfl z0 = p1 * (y0 * y0), z1 = m1 * (y1 * y1);  // (1 +- zeta)^(1/3)
+  // 1 +- zeta as 2 up / tden and 2 dn / tden (no cancellation near full
+  // polarisation), from the clamped zeta where a negative spin density pushed it past 1
+  const Dfl p1 = clamped ? dflc(1.0) + zeta : U2 * iT, m1 = clamped ? dflc(1.0) - zeta : D2 * iT;
+  const Dfl z0 = dfl_cbrt(p1), z1 = dfl_cbrt(m1);  // (1 +- zeta)^(1/3)
   const Dfl z02 = z0 * z0, z04 = z02 * z02, z12 = z1 * z1, z14 = z12 * z12;
   const Dfl t0 = (ExF + EcF) - (ExP + EcP);
   // switch 0 uses (1 +- zeta)^(4/3) directly

@@ -70,6 +70,12 @@ class Context:
         and unwinds; the call raises LCPError LCP_ETIMEDOUT)."""
         check(lib.lcp_ctx_set_fault_test(self._h, int(poll_limit), int(stall)))
 
+    def set_xc_arithmetic(self, double_float):
+        """Arithmetic of this context's drop-in GGA-PBE calls (Set_XC_Grid,
+        Calc_EXC1 with an XC_Func "GGA_PBE"): False = FP64 (default), True =
+        double-float as the precision forms' grid step."""
+        check(lib.lcp_ctx_set_xc_arithmetic(self._h, int(bool(double_float))))
+
     @property
     def launch_count(self):
         return int(lib.lcp_ctx_launch_count(self._h))
