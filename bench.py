@@ -33,8 +33,13 @@ METRIC = "ms per SCF grid step & jobs/s (p50/p99) split-BF16 vs FP64, <=1uHa/ato
 # DRAM bytes per table block of one split-BF16 stage launch (ncu, 8-atom 48^3
 # cell: density_tc_kernel 149.7 + 3.3 MB; hamiltonian_tc_kernel 150.1 + 55.9 MB
 # and h_reduce_kernel 93.6 + 3.2 MB, over 12076 blocks)
-TRAFFIC_PER_BLOCK = {"density": (149.71e6 + 3.85e6) / 12076,
-                     "hamiltonian": (150.05e6 + 56.28e6 + 93.62e6 + 3.18e6) / 12076}
+# DRAM bytes (read + write) per table block of a stage's big kernels, from
+# one ncu capture of the 64-atom 96^3 cell (96,608 table blocks): the density
+# kernel 1,199.0 + 9.4 MB; the H kernel 1,199.9 + 702.5 MB and the
+# partial-block reduction 656.1 + 5.0 MB
+TRAFFIC_BLOCKS = 96608
+TRAFFIC_PER_BLOCK = {"density": (1199.03e6 + 9.38e6) / TRAFFIC_BLOCKS,
+                     "hamiltonian": (1199.94e6 + 702.50e6 + 656.07e6 + 5.00e6) / TRAFFIC_BLOCKS}
 UNIT = "grid steps/s"
 
 
@@ -598,21 +603,26 @@ def run_ours(args):
         roof = {"bound": "tensor", "kernel": names[dom], "achieved": dom_flops / (stages[dom] * 1e-3) / 1e12,
                 "peak": pk, "unit": "TFLOP/s", "peak_source": psrc + " bf16_tflops_sustained", "traffic": None}
         if args.precision == "bf16x3":
-            # DRAM bytes (read + write) per launch of the stage's kernels, measured
-            # with ncu on the 8-atom cell of the same crystal and grid spacing and
-            # scaled by table blocks (every brick image is one block)
+            # DRAM bytes (read + write) per launch of the stage's big kernels,
+            # measured with ncu on the 64-atom cell and scaled by table blocks
+            # (every brick image is one block)
             per_block = TRAFFIC_PER_BLOCK.get(names[dom])
             nblocks = u.brick_info()["blocks"]
             if per_block is not None:
                 roof["traffic"] = per_block * nblocks
-                roof["traffic_note"] = ("ncu dram__bytes_read+write on the 8-atom 48^3 cell (12076 table blocks), "
-                                        "scaled by table blocks (%d here); partial blocks that stay in L2 there "
-                                        "make it a lower bound" % nblocks)
-                roof["note"] = ("achieved counts the FP64 algorithm's flops (folded pairs, no padding).  The "
+                roof["traffic_gbs"] = roof["traffic"] / (stages[dom] * 1e-3) / 1e9
+                roof["traffic_frac_hbm"] = roof["traffic_gbs"] / peaks.get("hbm_gbs", 6800.0)
+                roof["traffic_note"] = (
+                    "ncu dram__bytes_read+write of the stage's tensor-core kernel (and for H the partial-block "
+                    "reduction), one capture of the 64-atom 96^3 cell (%d table blocks), scaled by table blocks "
+                    "(%d here).  The split tables (1.2 GB with the 13 -> 16 orbital and brick-slot padding) are read "
+                    "from DRAM once per kernel; the H kernel also writes 0.70 GB of partial blocks that the "
+                    "reduction reads back" % (TRAFFIC_BLOCKS, nblocks))
+                roof["note"] = ("achieved counts the FP64 algorithm's flops (folded pairs, no padding) over the "
+                                "stage time (for H: V weights + tensor-core kernel + partial-block reduction).  The "
                                 "split-BF16 form issues nine bf16 products per product (four MMAs with the B parts "
                                 "stacked along N) on 16-orbital blocks (13 used), so frac is bounded near 1/9 of "
-                                "that before padding; ncu shows the tensor pipe 42.9 % active in the H kernel and "
-                                "DRAM at 29 % on the 8-atom cell")
+                                "that before padding; the stage moves traffic_frac_hbm of the HBM peak")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     # tabulation and Poisson against the HBM roofline (algorithmic bytes:
@@ -781,11 +791,21 @@ def si2_section(args, steps=50):
 
 def emit(line):
     """Prints the JSON line on stdout, with its bulky lists (the brick-shape
-    autotune log) moved to a second line on stderr, and a compact summary of
-    every form's numbers as the line's last key."""
+    autotune log, the serving pool's per-structure lists) moved to lines on
+    stderr, and a compact summary of every form's numbers as the line's last
+    key."""
     bat = line.get("batching")
     if isinstance(bat, dict) and "autotune" in bat:
         print(json.dumps({"batching_autotune": bat.pop("autotune")}), file=sys.stderr)
+    srv = line.get("serving")
+    if isinstance(srv, dict):
+        side = {}
+        if isinstance(srv.get("pool_step_ms"), dict) and "per_structure" in srv["pool_step_ms"]:
+            side["pool_step_ms_per_structure"] = srv["pool_step_ms"].pop("per_structure")
+        if isinstance(srv.get("structures"), dict) and "atoms" in srv["structures"]:
+            side["structure_atoms"] = srv["structures"].pop("atoms")
+        if side:
+            print(json.dumps({"serving_lists": side}), file=sys.stderr)
     line["summary"] = summary(line)
     print(json.dumps(line))
 
@@ -802,6 +822,7 @@ def summary(line):
          "fp64": g(line, "fp64_dropin", "ms_per_step"), "fp32": g(line, "fp32_form", "ms_per_step"),
          "err_uHa_atom": g(line, "energy", "err_per_atom_uHa"), "max_dH": g(line, "energy", "max_abs_dH"),
          "max_drho": g(line, "energy", "max_abs_drho"), "roof_frac": g(line, "roofline", "frac"),
+         "roof_traffic_frac_hbm": g(line, "roofline", "traffic_frac_hbm"),
          "tab_ms": g(line, "tabulation", "kernel_ms"), "tab_frac": g(line, "tabulation", "frac"),
          "split_tab_ms": g(line, "tabulation", "split_tables_ms"), "split_tab_frac": g(line, "tabulation", "split_frac"),
          "poisson_ms": g(line, "poisson", "ms"), "poisson_frac": g(line, "poisson", "frac"),
