@@ -292,6 +292,13 @@ lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job);
  * pass), energy sums (their final reduction), grid H, <D,H> + job energy
  * (the stage names of the reference's TimerOutputs sections). */
 lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms);
+/* One split-BF16 step with CUDA events around its tensor-core kernels alone
+ * (synchronises): ms[0] = the density kernel's time summed over the spin
+ * channels, ms[1] = the grid-H kernel's, without the D symmetrisation, the V
+ * weights and the partial-block reduction around them.  LCP_ENOTSUP unless
+ * the context runs split-BF16.  Replaces nothing of the reference (a
+ * measurement of this library's kernels). */
+lcp_status lcp_job_tc_kernel_ms(lcp_ctx* ctx, lcp_job* job, double* ms);
 /* Energies of the last step: [E_H1, EXC1[1], EXC1[2], sum_s <D_s,H_s>, E_grid]. */
 lcp_status lcp_job_energies(lcp_ctx* ctx, lcp_job* job, double* out5);
 /* The energies without waiting: an asynchronous copy on the context's stream

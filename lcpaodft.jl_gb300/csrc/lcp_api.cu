@@ -234,10 +234,12 @@ lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, co
                               o->geom.numorbs, dm[c], ctx->w_dscale.as<double>(),
                               ctx->w_dsym.as<__nv_bfloat16>(), ctx->stream),
              "dsym");
+    if (ctx->tc_ev) API_CUDA(cudaEventRecord(ctx->tc_ev[2 * c], ctx->stream), "event");
     API_CUDA(lcp::launch_density_tc(o->bgeom, o->b_tab.as<__nv_bfloat16>(), o->phi_scale,
                                     ctx->w_dsym.as<__nv_bfloat16>(), ctx->w_dscale.as<double>(), (int)nsub, rho[c],
                                     ctx->w_status.as<int>(), ctx->stream, ctx->fault_poll, ctx->fault_stall),
              "density_tc");
+    if (ctx->tc_ev) API_CUDA(cudaEventRecord(ctx->tc_ev[2 * c + 1], ctx->stream), "event");
     ctx->launches += 4;
   }
   return LCP_OK;
@@ -286,7 +288,9 @@ lcp_status hamiltonian_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nch, 
     API_CUDA(lcp::launch_hamiltonian_tc(o->bgeom, o->b_tabslot.as<int32_t>(), o->b_slotbase.as<int64_t>(),
                                         o->b_tab.as<__nv_bfloat16>(), o->phi_scale, vpot[c], ctx->w_vw.as<float2>(),
                                         ctx->w_vscale.as<float>(), ctx->w_hscratch.as<float>(),
-                                        ctx->w_status.as<int>(), ctx->stream),
+                                        ctx->w_status.as<int>(), ctx->stream,
+                                        ctx->tc_ev ? ctx->tc_ev[8 + 2 * c] : nullptr,
+                                        ctx->tc_ev ? ctx->tc_ev[8 + 2 * c + 1] : nullptr),
              "hamiltonian_tc");
     API_CUDA(lcp::launch_h_reduce((int64_t)o->bricks.sb_fold.size(), o->b_redoff.as<int64_t>(),
                                   o->b_redslot.as<int64_t>(), o->b_sbfold.as<int32_t>(), o->b_sbchunks.as<int32_t>(),
@@ -1558,6 +1562,40 @@ lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms) {
     if (e != cudaSuccess) s = cuda_fail(e, "stage timing");
   }
   for (int k = 0; k < 7; ++k) cudaEventDestroy(ev[k]);
+  return s;
+}
+
+lcp_status lcp_job_tc_kernel_ms(lcp_ctx* ctx, lcp_job* job, double* out2) {
+  if (!out2) return fail(LCP_EINVAL, "NULL argument");
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (ctx->precision != LCP_PREC_BF16X3) return fail(LCP_ENOTSUP, "the tensor-core kernels run in split-BF16 only");
+  cudaEvent_t ev[16];
+  int made = 0;
+  for (; made < 16; ++made)
+    if (cudaEventCreate(&ev[made]) != cudaSuccess) break;
+  if (made < 16) {
+    for (int k = 0; k < made; ++k) cudaEventDestroy(ev[k]);
+    return fail(LCP_EDEVICE, "cudaEventCreate");
+  }
+  ctx->tc_ev = ev;
+  s = job_step_impl(ctx, job, nullptr);
+  ctx->tc_ev = nullptr;
+  double sum[2] = {0.0, 0.0};
+  if (s == LCP_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    const int nd = job->nspin, nh = job->spinpol == LCP_SPIN_NC ? 4 : job->nspin;
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+      for (int c = 0; c < (k ? nh : nd) && e == cudaSuccess; ++c) {
+        float ms = 0.f;
+        e = cudaEventElapsedTime(&ms, ev[8 * k + 2 * c], ev[8 * k + 2 * c + 1]);
+        sum[k] += ms;
+      }
+    if (e != cudaSuccess) s = cuda_fail(e, "tensor-core kernel timing");
+  }
+  for (int k = 0; k < 16; ++k) cudaEventDestroy(ev[k]);
+  out2[0] = sum[0];
+  out2[1] = sum[1];
   return s;
 }
 

@@ -109,6 +109,9 @@ struct lcp_ctx {
   int32_t xc_dfl = 0;  // drop-in GGA-PBE entry points in double-float (lcp_ctx_set_xc_arithmetic)
   int32_t fault_stall = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // lcp_job_tc_kernel_ms: events around the tensor-core kernels of one step
+  // (pairs [density spin 0..3][H channel 0..3]); null when not timing
+  cudaEvent_t* tc_ev = nullptr;
   ~lcp_ctx() {
     cudaSetDevice(device);
     if (ev_fork) cudaEventDestroy(ev_fork);

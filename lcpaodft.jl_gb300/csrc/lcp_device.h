@@ -317,7 +317,9 @@ cudaError_t launch_h_reduce_batch(int32_t ncells, const RedCell* cells, const in
 // releases so that the kernel times out and unwinds.
 cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st,
                                     uint32_t poll = 0, int32_t stall = 0);
-cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st);
+// ev_begin / ev_end (optional): recorded around the tensor-core kernel itself
+cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st,
+                                        cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
 cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsigned long long* tmp, double* scale,
                                 cudaStream_t st);
 // The split-BF16 tables from the FP64 tables: first_block[nimg] lists the
@@ -341,7 +343,8 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 // per-brick V weights); scratch: the FP32 partial blocks.
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
                                   const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
-                                  float* vscale, float* scratch, int* status, cudaStream_t st);
+                                  float* vscale, float* scratch, int* status, cudaStream_t st,
+                                  cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
 cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* red_slot, const int32_t* sb_fold,
                             const int32_t* sb_chunks, const float* scratch, const DevPairs& pr,
                             const int32_t* numorbs, double dv, double* H, cudaStream_t st);

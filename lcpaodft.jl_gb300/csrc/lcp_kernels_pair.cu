@@ -105,14 +105,23 @@ __global__ void __launch_bounds__(kPairThreads) density_pairs_kernel(DevGeom g, 
 
 // ---------------------------------------------------------------- grid H
 
-template <typename T, int NOMAX>
+// Per item (a 512-entry chunk of a pair's lens list) the block stages kTile
+// lens points at a time -- phi_i V (per channel) and phi_j, NOMAX orbitals
+// each -- into shared memory, and thread e accumulates entry (a, b) =
+// (e / NOMAX, e % NOMAX) over them.  The gathers of the next tile are issued
+// into registers before the current tile's FMAs, so their latency overlaps
+// the FP64 arithmetic; MAXC is the largest channel count the instance serves
+// (1 for SpinPol "off", else 4), so the spin-off case keeps only one V value
+// per staged entry in registers.
+template <typename T, int NOMAX, int MAXC>
 __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom g, DevPairs pr, int nch,
                                                                          const T* __restrict__ phi, Ptr4 vpot,
                                                                          MPtr4 hks) {
   constexpr int kSlots = (NOMAX * NOMAX + kPairThreads - 1) / kPairThreads;
+  constexpr int kStage = (kTile * NOMAX + kPairThreads - 1) / kPairThreads;  // staged entries per thread
   extern __shared__ unsigned char smem_raw[];
-  T* W = reinterpret_cast<T*>(smem_raw);           // [nch][kTile][NOMAX]
-  T* P = W + (size_t)4 * kTile * NOMAX;            // [kTile][NOMAX]
+  T* W = reinterpret_cast<T*>(smem_raw);           // [MAXC][kTile][NOMAX]
+  T* P = W + (size_t)MAXC * kTile * NOMAX;         // [kTile][NOMAX]
   for (int64_t item = blockIdx.x; item < pr.nitems; item += gridDim.x) {
     const int64_t q = pr.item_pair[item];
     const int i = pr.atom[q], j = pr.jatom[q];
@@ -122,19 +131,25 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
     const T* phi_i = phi + g.phi_off[i];
     const T* phi_j = phi + g.phi_off[j];
     const int32_t* gl_i = g.glist + g.sph_off[i];
-    T acc[4][kSlots];
+    T acc[MAXC][kSlots];
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
+    for (int c = 0; c < MAXC; ++c)
 #pragma unroll
       for (int s = 0; s < kSlots; ++s) acc[c][s] = T(0);
-    for (int t0 = 0; t0 < count; t0 += kTile) {
+    // this thread's staged entries of one tile: idx = threadIdx.x + r kPairThreads
+    T rwi[kStage], rwj[kStage];
+    double rv[kStage][MAXC];
+    auto gather = [&](int t0) {
       const int nt = min(kTile, count - t0);
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < kTile * NOMAX; idx += blockDim.x) {
+#pragma unroll
+      for (int r = 0; r < kStage; ++r) {
+        const int idx = threadIdx.x + r * kPairThreads;
         const int pt = idx / NOMAX, a = idx - pt * NOMAX;
-        T wi = T(0), wj = T(0);
-        double v[4] = {0, 0, 0, 0};
-        if (pt < nt) {
+        rwi[r] = T(0);
+        rwj[r] = T(0);
+#pragma unroll
+        for (int c = 0; c < MAXC; ++c) rv[r][c] = 0.0;
+        if (idx < kTile * NOMAX && pt < nt) {
           const int64_t k = start + t0 + pt;
           const int g1 = pr.g1[k], g2 = pr.g2[k];
           // check build: an entry outside its sphere or grid contributes nothing
@@ -142,21 +157,33 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
                           bounds_ok(g2, g.sph_off[j + 1] - g.sph_off[j], 4) &&
                           bounds_ok(gl_i[g1], (int64_t)g.ngrid[0] * g.ngrid[1] * g.ngrid[2], 5);
           if (ok && a < noi) {
-            wi = ldg(phi_i + (int64_t)g1 * noi + a);
+            rwi[r] = ldg(phi_i + (int64_t)g1 * noi + a);
             const int gidx = gl_i[g1];
-            // channel loops unrolled over the fixed four, so v stays in registers
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-              if (c < nch) v[c] = ldg(vpot.c[c] + gidx);
+            for (int c = 0; c < MAXC; ++c)
+              if (c < nch) rv[r][c] = ldg(vpot.c[c] + gidx);
           }
-          if (ok && a < noj) wj = ldg(phi_j + (int64_t)g2 * noj + a);
+          if (ok && a < noj) rwj[r] = ldg(phi_j + (int64_t)g2 * noj + a);
         }
+      }
+    };
+    gather(0);
+    for (int t0 = 0; t0 < count; t0 += kTile) {
+      const int nt = min(kTile, count - t0);
+      __syncthreads();  // the previous tile's readers are done
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
-          if (c < nch) W[((size_t)c * kTile + pt) * NOMAX + a] = wi * (T)v[c];
-        P[pt * NOMAX + a] = wj;
+      for (int r = 0; r < kStage; ++r) {
+        const int idx = threadIdx.x + r * kPairThreads;
+        if (idx < kTile * NOMAX) {
+          const int pt = idx / NOMAX, a = idx - pt * NOMAX;
+#pragma unroll
+          for (int c = 0; c < MAXC; ++c)
+            if (c < nch) W[((size_t)c * kTile + pt) * NOMAX + a] = rwi[r] * (T)rv[r][c];
+          P[pt * NOMAX + a] = rwj[r];
+        }
       }
       __syncthreads();
+      if (t0 + kTile < count) gather(t0 + kTile);  // in flight during the FMAs below
 #pragma unroll
       for (int s = 0; s < kSlots; ++s) {
         const int e = threadIdx.x + s * kPairThreads;
@@ -164,7 +191,7 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
           const int a = e / NOMAX, b = e - (e / NOMAX) * NOMAX;
           if (a < noi && b < noj) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
+            for (int c = 0; c < MAXC; ++c) {
               if (c < nch) {
                 T sum = T(0);
                 const T* wr = W + (size_t)c * kTile * NOMAX + a;
@@ -189,7 +216,7 @@ __global__ void __launch_bounds__(kPairThreads) hamiltonian_pairs_kernel(DevGeom
         const int a = e / NOMAX, b = e - (e / NOMAX) * NOMAX;
         if (a < noi && b < noj) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) {
+          for (int c = 0; c < MAXC; ++c) {
             if (c < nch) {
               const double val = (double)acc[c][s] * g.gridvol;
               if (okp) atomicAdd(hks.c[c] + bp + (int64_t)a * noj + b, val);
@@ -362,6 +389,16 @@ cudaError_t run_force3(const DevGeom& g, const DevPairs& pr, int nch, const doub
   return cudaGetLastError();
 }
 
+template <typename T, int NOMAX, int MAXC>
+cudaError_t run_hamiltonian_c(const DevGeom& g, const DevPairs& pr, int nch, const T* phi, const Ptr4& v,
+                              const MPtr4& o, cudaStream_t st) {
+  const size_t smem = (size_t)(MAXC + 1) * kTile * NOMAX * sizeof(T);
+  LCP_CUDA_TRY(raise_smem(hamiltonian_pairs_kernel<T, NOMAX, MAXC>, smem));
+  hamiltonian_pairs_kernel<T, NOMAX, MAXC><<<persistent_blocks(pr.nitems, 4), kPairThreads, smem, st>>>(
+      g, pr, nch, phi, v, o);
+  return cudaGetLastError();
+}
+
 template <typename T, int NOMAX>
 cudaError_t run_hamiltonian(const DevGeom& g, const DevPairs& pr, int nch, const T* phi, const double* const* vp,
                             double* const* h, cudaStream_t st) {
@@ -371,12 +408,8 @@ cudaError_t run_hamiltonian(const DevGeom& g, const DevPairs& pr, int nch, const
     v.c[c] = vp[c];
     o.c[c] = h[c];
   }
-  size_t smem = (size_t)5 * kTile * NOMAX * sizeof(T);
-  LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_pairs_kernel<T, NOMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
-  hamiltonian_pairs_kernel<T, NOMAX><<<persistent_blocks(pr.nitems, 4), kPairThreads, smem, st>>>(g, pr, nch, phi,
-                                                                                                   v, o);
-  return cudaGetLastError();
+  if (nch == 1) return run_hamiltonian_c<T, NOMAX, 1>(g, pr, nch, phi, v, o, st);
+  return run_hamiltonian_c<T, NOMAX, 4>(g, pr, nch, phi, v, o, st);
 }
 
 }  // namespace

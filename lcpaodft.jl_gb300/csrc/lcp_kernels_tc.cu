@@ -1453,7 +1453,8 @@ cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, d
   return launch_density_tc_batch(c, TcBatch{}, status, st, poll, stall);
 }
 
-cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st) {
+cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batch, int* status, cudaStream_t st,
+                                        cudaEvent_t ev_begin, cudaEvent_t ev_end) {
   TcHamArgs a{};
   a.cell0 = cell0;
   a.batch = batch;
@@ -1466,13 +1467,17 @@ cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batc
   }
   LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
   static_assert(kHSmem > 120 * 1024, "one CTA per SM");
+  if (ev_begin) LCP_CUDA_TRY(cudaEventRecord(ev_begin, st));
   hamiltonian_tc_kernel<<<tc_grid(cell0, batch), 192 + 32 * kHXformWarps, kHSmem, st>>>(a);
-  return cudaGetLastError();
+  LCP_CUDA_TRY(cudaGetLastError());
+  if (ev_end) LCP_CUDA_TRY(cudaEventRecord(ev_end, st));
+  return cudaSuccess;
 }
 
 cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot, const int64_t* slot_base,
                                   const __nv_bfloat16* tab, double phi_scale, const double* vpot, float2* vw,
-                                  float* vscale, float* scratch, int* status, cudaStream_t st) {
+                                  float* vscale, float* scratch, int* status, cudaStream_t st, cudaEvent_t ev_begin,
+                                  cudaEvent_t ev_end) {
   TcCell c = tc_cell_of(bg, tab);
   c.tab_slot = tab_slot;
   c.slot_base = slot_base;
@@ -1481,7 +1486,7 @@ cudaError_t launch_hamiltonian_tc(const TcBrickGeom& bg, const int32_t* tab_slot
   c.vw = vw;
   c.vscale = vscale;
   c.scratch = scratch;
-  return launch_hamiltonian_tc_batch(c, TcBatch{}, status, st);
+  return launch_hamiltonian_tc_batch(c, TcBatch{}, status, st, ev_begin, ev_end);
 }
 
 cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* red_slot, const int32_t* sb_fold,

@@ -146,6 +146,7 @@ _SIGS = {
     "lcp_tc_selftest": ([_vp, _i32, _i32, _i32, _i32, _i32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                         _i32),
     "lcp_xc_selftest": ([_vp, _i32, _i32, _i64, _pd, _pd, _pd, _pd], _i32),
+    "lcp_job_tc_kernel_ms": ([_vp, _vp, _pd], _i32),
 }
 
 for _name, (_args, _res) in _SIGS.items():

@@ -684,6 +684,23 @@ class GridStepJob:
         check(lib.lcp_job_energies(self.ctx._h, self._h, dptr(out)))
         return out
 
+    def energies_async(self, out):
+        """Queues the copy of the last step's energies into ``out`` (5
+        float64, e.g. pinned) on the context stream without waiting: the next
+        call that synchronises (``hks``, ``density``, ``energies``) completes
+        it.  ``out`` must stay alive until then."""
+        if out.dtype != np.float64 or out.size != 5 or not out.flags["C_CONTIGUOUS"]:
+            raise TypeError("out must be 5 contiguous float64")
+        check(lib.lcp_job_energies_async(self.ctx._h, self._h, dptr(out)))
+        return out
+
+    def tc_kernel_ms(self):
+        """One split-BF16 step with CUDA events around its tensor-core kernels
+        alone: (density kernel ms, grid-H kernel ms), summed over channels."""
+        out = np.zeros(2)
+        check(lib.lcp_job_tc_kernel_ms(self.ctx._h, self._h, dptr(out)))
+        return float(out[0]), float(out[1])
+
     def prepare(self):
         """Builds what the context's precision needs of the orbital tables
         (split-BF16 brick tables, FP32 copy) ahead of the first step."""

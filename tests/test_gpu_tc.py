@@ -282,3 +282,31 @@ def test_bricks_of_many_images(ctx):
     assert u.brick_info()["max_images"] > 64
     orbs = L.Set_Orbitals_Grid([pao], u, ctx=ctx)
     _check_vs_fp64(ctx, u, orbs, 63)
+
+
+def test_tc_kernel_times_and_form():
+    """lcp_job_tc_kernel_ms: one split-BF16 step with events around the two
+    tensor-core kernels alone; they take part of the step, the step's results
+    are those of an ordinary step, and other precisions are refused."""
+    from test_gpu_parity import psd_dm
+    c = L.Context(0, precision="bf16x3")
+    u, orbs = _si2(c)
+    job = L.GridStepJob(u, orbs, "off", "LDA")
+    job.set_dm(psd_dm(u, 5))
+    job.step()
+    e_ref, h_ref = job.energies(), job.hks()[0].copy()
+    dens_ms, ham_ms = job.tc_kernel_ms()
+    assert dens_ms > 0 and ham_ms > 0
+    np.testing.assert_array_equal(job.energies(), e_ref)
+    np.testing.assert_array_equal(job.hks()[0], h_ref)
+    stages = job.step_timed()
+    assert dens_ms <= stages[0] * 1.5 and ham_ms <= stages[4] * 1.5
+    # the energies queued without waiting are complete after the synchronising H read
+    e = np.full(5, np.nan)
+    job.step()
+    job.energies_async(e)
+    job.hks()
+    np.testing.assert_array_equal(e, job.energies())
+    c.set_precision("fp64")
+    with pytest.raises(L.LCPError):
+        job.tc_kernel_ms()
