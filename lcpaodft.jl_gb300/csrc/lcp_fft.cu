@@ -267,6 +267,13 @@ __device__ __forceinline__ const Cx<T>* roots_of(const FftGeom& g, int axis) {
   return reinterpret_cast<const Cx<T>*>(std::is_same<T, double>::value ? g.roots64[axis] : g.roots32[axis]);
 }
 
+// Programmatic dependent launch between the passes: a pass lets the next one
+// launch once all its blocks have started (pdl_trigger), and the next one
+// loads its roots, then waits for this pass's writes (pdl_wait) before it
+// reads the spectrum.  Launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Copies the pencil length's roots into shared memory.
 template <class T>
 __device__ __forceinline__ void load_roots(Cx<T>* dst, const Cx<T>* src, int n) {
@@ -301,7 +308,9 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) fft_rows_fwd_kernel(const _
   Cx<T>* w = reinterpret_cast<Cx<T>*>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Cx<T>* buf = w + n + (size_t)warp * 2 * n;
+  pdl_trigger();
   load_roots(w, roots_of<T>(a.g, 2), n);
+  pdl_wait();
   __syncthreads();
   const int64_t pair = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
   const int64_t ra = 2 * pair, rb = ra + 1;
@@ -333,7 +342,9 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) fft_rows_inv_kernel(const _
   Cx<T>* w = reinterpret_cast<Cx<T>*>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Cx<T>* buf = w + n + (size_t)warp * 2 * n;
+  pdl_trigger();
   load_roots(w, roots_of<T>(a.g, 2), n);
+  pdl_wait();
   __syncthreads();
   const int64_t pair = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
   const int64_t ra = 2 * pair, rb = ra + 1;
@@ -384,7 +395,9 @@ __global__ void __launch_bounds__(256, 4) fft_cols_kernel(const __grid_constant_
   Cx<T>* w = reinterpret_cast<Cx<T>*>(smem);
   Cx<T>* bufs = w + n;  // [W][S], S >= 2n
   double* pf = reinterpret_cast<double*>(bufs + (size_t)W * S);  // MODE 2: [W][pfstride]
+  pdl_trigger();
   load_roots(w, roots_of<T>(a.g, axis), n);
+  pdl_wait();
   Cx<T>* spec = reinterpret_cast<Cx<T>*>(c.spec);
   const int col = threadIdx.x % W;
   const int64_t cid = (int64_t)blockIdx.x * W + col;
@@ -452,6 +465,23 @@ cudaError_t prefer_shared(const void* kernel) {
   return cudaSuccess;
 }
 
+// A launch that may begin while the previous kernel of the stream finishes
+// (programmatic stream serialisation); the kernel waits for it in pdl_wait.
+template <class K, class... Args>
+cudaError_t launch_pdl(K* kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <class T>
 cudaError_t launch_fft_t(const FftGeom& g, FftArgs args, int ncells, cudaStream_t st) {
   const int n1 = g.n[0], n2 = g.n[1], n3 = g.n[2], h = n3 / 2 + 1;
@@ -462,8 +492,7 @@ cudaError_t launch_fft_t(const FftGeom& g, FftArgs args, int ncells, cudaStream_
   LCP_CUDA_TRY(raise_smem(fft_rows_inv_kernel<T>, rsm));
   LCP_CUDA_TRY(prefer_shared(reinterpret_cast<const void*>(fft_rows_fwd_kernel<T>)));
   LCP_CUDA_TRY(prefer_shared(reinterpret_cast<const void*>(fft_rows_inv_kernel<T>)));
-  fft_rows_fwd_kernel<T><<<rgrid, 32 * kRowWarps, rsm, st>>>(args);
-  LCP_CUDA_TRY(cudaGetLastError());
+  LCP_CUDA_TRY(launch_pdl(fft_rows_fwd_kernel<T>, rgrid, dim3(32 * kRowWarps), rsm, st, args));
   auto cols = [&](auto kern, int axis, bool with_pf) -> cudaError_t {
     const int n = g.n[axis];
     const int W = cols_width(n, with_pf);
@@ -475,14 +504,13 @@ cudaError_t launch_fft_t(const FftGeom& g, FftArgs args, int ncells, cudaStream_
                       (with_pf ? (size_t)W * args.pfstride * 8 : 0);
     LCP_CUDA_TRY(raise_smem(kern, sm));
     LCP_CUDA_TRY(prefer_shared(reinterpret_cast<const void*>(kern)));
-    kern<<<dim3((unsigned)((ncols + W - 1) / W), (unsigned)ncells), 32 * W, sm, st>>>(args, axis);
-    return cudaGetLastError();
+    return launch_pdl(kern, dim3((unsigned)((ncols + W - 1) / W), (unsigned)ncells), dim3(32 * W), sm, st, args,
+                      axis);
   };
   LCP_CUDA_TRY(cols(fft_cols_kernel<T, 0>, 1, false));
   LCP_CUDA_TRY(cols(fft_cols_kernel<T, 2>, 0, true));
   LCP_CUDA_TRY(cols(fft_cols_kernel<T, 1>, 1, false));
-  fft_rows_inv_kernel<T><<<rgrid, 32 * kRowWarps, rsm, st>>>(args);
-  return cudaGetLastError();
+  return launch_pdl(fft_rows_inv_kernel<T>, rgrid, dim3(32 * kRowWarps), rsm, st, args);
 }
 
 }  // namespace
