@@ -36,6 +36,7 @@
 
 #include "lcp_device.h"
 #include "lcp_dfloat.cuh"
+#include "lcp_pdl.cuh"
 
 namespace lcp {
 
@@ -267,12 +268,8 @@ __device__ __forceinline__ const Cx<T>* roots_of(const FftGeom& g, int axis) {
   return reinterpret_cast<const Cx<T>*>(std::is_same<T, double>::value ? g.roots64[axis] : g.roots32[axis]);
 }
 
-// Programmatic dependent launch between the passes: a pass lets the next one
-// launch once all its blocks have started (pdl_trigger), and the next one
-// loads its roots, then waits for this pass's writes (pdl_wait) before it
-// reads the spectrum.  Launched without the attribute both are no-ops.
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// The passes are chained by programmatic dependent launch (lcp_pdl.cuh): a
+// pass loads its roots before it waits for the previous pass's writes.
 
 // Copies the pencil length's roots into shared memory.
 template <class T>
@@ -463,23 +460,6 @@ cudaError_t prefer_shared(const void* kernel) {
                                     (int)cudaSharedmemCarveoutMaxShared));
   d = true;
   return cudaSuccess;
-}
-
-// A launch that may begin while the previous kernel of the stream finishes
-// (programmatic stream serialisation); the kernel waits for it in pdl_wait.
-template <class K, class... Args>
-cudaError_t launch_pdl(K* kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 template <class T>

@@ -6,6 +6,7 @@
 
 #include "lcp_device.h"
 #include "lcp_grid_common.cuh"
+#include "lcp_pdl.cuh"
 
 namespace lcp {
 
@@ -481,6 +482,8 @@ __global__ void __launch_bounds__(kRedThreads) vpot_eh_g_kernel(const __grid_con
 
 // Sums of each cell's energy tile partials: sums[0..2] (one block per cell).
 __global__ void __launch_bounds__(kRedThreads) grid_sums_g_kernel(const __grid_constant__ GridArgs a) {
+  pdl_trigger();
+  pdl_wait();
   const GridCell& c = a.batch.cells ? a.batch.cells[blockIdx.x] : a.cell0;
   const int64_t nt = red_tiles(c.nn);
   double v[3] = {0, 0, 0};
@@ -491,6 +494,8 @@ __global__ void __launch_bounds__(kRedThreads) grid_sums_g_kernel(const __grid_c
 
 // Tile partials of sum_s <D_s, H_s> (one block per tile of matrix entries).
 __global__ void __launch_bounds__(kRedThreads) dot_g_kernel(const __grid_constant__ GridArgs a) {
+  pdl_trigger();
+  pdl_wait();
   int64_t t;
   const GridCell& c = grid_cell(a.cell0, a.batch, blockIdx.x, t);
   const int64_t x0 = t * kRedTile, x1 = min(c.hsize, x0 + kRedTile);
@@ -507,6 +512,8 @@ __global__ void __launch_bounds__(kRedThreads) dot_g_kernel(const __grid_constan
 // sums[8..12] = E_H1, E_xc1 (up), E_xc1 (down), sum <D,H>,
 // f_s sum <D,H> + E_H1 + E_xc1, with f_s = 2 for SpinPol "off".
 __global__ void __launch_bounds__(kRedThreads) dot_energy_g_kernel(const __grid_constant__ GridArgs a) {
+  pdl_trigger();
+  pdl_wait();
   const GridCell& c = a.batch.cells ? a.batch.cells[blockIdx.x] : a.cell0;
   const int64_t nt = red_tiles(c.hsize);
   double v[1] = {0.0};
@@ -714,19 +721,17 @@ cudaError_t launch_vpot_eh_g(int spinpol, const GridCell& c0, const GridBatch& b
 }
 
 cudaError_t launch_grid_sums_g(const GridCell& c0, const GridBatch& b, cudaStream_t st) {
-  grid_sums_g_kernel<<<cell_blocks(b), kRedThreads, 0, st>>>(grid_args(c0, b, 0, 0, 0));
-  return cudaGetLastError();
+  return launch_pdl(grid_sums_g_kernel, dim3(cell_blocks(b)), dim3(kRedThreads), 0, st, grid_args(c0, b, 0, 0, 0));
 }
 
 cudaError_t launch_dot_energy_g(int spinpol, int nspin, const GridCell& c0, const GridBatch& tiles,
                                 const GridBatch& cells, cudaStream_t st) {
   const unsigned n = tiled_blocks(tiles, red_tiles(c0.hsize));
   if (n > 0) {
-    dot_g_kernel<<<n, kRedThreads, 0, st>>>(grid_args(c0, tiles, 0, spinpol, nspin));
-    LCP_CUDA_TRY(cudaGetLastError());
+    LCP_CUDA_TRY(launch_pdl(dot_g_kernel, dim3(n), dim3(kRedThreads), 0, st, grid_args(c0, tiles, 0, spinpol, nspin)));
   }
-  dot_energy_g_kernel<<<cell_blocks(cells), kRedThreads, 0, st>>>(grid_args(c0, cells, 0, spinpol, nspin));
-  return cudaGetLastError();
+  return launch_pdl(dot_energy_g_kernel, dim3(cell_blocks(cells)), dim3(kRedThreads), 0, st,
+                    grid_args(c0, cells, 0, spinpol, nspin));
 }
 
 }  // namespace lcp

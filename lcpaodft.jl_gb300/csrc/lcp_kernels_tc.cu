@@ -9,6 +9,7 @@
 
 #include "lcp_bounds.cuh"
 #include "lcp_device.h"
+#include "lcp_pdl.cuh"
 #include "lcp_tc.cuh"
 
 namespace lcp {
@@ -283,6 +284,8 @@ __global__ void absmax_kernel(const double* __restrict__ x, int64_t n, unsigned 
 
 // scale[0] = power of two >= factor * max, scale[1] = its inverse
 __global__ void pow2_scale_kernel(const unsigned long long* mx, double factor, double* scale) {
+  pdl_trigger();
+  pdl_wait();
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     const double s = pow2_ceil(__longlong_as_double((long long)*mx) * factor);
     scale[0] = s;
@@ -412,6 +415,8 @@ __global__ void dsym_kernel(int64_t nsub, const int32_t* __restrict__ sub_pair, 
                             const int64_t* __restrict__ boff, const int32_t* __restrict__ partner,
                             const int32_t* __restrict__ numorbs, const double* __restrict__ dm,
                             const double* __restrict__ scale, __nv_bfloat16* __restrict__ out) {
+  pdl_trigger();
+  pdl_wait();
   const double inv = scale[1];
   const int64_t total = (nsub + 1) * 256;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
@@ -877,6 +882,8 @@ struct TcHamArgs {
 // element kernel; S_V * S_phi^2 per brick for its epilogue.  One block of 128
 // threads (point slots) per brick.
 __global__ void __launch_bounds__(128) vweight_kernel(const __grid_constant__ TcHamArgs args) {
+  pdl_trigger();
+  pdl_wait();
   __shared__ unsigned long long smax[4];
   const int p = threadIdx.x, warp = p >> 5, lane = p & 31;
   const int64_t ntotal = args.batch.cells ? args.batch.nbricks : args.cell0.nbricks;
@@ -1300,6 +1307,8 @@ __global__ void __launch_bounds__(256) h_reduce_kernel(int64_t nsb, const int64_
                                                        const int32_t* __restrict__ sb_chunks,
                                                        const float* __restrict__ scratch, DevPairs pr,
                                                        const int32_t* __restrict__ numorbs, double dv, double* H) {
+  pdl_trigger();
+  pdl_wait();
   extern __shared__ __align__(16) uint8_t hsm[];
   for (int64_t u = blockIdx.x; u < nsb; u += gridDim.x)
     h_reduce_block(u, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H, hsm);
@@ -1341,8 +1350,7 @@ cudaError_t launch_absmax_scale(const double* x, int64_t n, double factor, unsig
     absmax_kernel<<<blocks, 256, 0, st>>>(x, n, tmp);
     LCP_CUDA_TRY(cudaGetLastError());
   }
-  pow2_scale_kernel<<<1, 32, 0, st>>>(tmp, factor, scale);
-  return cudaGetLastError();
+  return launch_pdl(pow2_scale_kernel, dim3(1), dim3(32), 0, st, (const unsigned long long*)tmp, factor, scale);
 }
 
 cudaError_t launch_brick_table(const double* phi, const int64_t* phi_off, const int32_t* numorbs,
@@ -1368,9 +1376,8 @@ cudaError_t launch_dsym(int64_t nsub, const int32_t* sub_pair, const int32_t* su
                         const double* dm, const double* scale, __nv_bfloat16* out, cudaStream_t st) {
   int64_t total = (nsub + 1) * 256;
   int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
-  dsym_kernel<<<blocks, 256, 0, st>>>(nsub, sub_pair, sub_chunks, pair_atom, pair_jatom, boff, partner, numorbs, dm,
-                                      scale, out);
-  return cudaGetLastError();
+  return launch_pdl(dsym_kernel, dim3(blocks), dim3(256), 0, st, nsub, sub_pair, sub_chunks, pair_atom, pair_jatom, boff,
+                    partner, numorbs, dm, scale, out);
 }
 
 cudaError_t launch_dsym_batch(int32_t ncells, const DsymCell* cells, const int64_t* start, int64_t total_blocks,
@@ -1462,8 +1469,7 @@ cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batc
   const int64_t n = batch.cells ? batch.nbricks : cell0.nbricks;
   if (n > 0) {
     const int vgrid = (int)std::min<int64_t>(n, (int64_t)sm_count() * 16);
-    vweight_kernel<<<vgrid, 128, 0, st>>>(a);
-    LCP_CUDA_TRY(cudaGetLastError());
+    LCP_CUDA_TRY(launch_pdl(vweight_kernel, dim3(vgrid), dim3(128), 0, st, a));
   }
   LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
   static_assert(kHSmem > 120 * 1024, "one CTA per SM");
@@ -1495,8 +1501,8 @@ cudaError_t launch_h_reduce(int64_t nsb, const int64_t* red_off, const int64_t* 
   if (nsb == 0) return cudaSuccess;
   const int grid = (int)std::min<int64_t>(nsb, (int64_t)sm_count() * 8);
   LCP_CUDA_TRY(cudaFuncSetAttribute(h_reduce_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRedSmem));
-  h_reduce_kernel<<<grid, 256, kRedSmem, st>>>(nsb, red_off, red_slot, sb_fold, sb_chunks, scratch, pr, numorbs, dv, H);
-  return cudaGetLastError();
+  return launch_pdl(h_reduce_kernel, dim3(grid), dim3(256), kRedSmem, st, nsb, red_off, red_slot, sb_fold, sb_chunks,
+                    scratch, pr, numorbs, dv, H);
 }
 
 cudaError_t bounds_take_tc(unsigned long long* word) {
