@@ -578,6 +578,9 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+  // launched as a dependent of the D-block (or V-weight) kernel: its setup
+  // above overlaps that kernel's tail; its outputs are read only from here on
+  pdl_wait();
   const uint32_t tmem = tslot;
   const int64_t ntotal = args.batch.cells ? args.batch.nbricks : args.cell0.nbricks;
   auto give_up = [&]() {
@@ -940,6 +943,9 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+  // launched as a dependent of the D-block (or V-weight) kernel: its setup
+  // above overlaps that kernel's tail; its outputs are read only from here on
+  pdl_wait();
   const uint32_t tmem = tslot;
   const int64_t ntotal = args.batch.cells ? args.batch.nbricks : args.cell0.nbricks;
   auto give_up = [&]() {
@@ -1444,8 +1450,7 @@ cudaError_t launch_density_tc_batch(const TcCell& cell0, const TcBatch& batch, i
   // 512 TMEM columns per CTA: the shared-memory ring (> half an SM) keeps one CTA per SM
   static_assert(kDSmem > 120 * 1024, "one CTA per SM");
   LCP_CUDA_TRY(cudaFuncSetAttribute(density_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDSmem));
-  density_tc_kernel<<<tc_grid(cell0, batch), 192 + 32 * kDGatherWarps, kDSmem, st>>>(a);
-  return cudaGetLastError();
+  return launch_pdl(density_tc_kernel, tc_grid(cell0, batch), dim3(192 + 32 * kDGatherWarps), kDSmem, st, a);
 }
 
 cudaError_t launch_density_tc(const TcBrickGeom& bg, const __nv_bfloat16* tab, double phi_scale,
@@ -1474,8 +1479,7 @@ cudaError_t launch_hamiltonian_tc_batch(const TcCell& cell0, const TcBatch& batc
   LCP_CUDA_TRY(cudaFuncSetAttribute(hamiltonian_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHSmem));
   static_assert(kHSmem > 120 * 1024, "one CTA per SM");
   if (ev_begin) LCP_CUDA_TRY(cudaEventRecord(ev_begin, st));
-  hamiltonian_tc_kernel<<<tc_grid(cell0, batch), 192 + 32 * kHXformWarps, kHSmem, st>>>(a);
-  LCP_CUDA_TRY(cudaGetLastError());
+  LCP_CUDA_TRY(launch_pdl(hamiltonian_tc_kernel, tc_grid(cell0, batch), dim3(192 + 32 * kHXformWarps), kHSmem, st, a));
   if (ev_end) LCP_CUDA_TRY(cudaEventRecord(ev_end, st));
   return cudaSuccess;
 }
