@@ -245,6 +245,31 @@ lcp_status density_tc_device(lcp_ctx* ctx, const lcp_orbs* orbs_c, int nspin, co
   return LCP_OK;
 }
 
+// Runs launch(items, max orbitals, first item) on each orbital class of the
+// pair items (see lcp_orbs::nitems_small); returns the number of launches.
+template <class F>
+cudaError_t for_item_classes(const lcp_orbs* o, int* launches, F launch) {
+  const lcp::DevPairs& pr = o->pairs;
+  *launches = 0;
+  if (o->nitems_small > 0) {
+    lcp::DevPairs a = pr;
+    a.nitems = o->nitems_small;
+    LCP_CUDA_TRY(launch(a, o->max_no_small, (int64_t)0));
+    ++*launches;
+  }
+  const int64_t nl = pr.nitems - o->nitems_small;
+  if (nl > 0) {
+    lcp::DevPairs b = pr;
+    b.nitems = nl;
+    b.item_pair += o->nitems_small;
+    b.item_start += o->nitems_small;
+    b.item_count += o->nitems_small;
+    LCP_CUDA_TRY(launch(b, o->max_no_large, o->nitems_small));
+    ++*launches;
+  }
+  return cudaSuccess;
+}
+
 lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const double* const* dm, double* const* rho,
                           int64_t nn) {
   int prec = ctx->precision;
@@ -255,10 +280,14 @@ lcp_status density_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nspin, const d
     lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
     if (s != LCP_OK) return s;
   }
-  API_CUDA(lcp::launch_density_pairs(prec, orbs->geom, orbs->pairs, nspin, orbs->phi.as<double>(),
-                                     orbs->phi32.as<float>(), dm, rho, orbs->max_no, ctx->stream),
+  int nl = 0;
+  API_CUDA(for_item_classes(orbs, &nl,
+                            [&](const lcp::DevPairs& pr, int max_no, int64_t) {
+                              return lcp::launch_density_pairs(prec, orbs->geom, pr, nspin, orbs->phi.as<double>(),
+                                                               orbs->phi32.as<float>(), dm, rho, max_no, ctx->stream);
+                            }),
            "density kernel");
-  ctx->launches++;
+  ctx->launches += nl;
   return LCP_OK;
 }
 
@@ -312,10 +341,15 @@ lcp_status hamiltonian_device(lcp_ctx* ctx, const lcp_orbs* orbs, int nch, const
     lcp_status s = ensure_phi32(ctx, const_cast<lcp_orbs*>(orbs));
     if (s != LCP_OK) return s;
   }
-  API_CUDA(lcp::launch_hamiltonian_pairs(prec, orbs->geom, orbs->pairs, nch, orbs->phi.as<double>(),
-                                         orbs->phi32.as<float>(), vpot, hks, orbs->max_no, ctx->stream),
+  int nl = 0;
+  API_CUDA(for_item_classes(orbs, &nl,
+                            [&](const lcp::DevPairs& pr, int max_no, int64_t) {
+                              return lcp::launch_hamiltonian_pairs(prec, orbs->geom, pr, nch, orbs->phi.as<double>(),
+                                                                   orbs->phi32.as<float>(), vpot, hks, max_no,
+                                                                   ctx->stream);
+                            }),
            "hamiltonian kernel");
-  ctx->launches++;
+  ctx->launches += nl;
   return LCP_OK;
 }
 
@@ -668,6 +702,11 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
   std::vector<int64_t> ip, is;
   std::vector<int32_t> ic;
   const int64_t chunk = 512;
+  // items of pairs with at most 16 orbitals per atom first, then the others
+  // (e.g. the 13-orbital pairs of a cell with some 18-orbital atoms get exact
+  // 13-orbital tiles instead of 18)
+  std::vector<int64_t> ip_l, is_l;
+  std::vector<int32_t> ic_l;
   for (int64_t q = 0; q < nu; ++q) {
     int p = u.uniq_pair[q];
     pa[q] = u.pair_atom[p];
@@ -676,12 +715,20 @@ lcp_status lcp_set_orbitals_grid(lcp_ctx* ctx, const lcp_ucell* ucell, int32_t n
     bq[q] = u.block_off[u.partner[p]];
     pself[q] = u.partner[p] == p;
     if (u.numorbs[pa[q]] == 0 || u.numorbs[pj[q]] == 0) continue;
+    const int no = std::max(u.numorbs[pa[q]], u.numorbs[pj[q]]);
+    const bool small = no <= 16;
+    if (small) o->max_no_small = std::max(o->max_no_small, no);
+    else o->max_no_large = std::max(o->max_no_large, no);
     for (int64_t s0 = u.uniq_off[q]; s0 < u.uniq_off[q + 1]; s0 += chunk) {
-      ip.push_back(q);
-      is.push_back(s0);
-      ic.push_back((int32_t)std::min<int64_t>(chunk, u.uniq_off[q + 1] - s0));
+      (small ? ip : ip_l).push_back(q);
+      (small ? is : is_l).push_back(s0);
+      (small ? ic : ic_l).push_back((int32_t)std::min<int64_t>(chunk, u.uniq_off[q + 1] - s0));
     }
   }
+  o->nitems_small = (int64_t)ip.size();
+  ip.insert(ip.end(), ip_l.begin(), ip_l.end());
+  is.insert(is.end(), is_l.begin(), is_l.end());
+  ic.insert(ic.end(), ic_l.begin(), ic_l.end());
   API_CUDA(upload(o->p_atom, pa, st), "upload");
   API_CUDA(upload(o->p_jatom, pj, st), "upload");
   API_CUDA(upload(o->p_boffp, bp, st), "upload");
@@ -991,13 +1038,19 @@ lcp_status lcp_calc_force3(lcp_ctx* ctx, const lcp_ucell* ucell, const lcp_orbs*
   API_CUDA(ctx->w_part.ensure((size_t)std::max<int64_t>(nitems, 1) * 6 * sizeof(double)), "alloc");
   API_CUDA(ctx->w_out[0].ensure((size_t)std::max(u.natom, 1) * 3 * sizeof(double)), "alloc");
   const double* dphi[3] = {orbs->dphi[0].as<double>(), orbs->dphi[1].as<double>(), orbs->dphi[2].as<double>()};
-  API_CUDA(lcp::launch_force3_pairs(orbs->geom, orbs->pairs, nch, orbs->phi.as<double>(), dphi, dv, dd, w,
-                                    ctx->w_part.as<double>(), orbs->max_no, ctx->stream),
+  int nl = 0;
+  API_CUDA(for_item_classes(orbs, &nl,
+                            [&](const lcp::DevPairs& pr, int max_no, int64_t first) {
+                              // item k's six partial sums at w_part[6 k]
+                              return lcp::launch_force3_pairs(orbs->geom, pr, nch, orbs->phi.as<double>(), dphi, dv,
+                                                              dd, w, ctx->w_part.as<double>() + 6 * first, max_no,
+                                                              ctx->stream);
+                            }),
            "force3");
   API_CUDA(lcp::launch_force3_reduce(u.natom, orbs->f_off.as<int64_t>(), orbs->f_code.as<int64_t>(),
                                      ctx->w_part.as<double>(), u.gridvol, ctx->w_out[0].as<double>(), ctx->stream),
            "force3 reduce");
-  ctx->launches += 2;
+  ctx->launches += nl + 1;
   API_CUDA(cudaMemcpyAsync(force, ctx->w_out[0].p, (size_t)u.natom * 3 * sizeof(double), cudaMemcpyDeviceToHost,
                            ctx->stream),
            "D2H");

@@ -126,6 +126,10 @@ struct lcp_orbs {
   int device = 0;
   bool grad = false;
   int max_no = 0;
+  // the pair items in two orbital classes, pairs of at most 16 orbitals per
+  // atom first: each class's FP64/FP32 pair kernels use its own tile bound
+  int64_t nitems_small = 0;
+  int max_no_small = 0, max_no_large = 0;
   lcp::DevGeom geom{};
   lcp::DevPairs pairs{};
   // device arrays
