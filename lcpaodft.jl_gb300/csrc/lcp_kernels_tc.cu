@@ -106,8 +106,10 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 // in magnitude: 8 significant bits, and 256 = 2^8) and |e| <= 2^-27.  The
 // quantisation error of the energies scales with the last part's quantum,
 // so nine bits per part (27 in all) instead of eight cut it by 8x at no
-// cost.  All nine part products are formed (the mid*lo and lo*lo terms carry
-// the small tails of the orbitals, which a six-term product loses).  hi*hi'
+// cost.  Eight of the nine part products are formed: mid*lo and lo*mid carry
+// the small tails of the orbitals, which a six-term product loses, while
+// lo*lo is at most 2^-36 of the scales' product, 2^-9 of the bound 2^-27 on
+// the inputs' own quantisation, and is not formed.  hi*hi'
 // (integer multiples of 2^-16) has its own accumulator, exact while the sum
 // stays below 256 in magnitude (2^24 quanta: 512 terms of the largest size
 // for D, whose scale is twice its maximum, and 256 for the matrix elements);
@@ -534,7 +536,7 @@ __device__ __forceinline__ int64_t round_brick(int64_t j, int64_t ntotal) {
 //              ~35 cycles, a small bulk copy ~70, whatever its size), each
 //              warp publishing its share on full[stage] kDLag steps later,
 //              once landed and fenced for the tensor core;
-//   warp 1     MMA issuer (one elected lane): nine tcgen05 MMAs per K step
+//   warp 1     MMA issuer (one elected lane): eight tcgen05 MMAs per K step
 //              into one of two TMEM window buffers.  After step t of a
 //              window, column block t is final: the commit goes to
 //              mdone[stage]; other steps commit empty[stage] (4 arrivals);
@@ -742,7 +744,6 @@ __global__ void __launch_bounds__(192 + 32 * kDGatherWarps, 1) density_tc_kernel
             tc::mma_bf16(d1, dam, dbm, idesc, 1u);
             tc::mma_bf16(d1, dam, dbl, idesc, 1u);
             tc::mma_bf16(d1, dal, dbm, idesc, 1u);
-            tc::mma_bf16(d1, dal, dbl, idesc, 1u);
             if (t < c1) {
               // column block t is final once these MMAs finish; the epilogue
               // reads it with phi_t from this stage and then frees the stage
@@ -862,17 +863,19 @@ constexpr int kHABytes = kHGroup * kImgBytes;   // one part of the A operand
 constexpr int kHBBytes = kHWin * kImgBytes;     // one part of a B stage
 constexpr size_t kHSmem = 3 * (size_t)kHABytes + (size_t)kHStages * 3 * kHBBytes;  // 192 KB
 // TMEM: two tile buffers of 256 columns; inside one, the four accumulators
-// (64 columns each), one per quantum of the products: hi*hi (2^-16),
-// hi*mid + mid*hi (2^-25), hi*lo + lo*hi + mid*mid (2^-34),
-// mid*lo + lo*mid + lo*lo (2^-43; lo*lo is the only term finer than its
-// quantum).  Over the 128 points of a brick the first two sums stay within
-// 2^24 of their quanta (128 terms of at most 1, 256 of at most 2^-9), so
-// they are exact in FP32; the third could exceed it only if all of its 384
-// terms were near their bound with one sign.  Four MMAs per K step
-// fill them (B parts stacked along N), reading 34 KB of operands instead of
-// the 54 KB of nine separate products: the MMAs are bound by shared-memory
-// operand bandwidth (~128 B/clock), not by the tensor pipe.
-constexpr uint32_t kHBufCols = 256, kHAccCols = 64;
+// (W = 16 x the tile's t images columns each, at most 64), one per quantum
+// of the products: hi*hi (2^-16), hi*mid + mid*hi (2^-25),
+// hi*lo + lo*hi + mid*mid (2^-34), mid*lo + lo*mid (2^-43).  Over the 128
+// points of a brick the first two sums stay within 2^24 of their quanta (128
+// terms of at most 1, 256 of at most 2^-9), so they are exact in FP32; the
+// third could exceed it only if all of its 384 terms were near their bound
+// with one sign.  lo*lo (at most 2^-36 of the scales' product, 2^-9 of the
+// inputs' own quantisation bound 2^-27) is not formed.  Three MMAs per K
+// step fill them (B parts stacked along N, N = 3W, 3W, 2W): per-clock
+// tcgen05 traces showed the tile's MMAs set the kernel's pace (~93 cycles
+// per MMA, ~21 of them fixed cost), so fewer and wider MMAs, and N sized to
+// the images present, are what shorten a tile.
+constexpr uint32_t kHBufCols = 256;
 
 struct TcHamArgs {
   TcCell cell0;
@@ -1009,15 +1012,17 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
             break;
           }
           tc::fence_after_sync();
-          // B parts stacked along N: the stage is [hi | mid | lo] x kHWin images,
-          // one MN-major operand of N = 3 * 16 * kHWin with uniform SBO.  Image
-          // slots beyond the tile hold stale data and feed only unused columns.
+          // B parts stacked along N: the stage is [hi | mid | lo] x nt images,
+          // one MN-major operand of N = 3W (W = 16 nt) with uniform SBO.
           // Descriptors are warp-uniform; the lane elected by elect.sync (the
           // same lane every time) issues and commits.
-          const uint32_t idesc3 = tc::idesc_bf16_f32(128, 3 * 16 * kHWin, 1, 1);
-          const uint32_t idesc2 = tc::idesc_bf16_f32(128, 2 * 16 * kHWin, 1, 1);
-          const uint32_t idesc1 = tc::idesc_bf16_f32(128, 16 * kHWin, 1, 1);
+          const int nt = min(kHWin, m - t0);
+          const uint32_t W = 16u * (uint32_t)nt;
+          const uint32_t idesc3 = tc::idesc_bf16_f32(128, 3 * W, 1, 1);
+          const uint32_t idesc2 = tc::idesc_bf16_f32(128, 2 * W, 1, 1);
+          const uint32_t idesc1 = tc::idesc_bf16_f32(128, W, 1, 1);
           const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB0 + stage * 3 * kHBBytes);
+          const uint32_t bl = b0 + 2u * (uint32_t)nt * kImgBytes;  // the lo part of the stage
           const uint32_t d0 = tmem + buf * kHBufCols;
 #pragma unroll
           for (int ks = 0; ks < 8; ++ks) {
@@ -1026,16 +1031,23 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
                            dam = tc::smem_desc(a0 + kHABytes + ko, 128, 2048),
                            dal = tc::smem_desc(a0 + 2 * kHABytes + ko, 128, 2048);
             const uint64_t dbh = tc::smem_desc(b0 + ko, 128, 2048),  // [hi | mid | lo] from here
-                           dbl = tc::smem_desc(b0 + 2 * kHBBytes + ko, 128, 2048);
-            // Accumulator k (quantum 2^-(16+9k)) at columns d0 + 64k: a product
+                           dbl = tc::smem_desc(bl + ko, 128, 2048);
+            // Accumulator k (quantum 2^-(16+9k)) at columns d0 + kW: a product
             // of parts (i, j) lands in accumulator i + j when the MMA with
-            // A part i starts at column d0 + 64 i.  lo*lo shares the last one.
-            const uint32_t acc = ks > 0 ? 1u : 0u;
+            // A part i starts at column d0 + iW.  K step 0 writes every
+            // accumulator first (lo * [hi, mid] the last two, hi * [hi, mid]
+            // the first two) and adds hi * lo on its own; later steps take
+            // hi * [hi, mid, lo] and lo * [hi, mid] whole.
             if (tc::elect_one()) {
-              tc::mma_bf16(d0 + 3 * kHAccCols, dal, dbl, idesc1, acc);  // lo*lo (first write of acc 3)
-              tc::mma_bf16(d0, dah, dbh, idesc3, acc);                   // hi * [hi, mid, lo] -> acc 0, 1, 2
-              tc::mma_bf16(d0 + kHAccCols, dam, dbh, idesc3, 1u);        // mid * [hi, mid, lo] -> acc 1, 2, 3
-              tc::mma_bf16(d0 + 2 * kHAccCols, dal, dbh, idesc2, 1u);    // lo * [hi, mid] -> acc 2, 3
+              if (ks == 0) {
+                tc::mma_bf16(d0 + 2 * W, dal, dbh, idesc2, 0u);  // lo * [hi, mid] -> acc 2, 3 (first write)
+                tc::mma_bf16(d0, dah, dbh, idesc2, 0u);          // hi * [hi, mid] -> acc 0, 1 (first write)
+                tc::mma_bf16(d0 + 2 * W, dah, dbl, idesc1, 1u);  // hi * lo -> acc 2
+              } else {
+                tc::mma_bf16(d0, dah, dbh, idesc3, 1u);          // hi * [hi, mid, lo] -> acc 0, 1, 2
+                tc::mma_bf16(d0 + 2 * W, dal, dbh, idesc2, 1u);  // lo * [hi, mid] -> acc 2, 3
+              }
+              tc::mma_bf16(d0 + W, dam, dbh, idesc3, 1u);        // mid * [hi, mid, lo] -> acc 1, 2, 3
             }
           }
           if (tc::elect_one()) {
@@ -1098,6 +1110,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
             break;
           }
           uint8_t* sB = sB0 + stage * 3 * kHBBytes + tt * 16;
+          const int pbytes = nt * kImgBytes;  // one part of this tile's stage: [hi | mid | lo] x nt images
 #pragma unroll
           for (int j = 0; j < kHWin; ++j) {
             if (j < nt) {
@@ -1117,8 +1130,8 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
                 fx_split_f(pr, er, xh[e], xm[e], xl[e]);
               }
               *reinterpret_cast<uint4*>(sB + j * kImgBytes) = oh;
-              *reinterpret_cast<uint4*>(sB + kHBBytes + j * kImgBytes) = om;
-              *reinterpret_cast<uint4*>(sB + 2 * kHBBytes + j * kImgBytes) = ol;
+              *reinterpret_cast<uint4*>(sB + pbytes + j * kImgBytes) = om;
+              *reinterpret_cast<uint4*>(sB + 2 * pbytes + j * kImgBytes) = ol;
             }
           }
           tc::fence_proxy_async_smem();
@@ -1146,6 +1159,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
         const int s = s0 + (row >> 4), a = row & 15;
         for (int t0 = s0; t0 < m && !abort_flag; t0 += kHWin, ++it) {
           const int nt = min(kHWin, m - t0);
+          const uint32_t W = 16u * (uint32_t)nt;  // accumulator k at columns kW of the buffer
           const uint32_t buf = it & 1;
           int slot[kHWin];
 #pragma unroll
@@ -1162,7 +1176,7 @@ __global__ void __launch_bounds__(192 + 32 * kHXformWarps, 1) hamiltonian_tc_ker
               uint32_t y[4][16];
               const uint32_t col = buf * kHBufCols + 16 * j;
 #pragma unroll
-              for (int k = 0; k < 4; ++k) tc::tmem_ld16_nowait(tc::tmem_addr(tmem, quarter * 32, col + k * kHAccCols), y[k]);
+              for (int k = 0; k < 4; ++k) tc::tmem_ld16_nowait(tc::tmem_addr(tmem, quarter * 32, col + k * W), y[k]);
               tc::tmem_wait_ld();
 #pragma unroll
               for (int k = 0; k < 4; ++k) tc::tmem_regs_ready(y[k]);

@@ -61,8 +61,9 @@ def _density(ctx, u, orbs, dm, precision, spin="off"):
 
 
 # Split-BF16 bounds.  Every operand is quantised to 2^-27 of its power-of-two
-# scale (three BF16 parts of nine bits) and all nine part products are
-# accumulated exactly, so the error is the input quantisation: about 1.5e-7
+# scale (three BF16 parts of nine bits) and the part products down to
+# mid*lo are accumulated exactly (lo*lo, at most 2^-36 of the scales, is not
+# formed), so the error is the input quantisation: about 1.5e-7
 # of max|rho| / max|H| on these cells, electron count and <D,H> to ~1e-8
 # (with eight-bit parts the same cells gave 1e-6 and 4e-8; the bounds below
 # are the ones those passed with a 5x margin, tightened by 5x).
