@@ -120,9 +120,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
   return ok != 0;
 }
 
+// Non-blocking probe of the phase.  Every wait below probes with it first:
+// per-step clock64 traces showed ~200 cycles spent in waits whose phase had
+// completed long before, and the probe took the density kernel's stage from
+// 0.511 to 0.489 ms on the 64-atom cell (the grid-H stage did not change).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(mbar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait: returns false when the phase did not complete within
 // max_iters polls (the caller records an error and unwinds).
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_iters = (1u << 26)) {
+  if (mbar_test_wait(mbar, parity)) return true;
   for (uint32_t i = 0; i < max_iters; ++i)
     if (mbar_try_wait(mbar, parity)) return true;
   return false;
@@ -132,6 +149,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
 // the CTA.  Returns false on timeout or abort.
 __device__ __forceinline__ bool mbar_wait_abortable(uint64_t* mbar, uint32_t parity, const volatile int* abort,
                                                     uint32_t max_iters = (1u << 24)) {
+  if (mbar_test_wait(mbar, parity)) return true;
   for (uint32_t i = 0; i < max_iters; ++i) {
     if (mbar_try_wait(mbar, parity)) return true;
     if ((i & 63u) == 63u && *abort) return false;
