@@ -649,9 +649,10 @@ def run_ours(args):
                 roof["note"] = ("achieved counts the FP64 algorithm's flops (folded pairs, no padding) over the "
                                 "tensor-core kernel's own launch time (CUDA events around it; achieved_stage: over "
                                 "the stage, for H V weights + kernel + partial-block reduction).  The "
-                                "split-BF16 form issues nine bf16 products per product (four MMAs with the B parts "
-                                "stacked along N) on 16-orbital blocks (13 used), so frac is bounded near 1/9 of "
-                                "that before padding; the stage moves traffic_frac_hbm of the HBM peak")
+                                "split-BF16 form issues eight bf16 products per product (three MMAs per K step "
+                                "with the B parts stacked along N) on 16-orbital blocks (13 used) over every "
+                                "point of a brick, so frac is bounded near 1/8 of that before padding; the stage "
+                                "moves traffic_frac_hbm of the HBM peak")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     # tabulation and Poisson against the HBM roofline (algorithmic bytes:
