@@ -285,7 +285,8 @@ void lcp_job_destroy(lcp_job* job);
 lcp_status lcp_job_set_dm(lcp_ctx* ctx, lcp_job* job, const double* const* dm);
 /* Launch one grid step on the context stream (asynchronous).  Any context of
  * the job's device may run it (its workspaces and FFT plans are used); steps
- * of one job must not overlap. */
+ * of one job must not overlap.  From a job's second step on a context the
+ * launches are replayed as one CUDA graph (lcp_ctx_set_step_graphs). */
 lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job);
 /* The same step with CUDA events between its stages (synchronises); stage_ms[6] =
  * density, Poisson, xc+potential (with the energy partial sums of the same
@@ -487,6 +488,13 @@ lcp_status lcp_ctx_set_fault_test(lcp_ctx* ctx, uint32_t poll_limit, int32_t sta
  * whatever this says.  Replaces nothing of the reference (an option of this
  * library, src/XC/XC_PBE.jl:187-476, src/XC/GGA_PBE.jl:53-462). */
 lcp_status lcp_ctx_set_xc_arithmetic(lcp_ctx* ctx, int32_t double_float);
+
+/* Whether lcp_job_step replays its launches as a CUDA graph (1, the default)
+ * or launches them one by one (0).  Either gives the same results; the graph
+ * is captured at a job's second step on a context and captured again when
+ * the context's stream or options, or any device buffer of the library,
+ * changed.  Replaces nothing of the reference (an option of this library). */
+lcp_status lcp_ctx_set_step_graphs(lcp_ctx* ctx, int32_t on);
 
 /* The check build (liblcpgrid_check.so, compiled with LCP_BOUNDS_CHECK) tests
  * every index the pair and tensor-core kernels gather with (lens entries,

@@ -1596,7 +1596,82 @@ static lcp_status job_step_impl(lcp_ctx* ctx, lcp_job* job, cudaEvent_t* ev) {
   return LCP_OK;
 }
 
-lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job) { return job_step_impl(ctx, job, nullptr); }
+// What a captured step depends on besides the job's own buffers: the
+// context's stream and options, and every device buffer of the library (a
+// (re)allocation or a free anywhere moves one of the two counters).
+static void step_signature(const lcp_ctx* ctx, int64_t* sig) {
+  sig[0] = (int64_t)reinterpret_cast<intptr_t>(ctx->stream);
+  sig[1] = ctx->precision;
+  sig[2] = ctx->xc_dfl;
+  sig[3] = ctx->fault_poll;
+  sig[4] = ctx->fault_stall;
+  sig[5] = ctx->tc_ev != nullptr;
+  sig[6] = g_device_allocs.load(std::memory_order_relaxed);
+  sig[7] = g_device_frees.load(std::memory_order_relaxed);
+}
+
+// One step.  The first step of a job on a context runs its launches
+// directly (and makes every workspace it needs); the next one with the same
+// signature captures them into a CUDA graph, which later steps replay with
+// one launch: the step's ~20 kernels then reach the GPU at once instead of
+// one by one behind the host, which matters after a synchronising read
+// (the end-to-end loop: D in, step, H out).  A step that cannot be captured
+// (a stream without capture support, an unexpected call) runs without a
+// graph from then on.
+lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (!job) return fail(LCP_EINVAL, "NULL job");
+  if (!ctx->step_graphs) return job_step_impl(ctx, job, nullptr);
+  lcp_job::StepGraph& G = job->graphs[ctx];
+  int64_t sig[8];
+  step_signature(ctx, sig);
+  auto same = [](const int64_t* a, const int64_t* b) { return std::equal(a, a + 8, b); };
+  if (G.exec && same(G.sig, sig)) {
+    API_CUDA(cudaGraphLaunch(G.exec, ctx->stream), "graph launch");
+    ctx->launches += G.launches;
+    return LCP_OK;
+  }
+  if (G.exec) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  if (!G.off && G.have_prev && same(G.prev, sig)) {
+    const int64_t l0 = ctx->launches;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      s = job_step_impl(ctx, job, nullptr);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      int64_t after[8];
+      step_signature(ctx, after);
+      cudaGraphExec_t x = nullptr;
+      if (s == LCP_OK && e == cudaSuccess && g && same(after, sig) && cudaGraphInstantiate(&x, g, 0) == cudaSuccess) {
+        cudaGraphDestroy(g);
+        std::copy(sig, sig + 8, G.sig);
+        G.exec = x;
+        G.launches = ctx->launches - l0;
+        API_CUDA(cudaGraphLaunch(x, ctx->stream), "graph launch");
+        return LCP_OK;
+      }
+      if (g) cudaGraphDestroy(g);
+    }
+    (void)cudaGetLastError();  // the failed capture's error, if any
+    G.off = true;
+    ctx->launches = l0;
+  }
+  s = job_step_impl(ctx, job, nullptr);
+  step_signature(ctx, G.prev);
+  G.have_prev = true;
+  return s;
+}
+
+lcp_status lcp_ctx_set_step_graphs(lcp_ctx* ctx, int32_t on) {
+  lcp_status s = check_ctx(ctx);
+  if (s) return s;
+  if (on < 0 || on > 1) return fail(LCP_EINVAL, "on is 0 or 1");
+  ctx->step_graphs = on;
+  return LCP_OK;
+}
 
 lcp_status lcp_job_step_timed(lcp_ctx* ctx, lcp_job* job, double* stage_ms) {
   if (!stage_ms) return fail(LCP_EINVAL, "NULL argument");

@@ -33,6 +33,9 @@ static inline lcp_status cuda_fail(cudaError_t e, const char* where) {
 // Number of device allocations (cudaMalloc) made through DBuf since the
 // library was loaded, across all contexts; read by lcp_device_alloc_count.
 inline std::atomic<int64_t> g_device_allocs{0};
+// Number of DBuf frees: with the allocations, any change of a device buffer
+// a captured step graph could point into invalidates it (lcp_job_step).
+inline std::atomic<int64_t> g_device_frees{0};
 
 // Owning device buffer.
 struct DBuf {
@@ -42,11 +45,17 @@ struct DBuf {
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
   ~DBuf() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_device_frees.fetch_add(1, std::memory_order_relaxed);
+    }
   }
   cudaError_t ensure(size_t n) {
     if (n <= bytes && p) return cudaSuccess;
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_device_frees.fetch_add(1, std::memory_order_relaxed);
+    }
     p = nullptr;
     bytes = 0;
     cudaError_t e = cudaMalloc(&p, n ? n : 16);
@@ -55,7 +64,10 @@ struct DBuf {
     return e;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_device_frees.fetch_add(1, std::memory_order_relaxed);
+    }
     p = nullptr;
     bytes = 0;
   }
@@ -107,6 +119,7 @@ struct lcp_ctx {
   // kernel's poll limit (0: its default) and its stall switch
   uint32_t fault_poll = 0;
   int32_t xc_dfl = 0;  // drop-in GGA-PBE entry points in double-float (lcp_ctx_set_xc_arithmetic)
+  int32_t step_graphs = 1;  // lcp_job_step replays a captured CUDA graph (lcp_ctx_set_step_graphs)
   int32_t fault_stall = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // lcp_job_tc_kernel_ms: events around the tensor-core kernels of one step
@@ -167,6 +180,25 @@ struct lcp_job {
   DBuf dcoef, dexc;  // GGA_PBE: stencil weights [3][27] and dE/d(grad rho) [spin][xyz][nn]
   bool has_aden = false, has_pcc = false, has_vna = false;
   FftPlans* plans = nullptr;
+  // lcp_job_step's CUDA graphs, one per context that steps the job: the
+  // step's launches captured once and replayed by one graph launch while
+  // nothing they depend on changed (the signature: the context's stream and
+  // options, and the device allocation and free counters).
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    int64_t sig[8] = {};    // signature the graph was captured under
+    int64_t prev[8] = {};   // signature after the last step run without a graph
+    int64_t launches = 0;   // kernels of the captured step
+    bool have_prev = false, off = false;
+  };
+  std::map<const lcp_ctx*, StepGraph> graphs;
+  lcp_job() = default;
+  lcp_job(const lcp_job&) = delete;
+  lcp_job& operator=(const lcp_job&) = delete;
+  ~lcp_job() {
+    for (auto& kv : graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  }
 };
 
 

@@ -93,6 +93,7 @@ _SIGS = {
     "lcp_device_alloc_count": ([ctypes.POINTER(_i64)], _i32),
     "lcp_ctx_set_fault_test": ([_vp, ctypes.c_uint32, _i32], _i32),
     "lcp_ctx_set_xc_arithmetic": ([_vp, _i32], _i32),
+    "lcp_ctx_set_step_graphs": ([_vp, _i32], _i32),
     "lcp_bounds_check_status": ([_vp, ctypes.POINTER(_i64)], _i32),
     "lcp_orbs_timings": ([_vp, _pd], _i32),
     "lcp_solve_poisson": ([_vp, _pi32, _pd, _i32, _ppd, _pd, _pd], _i32),

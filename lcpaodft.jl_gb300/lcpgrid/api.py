@@ -76,6 +76,12 @@ class Context:
         double-float as the precision forms' grid step."""
         check(lib.lcp_ctx_set_xc_arithmetic(self._h, int(bool(double_float))))
 
+    def set_step_graphs(self, on):
+        """Whether GridStepJob.step on this context replays its launches as a
+        CUDA graph (True, the default; captured at a job's second step) or
+        launches them one by one (False).  Same results either way."""
+        check(lib.lcp_ctx_set_step_graphs(self._h, int(bool(on))))
+
     @property
     def launch_count(self):
         return int(lib.lcp_ctx_launch_count(self._h))
