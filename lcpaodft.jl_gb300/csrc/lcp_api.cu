@@ -1623,6 +1623,10 @@ lcp_status lcp_job_step(lcp_ctx* ctx, lcp_job* job) {
   if (s) return s;
   if (!job) return fail(LCP_EINVAL, "NULL job");
   if (!ctx->step_graphs) return job_step_impl(ctx, job, nullptr);
+  // a caller capturing the stream gets the launches in its own graph
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  API_CUDA(cudaStreamIsCapturing(ctx->stream, &cap), "capture status");
+  if (cap != cudaStreamCaptureStatusNone) return job_step_impl(ctx, job, nullptr);
   lcp_job::StepGraph& G = job->graphs[ctx];
   int64_t sig[8];
   step_signature(ctx, sig);
