@@ -118,27 +118,15 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 // per quantum (matrix elements).  What remains is the input quantisation e.
 // ==========================================================================
 
-// ==========================================================================
-
 namespace {
 
-constexpr int kPart = 2048;                    // bf16 per part of a table block
-constexpr int kBlockElems = 3 * kPart;         // table block: hi, mid, lo
+constexpr int kPart = 2048;                    // bf16 per part of a table block (hi, mid, lo parts)
 // The tables are part-major: part p of block b at tab + (p * nblocks + b) * kPart.
 constexpr int kDsymElems = 768;                // D block: hi, mid, lo (256 each)
 constexpr uint32_t kALbo = 2048, kASbo = 128;  // table block [h][g][8 pt][8 orb] as K-major A
 
-__device__ __forceinline__ void fx_split(double u, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
-  const double h = rint(u * 256.0) * (1.0 / 256.0);
-  const double r1 = u - h;
-  const double m = rint(r1 * 131072.0) * (1.0 / 131072.0);
-  const double l = rint((r1 - m) * 67108864.0) * (1.0 / 67108864.0);
-  hi = __float2bfloat16_rn((float)h);
-  mid = __float2bfloat16_rn((float)m);
-  lo = __float2bfloat16_rn((float)l);
-}
-
-// Same split for a float p (|p| <= 1) carrying a small correction e
+// The split above (hi, mid, lo: multiples of 2^-8, 2^-17, 2^-26) of a float
+// p (|p| <= 1) carrying a small correction e
 // (|e| <= 2^-23 |p|), in full-rate FP32 additions only.  Adding and
 // subtracting C = 1.5 * 2^k rounds x (|x| <= 2^(k-1)) to the nearest multiple
 // of ulp(C) = 2^(k-23) (ties to even), exactly: x + C lies in [2^k, 2^(k+1))
