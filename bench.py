@@ -640,19 +640,11 @@ def run_ours(args):
                 roof["traffic"] = per_block * nblocks
                 roof["traffic_gbs"] = roof["traffic"] / (stages[dom] * 1e-3) / 1e9
                 roof["traffic_frac_hbm"] = roof["traffic_gbs"] / peaks.get("hbm_gbs", 6800.0)
-                roof["traffic_note"] = (
-                    "ncu dram__bytes_read+write of the stage's tensor-core kernel (and for H the partial-block "
-                    "reduction), one capture of the 64-atom 96^3 cell (%d table blocks), scaled by table blocks "
-                    "(%d here).  The split tables (1.2 GB with the 13 -> 16 orbital and brick-slot padding) are read "
-                    "from DRAM once per kernel; the H kernel also writes 0.70 GB of partial blocks that the "
-                    "reduction reads back" % (TRAFFIC_BLOCKS, nblocks))
-                roof["note"] = ("achieved counts the FP64 algorithm's flops (folded pairs, no padding) over the "
-                                "tensor-core kernel's own launch time (CUDA events around it; achieved_stage: over "
-                                "the stage, for H V weights + kernel + partial-block reduction).  The "
-                                "split-BF16 form issues eight bf16 products per product (three MMAs per K step "
-                                "with the B parts stacked along N) on 16-orbital blocks (13 used) over every "
-                                "point of a brick, so frac is bounded near 1/8 of that before padding; the stage "
-                                "moves traffic_frac_hbm of the HBM peak")
+                roof["traffic_note"] = ("ncu DRAM read+write of the stage's kernels per table block (capture "
+                                        "of %d blocks), x %d blocks here" % (TRAFFIC_BLOCKS, nblocks))
+                roof["note"] = ("FP64-algorithm flops (folded pairs, no padding) over the kernel's launch time "
+                                "(achieved_stage: over the stage); split-BF16 forms 8 bf16 products on "
+                                "16-orbital blocks, so frac <= ~1/8 before padding")
     roof["frac"] = roof["achieved"] / roof["peak"] if roof["peak"] else None
 
     # tabulation and Poisson against the HBM roofline (algorithmic bytes:
